@@ -1,0 +1,421 @@
+#!/usr/bin/env python3
+"""Benchmark: the isolated big-integer multiply on one GB300.
+
+Headline workload: one balanced 2^30-bit x 2^30-bit product per step
+(2^24 x 2^24 limbs, Goldilocks NTT length N = 2^27), seeded synthetic limbs
+(uniform, top limb's bit 63 set).  The metric is NTT-multiply GB/s on the
+algorithmic-bytes model of a two-pass transform:
+
+    B_mul(N) = 96 N + 16 (la + lb) bytes per product.
+
+`value` times products whose operands are already resident in HBM (device
+API, CUDA events on the launching stream); `e2e` times the drop-in host API
+(pimul_mul) with pinned host buffers, so every step includes the
+host->device copy of both operands and the device->host copy of the product.
+
+`--impl reference` times the CPU restatement of the reference's multiply
+(the oracle, all host threads) on the same workload.  With --gpus N > 1
+under torchrun, every rank runs an independent replica (the multiply does
+not shard): value = all ranks' bytes / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BASELINE_METRIC = "1e9-digit pi wall-s; NTT-mul GB/s, batched ops/s & p99 vs plain GPU, bit-exact"
+METRIC = "NTT-mul GB/s (2^30 x 2^30-bit product)"
+BITS_A = 1 << 30
+BITS_B = 1 << 30
+
+# DRAM traffic per launch of the dominant kernel from ncu (bytes read +
+# written, profiles/ summaries); None until captured for the current build.
+NCU_TRAFFIC_PER_LAUNCH = None
+
+
+def b_mul(n, la, lb, square=False):
+    return (64 * n + 24 * la) if square else (96 * n + 16 * (la + lb))
+
+
+def next_pow2_log(x):
+    return (x - 1).bit_length()
+
+
+def make_operands(la, lb, seed=20241203):
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 1 << 64, size=la, dtype=np.uint64)
+    b = rng.integers(0, 1 << 64, size=lb, dtype=np.uint64)
+    a[-1] |= np.uint64(1 << 63)
+    b[-1] |= np.uint64(1 << 63)
+    return a, b
+
+
+# ----------------------------------------------------------------- distributed
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max(dist, x, device="cpu"):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is None:
+        return
+    if device is not None:
+        dist.barrier(device_ids=[device])
+    else:
+        dist.barrier()
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0, period_ms=50):
+        self.gpu = gpu_index
+        self.period = period_ms
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", f"-lms={self.period}"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- peaks
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- kernel stats
+def stats(lib):
+    out = {}
+    name = ctypes.c_char_p()
+    launches = ctypes.c_uint64()
+    timed = ctypes.c_uint64()
+    ms = ctypes.c_double()
+    k = 0
+    while lib.pimul_stats_get(k, ctypes.byref(name), ctypes.byref(launches), ctypes.byref(timed),
+                              ctypes.byref(ms)) == 0:
+        out[name.value.decode()] = {"launches": launches.value, "timed": timed.value, "ms": ms.value}
+        k += 1
+    return out
+
+
+def kernel_bytes_per_launch(kind, n, la, lb):
+    """Algorithmic bytes of one launch of each kernel class."""
+    if kind in ("pass_fwd", "pass_inv"):
+        return 16 * n              # read and write the N-word array once
+    if kind == "pack":
+        return 8 * n + 8 * la      # read limbs, write N coefficients
+    if kind == "pointwise":
+        return 24 * n              # read two arrays, write one
+    if kind == "carry":
+        return 8 * n + 8 * (la + lb)
+    return 0
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    import pi_gb300 as pm
+    lib = pm.lib()
+    pm.init(local)
+    la, lb = BITS_A // 64, BITS_B // 64
+    L = next_pow2_log(4 * la + 4 * lb - 1)
+    N = 1 << L
+    bytes_step = b_mul(N, la, lb)
+    a, b = make_operands(la, lb, seed=20241203 + rank)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        db = torch.from_numpy(b.view(np.int64)).cuda()
+        dout = torch.empty(la + lb, dtype=torch.int64, device="cuda")
+    stream.synchronize()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        rc = lib.pimul_mul_device(ctypes.c_void_p(da.data_ptr()), la, ctypes.c_void_p(db.data_ptr()), lb,
+                                  ctypes.c_void_p(dout.data_ptr()), sp)
+        if rc:
+            raise RuntimeError(lib.pimul_last_error().decode())
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    # correctness spot check of the warm-up result (low limbs exact)
+    low = dout[:8].cpu().numpy().view(np.uint64)
+    ia = sum(int(x) << (64 * i) for i, x in enumerate(a[:8]))
+    ib = sum(int(x) << (64 * i) for i, x in enumerate(b[:8]))
+    want = (ia * ib) % (1 << 512)
+    got = sum(int(x) << (64 * i) for i, x in enumerate(low))
+    if got != want:
+        raise RuntimeError("bench: product low limbs mismatch")
+
+    lib.pimul_stats_reset()
+    lib.pimul_stats_enable(1)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(dist, local)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier(dist, local)
+    lib.pimul_stats_enable(0)
+    ks = stats(lib)
+    ms_total = ev0.elapsed_time(ev1)
+    ms_total = reduce_max(dist, ms_total, device=f"cuda:{local}")
+    ms_step = ms_total / args.steps
+    value = ws * bytes_step * args.steps / (ms_total * 1e-3) / 1e9
+
+    # ---- e2e through the drop-in host API, pinned host buffers
+    pa = torch.from_numpy(a.view(np.int64)).pin_memory()
+    pb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    pout = torch.empty(la + lb, dtype=torch.int64).pin_memory()
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    ap = ctypes.cast(ctypes.c_void_p(pa.data_ptr()), u64p)
+    bp = ctypes.cast(ctypes.c_void_p(pb.data_ptr()), u64p)
+    op = ctypes.cast(ctypes.c_void_p(pout.data_ptr()), u64p)
+    olen = ctypes.c_size_t(0)
+
+    def e2e_step():
+        rc = lib.pimul_mul(ap, la, bp, lb, op, la + lb, ctypes.byref(olen))
+        if rc:
+            raise RuntimeError(lib.pimul_last_error().decode())
+
+    e2e_steps = max(3, min(args.steps, 10))
+    e2e_step()
+    barrier(dist, local)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    e2e_s = reduce_max(dist, t1 - t0, device=f"cuda:{local}")
+    e2e_value = ws * bytes_step * e2e_steps / e2e_s / 1e9
+
+    # ---- roofline of the dominant kernel class
+    peak, peak_kind = measured_peaks()
+    dom = max((k for k in ks if ks[k]["timed"]), key=lambda k: ks[k]["ms"])
+    avg_ms = ks[dom]["ms"] / ks[dom]["timed"]
+    per_launch = kernel_bytes_per_launch(dom, N, la, lb)
+    achieved = per_launch / (avg_ms * 1e-3) / 1e9
+    step_achieved = bytes_step / (ms_step * 1e-3) / 1e9
+    launches = sum(v["launches"] for v in ks.values())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(la, lb, N)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "baseline_metric": BASELINE_METRIC,
+            "value": round(value, 2),
+            "unit": "GB/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "u64",
+            "data": "synthetic: seeded uniform u64 limbs, top limb bit 63 set (numpy PCG64)",
+            "config": {
+                "workload": "isolated multiply, balanced 2^30 x 2^30 bits (2^24 x 2^24 limbs), N = 2^27",
+                "bits_a": BITS_A, "bits_b": BITS_B, "la": la, "lb": lb, "transform_len": N,
+                "bytes_per_step_model": "B_mul(N) = 96N + 16(la+lb)",
+                "bytes_per_step": bytes_step,
+                "l2": "inputs + scratch (2.3 GiB) exceed the 129 MB L2; no flush needed",
+                "parallelism": f"replicas x{ws}",
+            },
+            "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
+                    "h2d_bytes_per_step": 8 * (la + lb), "d2h_bytes_per_step": 8 * (la + lb),
+                    "api": "pimul_mul (host buffers, pinned)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": NCU_TRAFFIC_PER_LAUNCH,
+                         "bytes_per_launch": per_launch, "avg_launch_ms": round(avg_ms, 4),
+                         "step_achieved": round(step_achieved, 1),
+                         "step_frac": round(step_achieved / peak, 4)},
+            "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ks.items()},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------- CPU legs
+def cpu_baseline_sample(la, lb, n):
+    """The oracle (CPU restatement of the reference's mul_mag_ntt) on one
+    full-size product, all host threads."""
+    import oracle
+    oracle.build()
+    threads = oracle.max_threads()
+    a, b = make_operands(la, lb, seed=7)
+    t0 = time.perf_counter()
+    oracle.mul_mag_ntt(a, b)
+    dt = time.perf_counter() - t0
+    return {"value": round(b_mul(n, la, lb) / dt / 1e9, 3), "unit": "GB/s", "cores": threads,
+            "kind": "port", "seconds": round(dt, 2),
+            "sample": f"one {la}x{lb}-limb product (the full workload) through the C restatement of "
+                      f"mul_mag_ntt (crates/bignum/src/ntt.rs:806-865), OpenMP on {threads} threads"}
+
+
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = oracle.max_threads()
+    la, lb = BITS_A // 64, BITS_B // 64
+    L = next_pow2_log(4 * la + 4 * lb - 1)
+    N = 1 << L
+    a, b = make_operands(la, lb)
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 3))
+    for _ in range(warm):
+        oracle.mul_mag_ntt(a, b)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.mul_mag_ntt(a, b)
+    dt = time.perf_counter() - t0
+    value = b_mul(N, la, lb) * steps / dt / 1e9
+    sample = (f"{steps} timed + {warm} warm-up full {la}x{lb}-limb products (requested {args.steps}/"
+              f"{args.warmup}; capped so the CPU run stays within minutes)")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "baseline_metric": BASELINE_METRIC,
+        "value": round(value, 3),
+        "unit": "GB/s",
+        "n_gpus": ws,
+        "steps": steps,
+        "warmup": warm,
+        "ms_per_step": round(1e3 * dt / steps, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic: seeded uniform u64 limbs, top limb bit 63 set (numpy PCG64)",
+        "config": {"workload": "isolated multiply, balanced 2^30 x 2^30 bits (2^24 x 2^24 limbs), N = 2^27",
+                   "bits_a": BITS_A, "bits_b": BITS_B, "la": la, "lb": lb, "transform_len": N,
+                   "bytes_per_step_model": "B_mul(N) = 96N + 16(la+lb)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; C restatement of crates/bignum/src/ntt.rs:806-865 "
+                                            "(the Rust reference cannot be built here: no cargo/rustc)"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "engine":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

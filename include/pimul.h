@@ -1,0 +1,95 @@
+/*
+ * pimul — GB300-native big-integer multiply engine (C ABI).
+ *
+ * Numbers are little-endian arrays of 64-bit limbs, as in the reference's
+ * `Integer` magnitude (joelodom/pi crates/bignum/src/integer.rs:22-27).  An
+ * empty array (length 0) is zero.  Products are exact: every result equals
+ * the reference's CPU multiply bit for bit.
+ *
+ * The multiply is a Goldilocks-prime (p = 2^64 - 2^32 + 1) number-theoretic
+ * transform with the reference's own rules: 16-bit coefficients, four per
+ * limb, transform length N = next_pow2(4*la + 4*lb - 1)
+ * (crates/bignum/src/ntt.rs:633-634, ntt.rs:810-813), N <= 2^32.
+ *
+ * Every entry point returns PIMUL_OK (0) or one of the error codes below;
+ * pimul_last_error() gives a message for the calling thread's last failure.
+ * All entry points are thread-safe and re-entrant.
+ */
+#ifndef PIMUL_H
+#define PIMUL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIMUL_OK 0
+#define PIMUL_EINVAL 1     /* bad argument (null pointer, capacity too small, N > 2^32) */
+#define PIMUL_ENOMEM 2     /* device allocation failed or HBM budget exceeded */
+#define PIMUL_ECUDA 3      /* a CUDA call failed */
+#define PIMUL_ETIMEDOUT 4  /* a bounded wait ran out */
+#define PIMUL_ENOTFOUND 5  /* unknown handle or ticket */
+#define PIMUL_ECANCELED 6  /* request was cancelled */
+
+/* Library version string. */
+const char* pimul_version(void);
+
+/* Message for the calling thread's last failed call ("" if none). */
+const char* pimul_last_error(void);
+
+/* Select and initialise the CUDA device (twiddle tables, pools).  Optional:
+ * every other entry point initialises device 0 on first use.  Idempotent. */
+int pimul_init(int device);
+
+/* Release pooled device memory and tables.  Later calls re-initialise. */
+int pimul_shutdown(void);
+
+/*
+ * Plain drop-in multiply with HOST buffers: out = a * b, trimmed of top zero
+ * limbs; *out_len receives the trimmed length.  out_cap must be >= la + lb
+ * (or 0 when la == 0 or lb == 0).  a == b with la == lb takes the squaring
+ * path (two transforms instead of three); the bits are the same.
+ *
+ * Replaces: crates/bignum/src/ntt.rs:806 `mul_mag_ntt(a: &[u64], b: &[u64])
+ * -> Vec<u64>`, called from mul_mag_dispatch at crates/bignum/src/integer.rs:480.
+ */
+int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb,
+              uint64_t* out, size_t out_cap, size_t* out_len);
+
+/*
+ * Same multiply on DEVICE buffers, asynchronous on `stream` (a cudaStream_t;
+ * NULL = the calling thread's own stream).  Writes exactly la + lb limbs to
+ * d_out (the top limb may be zero); d_out must not overlap the inputs.
+ * Scratch comes from the engine's device pool.
+ *
+ * Replaces: crates/bignum/src/ntt.rs:806 `mul_mag_ntt`, for callers whose
+ * operands already live in HBM.
+ */
+int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
+                     uint64_t* d_out, void* stream);
+
+/* Transform plan for a product: N and the number of HBM passes per transform.
+ * Mirrors the sizing of crates/bignum/src/ntt.rs:810-813. */
+int pimul_plan(size_t la, size_t lb, uint64_t* n_transform, int* passes);
+
+/* Kernel launch statistics (this engine's own instrumentation; the
+ * reference's counterpart is its perf JSONL recorder,
+ * crates/pi-core/src/perf.rs).  Launch counts are always kept; with
+ * pimul_stats_enable(1) every launch is also timed with CUDA events on its
+ * stream.  kclass indexes the kernel classes 0 .. n-1; an out-of-range
+ * index returns PIMUL_EINVAL, so callers can enumerate them. */
+int pimul_stats_enable(int on);
+int pimul_stats_reset(void);
+int pimul_stats_get(int kclass, const char** name, uint64_t* launches, uint64_t* timed_launches,
+                    double* total_ms);
+
+/* Synchronise the calling thread's own stream. */
+int pimul_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PIMUL_H */
