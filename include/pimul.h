@@ -70,6 +70,25 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb,
 int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
                      uint64_t* d_out, void* stream);
 
+/*
+ * The same device multiply for callers that cannot allocate device memory
+ * when they multiply (a GPU whose memory belongs to another allocator, a
+ * loop where cudaMalloc's implicit synchronisation is not allowed, a runtime
+ * that allocates only at start-up).  It uses no memory pool: its scratch is
+ * a fixed device array inside this library (16 MiB, resident on every GPU
+ * that loads the library until exit), so products are limited to
+ * la + lb <= 262144 limbs (transform length <= 2^20); larger ones return
+ * PIMUL_EINVAL.  All calls share that array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  The first call on a device
+ * sets the array up (address lookup and a synchronous table copy), so make
+ * it before any stream capture.  `stream` NULL means the CUDA default stream.
+ *
+ * No counterpart in the reference (its multiply allocates per call:
+ * crates/bignum/src/ntt.rs:823-824 acquires pooled heap buffers).
+ */
+int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
+                             uint64_t* d_out, void* stream);
+
 /* Transform plan for a product: N and the number of HBM passes per transform.
  * Mirrors the sizing of crates/bignum/src/ntt.rs:810-813. */
 int pimul_plan(size_t la, size_t lb, uint64_t* n_transform, int* passes);

@@ -822,3 +822,148 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Multiply entry point that allocates nothing (pimul_mul_device_noalloc)
+// ====================================================================
+// Some callers cannot allocate device memory at the moment they multiply:
+// a host that has handed the whole GPU to another allocator (a framework's
+// caching allocator, a fixed arena reserved at start-up), a latency-bound
+// loop where cudaMalloc's implicit device synchronisation is not allowed,
+// or an embedding runtime whose rule is "allocate at init, never in the
+// steady state".  For them this variant takes its scratch from a
+// file-scope device array instead of the stream-ordered pool.
+//
+// Limits and sharing rules:
+//  * scratch holds two transform arrays of at most 2^20 words plus the carry
+//    scan's flags: la + lb <= 262144 limbs (transform length N <= 2^20);
+//    larger products are rejected with PIMUL_EINVAL.  The array (16 MiB
+//    plus 1 MiB of root tables) stays resident on every GPU that loads this
+//    library, until the process exits.
+//  * every call uses the same array, and the array keeps the previous call's
+//    contents; the kernels overwrite every scratch word before reading it,
+//    so nothing needs clearing.  Calls whose work overlaps on the GPU
+//    (different streams, or different host threads without ordering) race
+//    on the array and corrupt each other's results: serialise them.
+//  * the first call on each device does a one-time set-up with that device
+//    current: it resolves the arrays' device addresses with
+//    cudaGetSymbolAddress and copies the root tables in with a synchronous
+//    cudaMemcpyToSymbol.  Make that first call before any stream capture.
+constexpr int NOALLOC_LOG_MAX = 20;
+constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;
+constexpr uint64_t NOALLOC_WIN_MAX = NOALLOC_N_MAX / 16;
+constexpr uint64_t NOALLOC_CHUNK_MAX = (NOALLOC_WIN_MAX + CARRY_THREADS - 1) / CARRY_THREADS;
+constexpr uint64_t NOALLOC_AUX_WORDS = (NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64) / 8 + 1;
+constexpr size_t NOALLOC_ROOT_WORDS = 2 * 65536 + 4096;
+
+static __device__ __align__(256) uint64_t g_noalloc_scratch[2 * NOALLOC_N_MAX + NOALLOC_AUX_WORDS];
+static __device__ __align__(256) uint64_t g_noalloc_roots[NOALLOC_ROOT_WORDS];
+
+struct NoAllocDev {
+  bool ready = false;
+  uint64_t* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+  Roots roots{};
+};
+static std::mutex g_na_mu;
+static NoAllocDev g_na[64];
+static uint64_t g_na_host_roots[NOALLOC_ROOT_WORDS];  // staging, no heap use
+
+static int noalloc_setup(NoAllocDev** out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(PIMUL_EINVAL, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_na_mu);
+  NoAllocDev& d = g_na[dev];
+  if (!d.ready) {
+    uint64_t rho = find_rho();
+    if (!rho) return fail(PIMUL_ECUDA, "root-of-unity search failed");
+    uint64_t* lo = g_na_host_roots;
+    uint64_t* hi = lo + 65536;
+    uint64_t* w12 = hi + 65536;
+    uint64_t x = 1;
+    for (int i = 0; i < 65536; i++) { lo[i] = x; x = hf::mul(x, rho); }
+    uint64_t step = x;
+    x = 1;
+    for (int i = 0; i < 65536; i++) { hi[i] = x; x = hf::mul(x, step); }
+    uint64_t w4096 = hf::pow(rho, 1ull << 20);
+    x = 1;
+    for (int i = 0; i < 4096; i++) { w12[i] = x; x = hf::mul(x, w4096); }
+    uint64_t* scratch = nullptr;
+    uint64_t* roots = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    e = cudaGetSymbolAddress((void**)&roots, g_noalloc_roots);
+    if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("cudaGetSymbolAddress(roots): ") + cudaGetErrorString(e));
+    CU(cudaMemcpyToSymbol(g_noalloc_roots, g_na_host_roots, sizeof(g_na_host_roots)));
+    CU(cudaFuncSetAttribute(k_pass_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem_bytes(TILE_LOG_MAX)));
+    CU(cudaFuncSetAttribute(k_pass_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem_bytes(TILE_LOG_MAX)));
+    CU(cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem_bytes(SMALL_LOG_MAX)));
+    d.scratch = scratch;
+    d.roots = Roots{roots, roots + 65536, roots + 2 * 65536};
+    d.ready = true;
+  }
+  *out = &d;
+  return PIMUL_OK;
+}
+
+// A pass launch without the statistics hook (whose event timing would
+// create CUDA events).
+static void noalloc_pass(const PassArgs& a, bool inverse, const Roots& R, cudaStream_t st) {
+  uint64_t tiles = 1ull << (a.L - (a.r + a.t + a.bc));
+  size_t smem = pass_smem_bytes(a.r + a.t + a.bc);
+  if (inverse) k_pass_inv<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
+  else k_pass_fwd<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
+}
+
+static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
+                              cudaStream_t st) {
+  NoAllocDev* nd = nullptr;
+  int rc = noalloc_setup(&nd);
+  if (rc) return rc;
+  const uint64_t n_out = 4 * la + 4 * lb - 1;
+  const int L = log2_ceil(n_out);
+  const Roots& R = nd->roots;
+  const bool square = d_a == d_b && la == lb;
+  if (L <= SMALL_LOG_MAX) {  // whole product in one CTA's shared memory: no scratch
+    SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
+    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(L), st>>>(job, R);
+    CU(cudaGetLastError());
+    return PIMUL_OK;
+  }
+  const uint64_t N = 1ull << L;
+  const Plan pl = make_plan(L);
+  const uint64_t nwin = (n_out + 15) / 16;
+  const uint64_t nchunk = (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
+  const uint64_t nwarp = nchunk * (CARRY_THREADS / 32);
+  uint64_t* A = nd->scratch;
+  uint64_t* B = nd->scratch + NOALLOC_N_MAX;
+  uint8_t* aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX);
+  k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_a, la, A, N);
+  for (int p = 0; p < pl.np; p++) noalloc_pass(pass_args(A, pl, p), false, R, st);
+  if (!square) {
+    k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_b, lb, B, N);
+    for (int p = 0; p < pl.np; p++) noalloc_pass(pass_args(B, pl, p), false, R, st);
+  }
+  uint64_t ninv = hf::pow(hf::pow(2, 191), L);
+  k_pointwise<<<grid_for(N, 256), 256, 0, st>>>(A, square ? A : B, N, ninv);
+  for (int p = pl.np - 1; p >= 0; p--) noalloc_pass(pass_args(A, pl, p), true, R, st);
+  uint32_t* masks = reinterpret_cast<uint32_t*>(aux);
+  uint8_t* chunk_gp = aux + nwarp * 8;
+  uint8_t* chunk_cin = chunk_gp + nchunk;
+  const uint64_t nlimbs = la + lb;
+  k_carry_local<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(A, nwin, d_out, nlimbs, masks, chunk_gp);
+  k_carry_scan<<<1, SCAN_THREADS, 0, st>>>(chunk_gp, nchunk, chunk_cin);
+  k_carry_apply<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(nwin, d_out, nlimbs, masks, chunk_cin);
+  CU(cudaGetLastError());
+  return PIMUL_OK;
+}
+
+extern "C" int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
+                                        uint64_t* d_out, void* stream) {
+  if (la == 0 || lb == 0) return PIMUL_OK;
+  if (!d_a || !d_b || !d_out) return fail(PIMUL_EINVAL, "null device pointer");
+  if (la + lb > NOALLOC_N_MAX / 4)
+    return fail(PIMUL_EINVAL, "product too large for the no-alloc scratch: la + lb must be <= 262144 limbs "
+                              "(transform length <= 2^20)");
+  return mul_device_noalloc(d_a, la, d_b, lb, d_out, (cudaStream_t)stream);
+}
