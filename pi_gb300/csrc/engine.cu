@@ -71,7 +71,8 @@ struct KTimer {
   int cls;
   cudaStream_t st;
   cudaEvent_t a = nullptr;
-  KTimer(int c, cudaStream_t s) : cls(c), st(s) {
+  KTimer(int c, cudaStream_t s, bool on = true) : cls(c), st(s) {
+    if (!on) return;
     g_launch[c].fetch_add(1, std::memory_order_relaxed);
     if (g_timing.load(std::memory_order_relaxed)) {
       a = ev_get();
@@ -144,100 +145,134 @@ static uint64_t find_rho() {
 }
 
 // ------------------------------------------------------------------ kernels
-struct PassArgs {
-  uint64_t* data;
-  int L;   // log2 N
-  int r;   // log2 rows (radix of this pass)
-  int s;   // log2 row stride (columns of a block)
-  int t;   // log2 columns per tile
-  int bc;  // log2 blocks per tile
-  RoundPlan rp;
-};
+// Geometry of the HBM passes.  All pass tiles hold 2^13 words (64 KiB plus
+// padding) and are processed by 256 threads:
+//   first pass (p = 0):   2^R rows x 2^(13-R) columns of the single block
+//   middle passes:        2^(9-R) blocks x 2^R rows x 16 columns
+//   last pass (S = 1):    2^(13-R) contiguous blocks of 2^R words
+// Column tiles read 128-byte (or wider) row segments.
+constexpr int PASS_THREADS = 256;
+constexpr int TILE_LOG = 13;
 
-constexpr int PASS_THREADS = 512;
-constexpr int TILE_LOG_MAX = 13;  // 8192 words (64 KiB) per tile
+static inline size_t pass_smem_bytes(int tile_log) { return ((size_t)1 << tile_log) * 17 / 16 * 8 + 512 * 8; }
 
-// Dynamic shared memory of a pass tile of 2^tile_log words (padded).
-static inline size_t pass_smem_bytes(int tile_log) { return ((size_t)1 << tile_log) * 17 / 16 * 8; }
-
-__device__ __forceinline__ uint64_t tile_gaddr(const PassArgs& a, uint32_t lin, uint64_t b0, uint64_t j0) {
-  uint32_t j = lin & ((1u << a.t) - 1);
-  uint32_t i = (lin >> a.t) & ((1u << a.r) - 1);
-  uint32_t blk = lin >> (a.t + a.r);
-  return ((b0 + blk) << (a.r + a.s)) + ((uint64_t)i << a.s) + j0 + j;
+// Load the 512 forward roots w_512^t into shared memory (round twiddles).
+__device__ __forceinline__ void load_tw512(uint64_t* tw, const Roots& R) {
+  for (int t = threadIdx.x; t < 512; t += blockDim.x) tw[t] = __ldg(R.w20 + ((uint64_t)t << (W20_LOG - 9)));
 }
 
-// One forward pass: load tile, R-point DFT per column, outgoing twiddle
-// w_M^(f*j) with M = 2^(r+s), store in place.
-__global__ void __launch_bounds__(PASS_THREADS) k_pass_fwd(PassArgs a, Roots R) {
+// Forward pass 0 with the limb -> 16-bit coefficient split fused in
+// (crates/bignum/src/ntt.rs:640-665): element (i, j) of the tile is
+// coefficient n = i * 2^S + j0 + j, i.e. 16-bit slice n % 4 of limb n / 4;
+// limbs past nl are zero (the reference's zero tail).
+template <int R>
+__global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const uint64_t* __restrict__ limbs, uint64_t nl,
+                                                             uint64_t* __restrict__ data, int L, Roots RT) {
+  constexpr int T = TILE_LOG - R;
   extern __shared__ uint64_t sm[];
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
-  const uint32_t E = 1u << (a.r + a.t + a.bc);
-  const uint64_t ct = blockIdx.x & ((1u << (a.s - a.t)) - 1);
-  const uint64_t bt = (uint64_t)blockIdx.x >> (a.s - a.t);
-  const uint64_t j0 = ct << a.t, b0 = bt << a.bc;
-  for (uint32_t lin = tid; lin < E; lin += PASS_THREADS) sm[spad(lin)] = a.data[tile_gaddr(a, lin, b0, j0)];
+  const int S = L - R;
+  const uint64_t j0 = (uint64_t)blockIdx.x << T;
+  load_tw512(tw, RT);
+  // each thread expands whole limbs: 2^R rows x 2^(T-2) limbs
+  for (uint32_t q = tid; q < (1u << (R + T - 2)); q += PASS_THREADS) {
+    uint32_t i = q >> (T - 2), c4 = q & ((1u << (T - 2)) - 1);
+    uint64_t li = (((uint64_t)i << S) + j0) / 4 + c4;
+    uint64_t x = li < nl ? __ldg(limbs + li) : 0;
+    uint32_t base = (i << T) + 4 * c4;
+    sm[spad(base + 0)] = x & 0xFFFF;
+    sm[spad(base + 1)] = (x >> 16) & 0xFFFF;
+    sm[spad(base + 2)] = (x >> 32) & 0xFFFF;
+    sm[spad(base + 3)] = x >> 48;
+  }
   __syncthreads();
-  TileGeom g{a.r, a.t, a.bc};
-  tile_dft_fwd(sm, g, a.rp, R, tid, PASS_THREADS);
-  const int mlog = a.r + a.s;
-  for (uint32_t lin = tid; lin < E; lin += PASS_THREADS) {
-    uint64_t v = sm[spad(lin)];
-    if (a.s > 0) {
-      uint32_t i = (lin >> a.t) & ((1u << a.r) - 1);
-      uint64_t jg = j0 + (lin & ((1u << a.t) - 1));
-      uint64_t f = row_freq(i, a.r, a.rp);
-      uint32_t e = (uint32_t)((f * jg) << (32 - mlog));
-      if (e) v = gl::mul(v, rho_pow(R, e));
-    }
-    a.data[tile_gaddr(a, lin, b0, j0)] = v;
+  tile_fwd_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
+    uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+    uint64_t f = row_freq_t<R>(i);
+    uint64_t v = gl::mul(sm[spad(lin)], root_pow(RT, L, f * (j0 + j), false));
+    data[((uint64_t)i << S) + j0 + j] = v;
   }
 }
 
-// Mirror of k_pass_fwd: incoming twiddle w_M^(-f*j), inverse rounds.
-__global__ void __launch_bounds__(PASS_THREADS) k_pass_inv(PassArgs a, Roots R) {
+// Middle column pass: 2^(9-R) blocks x 2^R rows x 16 columns; forward pass
+// twiddles w_M^(f*j) after the rounds, inverse ones before.
+template <int R, bool FWD>
+__global__ void __launch_bounds__(PASS_THREADS) k_col_mid(uint64_t* __restrict__ data, int S, Roots RT) {
+  constexpr int T = 4, BC = 9 - R;
   extern __shared__ uint64_t sm[];
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
-  const uint32_t E = 1u << (a.r + a.t + a.bc);
-  const uint64_t ct = blockIdx.x & ((1u << (a.s - a.t)) - 1);
-  const uint64_t bt = (uint64_t)blockIdx.x >> (a.s - a.t);
-  const uint64_t j0 = ct << a.t, b0 = bt << a.bc;
-  const int mlog = a.r + a.s;
-  for (uint32_t lin = tid; lin < E; lin += PASS_THREADS) {
-    uint64_t v = a.data[tile_gaddr(a, lin, b0, j0)];
-    if (a.s > 0) {
-      uint32_t i = (lin >> a.t) & ((1u << a.r) - 1);
-      uint64_t jg = j0 + (lin & ((1u << a.t) - 1));
-      uint64_t f = row_freq(i, a.r, a.rp);
-      uint32_t e = (uint32_t)((f * jg) << (32 - mlog));
-      if (e) v = gl::mul(v, rho_pow(R, (uint32_t)(0u - e)));
+  const int mlog = R + S;
+  const uint64_t ct = blockIdx.x & ((1u << (S - T)) - 1);
+  const uint64_t b0 = ((uint64_t)blockIdx.x >> (S - T)) << BC;
+  const uint64_t j0 = ct << T;
+  load_tw512(tw, RT);
+  auto gaddr = [&](uint32_t lin) {
+    uint32_t j = lin & 15, i = (lin >> 4) & ((1u << R) - 1), blk = lin >> (4 + R);
+    return ((b0 + blk) << mlog) + ((uint64_t)i << S) + j0 + j;
+  };
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
+    uint64_t v = data[gaddr(lin)];
+    if (!FWD) {
+      uint32_t i = (lin >> 4) & ((1u << R) - 1);
+      v = gl::mul(v, root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), true));
     }
     sm[spad(lin)] = v;
   }
   __syncthreads();
-  TileGeom g{a.r, a.t, a.bc};
-  tile_dft_inv(sm, g, a.rp, R, tid, PASS_THREADS);
-  for (uint32_t lin = tid; lin < E; lin += PASS_THREADS) a.data[tile_gaddr(a, lin, b0, j0)] = sm[spad(lin)];
-}
-
-// Limbs -> 16-bit coefficients, zero tail (crates/bignum/src/ntt.rs:640-665).
-__global__ void k_pack(const uint64_t* __restrict__ limbs, uint64_t nl, uint64_t* __restrict__ c, uint64_t n) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (; i < n / 4; i += stride) {
-    uint64_t l = i < nl ? limbs[i] : 0;
-    ulonglong2 lo = make_ulonglong2(l & 0xFFFF, (l >> 16) & 0xFFFF);
-    ulonglong2 hi = make_ulonglong2((l >> 32) & 0xFFFF, l >> 48);
-    reinterpret_cast<ulonglong2*>(c)[2 * i] = lo;
-    reinterpret_cast<ulonglong2*>(c)[2 * i + 1] = hi;
+  if (FWD) tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
+  else tile_inv_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
+    uint64_t v = sm[spad(lin)];
+    if (FWD) {
+      uint32_t i = (lin >> 4) & ((1u << R) - 1);
+      v = gl::mul(v, root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), false));
+    }
+    data[gaddr(lin)] = v;
   }
 }
 
-// Pointwise a <- a * b * n^-1 (the inverse's 1/N folded in).
-__global__ void k_pointwise(uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t n, uint64_t ninv) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) a[i] = gl::mul(gl::mul(a[i], b[i]), ninv);
+// Last forward pass (stride 1): 2^(13-R) contiguous blocks of 2^R words.
+template <int R>
+__global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(uint64_t* __restrict__ data, Roots RT) {
+  constexpr int BC = TILE_LOG - R;
+  extern __shared__ uint64_t sm[];
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
+  const int tid = threadIdx.x;
+  uint64_t* base = data + ((uint64_t)blockIdx.x << TILE_LOG);
+  load_tw512(tw, RT);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = base[lin];
+  __syncthreads();
+  tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) base[lin] = sm[spad(lin)];
+}
+
+// Fused middle of the multiply on one contiguous tile: last forward pass of
+// b, pointwise product with the spectrum of a (times N^-1, the inverse's
+// 1/N, crates/bignum/src/ntt.rs:383-390 and 845-853), first inverse pass;
+// the result overwrites b's array.  SQUARE: a's own spectrum is squared.
+template <int R, bool SQUARE>
+__global__ void __launch_bounds__(PASS_THREADS) k_mid(uint64_t* __restrict__ b, const uint64_t* __restrict__ a,
+                                                       uint64_t ninv, Roots RT) {
+  constexpr int BC = TILE_LOG - R;
+  extern __shared__ uint64_t sm[];
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
+  const int tid = threadIdx.x;
+  const uint64_t off = (uint64_t)blockIdx.x << TILE_LOG;
+  load_tw512(tw, RT);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = b[off + lin];
+  __syncthreads();
+  tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
+    uint64_t x = sm[spad(lin)];
+    uint64_t y = SQUARE ? x : a[off + lin];
+    sm[spad(lin)] = gl::mul(gl::mul(x, y), ninv);
+  }
+  __syncthreads();
+  tile_inv_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) b[off + lin] = sm[spad(lin)];
 }
 
 // ---- carry normalisation (crates/bignum/src/ntt.rs:676-791) --------------
@@ -254,17 +289,15 @@ struct Win {
   uint64_t hi;
 };
 
-__device__ __forceinline__ Win window_value(const uint64_t* c) {
+// Window value from 16 canonical coefficients (u128 accumulator, as the
+// reference's unpack loop, ntt.rs:694-707).
+__device__ __forceinline__ Win fold16(const uint64_t* c16, int stride) {
   Win r;
   unsigned __int128 acc = 0;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(c + 4 * k);
-    ulonglong2 x = p[0], y = p[1];
-    acc += (unsigned __int128)x.x;
-    acc += (unsigned __int128)x.y << 16;
-    acc += (unsigned __int128)y.x << 32;
-    acc += (unsigned __int128)y.y << 48;
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc += (unsigned __int128)c16[(4 * k + q) * stride] << (16 * q);
     r.l[k] = (uint64_t)acc;
     acc >>= 64;
   }
@@ -272,30 +305,70 @@ __device__ __forceinline__ Win window_value(const uint64_t* c) {
   return r;
 }
 
+// Inverse pass 0 (natural order out) fused with the window fold: each tile
+// row holds 2^T consecutive coefficients = 2^(T-4) windows; every window
+// writes its low 4 limbs to the output and its high part to H.
+template <int R>
+__global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const uint64_t* __restrict__ data, int L,
+                                                                   uint64_t* __restrict__ out, uint64_t nlimbs,
+                                                                   uint64_t* __restrict__ H, uint64_t nwin,
+                                                                   Roots RT) {
+  constexpr int T = TILE_LOG - R;
+  extern __shared__ uint64_t sm[];
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
+  const int tid = threadIdx.x;
+  const int S = L - R;
+  const uint64_t j0 = (uint64_t)blockIdx.x << T;
+  load_tw512(tw, RT);
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
+    uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+    uint64_t v = data[((uint64_t)i << S) + j0 + j];
+    sm[spad(lin)] = gl::mul(v, root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), true));
+  }
+  __syncthreads();
+  tile_inv_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
+  for (uint32_t q = tid; q < (1u << (TILE_LOG - 4)); q += PASS_THREADS) {
+    uint32_t i = q >> (T - 4), k = q & ((1u << (T - 4)) - 1);
+    uint64_t w = ((((uint64_t)i << S) + j0) >> 4) + k;
+    if (w >= nwin) continue;
+    uint64_t c[16];
+    uint32_t b = (i << T) + 16 * k;
+#pragma unroll
+    for (int t = 0; t < 16; t++) c[t] = gl::canon(sm[spad(b + t)]);
+    Win v = fold16(c, 1);
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      if (4 * w + t < nlimbs) out[4 * w + t] = v.l[t];
+    H[w] = v.hi;
+  }
+}
+
 constexpr int CARRY_THREADS = 256;  // windows per CTA
 
-// Pass 1: per window s_w (stored as output limbs), flags; per warp the
-// (A, B) masks; per CTA the chunk's (generate, propagate) pair.
+// Carry pass 1: s_w = lo_w + hi_(w-1) written back as the output limbs; per
+// window (g, p), per warp the (A, B) masks, per CTA the chunk's carry out
+// for carry in 0 and 1.
 __global__ void __launch_bounds__(CARRY_THREADS)
-k_carry_local(const uint64_t* __restrict__ coef, uint64_t nwin, uint64_t* __restrict__ out, uint64_t nlimbs,
+k_carry_local(uint64_t* __restrict__ out, uint64_t nlimbs, const uint64_t* __restrict__ H, uint64_t nwin,
               uint32_t* __restrict__ masks, uint8_t* __restrict__ chunk_gp) {
   __shared__ uint32_t sA[CARRY_THREADS / 32], sB[CARRY_THREADS / 32];
   const uint64_t w = (uint64_t)blockIdx.x * CARRY_THREADS + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  Win v{{0, 0, 0, 0}, 0};
-  if (w < nwin) v = window_value(coef + 16 * w);
-  uint64_t hprev = __shfl_up_sync(0xFFFFFFFFu, v.hi, 1);
-  if (lane == 0) hprev = (w > 0 && w - 1 < nwin) ? window_value(coef + 16 * (w - 1)).hi : 0;
-  // s = lo + hprev
-  uint64_t s0 = v.l[0] + hprev;
-  uint64_t c = s0 < hprev;
-  uint64_t s1 = v.l[1] + c;  c = c && s1 == 0;
-  uint64_t s2 = v.l[2] + c;  c = c && s2 == 0;
-  uint64_t s3 = v.l[3] + c;  c = c && s3 == 0;
-  bool g = c != 0 && w < nwin;
-  bool p = w < nwin && (s0 & s1 & s2 & s3) == ~0ull;
+  bool g = false, p = false;
   if (w < nwin) {
     uint64_t base = 4 * w;
+    uint64_t l0 = base + 0 < nlimbs ? out[base + 0] : 0;
+    uint64_t l1 = base + 1 < nlimbs ? out[base + 1] : 0;
+    uint64_t l2 = base + 2 < nlimbs ? out[base + 2] : 0;
+    uint64_t l3 = base + 3 < nlimbs ? out[base + 3] : 0;
+    uint64_t hprev = w > 0 ? H[w - 1] : 0;
+    uint64_t s0 = l0 + hprev;
+    uint64_t c = s0 < hprev;
+    uint64_t s1 = l1 + c;  c = c && s1 == 0;
+    uint64_t s2 = l2 + c;  c = c && s2 == 0;
+    uint64_t s3 = l3 + c;  c = c && s3 == 0;
+    g = c != 0;
+    p = (s0 & s1 & s2 & s3) == ~0ull;
     if (base + 0 < nlimbs) out[base + 0] = s0;
     if (base + 1 < nlimbs) out[base + 1] = s1;
     if (base + 2 < nlimbs) out[base + 2] = s2;
@@ -312,8 +385,7 @@ k_carry_local(const uint64_t* __restrict__ coef, uint64_t nwin, uint64_t* __rest
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    // chunk generate: carry out with cin = 0; propagate: carry out with cin = 1
-    uint32_t cg = 0, cp = 1;
+    uint32_t cg = 0, cp = 1;  // chunk carry out for carry in 0 / 1
     for (int k = 0; k < CARRY_THREADS / 32; k++) {
       uint64_t sg = (uint64_t)sA[k] + sB[k] + cg;
       uint64_t sp = (uint64_t)sA[k] + sB[k] + cp;
@@ -324,20 +396,20 @@ k_carry_local(const uint64_t* __restrict__ coef, uint64_t nwin, uint64_t* __rest
   }
 }
 
-// Pass 2: carry into every chunk.  One CTA; each thread walks a contiguous
-// segment of chunks, the segment results are chained by thread 0.
+// Carry pass 2: carry into every chunk.  One CTA; each thread walks a
+// contiguous segment of chunks, the segment results are chained by thread 0.
 constexpr int SCAN_THREADS = 1024;
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_carry_scan(const uint8_t* __restrict__ chunk_gp, uint64_t nchunk, uint8_t* __restrict__ chunk_cin) {
   __shared__ uint8_t seg_g[SCAN_THREADS], seg_p[SCAN_THREADS], seg_cin[SCAN_THREADS];
   const uint64_t per = (nchunk + SCAN_THREADS - 1) / SCAN_THREADS;
   const uint64_t lo = threadIdx.x * per, hi = lo + per < nchunk ? lo + per : nchunk;
-  uint8_t cg = 0, cp = 1;  // carry out for cin = 0 / cin = 1
+  uint8_t cg = 0, cp = 1;  // segment carry out for carry in 0 / 1
   for (uint64_t k = lo; k < hi; k++) {
     uint8_t gp = chunk_gp[k];
-    uint8_t g0 = gp & 1, g1 = (gp >> 1) & 1;
-    cg = cg ? g1 : g0;
-    cp = cp ? g1 : g0;
+    uint8_t o0 = gp & 1, o1 = (gp >> 1) & 1;
+    cg = cg ? o1 : o0;
+    cp = cp ? o1 : o0;
   }
   seg_g[threadIdx.x] = cg;
   seg_p[threadIdx.x] = cp;
@@ -358,7 +430,7 @@ k_carry_scan(const uint8_t* __restrict__ chunk_gp, uint64_t nchunk, uint8_t* __r
   }
 }
 
-// Pass 3: add the incoming carry to every window that receives one.
+// Carry pass 3: add the incoming carry to every window that receives one.
 __global__ void __launch_bounds__(CARRY_THREADS)
 k_carry_apply(uint64_t nwin, uint64_t* __restrict__ out, uint64_t nlimbs, const uint32_t* __restrict__ masks,
               const uint8_t* __restrict__ chunk_cin) {
@@ -409,17 +481,17 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
   }
   __syncthreads();
   TileGeom g{L, 0, 0};
-  RoundPlan rp = round_plan(L);
-  tile_dft_fwd(smA, g, rp, R, tid, SMALL_THREADS);
-  if (!square) tile_dft_fwd(smB, g, rp, R, tid, SMALL_THREADS);
-  // n^-1 = (p+1)/2 raised to L, i.e. 2^(-L) = 2^(192-L)
+  tile_dft_fwd(smA, g, R, tid, SMALL_THREADS);
+  if (!square) tile_dft_fwd(smB, g, R, tid, SMALL_THREADS);
+  // times N^-1 = 2^(-L) = 2^(192 - L)
+  const uint64_t ninv = gl::pow(2, 192 - L);
   for (uint32_t i = tid; i < N; i += SMALL_THREADS) {
     uint64_t x = smA[spad(i)];
     uint64_t y = square ? x : smB[spad(i)];
-    smA[spad(i)] = gl::shl(gl::mul(x, y), 192 - L);
+    smA[spad(i)] = gl::mul(gl::mul(x, y), ninv);
   }
   __syncthreads();
-  tile_dft_inv(smA, g, rp, R, tid, SMALL_THREADS);
+  tile_dft_inv(smA, g, R, tid, SMALL_THREADS);
   // carry: windows of 16 coefficients, one per thread (N/16 <= 256)
   const uint32_t nwin = (n_out + 15) / 16, nl = la + lb;
   uint64_t* sH = smB;  // reuse: B no longer needed
@@ -427,19 +499,13 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
   Win v{{0, 0, 0, 0}, 0};
   const uint32_t w = tid;
   if (w < nwin) {
-    unsigned __int128 acc = 0;
+    uint64_t c[16];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        uint32_t idx = 16 * w + 4 * k + q;
-        uint64_t cv = idx < N ? smA[spad(idx)] : 0;
-        acc += (unsigned __int128)cv << (16 * q);
-      }
-      v.l[k] = (uint64_t)acc;
-      acc >>= 64;
+    for (int t = 0; t < 16; t++) {
+      uint32_t idx = 16 * w + t;
+      c[t] = idx < N ? gl::canon(smA[spad(idx)]) : 0;
     }
-    v.hi = (uint64_t)acc;
+    v = fold16(c, 1);
   }
   __syncthreads();
   if (w < nwin) sH[w] = v.hi;  // nwin <= N/16 words fit in the B region
@@ -483,12 +549,42 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_mul(SmallJob job, Roots
 }
 
 // ------------------------------------------------------------------ host side
+static int log2_ceil(uint64_t x) {
+  int L = 0;
+  while ((1ull << L) < x) L++;
+  return L;
+}
+
+// Host copies of the root tables: lo, hi, w12, w20 (in this order).
+constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (1u << W20_LOG);
+
+static void build_roots(uint64_t* t) {
+  uint64_t rho = find_rho();
+  uint64_t* lo = t;
+  uint64_t* hi = lo + 65536;
+  uint64_t* w12 = hi + 65536;
+  uint64_t* w20 = w12 + 4096;
+  uint64_t x = 1;
+  for (int i = 0; i < 65536; i++) { lo[i] = x; x = hf::mul(x, rho); }
+  uint64_t step = x;  // rho^(2^16)
+  x = 1;
+  for (int i = 0; i < 65536; i++) { hi[i] = x; x = hf::mul(x, step); }
+  uint64_t w4096 = hf::pow(rho, 1ull << 20);
+  x = 1;
+  for (int i = 0; i < 4096; i++) { w12[i] = x; x = hf::mul(x, w4096); }
+  uint64_t wm = hf::pow(rho, 1ull << (32 - W20_LOG));
+  x = 1;
+  for (uint32_t i = 0; i < (1u << W20_LOG); i++) { w20[i] = x; x = hf::mul(x, wm); }
+}
+
+static Roots roots_at(const uint64_t* d) {
+  return Roots{d, d + 65536, d + 2 * 65536, d + 2 * 65536 + 4096};
+}
+
 struct DeviceState {
   int device = -1;
   bool ready = false;
-  uint64_t* d_lo = nullptr;
-  uint64_t* d_hi = nullptr;
-  uint64_t* d_w12 = nullptr;
+  uint64_t* d_roots = nullptr;
   Roots roots{};
   cudaMemPool_t pool = nullptr;
 };
@@ -497,6 +593,34 @@ static std::mutex g_mu;
 static DeviceState g_dev;
 static thread_local cudaStream_t t_stream = nullptr;
 static thread_local int t_stream_dev = -1;
+
+// Opt every pass kernel into its dynamic shared memory.
+template <int R>
+static cudaError_t set_smem_attrs_r() {
+  int bytes = (int)pass_smem_bytes(TILE_LOG);
+  cudaError_t e = cudaSuccess;
+  if (R >= 7) {
+    e = cudaFuncSetAttribute(k_fwd_first<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_inv_first_carry<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd_last<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
+static cudaError_t set_smem_attrs() {
+  cudaError_t e = set_smem_attrs_r<6>();
+  if (e == cudaSuccess) e = set_smem_attrs_r<7>();
+  if (e == cudaSuccess) e = set_smem_attrs_r<8>();
+  if (e == cudaSuccess) e = set_smem_attrs_r<9>();
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem_bytes(SMALL_LOG_MAX));
+  return e;
+}
 
 static int ensure_init(int device) {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -507,35 +631,15 @@ static int ensure_init(int device) {
   }
   if (device < 0) device = 0;
   CU(cudaSetDevice(device));
-  uint64_t rho = find_rho();
-  if (!rho) return fail(PIMUL_ECUDA, "root-of-unity search failed");
-  std::vector<uint64_t> lo(1 << 16), hi(1 << 16), w12(4096);
-  // powers by repeated multiplication; tables are exact field values
-  uint64_t x = 1;
-  for (int i = 0; i < (1 << 16); i++) { lo[i] = x; x = hf::mul(x, rho); }
-  uint64_t step = x;  // rho^(2^16)
-  x = 1;
-  for (int i = 0; i < (1 << 16); i++) { hi[i] = x; x = hf::mul(x, step); }
-  uint64_t w4096 = hf::pow(rho, 1ull << 20);
-  x = 1;
-  for (int i = 0; i < 4096; i++) { w12[i] = x; x = hf::mul(x, w4096); }
-  CU(cudaMalloc(&g_dev.d_lo, lo.size() * 8));
-  CU(cudaMalloc(&g_dev.d_hi, hi.size() * 8));
-  CU(cudaMalloc(&g_dev.d_w12, w12.size() * 8));
-  CU(cudaMemcpy(g_dev.d_lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(g_dev.d_hi, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(g_dev.d_w12, w12.data(), w12.size() * 8, cudaMemcpyHostToDevice));
-  g_dev.roots = Roots{g_dev.d_lo, g_dev.d_hi, g_dev.d_w12};
+  std::vector<uint64_t> tables(ROOT_WORDS);
+  build_roots(tables.data());
+  CU(cudaMalloc(&g_dev.d_roots, ROOT_WORDS * 8));
+  CU(cudaMemcpy(g_dev.d_roots, tables.data(), ROOT_WORDS * 8, cudaMemcpyHostToDevice));
+  g_dev.roots = roots_at(g_dev.d_roots);
   CU(cudaDeviceGetDefaultMemPool(&g_dev.pool, device));
   uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
   CU(cudaMemPoolSetAttribute(g_dev.pool, cudaMemPoolAttrReleaseThreshold, &thr));
-  int smem_max = 0;
-  CU(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-  size_t pass_smem = pass_smem_bytes(TILE_LOG_MAX);
-  size_t small_smem = small_smem_bytes(SMALL_LOG_MAX);
-  CU(cudaFuncSetAttribute(k_pass_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem));
-  CU(cudaFuncSetAttribute(k_pass_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem));
-  CU(cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+  CU(set_smem_attrs());
   g_dev.device = device;
   g_dev.ready = true;
   return PIMUL_OK;
@@ -554,13 +658,7 @@ static int get_stream(cudaStream_t* s) {
   return PIMUL_OK;
 }
 
-static int log2_ceil(uint64_t x) {
-  int L = 0;
-  while ((1ull << L) < x) L++;
-  return L;
-}
-
-// Split L bits into HBM passes of at most 9 bits.
+// Split L bits into HBM passes of at most 9 bits (each radix 2^6 .. 2^9).
 struct Plan {
   int L;
   int np;
@@ -570,129 +668,159 @@ struct Plan {
 static Plan make_plan(int L) {
   Plan p{L, 0, {0, 0, 0, 0, 0}};
   int np = (L + 8) / 9;
-  if (np < 1) np = 1;
+  if (np < 2) np = 2;
   int base = L / np, extra = L % np;
   for (int i = 0; i < np; i++) p.r[i] = base + (i < extra ? 1 : 0);
   p.np = np;
   return p;
 }
 
-static PassArgs pass_args(uint64_t* data, const Plan& pl, int p) {
-  PassArgs a;
-  a.data = data;
-  a.L = pl.L;
-  a.r = pl.r[p];
-  int consumed = 0;
-  for (int q = 0; q <= p; q++) consumed += pl.r[q];
-  a.s = pl.L - consumed;
-  a.t = a.s < 4 ? a.s : 4;
-  int bc = TILE_LOG_MAX - a.r - a.t;
-  int nblocks_log = pl.L - (a.r + a.s);
-  if (bc > nblocks_log) bc = nblocks_log;
-  if (bc < 0) bc = 0;
-  a.bc = bc;
-  a.rp = round_plan(a.r);
-  return a;
+// Scratch of one large product.
+struct Scratch {
+  uint64_t* A;     // N words
+  uint64_t* B;     // N words (unused for a square)
+  uint64_t* H;     // high parts of the carry windows, nwin words
+  uint8_t* aux;    // carry-scan flags
+};
+
+struct Sizes {
+  uint64_t n_out, N, nwin, nchunk, nwarp, aux_bytes;
+  int L;
+};
+
+static Sizes sizes_for(uint64_t la, uint64_t lb) {
+  Sizes z;
+  z.n_out = 4 * la + 4 * lb - 1;
+  z.L = log2_ceil(z.n_out);
+  z.N = 1ull << z.L;
+  z.nwin = (z.n_out + 15) / 16;
+  z.nchunk = (z.nwin + CARRY_THREADS - 1) / CARRY_THREADS;
+  z.nwarp = z.nchunk * (CARRY_THREADS / 32);
+  z.aux_bytes = z.nwarp * 8 + z.nchunk * 2 + 64;
+  return z;
 }
 
-static void launch_pass(const PassArgs& a, bool inverse, const Roots& R, cudaStream_t st) {
-  uint64_t tiles = 1ull << (a.L - (a.r + a.t + a.bc));
-  size_t smem = pass_smem_bytes(a.r + a.t + a.bc);
-  KTimer kt(inverse ? K_PASS_INV : K_PASS_FWD, st);
-  if (inverse) k_pass_inv<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
-  else k_pass_fwd<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
-}
 
-static void transform(uint64_t* data, const Plan& pl, bool inverse, const Roots& R, cudaStream_t st) {
-  if (!inverse) {
-    for (int p = 0; p < pl.np; p++) launch_pass(pass_args(data, pl, p), false, R, st);
-  } else {
-    for (int p = pl.np - 1; p >= 0; p--) launch_pass(pass_args(data, pl, p), true, R, st);
+// Launch helpers (template dispatch on the pass radix).
+#define PIMUL_DISPATCH_R(r, CALL)          \
+  switch (r) {                             \
+    case 6: { constexpr int RR = 6; CALL; } break; \
+    case 7: { constexpr int RR = 7; CALL; } break; \
+    case 8: { constexpr int RR = 8; CALL; } break; \
+    default: { constexpr int RR = 9; CALL; } break; \
+  }
+
+struct Launcher {
+  cudaStream_t st;
+  bool stats;  // count and (optionally) time launches
+  const Roots& R;
+};
+
+static void run_transform_fwd(const Launcher& X, const uint64_t* limbs, uint64_t nl, uint64_t* data,
+                              const Plan& pl, bool last) {
+  const int L = pl.L;
+  const unsigned grid = (unsigned)(1ull << (L - TILE_LOG));
+  const size_t smem = pass_smem_bytes(TILE_LOG);
+  {
+    KTimer kt(K_PACK, X.st, X.stats);
+    PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(limbs, nl, data, L, X.R)));
+  }
+  int consumed = pl.r[0];
+  for (int p = 1; p < pl.np - 1; p++) {
+    consumed += pl.r[p];
+    int S = L - consumed;
+    KTimer kt(K_PASS_FWD, X.st, X.stats);
+    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(data, S, X.R)));
+  }
+  if (last) {
+    KTimer kt(K_PASS_FWD, X.st, X.stats);
+    PIMUL_DISPATCH_R(pl.r[pl.np - 1], (k_fwd_last<RR><<<grid, PASS_THREADS, smem, X.st>>>(data, X.R)));
   }
 }
 
-static unsigned grid_for(uint64_t n, int threads) {
-  uint64_t b = (n + threads - 1) / threads;
-  uint64_t cap = 152ull * 16;
-  return (unsigned)(b < cap ? (b ? b : 1) : cap);
+// out[0 .. la+lb) = a * b for N >= 2^13 using the given scratch.
+static void run_multiply(const Launcher& X, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
+                         uint64_t* d_out, const Scratch& sc, const Sizes& z) {
+  const bool square = d_a == d_b && la == lb;
+  const Plan pl = make_plan(z.L);
+  const unsigned grid = (unsigned)(1ull << (z.L - TILE_LOG));
+  const size_t smem = pass_smem_bytes(TILE_LOG);
+  const uint64_t ninv = hf::pow(hf::pow(2, 191), z.L);  // 2^-L (2^192 = 1)
+  const int rl = pl.r[pl.np - 1];
+  uint64_t* C;
+  if (square) {
+    run_transform_fwd(X, d_a, la, sc.A, pl, false);
+    KTimer kt(K_POINTWISE, X.st, X.stats);
+    PIMUL_DISPATCH_R(rl, (k_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(sc.A, sc.A, ninv, X.R)));
+    C = sc.A;
+  } else {
+    run_transform_fwd(X, d_a, la, sc.A, pl, true);
+    run_transform_fwd(X, d_b, lb, sc.B, pl, false);
+    KTimer kt(K_POINTWISE, X.st, X.stats);
+    PIMUL_DISPATCH_R(rl, (k_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(sc.B, sc.A, ninv, X.R)));
+    C = sc.B;
+  }
+  int consumed = z.L - rl;
+  for (int p = pl.np - 2; p >= 1; p--) {
+    int S = z.L - consumed;
+    consumed -= pl.r[p];
+    KTimer kt(K_PASS_INV, X.st, X.stats);
+    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(C, S, X.R)));
+  }
+  const uint64_t nlimbs = la + lb;
+  {
+    KTimer kt(K_PASS_INV, X.st, X.stats);
+    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(
+                                  C, z.L, d_out, nlimbs, sc.H, z.nwin, X.R)));
+  }
+  uint32_t* masks = reinterpret_cast<uint32_t*>(sc.aux);
+  uint8_t* chunk_gp = sc.aux + z.nwarp * 8;
+  uint8_t* chunk_cin = chunk_gp + z.nchunk;
+  {
+    KTimer kt(K_CARRY, X.st, X.stats);
+    k_carry_local<<<(unsigned)z.nchunk, CARRY_THREADS, 0, X.st>>>(d_out, nlimbs, sc.H, z.nwin, masks, chunk_gp);
+    k_carry_scan<<<1, SCAN_THREADS, 0, X.st>>>(chunk_gp, z.nchunk, chunk_cin);
+    k_carry_apply<<<(unsigned)z.nchunk, CARRY_THREADS, 0, X.st>>>(z.nwin, d_out, nlimbs, masks, chunk_cin);
+  }
+  if (X.stats) g_launch[K_CARRY].fetch_add(2, std::memory_order_relaxed);
 }
 
-// Device multiply: d_out[0 .. la+lb) = a * b.
+// Device multiply: d_out[0 .. la+lb) = a * b, scratch from the memory pool.
 static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
                       cudaStream_t st) {
   if (la == 0 || lb == 0) return PIMUL_OK;
-  const uint64_t n_out = 4 * la + 4 * lb - 1;
-  const int L = log2_ceil(n_out);
-  if (L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
+  const Sizes z = sizes_for(la, lb);
+  if (z.L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
   const Roots& R = g_dev.roots;
   const bool square = d_a == d_b && la == lb;
-  if (L <= SMALL_LOG_MAX) {
+  if (z.L <= SMALL_LOG_MAX) {
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
-    size_t smem = small_smem_bytes(L);
     {
-      KTimer kt(K_SMALL, st);
-      k_small_mul<<<1, SMALL_THREADS, smem, st>>>(job, R);
+      KTimer kt(K_SMALL, st, true);
+      k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(job, R);
     }
     CU(cudaGetLastError());
     return PIMUL_OK;
   }
-  const uint64_t N = 1ull << L;
-  const Plan pl = make_plan(L);
-  const uint64_t nwin = (n_out + 15) / 16;
-  const uint64_t nchunk = (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
-  const uint64_t nwarp = nchunk * (CARRY_THREADS / 32);
-  uint64_t *A = nullptr, *B = nullptr;
-  uint8_t* aux = nullptr;
-  size_t aux_bytes = nwarp * 8 + nchunk * 2 + 64;
-  CU(cudaMallocAsync((void**)&A, N * 8, g_dev.pool, st));
-  if (!square) {
-    cudaError_t e = cudaMallocAsync((void**)&B, N * 8, g_dev.pool, st);
-    if (e != cudaSuccess) {
-      cudaFreeAsync(A, st);
-      return fail(PIMUL_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
-    }
+  Scratch sc{nullptr, nullptr, nullptr, nullptr};
+  cudaError_t e = cudaMallocAsync((void**)&sc.A, z.N * 8, g_dev.pool, st);
+  if (e == cudaSuccess && !square) e = cudaMallocAsync((void**)&sc.B, z.N * 8, g_dev.pool, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.H, z.nwin * 8, g_dev.pool, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.aux, z.aux_bytes, g_dev.pool, st);
+  if (e != cudaSuccess) {
+    if (sc.A) cudaFreeAsync(sc.A, st);
+    if (sc.B) cudaFreeAsync(sc.B, st);
+    if (sc.H) cudaFreeAsync(sc.H, st);
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
   }
-  {
-    cudaError_t e = cudaMallocAsync((void**)&aux, aux_bytes, g_dev.pool, st);
-    if (e != cudaSuccess) {
-      cudaFreeAsync(A, st);
-      if (B) cudaFreeAsync(B, st);
-      return fail(PIMUL_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
-    }
-  }
-  {
-    KTimer kt(K_PACK, st);
-    k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_a, la, A, N);
-  }
-  transform(A, pl, false, R, st);
-  if (!square) {
-    {
-      KTimer kt(K_PACK, st);
-      k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_b, lb, B, N);
-    }
-    transform(B, pl, false, R, st);
-  }
-  uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L = (2^191)^L since 2^192 = 1
-  {
-    KTimer kt(K_POINTWISE, st);
-    k_pointwise<<<grid_for(N, 256), 256, 0, st>>>(A, square ? A : B, N, ninv);
-  }
-  transform(A, pl, true, R, st);
-  uint32_t* masks = reinterpret_cast<uint32_t*>(aux);
-  uint8_t* chunk_gp = aux + nwarp * 8;
-  uint8_t* chunk_cin = chunk_gp + nchunk;
-  const uint64_t nlimbs = la + lb;
-  {
-    KTimer kt(K_CARRY, st);
-    k_carry_local<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(A, nwin, d_out, nlimbs, masks, chunk_gp);
-    k_carry_scan<<<1, SCAN_THREADS, 0, st>>>(chunk_gp, nchunk, chunk_cin);
-    k_carry_apply<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(nwin, d_out, nlimbs, masks, chunk_cin);
-  }
-  g_launch[K_CARRY].fetch_add(2, std::memory_order_relaxed);
+  Launcher X{st, true, R};
+  run_multiply(X, d_a, la, d_b, lb, d_out, sc, z);
   cudaError_t le = cudaGetLastError();
-  cudaFreeAsync(A, st);
-  if (B) cudaFreeAsync(B, st);
-  cudaFreeAsync(aux, st);
+  cudaFreeAsync(sc.A, st);
+  if (sc.B) cudaFreeAsync(sc.B, st);
+  cudaFreeAsync(sc.H, st);
+  cudaFreeAsync(sc.aux, st);
   if (le != cudaSuccess) return fail(PIMUL_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
   return PIMUL_OK;
 }
@@ -704,7 +832,7 @@ using namespace pimul;
 
 extern "C" {
 
-const char* pimul_version(void) { return "pimul 0.1 (sm_103a)"; }
+const char* pimul_version(void) { return "pimul 0.2 (sm_103a)"; }
 
 const char* pimul_last_error(void) { return t_err.c_str(); }
 
@@ -715,9 +843,7 @@ int pimul_shutdown(void) {
   if (!g_dev.ready) return PIMUL_OK;
   cudaSetDevice(g_dev.device);
   cudaDeviceSynchronize();
-  cudaFree(g_dev.d_lo);
-  cudaFree(g_dev.d_hi);
-  cudaFree(g_dev.d_w12);
+  cudaFree(g_dev.d_roots);
   if (g_dev.pool) cudaMemPoolTrimTo(g_dev.pool, 0);
   g_dev = DeviceState{};
   return PIMUL_OK;
@@ -792,18 +918,14 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
   if (rc) return rc;
   const bool square = a == b && la == lb;
   uint64_t *da = nullptr, *db = nullptr, *dout = nullptr;
-  CU(cudaMallocAsync((void**)&da, la * 8, g_dev.pool, st));
-  if (!square) {
-    cudaError_t e = cudaMallocAsync((void**)&db, lb * 8, g_dev.pool, st);
-    if (e != cudaSuccess) { cudaFreeAsync(da, st); return fail(PIMUL_ENOMEM, "input allocation failed"); }
-  }
-  {
-    cudaError_t e = cudaMallocAsync((void**)&dout, (la + lb) * 8, g_dev.pool, st);
-    if (e != cudaSuccess) {
-      cudaFreeAsync(da, st);
-      if (db) cudaFreeAsync(db, st);
-      return fail(PIMUL_ENOMEM, "output allocation failed");
-    }
+  cudaError_t e = cudaMallocAsync((void**)&da, la * 8, g_dev.pool, st);
+  if (e == cudaSuccess && !square) e = cudaMallocAsync((void**)&db, lb * 8, g_dev.pool, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dout, (la + lb) * 8, g_dev.pool, st);
+  if (e != cudaSuccess) {
+    if (da) cudaFreeAsync(da, st);
+    if (db) cudaFreeAsync(db, st);
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("operand allocation: ") + cudaGetErrorString(e));
   }
   cudaMemcpyAsync(da, a, la * 8, cudaMemcpyHostToDevice, st);
   if (!square) cudaMemcpyAsync(db, b, lb * 8, cudaMemcpyHostToDevice, st);
@@ -836,10 +958,10 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //
 // Limits and sharing rules:
 //  * scratch holds two transform arrays of at most 2^20 words plus the carry
-//    scan's flags: la + lb <= 262144 limbs (transform length N <= 2^20);
-//    larger products are rejected with PIMUL_EINVAL.  The array (16 MiB
-//    plus 1 MiB of root tables) stays resident on every GPU that loads this
-//    library, until the process exits.
+//    windows and scan flags: la + lb <= 262144 limbs (transform length
+//    N <= 2^20); larger products are rejected with PIMUL_EINVAL.  The
+//    scratch (16.5 MiB) and this path's own root tables (9 MiB) stay resident
+//    on every GPU that loads this library, until the process exits.
 //  * every call uses the same array, and the array keeps the previous call's
 //    contents; the kernels overwrite every scratch word before reading it,
 //    so nothing needs clearing.  Calls whose work overlaps on the GPU
@@ -849,15 +971,15 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //    current: it resolves the arrays' device addresses with
 //    cudaGetSymbolAddress and copies the root tables in with a synchronous
 //    cudaMemcpyToSymbol.  Make that first call before any stream capture.
+namespace pimul {
 constexpr int NOALLOC_LOG_MAX = 20;
 constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;
 constexpr uint64_t NOALLOC_WIN_MAX = NOALLOC_N_MAX / 16;
 constexpr uint64_t NOALLOC_CHUNK_MAX = (NOALLOC_WIN_MAX + CARRY_THREADS - 1) / CARRY_THREADS;
 constexpr uint64_t NOALLOC_AUX_WORDS = (NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64) / 8 + 1;
-constexpr size_t NOALLOC_ROOT_WORDS = 2 * 65536 + 4096;
 
-static __device__ __align__(256) uint64_t g_noalloc_scratch[2 * NOALLOC_N_MAX + NOALLOC_AUX_WORDS];
-static __device__ __align__(256) uint64_t g_noalloc_roots[NOALLOC_ROOT_WORDS];
+static __device__ __align__(256) uint64_t g_noalloc_scratch[2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX + NOALLOC_AUX_WORDS];
+static __device__ __align__(256) uint64_t g_noalloc_roots[ROOT_WORDS];
 
 struct NoAllocDev {
   bool ready = false;
@@ -866,7 +988,7 @@ struct NoAllocDev {
 };
 static std::mutex g_na_mu;
 static NoAllocDev g_na[64];
-static uint64_t g_na_host_roots[NOALLOC_ROOT_WORDS];  // staging, no heap use
+static uint64_t g_na_host_roots[ROOT_WORDS];  // staging, no heap use
 
 static int noalloc_setup(NoAllocDev** out) {
   int dev = 0;
@@ -875,19 +997,7 @@ static int noalloc_setup(NoAllocDev** out) {
   std::lock_guard<std::mutex> lk(g_na_mu);
   NoAllocDev& d = g_na[dev];
   if (!d.ready) {
-    uint64_t rho = find_rho();
-    if (!rho) return fail(PIMUL_ECUDA, "root-of-unity search failed");
-    uint64_t* lo = g_na_host_roots;
-    uint64_t* hi = lo + 65536;
-    uint64_t* w12 = hi + 65536;
-    uint64_t x = 1;
-    for (int i = 0; i < 65536; i++) { lo[i] = x; x = hf::mul(x, rho); }
-    uint64_t step = x;
-    x = 1;
-    for (int i = 0; i < 65536; i++) { hi[i] = x; x = hf::mul(x, step); }
-    uint64_t w4096 = hf::pow(rho, 1ull << 20);
-    x = 1;
-    for (int i = 0; i < 4096; i++) { w12[i] = x; x = hf::mul(x, w4096); }
+    build_roots(g_na_host_roots);
     uint64_t* scratch = nullptr;
     uint64_t* roots = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch);
@@ -895,24 +1005,13 @@ static int noalloc_setup(NoAllocDev** out) {
     e = cudaGetSymbolAddress((void**)&roots, g_noalloc_roots);
     if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("cudaGetSymbolAddress(roots): ") + cudaGetErrorString(e));
     CU(cudaMemcpyToSymbol(g_noalloc_roots, g_na_host_roots, sizeof(g_na_host_roots)));
-    CU(cudaFuncSetAttribute(k_pass_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem_bytes(TILE_LOG_MAX)));
-    CU(cudaFuncSetAttribute(k_pass_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem_bytes(TILE_LOG_MAX)));
-    CU(cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem_bytes(SMALL_LOG_MAX)));
+    CU(set_smem_attrs());
     d.scratch = scratch;
-    d.roots = Roots{roots, roots + 65536, roots + 2 * 65536};
+    d.roots = roots_at(roots);
     d.ready = true;
   }
   *out = &d;
   return PIMUL_OK;
-}
-
-// A pass launch without the statistics hook (whose event timing would
-// create CUDA events).
-static void noalloc_pass(const PassArgs& a, bool inverse, const Roots& R, cudaStream_t st) {
-  uint64_t tiles = 1ull << (a.L - (a.r + a.t + a.bc));
-  size_t smem = pass_smem_bytes(a.r + a.t + a.bc);
-  if (inverse) k_pass_inv<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
-  else k_pass_fwd<<<(unsigned)tiles, PASS_THREADS, smem, st>>>(a, R);
 }
 
 static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
@@ -920,43 +1019,25 @@ static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* 
   NoAllocDev* nd = nullptr;
   int rc = noalloc_setup(&nd);
   if (rc) return rc;
-  const uint64_t n_out = 4 * la + 4 * lb - 1;
-  const int L = log2_ceil(n_out);
+  const Sizes z = sizes_for(la, lb);
   const Roots& R = nd->roots;
-  const bool square = d_a == d_b && la == lb;
-  if (L <= SMALL_LOG_MAX) {  // whole product in one CTA's shared memory: no scratch
+  if (z.L <= SMALL_LOG_MAX) {  // whole product in one CTA's shared memory: no scratch
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
-    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(L), st>>>(job, R);
+    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(job, R);
     CU(cudaGetLastError());
     return PIMUL_OK;
   }
-  const uint64_t N = 1ull << L;
-  const Plan pl = make_plan(L);
-  const uint64_t nwin = (n_out + 15) / 16;
-  const uint64_t nchunk = (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
-  const uint64_t nwarp = nchunk * (CARRY_THREADS / 32);
-  uint64_t* A = nd->scratch;
-  uint64_t* B = nd->scratch + NOALLOC_N_MAX;
-  uint8_t* aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX);
-  k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_a, la, A, N);
-  for (int p = 0; p < pl.np; p++) noalloc_pass(pass_args(A, pl, p), false, R, st);
-  if (!square) {
-    k_pack<<<grid_for(N / 4, 256), 256, 0, st>>>(d_b, lb, B, N);
-    for (int p = 0; p < pl.np; p++) noalloc_pass(pass_args(B, pl, p), false, R, st);
-  }
-  uint64_t ninv = hf::pow(hf::pow(2, 191), L);
-  k_pointwise<<<grid_for(N, 256), 256, 0, st>>>(A, square ? A : B, N, ninv);
-  for (int p = pl.np - 1; p >= 0; p--) noalloc_pass(pass_args(A, pl, p), true, R, st);
-  uint32_t* masks = reinterpret_cast<uint32_t*>(aux);
-  uint8_t* chunk_gp = aux + nwarp * 8;
-  uint8_t* chunk_cin = chunk_gp + nchunk;
-  const uint64_t nlimbs = la + lb;
-  k_carry_local<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(A, nwin, d_out, nlimbs, masks, chunk_gp);
-  k_carry_scan<<<1, SCAN_THREADS, 0, st>>>(chunk_gp, nchunk, chunk_cin);
-  k_carry_apply<<<(unsigned)nchunk, CARRY_THREADS, 0, st>>>(nwin, d_out, nlimbs, masks, chunk_cin);
+  Scratch sc;
+  sc.A = nd->scratch;
+  sc.B = nd->scratch + NOALLOC_N_MAX;
+  sc.H = nd->scratch + 2 * NOALLOC_N_MAX;
+  sc.aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX);
+  Launcher X{st, false, R};  // no statistics hook: its event timing would create CUDA events
+  run_multiply(X, d_a, la, d_b, lb, d_out, sc, z);
   CU(cudaGetLastError());
   return PIMUL_OK;
 }
+}  // namespace pimul
 
 extern "C" int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
                                         uint64_t* d_out, void* stream) {

@@ -1,36 +1,39 @@
 // Goldilocks NTT building blocks shared by the multiply kernels.
 //
-// Transform structure (design of this engine, not of the reference): a
+// Transform structure (this engine's design, not the reference's): a
 // length-N = 2^L transform is split into HBM passes of radix R_p = 2^r_p.
 // Pass p works on blocks of M_p = R_p * S_p consecutive words and, inside a
 // block, on R_p rows of stride S_p.  The forward direction is a
 // decimation-in-frequency split: per column j it takes the R_p-point DFT
 // over the rows, multiplies output row f by w_M^(f*j) and stores it back in
-// place, so that every output row is an independent length-S_p problem for
-// the next pass.  The spectrum ends in a fixed digit-reversed order; the
+// place, so every output row is an independent length-S_p problem for the
+// next pass.  The spectrum ends in a fixed digit-reversed order; the
 // pointwise product does not care, and the inverse passes (the exact mirror)
-// restore natural order.  This is the same decomposition as the reference's
-// four-step transform (crates/bignum/src/ntt.rs:905-1105) without the
-// transposes: strided tiles are read with coalesced 128-byte row segments.
+// restore natural order.  This is the reference's four-step decomposition
+// (crates/bignum/src/ntt.rs:905-1105) without the transposes: strided tiles
+// are read as coalesced 128-byte row segments.
 //
-// Inside a pass the R_p-point DFT runs in shared memory as rounds of
-// radix 2, 4 or 8 held in registers; the radix-8 butterflies use the
-// 8th roots of unity 2^24 and 2^48 (2 is a 192nd root of unity mod p), so
-// their internal twiddles are shifts rather than general multiplies.
+// Inside a pass the R_p-point DFT runs in shared memory as rounds of radix
+// 8 (or 4 / 2) held in registers.  2 is a 192nd root of unity mod p, and the
+// root tables are built so that the 8th root of unity is 2^24: the
+// butterflies' internal twiddles are constant shifts.
 #pragma once
 #include <cstdint>
 #include "gl.cuh"
 
 namespace pimul {
 
-// Root tables: rho is a primitive 2^32-th root of unity chosen so that
-// rho^(2^26) = 8, i.e. the 64th root of unity is 2^3.  Every twiddle of every
+// Root tables.  rho is a primitive 2^32-th root of unity with
+// rho^(2^26) = 8 (the 64th root of unity is 2^3).  Every twiddle of every
 // transform length is a power of rho.
 struct Roots {
   const uint64_t* lo;   // rho^e, e in [0, 2^16)
   const uint64_t* hi;   // rho^(e * 2^16), e in [0, 2^16)
   const uint64_t* w12;  // w_4096^t = rho^(t * 2^20), t in [0, 4096)
+  const uint64_t* w20;  // w_(2^20)^t = rho^(t * 2^12), t in [0, 2^20)
 };
+
+constexpr int W20_LOG = 20;
 
 // rho^e for e in [0, 2^32).
 __device__ __forceinline__ uint64_t rho_pow(const Roots& R, uint32_t e) {
@@ -39,7 +42,16 @@ __device__ __forceinline__ uint64_t rho_pow(const Roots& R, uint32_t e) {
   return h ? gl::mul(a, __ldg(R.hi + h)) : a;
 }
 
-// w_(2^mlog)^x for x < 2^mlog <= 4096 (forward), or its inverse.
+// w_M^x for M = 2^mlog, x in [0, M); inverse gives w_M^(-x).
+__device__ __forceinline__ uint64_t root_pow(const Roots& R, int mlog, uint64_t x, bool inverse) {
+  uint64_t m = 1ull << mlog;
+  x &= m - 1;
+  if (inverse) x = (m - x) & (m - 1);
+  if (mlog <= W20_LOG) return __ldg(R.w20 + (x << (W20_LOG - mlog)));
+  return rho_pow(R, (uint32_t)(x << (32 - mlog)));
+}
+
+// w_(2^mlog)^x for x < 2^mlog <= 4096 from the 4096-entry table (forward or inverse).
 __device__ __forceinline__ uint64_t round_tw(const Roots& R, int mlog, uint32_t x, bool inverse) {
   uint32_t t = x << (12 - mlog);
   if (inverse) t = (4096u - t) & 4095u;
@@ -59,22 +71,47 @@ __device__ __forceinline__ void reg_bitrev(uint64_t* v) {
   }
 }
 
+// DIF radix-2 butterfly with a constant shift twiddle 2^S (S = 0: none).
+template <int S>
+__device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
+  uint64_t u = a, w = b;
+  a = gl::add(u, w);
+  b = gl::shl<S>(gl::sub(u, w));
+}
+
+// DIT radix-2 butterfly with the inverse shift twiddle 2^(-S) = 2^(192-S).
+template <int S>
+__device__ __forceinline__ void bfly_dit(uint64_t& a, uint64_t& b) {
+  uint64_t u = a, w = (S == 0) ? b : gl::shl<(192 - S) % 192>(b);
+  a = gl::add(u, w);
+  b = gl::sub(u, w);
+}
+
 // Forward DFT of 2^B values in registers: v[k] <- sum_m v[m] w^(m k), with
-// w = 2^(192 / 2^B).  Output in natural order.
+// w = 2^(192 / 2^B) (the 8th root of unity is 2^24).  Natural-order output.
 template <int B>
 __device__ __forceinline__ void dft_fwd(uint64_t* v) {
-#pragma unroll
-  for (int h = (1 << B) / 2; h >= 1; h >>= 1) {
-#pragma unroll
-    for (int g = 0; g < (1 << B); g += 2 * h) {
-#pragma unroll
-      for (int m = 0; m < h; m++) {
-        uint64_t u = v[g + m], w = v[g + m + h];
-        v[g + m] = gl::add(u, w);
-        uint64_t d = gl::sub(u, w);
-        v[g + m + h] = (m == 0) ? d : gl::shl(d, (96 / h) * m);
-      }
-    }
+  if constexpr (B == 1) {
+    bfly_dif<0>(v[0], v[1]);
+  } else if constexpr (B == 2) {
+    bfly_dif<0>(v[0], v[2]);
+    bfly_dif<48>(v[1], v[3]);
+    bfly_dif<0>(v[0], v[1]);
+    bfly_dif<0>(v[2], v[3]);
+  } else {
+    static_assert(B == 3, "radix 2, 4 or 8");
+    bfly_dif<0>(v[0], v[4]);
+    bfly_dif<24>(v[1], v[5]);
+    bfly_dif<48>(v[2], v[6]);
+    bfly_dif<72>(v[3], v[7]);
+    bfly_dif<0>(v[0], v[2]);
+    bfly_dif<48>(v[1], v[3]);
+    bfly_dif<0>(v[4], v[6]);
+    bfly_dif<48>(v[5], v[7]);
+    bfly_dif<0>(v[0], v[1]);
+    bfly_dif<0>(v[2], v[3]);
+    bfly_dif<0>(v[4], v[5]);
+    bfly_dif<0>(v[6], v[7]);
   }
   reg_bitrev<B>(v);
 }
@@ -83,32 +120,159 @@ __device__ __forceinline__ void dft_fwd(uint64_t* v) {
 template <int B>
 __device__ __forceinline__ void dft_inv(uint64_t* v) {
   reg_bitrev<B>(v);
-#pragma unroll
-  for (int h = 1; h < (1 << B); h <<= 1) {
-#pragma unroll
-    for (int g = 0; g < (1 << B); g += 2 * h) {
-#pragma unroll
-      for (int m = 0; m < h; m++) {
-        uint64_t u = v[g + m];
-        uint64_t w = (m == 0) ? v[g + m + h] : gl::shl(v[g + m + h], 192 - (96 / h) * m);
-        v[g + m] = gl::add(u, w);
-        v[g + m + h] = gl::sub(u, w);
-      }
-    }
+  if constexpr (B == 1) {
+    bfly_dit<0>(v[0], v[1]);
+  } else if constexpr (B == 2) {
+    bfly_dit<0>(v[0], v[1]);
+    bfly_dit<0>(v[2], v[3]);
+    bfly_dit<0>(v[0], v[2]);
+    bfly_dit<48>(v[1], v[3]);
+  } else {
+    static_assert(B == 3, "radix 2, 4 or 8");
+    bfly_dit<0>(v[0], v[1]);
+    bfly_dit<0>(v[2], v[3]);
+    bfly_dit<0>(v[4], v[5]);
+    bfly_dit<0>(v[6], v[7]);
+    bfly_dit<0>(v[0], v[2]);
+    bfly_dit<48>(v[1], v[3]);
+    bfly_dit<0>(v[4], v[6]);
+    bfly_dit<48>(v[5], v[7]);
+    bfly_dit<0>(v[0], v[4]);
+    bfly_dit<24>(v[1], v[5]);
+    bfly_dit<48>(v[2], v[6]);
+    bfly_dit<72>(v[3], v[7]);
   }
 }
 
-// Tile geometry in shared memory: (2^bc blocks) x (2^r rows) x (2^t columns),
-// element (blk,row,col) at spad(((blk << r) + row) << t | col).  A round
-// treats the 2^(bc+r) tile rows as consecutive sub-problems of 2^mlog rows.
+// ---------------------------------------------------------------- rounds
+// Round split of an r-bit in-tile DFT: radix-8 rounds first, then radix 4
+// or 2 (two radix-4 rounds instead of 8 + 2).
+__host__ __device__ constexpr int rp_count(int r) {
+  int n = 0;
+  while (r > 0) {
+    int b = r >= 3 ? 3 : r;
+    if (r == 4) b = 2;
+    r -= b;
+    n++;
+  }
+  return n;
+}
+
+__host__ __device__ constexpr int rp_bits(int r, int q) {
+  int i = 0;
+  while (r > 0) {
+    int b = r >= 3 ? 3 : r;
+    if (r == 4) b = 2;
+    if (i == q) return b;
+    r -= b;
+    i++;
+  }
+  return 0;
+}
+
+// Sub-problem size (log2) at the start of round q.
+__host__ __device__ constexpr int rp_mlog(int r, int q) {
+  int m = r;
+  for (int i = 0; i < q; i++) m -= rp_bits(r, i);
+  return m;
+}
+
+// Tile of 2^BC blocks x 2^R rows x 2^T columns in shared memory; element
+// (row, col) of the flattened (BC+R)-bit row index at spad(row << T | col).
+// One forward round of radix 2^B over sub-problems of 2^MLOG rows.
+template <int R, int T, int BC, int B, int MLOG, int NT>
+__device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+  constexpr int SLOG = MLOG - B;
+  constexpr int ITEMS = 1 << (BC + R + T - B);
+  static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
+#pragma unroll 2
+  for (int it = 0; it < ITEMS / NT; it++) {
+    const uint32_t w = it * NT + tid;
+    const uint32_t j = w & ((1u << T) - 1);
+    const uint32_t rest = w >> T;
+    const uint32_t jp = rest & ((1u << SLOG) - 1);
+    const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
+    uint64_t v[1 << B];
+#pragma unroll
+    for (int m = 0; m < (1 << B); m++) v[m] = sm[spad(((row0 + (m << SLOG)) << T) | j)];
+    dft_fwd<B>(v);
+    if constexpr (SLOG > 0) {
+#pragma unroll
+      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[(k * jp) << (9 - MLOG)]);
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << B); k++) sm[spad(((row0 + (k << SLOG)) << T) | j)] = v[k];
+  }
+}
+
+template <int R, int T, int BC, int B, int MLOG, int NT>
+__device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+  constexpr int SLOG = MLOG - B;
+  constexpr int ITEMS = 1 << (BC + R + T - B);
+  static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
+#pragma unroll 2
+  for (int it = 0; it < ITEMS / NT; it++) {
+    const uint32_t w = it * NT + tid;
+    const uint32_t j = w & ((1u << T) - 1);
+    const uint32_t rest = w >> T;
+    const uint32_t jp = rest & ((1u << SLOG) - 1);
+    const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
+    uint64_t v[1 << B];
+#pragma unroll
+    for (int k = 0; k < (1 << B); k++) v[k] = sm[spad(((row0 + (k << SLOG)) << T) | j)];
+    if constexpr (SLOG > 0) {
+#pragma unroll
+      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
+    }
+    dft_inv<B>(v);
+#pragma unroll
+    for (int m = 0; m < (1 << B); m++) sm[spad(((row0 + (m << SLOG)) << T) | j)] = v[m];
+  }
+}
+
+template <int R, int T, int BC, int NT, int Q = 0>
+__device__ __forceinline__ void tile_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+  if constexpr (Q < rp_count(R)) {
+    round_fwd_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid);
+    __syncthreads();
+    tile_fwd_t<R, T, BC, NT, Q + 1>(sm, tw512, tid);
+  }
+}
+
+template <int R, int T, int BC, int NT, int Q = rp_count(R) - 1>
+__device__ __forceinline__ void tile_inv_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+  if constexpr (Q >= 0) {
+    round_inv_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid);
+    __syncthreads();
+    tile_inv_t<R, T, BC, NT, Q - 1>(sm, tw512, tid);
+  }
+}
+
+// Frequency index held at tile row `row` after the rounds of an R-bit DFT
+// (mixed-radix digit reversal of the row index).
+template <int R>
+__device__ __forceinline__ uint32_t row_freq_t(uint32_t row) {
+  uint32_t f = 0;
+  int rem = R, sh = 0;
+#pragma unroll
+  for (int q = 0; q < rp_count(R); q++) {
+    int b = rp_bits(R, q);
+    rem -= b;
+    f |= ((row >> rem) & ((1u << b) - 1)) << sh;
+    sh += b;
+  }
+  return f;
+}
+
+// ------------------------------------------------- runtime-geometry rounds
+// Used by the one-CTA multiply, whose transform length varies per call.
 struct TileGeom {
   int r, t, bc;
 };
 
-// One forward round of radix 2^B on sub-problems of size 2^mlog.
 template <int B>
-__device__ __forceinline__ void round_fwd(uint64_t* sm, TileGeom g, int mlog, const Roots& R,
-                                          int tid, int nthreads) {
+__device__ __forceinline__ void round_fwd(uint64_t* sm, TileGeom g, int mlog, const Roots& R, int tid,
+                                          int nthreads) {
   const int slog = mlog - B;
   const int items_log = g.bc + g.r + g.t - B;
   const uint32_t tmask = (1u << g.t) - 1, smask = (1u << slog) - 1;
@@ -130,10 +294,9 @@ __device__ __forceinline__ void round_fwd(uint64_t* sm, TileGeom g, int mlog, co
   }
 }
 
-// Mirror of round_fwd (unscaled).
 template <int B>
-__device__ __forceinline__ void round_inv(uint64_t* sm, TileGeom g, int mlog, const Roots& R,
-                                          int tid, int nthreads) {
+__device__ __forceinline__ void round_inv(uint64_t* sm, TileGeom g, int mlog, const Roots& R, int tid,
+                                          int nthreads) {
   const int slog = mlog - B;
   const int items_log = g.bc + g.r + g.t - B;
   const uint32_t tmask = (1u << g.t) - 1, smask = (1u << slog) - 1;
@@ -155,64 +318,37 @@ __device__ __forceinline__ void round_inv(uint64_t* sm, TileGeom g, int mlog, co
   }
 }
 
-// Round split of an r-bit pass: radix-8 rounds first, then one radix-4 or
-// radix-2 round (or two radix-4 rounds instead of 8 + 2).
-struct RoundPlan {
-  int n;
-  int bits[6];
-};
-
-__host__ __device__ inline RoundPlan round_plan(int r) {
-  RoundPlan p{0, {0, 0, 0, 0, 0, 0}};
-  int rem = r;
+__device__ __forceinline__ void tile_dft_fwd(uint64_t* sm, TileGeom g, const Roots& R, int tid, int nthreads) {
+  int mlog = g.r, rem = g.r;
   while (rem > 0) {
     int b = rem >= 3 ? 3 : rem;
     if (rem == 4) b = 2;
-    p.bits[p.n++] = b;
-    rem -= b;
-  }
-  return p;
-}
-
-// All rounds of an r-bit in-tile DFT (forward).
-__device__ __forceinline__ void tile_dft_fwd(uint64_t* sm, TileGeom g, const RoundPlan& rp,
-                                             const Roots& R, int tid, int nthreads) {
-  int mlog = g.r;
-  for (int q = 0; q < rp.n; q++) {
-    int b = rp.bits[q];
     if (b == 3) round_fwd<3>(sm, g, mlog, R, tid, nthreads);
     else if (b == 2) round_fwd<2>(sm, g, mlog, R, tid, nthreads);
     else round_fwd<1>(sm, g, mlog, R, tid, nthreads);
     mlog -= b;
+    rem -= b;
     __syncthreads();
   }
 }
 
-__device__ __forceinline__ void tile_dft_inv(uint64_t* sm, TileGeom g, const RoundPlan& rp,
-                                             const Roots& R, int tid, int nthreads) {
+__device__ __forceinline__ void tile_dft_inv(uint64_t* sm, TileGeom g, const Roots& R, int tid, int nthreads) {
+  int bits[8], n = 0, rem = g.r;
+  while (rem > 0) {
+    int b = rem >= 3 ? 3 : rem;
+    if (rem == 4) b = 2;
+    bits[n++] = b;
+    rem -= b;
+  }
   int mlog = 0;
-  for (int q = rp.n - 1; q >= 0; q--) {
-    int b = rp.bits[q];
+  for (int q = n - 1; q >= 0; q--) {
+    int b = bits[q];
     mlog += b;
     if (b == 3) round_inv<3>(sm, g, mlog, R, tid, nthreads);
     else if (b == 2) round_inv<2>(sm, g, mlog, R, tid, nthreads);
     else round_inv<1>(sm, g, mlog, R, tid, nthreads);
     __syncthreads();
   }
-}
-
-// Frequency index held at tile row `row` after the rounds of `rp`
-// (mixed-radix digit reversal of the row index).
-__device__ __forceinline__ uint32_t row_freq(uint32_t row, int r, const RoundPlan& rp) {
-  uint32_t f = 0;
-  int rem = r, sh = 0;
-  for (int q = 0; q < rp.n; q++) {
-    int b = rp.bits[q];
-    rem -= b;
-    f |= ((row >> rem) & ((1u << b) - 1)) << sh;
-    sh += b;
-  }
-  return f;
 }
 
 }  // namespace pimul
