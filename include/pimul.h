@@ -75,8 +75,8 @@ int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t
  * when they multiply (a GPU whose memory belongs to another allocator, a
  * loop where cudaMalloc's implicit synchronisation is not allowed, a runtime
  * that allocates only at start-up).  It uses no memory pool: its scratch is
- * a fixed device array inside this library (16 MiB, resident on every GPU
- * that loads the library until exit), so products are limited to
+ * a fixed device array inside this library (16.5 MiB of scratch plus 17 MiB
+ * of root tables, resident on every GPU that loads the library until exit), so products are limited to
  * la + lb <= 262144 limbs (transform length <= 2^20); larger ones return
  * PIMUL_EINVAL.  All calls share that array: calls that overlap on the GPU
  * race and must be serialised by the caller.  The first call on a device
@@ -103,6 +103,22 @@ int pimul_stats_enable(int on);
 int pimul_stats_reset(void);
 int pimul_stats_get(int kclass, const char** name, uint64_t* launches, uint64_t* timed_launches,
                     double* total_ms);
+
+/*
+ * Batched BBP hex digits of pi: digits[i] = the 8 hex digits starting at
+ * fractional position positions[i], packed with the first digit in the top
+ * nibble (positions[0] == 0 gives 0x243F6A88).  Bit-identical to the
+ * reference's extractor; positions must be <= 2^31.  When `stop` is not
+ * NULL the call polls *stop and, once it reads non-zero, stops the kernels
+ * early and returns PIMUL_ECANCELED (digits untouched).
+ *
+ * Replaces: crates/pi-core/src/bbp.rs:52 `hex_digits_at(n: u64) -> u32` and
+ * bbp.rs:63 `hex_digits_at_interruptible(n, stop: &AtomicBool) -> Option<u32>`,
+ * one call per position in crates/pi-cli/src/verify_hex.rs:811-861.
+ */
+int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uint32_t* digits,
+                         const volatile int* stop);
+const char* pimul_bbp_last_error(void);
 
 /* Synchronise the calling thread's own stream. */
 int pimul_sync(void);

@@ -24,7 +24,7 @@ from . import build as _build
 
 __all__ = [
     "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device",
-    "plan", "sync", "LIB_PATH",
+    "plan", "sync", "bbp_hex_digits", "LIB_PATH",
 ]
 
 LIB_PATH = _build.LIB
@@ -62,6 +62,8 @@ def load(build_if_stale: bool = True):
     L.pimul_mul_device.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]
     L.pimul_plan.argtypes = [_sz, _sz, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]
     L.pimul_sync.argtypes = []
+    L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
+    L.pimul_bbp_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -118,6 +120,24 @@ def mul_device(d_a, d_b, d_out, stream=None):
         stream = torch.cuda.current_stream(d_out.device).cuda_stream
     _check(lib().pimul_mul_device(d_a.data_ptr(), la, d_b.data_ptr(), lb, d_out.data_ptr(),
                                   ctypes.c_void_p(stream)))
+
+
+def bbp_hex_digits(positions, stop=None) -> np.ndarray:
+    """8 hex digits of pi at each position (crates/pi-core/src/bbp.rs:52).
+
+    `stop` may be a ctypes.c_int; setting it non-zero from another thread
+    cancels the call (PimulError with code ECANCELED), like the reference's
+    hex_digits_at_interruptible (bbp.rs:63)."""
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=np.uint64))
+    out = np.zeros(pos.size, dtype=np.uint32)
+    if pos.size == 0:
+        return out
+    rc = lib().pimul_bbp_hex_digits(pos.ctypes.data_as(_u64p), pos.size,
+                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                    ctypes.byref(stop) if stop is not None else None)
+    if rc:
+        raise PimulError(rc, lib().pimul_bbp_last_error().decode())
+    return out
 
 
 def plan(la: int, lb: int):

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimul.so")
 
-SOURCES = ["engine.cu"]
+SOURCES = ["engine.cu", "bbp.cu"]
 HEADERS = ["gl.cuh", "ntt_kernels.cuh"]
 
 NVCC_FLAGS = [

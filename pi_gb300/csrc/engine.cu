@@ -158,8 +158,12 @@ static inline size_t pass_smem_bytes(int tile_log) { return ((size_t)1 << tile_l
 
 // Load the 512 forward roots w_512^t into shared memory (round twiddles).
 __device__ __forceinline__ void load_tw512(uint64_t* tw, const Roots& R) {
-  for (int t = threadIdx.x; t < 512; t += blockDim.x) tw[t] = __ldg(R.w20 + ((uint64_t)t << (W20_LOG - 9)));
+  for (int t = threadIdx.x; t < 512; t += blockDim.x) tw[t] = __ldg(R.lvl + 512 + t);
 }
+
+// Elements per thread in a 2^13-word tile, processed in groups of 8 so that
+// every thread keeps 16 independent global loads in flight.
+constexpr int PER_THREAD = (1 << 13) / 256;
 
 // Forward pass 0 with the limb -> 16-bit coefficient split fused in
 // (crates/bignum/src/ntt.rs:640-665): element (i, j) of the tile is
@@ -188,11 +192,21 @@ __global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const uint64_t* __re
   }
   __syncthreads();
   tile_fwd_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
-    uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-    uint64_t f = row_freq_t<R>(i);
-    uint64_t v = gl::mul(sm[spad(lin)], root_pow(RT, L, f * (j0 + j), false));
-    data[((uint64_t)i << S) + j0 + j] = v;
+#pragma unroll 1
+  for (int g = 0; g < PER_THREAD; g += 8) {
+    uint64_t t8[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t lin = (g + q) * PASS_THREADS + tid;
+      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+      t8[q] = root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), false);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t lin = (g + q) * PASS_THREADS + tid;
+      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+      data[((uint64_t)i << S) + j0 + j] = gl::mul(sm[spad(lin)], t8[q]);
+    }
   }
 }
 
@@ -213,24 +227,44 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(uint64_t* __restrict__
     uint32_t j = lin & 15, i = (lin >> 4) & ((1u << R) - 1), blk = lin >> (4 + R);
     return ((b0 + blk) << mlog) + ((uint64_t)i << S) + j0 + j;
   };
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
-    uint64_t v = data[gaddr(lin)];
+#pragma unroll 1
+  for (int g = 0; g < PER_THREAD; g += 8) {
+    uint64_t v8[8], t8[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) v8[q] = data[gaddr((g + q) * PASS_THREADS + tid)];
     if (!FWD) {
-      uint32_t i = (lin >> 4) & ((1u << R) - 1);
-      v = gl::mul(v, root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), true));
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        uint32_t lin = (g + q) * PASS_THREADS + tid;
+        uint32_t i = (lin >> 4) & ((1u << R) - 1);
+        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), true);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) v8[q] = gl::mul(v8[q], t8[q]);
     }
-    sm[spad(lin)] = v;
+#pragma unroll
+    for (int q = 0; q < 8; q++) sm[spad((g + q) * PASS_THREADS + tid)] = v8[q];
   }
   __syncthreads();
   if (FWD) tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
   else tile_inv_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
-    uint64_t v = sm[spad(lin)];
+#pragma unroll 1
+  for (int g = 0; g < PER_THREAD; g += 8) {
+    uint64_t t8[8];
     if (FWD) {
-      uint32_t i = (lin >> 4) & ((1u << R) - 1);
-      v = gl::mul(v, root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), false));
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        uint32_t lin = (g + q) * PASS_THREADS + tid;
+        uint32_t i = (lin >> 4) & ((1u << R) - 1);
+        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), false);
+      }
     }
-    data[gaddr(lin)] = v;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t lin = (g + q) * PASS_THREADS + tid;
+      uint64_t v = sm[spad(lin)];
+      data[gaddr(lin)] = FWD ? gl::mul(v, t8[q]) : v;
+    }
   }
 }
 
@@ -320,10 +354,23 @@ __global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const uint64_t
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
   load_tw512(tw, RT);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
-    uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-    uint64_t v = data[((uint64_t)i << S) + j0 + j];
-    sm[spad(lin)] = gl::mul(v, root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), true));
+#pragma unroll 1
+  for (int g = 0; g < PER_THREAD; g += 8) {
+    uint64_t v8[8], t8[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t lin = (g + q) * PASS_THREADS + tid;
+      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+      v8[q] = data[((uint64_t)i << S) + j0 + j];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t lin = (g + q) * PASS_THREADS + tid;
+      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+      t8[q] = root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), true);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) sm[spad((g + q) * PASS_THREADS + tid)] = gl::mul(v8[q], t8[q]);
   }
   __syncthreads();
   tile_inv_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
@@ -555,15 +602,15 @@ static int log2_ceil(uint64_t x) {
   return L;
 }
 
-// Host copies of the root tables: lo, hi, w12, w20 (in this order).
-constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (1u << W20_LOG);
+// Host copies of the root tables: lo, hi, w12, level tables (in this order).
+constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (2u << LVL_MAX);
 
 static void build_roots(uint64_t* t) {
   uint64_t rho = find_rho();
   uint64_t* lo = t;
   uint64_t* hi = lo + 65536;
   uint64_t* w12 = hi + 65536;
-  uint64_t* w20 = w12 + 4096;
+  uint64_t* lvl = w12 + 4096;
   uint64_t x = 1;
   for (int i = 0; i < 65536; i++) { lo[i] = x; x = hf::mul(x, rho); }
   uint64_t step = x;  // rho^(2^16)
@@ -572,9 +619,15 @@ static void build_roots(uint64_t* t) {
   uint64_t w4096 = hf::pow(rho, 1ull << 20);
   x = 1;
   for (int i = 0; i < 4096; i++) { w12[i] = x; x = hf::mul(x, w4096); }
-  uint64_t wm = hf::pow(rho, 1ull << (32 - W20_LOG));
+  // level k (1 <= k <= LVL_MAX): w_(2^k)^x at lvl[2^k + x]; level k is every
+  // other entry of level k+1, starting from the longest
+  const uint32_t top = 1u << LVL_MAX;
+  uint64_t wm = hf::pow(rho, 1ull << (32 - LVL_MAX));
   x = 1;
-  for (uint32_t i = 0; i < (1u << W20_LOG); i++) { w20[i] = x; x = hf::mul(x, wm); }
+  for (uint32_t i = 0; i < top; i++) { lvl[top + i] = x; x = hf::mul(x, wm); }
+  for (int k = LVL_MAX - 1; k >= 1; k--)
+    for (uint32_t i = 0; i < (1u << k); i++) lvl[(1u << k) + i] = lvl[(2u << k) + 2 * i];
+  lvl[0] = lvl[1] = 1;
 }
 
 static Roots roots_at(const uint64_t* d) {
@@ -960,8 +1013,8 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //  * scratch holds two transform arrays of at most 2^20 words plus the carry
 //    windows and scan flags: la + lb <= 262144 limbs (transform length
 //    N <= 2^20); larger products are rejected with PIMUL_EINVAL.  The
-//    scratch (16.5 MiB) and this path's own root tables (9 MiB) stay resident
-//    on every GPU that loads this library, until the process exits.
+//    scratch (16.5 MiB) and this path's own root tables (17 MiB) stay
+//    resident on every GPU that loads this library, until the process exits.
 //  * every call uses the same array, and the array keeps the previous call's
 //    contents; the kernels overwrite every scratch word before reading it,
 //    so nothing needs clearing.  Calls whose work overlaps on the GPU

@@ -30,10 +30,10 @@ struct Roots {
   const uint64_t* lo;   // rho^e, e in [0, 2^16)
   const uint64_t* hi;   // rho^(e * 2^16), e in [0, 2^16)
   const uint64_t* w12;  // w_4096^t = rho^(t * 2^20), t in [0, 4096)
-  const uint64_t* w20;  // w_(2^20)^t = rho^(t * 2^12), t in [0, 2^20)
+  const uint64_t* lvl;  // per-level tables: w_(2^k)^x at lvl[2^k + x], 1 <= k <= LVL_MAX
 };
 
-constexpr int W20_LOG = 20;
+constexpr int LVL_MAX = 20;
 
 // rho^e for e in [0, 2^32).
 __device__ __forceinline__ uint64_t rho_pow(const Roots& R, uint32_t e) {
@@ -42,12 +42,13 @@ __device__ __forceinline__ uint64_t rho_pow(const Roots& R, uint32_t e) {
   return h ? gl::mul(a, __ldg(R.hi + h)) : a;
 }
 
-// w_M^x for M = 2^mlog, x in [0, M); inverse gives w_M^(-x).
+// w_M^x for M = 2^mlog, x in [0, M); inverse gives w_M^(-x).  Levels up
+// to 2^20 read one contiguous table; longer ones combine two table entries.
 __device__ __forceinline__ uint64_t root_pow(const Roots& R, int mlog, uint64_t x, bool inverse) {
   uint64_t m = 1ull << mlog;
   x &= m - 1;
   if (inverse) x = (m - x) & (m - 1);
-  if (mlog <= W20_LOG) return __ldg(R.w20 + (x << (W20_LOG - mlog)));
+  if (mlog <= LVL_MAX) return __ldg(R.lvl + m + x);
   return rho_pow(R, (uint32_t)(x << (32 - mlog)));
 }
 

@@ -1,0 +1,66 @@
+"""Batched BBP hex digits on the GPU vs the reference's known values and the
+CPU oracle (crates/pi-core/src/bbp.rs:52-140)."""
+import ctypes
+import threading
+
+import numpy as np
+import pytest
+
+import oracle as O
+import pi_gb300 as pm
+
+pytestmark = pytest.mark.gpu
+
+
+def test_known_values(golden):
+    # bbp.rs:153-175
+    for n, v in golden["bbp_known"].items():
+        assert int(pm.bbp_hex_digits([int(n)])[0]) == v
+    d = pm.bbp_hex_digits(np.arange(16))
+    assert [int(x) >> 28 for x in d] == golden["pi_hex_prefix"]
+
+
+def test_overlap_property():
+    # bbp.rs:177-187: low 7 nibbles at n equal the top 7 at n + 1
+    d = pm.bbp_hex_digits(np.arange(64))
+    for n in range(63):
+        assert int(d[n]) & 0x0FFFFFFF == int(d[n + 1]) >> 4
+
+
+def test_matches_oracle_on_seeded_positions():
+    rng = np.random.default_rng(8)
+    pos = np.concatenate([np.arange(0, 40), rng.integers(0, 200_000, 200), [99_999, 100_000, 131_071]])
+    got = pm.bbp_hex_digits(pos)
+    want = O.bbp_batch(pos)
+    assert np.array_equal(got, want)
+
+
+def test_deeper_positions_match_oracle():
+    pos = np.array([300_000, 999_983, 1_000_000], dtype=np.uint64)
+    assert np.array_equal(pm.bbp_hex_digits(pos), O.bbp_batch(pos))
+
+
+def test_stop_flag_cancels():
+    # bbp.rs:199-204: a stop flag set before the call returns without digits
+    flag = ctypes.c_int(1)
+    with pytest.raises(pm.PimulError) as e:
+        pm.bbp_hex_digits(np.full(64, 3_000_000, dtype=np.uint64), stop=flag)
+    assert e.value.code == 6
+
+
+def test_stop_flag_from_another_thread():
+    import time
+    flag = ctypes.c_int(0)
+    t = threading.Timer(0.3, lambda: setattr(flag, "value", 1))
+    t.start()
+    t0 = time.perf_counter()
+    with pytest.raises(pm.PimulError):
+        # a few seconds of work if not cancelled (bounded either way)
+        pm.bbp_hex_digits(np.full(256, 100_000_000, dtype=np.uint64), stop=flag)
+    t.join()
+    assert time.perf_counter() - t0 < 2.0
+
+
+def test_rejects_positions_above_limit():
+    with pytest.raises(pm.PimulError):
+        pm.bbp_hex_digits([1 << 32])
