@@ -272,14 +272,17 @@ def run_gpu(args):
             raise RuntimeError(lib.pimul_last_error().decode())
 
     e2e_steps = max(3, min(args.steps, 10))
-    e2e_step()
+    if args.no_e2e:
+        e2e_steps = 0
+    else:
+        e2e_step()
     barrier(dist, local)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     t1 = time.perf_counter()
     e2e_s = reduce_max(dist, t1 - t0, device=f"cuda:{local}")
-    e2e_value = ws * bytes_step * e2e_steps / e2e_s / 1e9
+    e2e_value = ws * bytes_step * e2e_steps / e2e_s / 1e9 if e2e_steps else None
 
     # ---- roofline of the dominant kernel class
     peak, peak_kind = measured_peaks()
@@ -310,14 +313,15 @@ def run_gpu(args):
             "dtype": "u64",
             "data": "synthetic: seeded uniform u64 limbs, top limb bit 63 set (numpy PCG64)",
             "config": {
-                "workload": "isolated multiply, balanced 2^30 x 2^30 bits (2^24 x 2^24 limbs), N = 2^27",
+                "workload": f"isolated multiply, balanced 2^{BITS_A.bit_length()-1} x 2^{BITS_B.bit_length()-1} bits ({la} x {lb} limbs), N = 2^{L}",
                 "bits_a": BITS_A, "bits_b": BITS_B, "la": la, "lb": lb, "transform_len": N,
                 "bytes_per_step_model": "B_mul(N) = 96N + 16(la+lb)",
                 "bytes_per_step": bytes_step,
                 "l2": "inputs + scratch (2.3 GiB) exceed the 129 MB L2; no flush needed",
                 "parallelism": f"replicas x{ws}",
             },
-            "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
+            "e2e": None if not e2e_steps else {
+                    "value": round(e2e_value, 2), "unit": "GB/s", "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
                     "h2d_bytes_per_step": 8 * (la + lb), "d2h_bytes_per_step": 8 * (la + lb),
                     "api": "pimul_mul (host buffers, pinned)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
@@ -334,6 +338,291 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------- batched form
+def batch_sizes(n=4096, lo=10, hi=22, seed=20241203):
+    """Operand bit lengths log-uniform in [2^lo, 2^hi], independent per operand."""
+    rng = np.random.default_rng(seed)
+    bits = np.exp(rng.uniform(lo * np.log(2), hi * np.log(2), size=(n, 2))).astype(np.int64)
+    return np.maximum(bits, 1)
+
+
+def make_exact_bits(rng, bits):
+    limbs = (bits + 63) // 64
+    x = rng.integers(0, 1 << 64, size=limbs, dtype=np.uint64)
+    top = (bits - 1) % 64
+    x[-1] &= np.uint64((1 << (top + 1)) - 1) if top < 63 else np.uint64(0xFFFFFFFFFFFFFFFF)
+    x[-1] |= np.uint64(1 << top)
+    return x
+
+
+def run_batch(args):
+    """Config 3: 4,096 independent products of uneven sizes; the graph-planned
+    batch vs the direct batch vs one pimul_mul_device call per product."""
+    import torch
+    import pi_gb300 as pm
+    pm.init(0)
+    lib = pm.lib()
+    bits = batch_sizes()
+    rng = np.random.default_rng(7)
+    ops_a = [make_exact_bits(rng, int(b)) for b in bits[:, 0]]
+    ops_b = [make_exact_bits(rng, int(b)) for b in bits[:, 1]]
+    la = np.array([x.size for x in ops_a])
+    lb = np.array([x.size for x in ops_b])
+    flat = np.concatenate(ops_a + ops_b)
+    d_in = torch.from_numpy(flat.view(np.int64)).cuda()
+    offs_a = np.concatenate([[0], np.cumsum(la)[:-1]])
+    offs_b = la.sum() + np.concatenate([[0], np.cumsum(lb)[:-1]])
+    out_off = np.concatenate([[0], np.cumsum(la + lb)[:-1]])
+    d_out = torch.zeros(int((la + lb).sum()), dtype=torch.int64, device="cuda")
+    d_ref = torch.zeros_like(d_out)
+    base, obase, rbase = d_in.data_ptr(), d_out.data_ptr(), d_ref.data_ptr()
+    jobs = [(base + 8 * int(offs_a[i]), int(la[i]), base + 8 * int(offs_b[i]), int(lb[i]),
+             obase + 8 * int(out_off[i])) for i in range(len(la))]
+    rjobs = [(a, x, b, y, rbase + 8 * int(out_off[i])) for i, (a, x, b, y, _) in enumerate(jobs)]
+    tune = pm.autotune(7, 19, 4) if not args.no_tune else {}
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    plan = pm.BatchPlan(la, lb)
+    arr, n = pm._job_array(jobs)
+
+    def step_plan():
+        lib.pimul_batch_plan_run(plan._h, ctypes.cast(arr, ctypes.c_void_p), n, ctypes.c_void_p(sp))
+
+    def step_direct():
+        lib.pimul_mul_batch(ctypes.cast(arr, ctypes.c_void_p), n, ctypes.c_void_p(sp))
+
+    def step_plain():
+        for (a, x, b, y, o) in rjobs:
+            lib.pimul_mul_device(ctypes.c_void_p(a), x, ctypes.c_void_p(b), y, ctypes.c_void_p(o),
+                                 ctypes.c_void_p(sp))
+
+    def timeit(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lat = []
+        e0.record(stream)
+        for _ in range(steps):
+            t = time.perf_counter()
+            fn()
+            lat.append(time.perf_counter() - t)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_plan = timeit(step_plan, args.steps, args.warmup)
+    ms_direct = timeit(step_direct, args.steps, args.warmup)
+    ms_plain = timeit(step_plain, max(2, args.steps // 4), 1)
+    step_plan()
+    step_plain()
+    stream.synchronize()
+    exact = bool(torch.equal(d_out, d_ref))
+    nprod = len(la)
+    total_bits = float((la.astype(np.float64) * 64).sum() + (lb.astype(np.float64) * 64).sum())
+    bytes_model = 0
+    for x, y in zip(la, lb):
+        N = 1 << next_pow2_log(4 * int(x) + 4 * int(y) - 1)
+        bytes_model += b_mul(N, int(x), int(y))
+    line = {
+        "metric": "batched products/s (4096 uneven products)",
+        "baseline_metric": BASELINE_METRIC,
+        "value": round(nprod / (ms_plan * 1e-3), 1),
+        "unit": "products/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_plan, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic: operand bit lengths log-uniform in [2^10, 2^22], uniform limbs (seeded)",
+        "config": {"workload": "4096 independent products, each operand's bit length log-uniform in [2^10, 2^22]",
+                   "limbs_total": int(la.sum() + lb.sum())},
+        "plain_per_call_ms": round(ms_plain, 3),
+        "direct_batch_ms": round(ms_direct, 3),
+        "speedup_plan_vs_plain": round(ms_plain / ms_plan, 2),
+        "speedup_direct_vs_plain": round(ms_plain / ms_direct, 2),
+        "bits_per_s": round(total_bits / (ms_plan * 1e-3), 1),
+        "model_gbs": round(bytes_model / (ms_plan * 1e-3) / 1e9, 1),
+        "bit_exact_vs_plain": exact,
+        "autotune": tune,
+    }
+    plan.close()
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- served form
+def served_stream(n, seed=20241204, lo=12, hi=28, chain=0.3, sq=0.25):
+    """Config 4 request stream: operand bit lengths log-uniform in
+    [2^lo, 2^hi]; about 30 % of requests consume an earlier result (only
+    results below 2^27 bits are chained, so chains stay bounded); a quarter
+    of the requests are squares."""
+    rng = np.random.default_rng(seed)
+    bits = np.exp(rng.uniform(lo * np.log(2), hi * np.log(2), size=n)).astype(np.int64)
+    base = [make_exact_bits(rng, int(b)) for b in bits]
+    reqs, out_limbs = [], []
+    for k in range(n):
+        x = k
+        if k > 0 and rng.random() < chain:
+            cands = [j for j in range(max(0, k - 64), k) if out_limbs[j] * 64 < (1 << 27)]
+            if cands:
+                x = -(int(rng.choice(cands)) + 1)
+        la = base[x].size if x >= 0 else out_limbs[-x - 1]
+        if rng.random() < sq:
+            reqs.append(("sqr", x, x))
+            out_limbs.append(2 * la)
+        else:
+            y = int(rng.integers(0, n))
+            reqs.append(("mul", x, y))
+            out_limbs.append(la + base[y].size)
+    return base, reqs
+
+
+def run_served(args):
+    """Config 4: Poisson request stream through the device-resident service
+    (continuous batching, chained handles, HBM budget) vs the plain per-call
+    path fed by one worker in arrival order.  Latency = completion - arrival."""
+    import threading
+    import torch
+    import pi_gb300 as pm
+    pm.init(0)
+    lib = pm.lib()
+    n = args.requests
+    base, reqs = served_stream(n)
+    pm.set_budget(120 << 30)
+    # ---- plain path: device operands as torch tensors, results kept
+    dbase = [torch.from_numpy(x.view(np.int64)).cuda() for x in base]
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def plain_one(k, res):
+        op, x, y = reqs[k]
+        a = dbase[x] if x >= 0 else res[-x - 1]
+        b = a if op == "sqr" else (dbase[y] if y >= 0 else res[-y - 1])
+        out = torch.empty(a.numel() + b.numel(), dtype=torch.int64, device="cuda")
+        lib.pimul_mul_device(ctypes.c_void_p(a.data_ptr()), a.numel(), ctypes.c_void_p(b.data_ptr()), b.numel(),
+                             ctypes.c_void_p(out.data_ptr()), sp)
+        stream.synchronize()
+        return out
+
+    # capacity of the plain path (back to back, no arrivals)
+    res = []
+    for k in range(min(n, 32)):  # warm-up
+        res.append(plain_one(k, res))
+    res = []
+    t0 = time.perf_counter()
+    for k in range(n):
+        res.append(plain_one(k, res))
+    t_serial = time.perf_counter() - t0
+    capacity = n / t_serial
+    lam = args.load * capacity
+    rng = np.random.default_rng(99)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
+    # ---- plain path under the arrival process (one worker, FIFO)
+    del res
+    torch.cuda.empty_cache()
+    res = []
+    lat_plain = []
+    t0 = time.perf_counter()
+    for k in range(n):
+        while time.perf_counter() - t0 < arrivals[k]:
+            pass
+        res.append(plain_one(k, res))
+        lat_plain.append(time.perf_counter() - t0 - arrivals[k])
+    span_plain = time.perf_counter() - t0
+    plain_host = [np.trim_zeros(r.cpu().numpy().view(np.uint64), "b") for r in res]
+    del res
+    torch.cuda.empty_cache()
+    # ---- served path
+    hb = [pm.upload(x) for x in base]
+    pm.service_reset_stats()
+    outs, tickets = [], []
+    t0 = time.perf_counter()
+    for k, (op, x, y) in enumerate(reqs):
+        while time.perf_counter() - t0 < arrivals[k]:
+            pass
+        ha = hb[x] if x >= 0 else outs[-x - 1]
+        if op == "sqr":
+            h, t = pm.submit(ha)
+        else:
+            h, t = pm.submit(ha, hb[y] if y >= 0 else outs[-y - 1])
+        outs.append(h)
+        tickets.append(t)
+    for t in tickets:
+        pm.wait(t)
+    span_served = time.perf_counter() - t0
+    st = pm.service_stats()
+    served_host = [pm.download(h) for h in outs]
+    exact = all(np.array_equal(a, b) for a, b in zip(served_host, plain_host))
+    for h in outs + hb:
+        pm.free(h)
+    lp = np.array(lat_plain) * 1e3
+    line = {
+        "metric": "served request stream: p50/p99 latency and ops/s vs plain per-call",
+        "baseline_metric": BASELINE_METRIC,
+        "value": round(n / span_served, 1), "unit": "requests/s",
+        "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * span_served, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic: Poisson arrivals (seeded), operand bits log-uniform in [2^12, 2^28], "
+                "30% chained on earlier results, 25% squares",
+        "config": {"workload": f"{n} requests, offered load {args.load} of the plain path's capacity",
+                   "plain_capacity_rps": round(capacity, 1), "lambda_rps": round(lam, 1),
+                   "hbm_budget_bytes": 120 << 30},
+        "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                   "ops_per_s": round(n / span_served, 1), "batches": st["batches"]},
+        "plain": {"p50_ms": round(float(np.percentile(lp, 50)), 3), "p99_ms": round(float(np.percentile(lp, 99)), 3),
+                  "ops_per_s": round(n / span_plain, 1)},
+        "bit_exact_served_vs_plain": bool(exact),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- pi runs
+def run_pi(args):
+    """Config 1: Chudnovsky pi to D digits; every product at or above the
+    reference's NTT threshold goes through the GPU multiply, one call per
+    product.  The same pipeline with the CPU restatement of the reference's
+    multiply is the CPU run; digits must be byte-identical."""
+    import hashlib
+    import pi_gb300 as pm
+    pm.init(0)
+    D = args.digits
+    pm.pi_chudnovsky(min(D, 100_000))  # warm-up (tables, pools, kernels)
+    t0 = time.perf_counter()
+    s, info = pm.pi_chudnovsky(D)
+    wall = time.perf_counter() - t0
+    cpu = None
+    same = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        t1 = time.perf_counter()
+        sc, cinfo = pm.pi_chudnovsky(D, backend=oracle.mul_abi_pointer())
+        cwall = time.perf_counter() - t1
+        same = sc == s
+        cpu = {"value": round(cwall, 3), "unit": "s", "cores": oracle.max_threads(), "kind": "port",
+               "sample": f"the same {D}-digit run with the C restatement of mul_mag_ntt "
+                         "(crates/bignum/src/ntt.rs:806-865) as the multiply",
+               "phases_ms": {k: round(v, 1) for k, v in cinfo.items() if k.endswith("_ms")}}
+    golden = None
+    path = os.path.join(ROOT, "tests", "golden", "pi_digits_hashes.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            g = json.load(f).get(str(D))
+        if g:
+            golden = hashlib.sha256(s.encode()).hexdigest() == g["sha256"]
+    line = {
+        "metric": f"pi wall-s (Chudnovsky, {D} digits)", "baseline_metric": BASELINE_METRIC,
+        "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "deterministic (no random input)",
+        "config": {"workload": f"Chudnovsky binary splitting for pi to {D} decimal digits, "
+                               "products >= 8192 limbs on the GPU (one call per product)"},
+        "phases_ms": {k: round(v, 1) for k, v in info.items() if k.endswith("_ms")},
+        "gpu_products": info["ntt_products"], "gpu_products_by_length": info["ntt_hist"],
+        "digits_match_cpu_run": same, "digits_match_mpmath_sha256": golden,
+        "last_digits": s[-20:], "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------- CPU legs
@@ -408,11 +697,29 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-API leg (profiling runs)")
+    ap.add_argument("--digits", type=int, default=1_000_000)
+    ap.add_argument("--workload", choices=["mul", "batch", "served", "pi"], default="mul",
+                    help="mul: the 2^30-bit product (headline); batch: 4096 uneven products; "
+                         "served: Poisson request stream through the multiply service")
+    ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--load", type=float, default=0.8)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--bits", type=int, default=30,
+                    help="log2 bits per operand (30 = the headline workload; smaller for profiling)")
     args = ap.parse_args()
+    global BITS_A, BITS_B
+    BITS_A = BITS_B = 1 << args.bits
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "served":
+        run_served(args)
+    elif args.workload == "pi":
+        run_pi(args)
     else:
         run_gpu(args)
 

@@ -62,6 +62,7 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb,
  * Same multiply on DEVICE buffers, asynchronous on `stream` (a cudaStream_t;
  * NULL = the calling thread's own stream).  Writes exactly la + lb limbs to
  * d_out (the top limb may be zero); d_out must not overlap the inputs.
+ * la == 0 or lb == 0 is a zero product: nothing is written.
  * Scratch comes from the engine's device pool.
  *
  * Replaces: crates/bignum/src/ntt.rs:806 `mul_mag_ntt`, for callers whose
@@ -88,6 +89,109 @@ int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t
  */
 int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb,
                              uint64_t* d_out, void* stream);
+
+/* One product of a batch: device pointers; out receives la + lb limbs. */
+typedef struct pimul_job {
+  const uint64_t* a;
+  size_t la;
+  const uint64_t* b;
+  size_t lb;
+  uint64_t* out;
+} pimul_job;
+
+/*
+ * Batched form: n independent products on device buffers in one call
+ * (asynchronous on `stream`, NULL = the calling thread's stream).  Products
+ * are grouped by transform length: up to 2^12 one CTA per product in a
+ * persistent kernel, longer ones one launch per pass for the whole group.
+ * Each out[i] is written exactly as pimul_mul_device would write it.
+ *
+ * Replaces: the independent mul_mag calls of one binary-splitting level
+ * (crates/pi-core/src/algorithm/chudnovsky.rs:399-413, run through
+ * rayon::join), each of which reaches crates/bignum/src/ntt.rs:806.
+ */
+int pimul_mul_batch(const pimul_job* jobs, size_t n, void* stream);
+
+/*
+ * Batch plans: a fixed batch shape (la[i], lb[i]) laid out once, with all its
+ * launches captured into a CUDA graph.  plan_run takes jobs of exactly that
+ * shape (new pointers each time) and replays the graph; runs of one plan are
+ * serialised (a run waits until the previous run has read its descriptors).
+ * This engine's own addition (the per-level schedule of a product tree).
+ */
+typedef struct pimul_batch_plan pimul_batch_plan;
+int pimul_batch_plan_create(const size_t* la, const size_t* lb, size_t n, pimul_batch_plan** plan);
+int pimul_batch_plan_run(pimul_batch_plan* plan, const pimul_job* jobs, size_t n, void* stream);
+int pimul_batch_plan_destroy(pimul_batch_plan* plan);
+
+/*
+ * Autotuner: times the candidate radix splits (passes per transform) for
+ * every transform length 2^log_n_min .. 2^log_n_max on `reps` synthetic
+ * products, and the one-CTA kernel's persistent grid (CTAs per SM); keeps
+ * the fastest for later calls and writes a JSON report.  pimul_tuning_set
+ * applies saved choices (passes = 0: default split; ctas <= 0: unchanged).
+ * The transform length itself is the reference's rule and is not tuned.
+ */
+int pimul_autotune(int log_n_min, int log_n_max, int reps, char* report, size_t report_cap);
+int pimul_tuning_set(int log_n, int passes, int small_ctas_per_sm);
+
+/*
+ * Served form: a device-resident multiply service.
+ *
+ * Integers live on the device as handles.  pimul_submit queues a product
+ * (op PIMUL_OP_MUL: a * b; PIMUL_OP_SQR: a * a) and returns its result
+ * handle and a ticket at once; the result handle may be an input of later
+ * submits before it is computed (the dependency is a CUDA event: no host
+ * round trip).  A service thread admits queued requests in order while
+ * their result and scratch memory fit the HBM budget (pimul_set_budget,
+ * default 120 GiB; handles count against it until freed), launches each
+ * admitted group as one batch on one of four streams, and releases the
+ * scratch when the group completes; requests that arrive meanwhile join the
+ * next group (continuous batching).  pimul_wait blocks until a ticket's
+ * product is done (timeout_us < 0: no limit) or returns PIMUL_ETIMEDOUT.
+ * pimul_free waits for the handle's producer and readers.  A result handle
+ * stores la + lb limbs; pimul_download returns the trimmed value.
+ * pimul_service_stats reports submit-to-completion latency percentiles.
+ *
+ * Replaces: the per-level products of the binary-splitting tree with their
+ * operands kept in HBM between levels (crates/pi-core/src/algorithm/
+ * chudnovsky.rs:377-413, where each Integer * Integer reaches
+ * crates/bignum/src/ntt.rs:806 through crates/bignum/src/integer.rs:637).
+ */
+#define PIMUL_OP_MUL 0
+#define PIMUL_OP_SQR 1
+int pimul_set_budget(uint64_t bytes);
+int pimul_upload(const uint64_t* host, size_t n, uint64_t* handle);
+int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t* ticket);
+int pimul_wait(uint64_t ticket, int64_t timeout_us);
+int pimul_handle_size(uint64_t handle, size_t* limbs);
+int pimul_download(uint64_t handle, uint64_t* host, size_t cap, size_t* len);
+int pimul_free(uint64_t handle);
+int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uint64_t* batches,
+                        uint64_t* bytes_in_use);
+int pimul_service_reset_stats(void);
+
+/* Signature of a multiply backend: pimul_mul's own. */
+typedef int (*pimul_mul_fn)(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64_t* out,
+                            size_t out_cap, size_t* out_len);
+
+/*
+ * Digits of pi by Chudnovsky binary splitting, driven from the host with
+ * every product at or above the NTT threshold (ntt_threshold limbs of the
+ * smaller operand; 0 = the reference's 8192) sent to `backend`
+ * (NULL = pimul_mul, the GPU engine; one call per product).  Writes
+ * `digits` characters "31415..." (no decimal point) to out.  Optional
+ * outputs: phase_ms[3] = binary splitting, final assembly, decimal
+ * conversion wall times; ntt_products = number of backend calls;
+ * ntt_hist33[L] = backend calls with transform length 2^L.
+ *
+ * Replaces: crates/pi-core/src/algorithm/chudnovsky.rs:75 Chudnovsky::compute
+ * with crates/pi-core/src/algorithm/util.rs:25 write_decimal_digits, whose
+ * multiplies all reach crates/bignum/src/ntt.rs:806 through
+ * crates/bignum/src/integer.rs:445.
+ */
+int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
+                        double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33);
 
 /* Transform plan for a product: N and the number of HBM passes per transform.
  * Mirrors the sizing of crates/bignum/src/ntt.rs:810-813. */

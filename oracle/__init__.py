@@ -69,6 +69,8 @@ def lib():
         L.orc_max_threads.argtypes = []
         L.orc_bbp_hex_digits_at.restype = ctypes.c_int
         L.orc_bbp_hex_digits_at.argtypes = [_u64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_mul_abi.restype = ctypes.c_int
+        L.orc_mul_abi.argtypes = [_u64p, _sz, _u64p, _sz, _u64p, _sz, ctypes.POINTER(_sz)]
         L.orc_bbp_batch.restype = None
         L.orc_bbp_batch.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32)]
         _lib = L
@@ -156,6 +158,11 @@ def set_threads(n: int):
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+def mul_abi_pointer():
+    """Address of orc_mul_abi (a pimul_mul_fn-compatible multiply)."""
+    return ctypes.cast(lib().orc_mul_abi, ctypes.c_void_p).value
 
 
 # ---------------------------------------------------------------- BBP

@@ -585,3 +585,14 @@ void orc_bbp_batch(const uint64_t* pos, size_t n, uint32_t* out) {
 #pragma omp parallel for schedule(dynamic, 1)
   for (size_t i = 0; i < n; i++) orc_bbp_hex_digits_at(pos[i], 0, &out[i]);
 }
+
+/* Adapter with the engine's C-ABI multiply signature (include/pimul.h
+ * pimul_mul_fn): lets a host driver use this CPU restatement as its
+ * multiply backend (the reference's own CPU multiply path). */
+int orc_mul_abi(const uint64_t* a, size_t la, const uint64_t* b, size_t lb,
+                uint64_t* out, size_t cap, size_t* out_len) {
+  size_t n = orc_mul_mag_ntt(a, la, b, lb, out, cap);
+  if (n == (size_t)-1) return 1;
+  *out_len = n;
+  return 0;
+}

@@ -24,7 +24,9 @@ from . import build as _build
 
 __all__ = [
     "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device",
-    "plan", "sync", "bbp_hex_digits", "LIB_PATH",
+    "plan", "sync", "bbp_hex_digits", "mul_batch", "BatchPlan", "autotune",
+    "tuning_apply", "PimulJob", "set_budget", "upload", "submit", "wait", "download", "free",
+    "handle_size", "pi_chudnovsky", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
 ]
 
 LIB_PATH = _build.LIB
@@ -62,6 +64,25 @@ def load(build_if_stale: bool = True):
     L.pimul_mul_device.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]
     L.pimul_plan.argtypes = [_sz, _sz, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]
     L.pimul_sync.argtypes = []
+    L.pimul_mul_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_batch_plan_create.argtypes = [ctypes.POINTER(_sz), ctypes.POINTER(_sz), _sz, ctypes.POINTER(ctypes.c_void_p)]
+    L.pimul_batch_plan_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_batch_plan_destroy.argtypes = [ctypes.c_void_p]
+    L.pimul_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _sz]
+    L.pimul_tuning_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.pimul_set_budget.argtypes = [ctypes.c_uint64]
+    L.pimul_upload.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_submit.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                               ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_wait.argtypes = [ctypes.c_uint64, ctypes.c_int64]
+    L.pimul_handle_size.argtypes = [ctypes.c_uint64, ctypes.POINTER(_sz)]
+    L.pimul_download.argtypes = [ctypes.c_uint64, _u64p, _sz, ctypes.POINTER(_sz)]
+    L.pimul_free.argtypes = [ctypes.c_uint64]
+    L.pimul_service_stats.argtypes = [ctypes.POINTER(ctypes.c_double)] * 2 + [ctypes.POINTER(ctypes.c_uint64)] * 3
+    L.pimul_service_reset_stats.argtypes = []
+    L.pimul_pi_chudnovsky.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
     L.pimul_bbp_last_error.restype = ctypes.c_char_p
     _lib = L
@@ -120,6 +141,166 @@ def mul_device(d_a, d_b, d_out, stream=None):
         stream = torch.cuda.current_stream(d_out.device).cuda_stream
     _check(lib().pimul_mul_device(d_a.data_ptr(), la, d_b.data_ptr(), lb, d_out.data_ptr(),
                                   ctypes.c_void_p(stream)))
+
+
+class PimulJob(ctypes.Structure):
+    """struct pimul_job of include/pimul.h (device pointers)."""
+    _fields_ = [("a", ctypes.c_void_p), ("la", ctypes.c_size_t), ("b", ctypes.c_void_p),
+                ("lb", ctypes.c_size_t), ("out", ctypes.c_void_p)]
+
+
+def _job_array(jobs):
+    """jobs: iterable of (d_a, d_b, d_out) torch CUDA tensors, or of
+    (a_ptr, la, b_ptr, lb, out_ptr) integer tuples."""
+    items = list(jobs)
+    arr = (PimulJob * max(len(items), 1))()
+    for i, j in enumerate(items):
+        if len(j) == 3:
+            a, b, o = j
+            arr[i] = PimulJob(a.data_ptr(), a.numel(), b.data_ptr(), b.numel(), o.data_ptr())
+        else:
+            arr[i] = PimulJob(*j)
+    return arr, len(items)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream
+
+
+def mul_batch(jobs, stream=None):
+    """Batched device products (one call for many independent products)."""
+    arr, n = _job_array(jobs)
+    _check(lib().pimul_mul_batch(ctypes.cast(arr, ctypes.c_void_p), n, ctypes.c_void_p(_stream_ptr(stream))))
+
+
+class BatchPlan:
+    """A fixed batch shape with its launch schedule captured in a CUDA graph."""
+
+    def __init__(self, la, lb):
+        la = list(la)
+        lb = list(lb)
+        if len(la) != len(lb):
+            raise PimulError(1, "la and lb differ in length")
+        self.n = len(la)
+        A = (ctypes.c_size_t * max(self.n, 1))(*la)
+        B = (ctypes.c_size_t * max(self.n, 1))(*lb)
+        h = ctypes.c_void_p()
+        _check(lib().pimul_batch_plan_create(A, B, self.n, ctypes.byref(h)))
+        self._h = h
+
+    def run(self, jobs, stream=None):
+        arr, n = _job_array(jobs)
+        _check(lib().pimul_batch_plan_run(self._h, ctypes.cast(arr, ctypes.c_void_p), n,
+                                          ctypes.c_void_p(_stream_ptr(stream))))
+
+    def close(self):
+        if self._h:
+            lib().pimul_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def autotune(log_n_min=7, log_n_max=19, reps=8) -> dict:
+    """Run the autotuner; returns its choices (also applied in-process)."""
+    import json
+    buf = ctypes.create_string_buffer(4096)
+    _check(lib().pimul_autotune(log_n_min, log_n_max, reps, buf, 4096))
+    return json.loads(buf.value.decode() or "{}")
+
+
+def tuning_apply(choices: dict):
+    """Re-apply choices returned by autotune() (e.g. loaded from a file)."""
+    for k, v in choices.items():
+        if k.startswith("np_"):
+            _check(lib().pimul_tuning_set(int(k[3:]), int(v), 0))
+        elif k == "small_ctas_per_sm":
+            _check(lib().pimul_tuning_set(-1, 0, int(v)))
+
+
+# ----------------------------------------------------------------- served form
+OP_MUL, OP_SQR = 0, 1
+
+
+def set_budget(nbytes: int):
+    """HBM admission budget of the multiply service (default 120 GiB)."""
+    _check(lib().pimul_set_budget(int(nbytes)))
+
+
+def upload(limbs) -> int:
+    """Copy an integer (u64 limbs) to the device; returns its handle."""
+    x = _limbs(limbs)
+    h = ctypes.c_uint64(0)
+    _check(lib().pimul_upload(x.ctypes.data_as(_u64p), x.size, ctypes.byref(h)))
+    return h.value
+
+
+def submit(a: int, b: int = None, op: int = None):
+    """Queue a * b (or a * a); returns (result_handle, ticket) immediately."""
+    if op is None:
+        op = OP_SQR if b is None else OP_MUL
+    h, t = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(lib().pimul_submit(op, a, a if b is None else b, ctypes.byref(h), ctypes.byref(t)))
+    return h.value, t.value
+
+
+def wait(ticket: int, timeout_us: int = -1):
+    _check(lib().pimul_wait(ticket, timeout_us))
+
+
+def handle_size(h: int) -> int:
+    n = _sz(0)
+    _check(lib().pimul_handle_size(h, ctypes.byref(n)))
+    return n.value
+
+
+def download(h: int) -> np.ndarray:
+    """The handle's value (trimmed limbs); waits for its producer."""
+    cap = handle_size(h)
+    out = np.zeros(max(cap, 1), dtype=np.uint64)
+    n = _sz(0)
+    _check(lib().pimul_download(h, out.ctypes.data_as(_u64p), out.size, ctypes.byref(n)))
+    return out[: n.value].copy()
+
+
+def free(h: int):
+    _check(lib().pimul_free(h))
+
+
+def service_stats() -> dict:
+    p50, p99 = ctypes.c_double(0), ctypes.c_double(0)
+    c, b, u = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(lib().pimul_service_stats(ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(c), ctypes.byref(b),
+                                     ctypes.byref(u)))
+    return {"p50_ms": p50.value, "p99_ms": p99.value, "completed": c.value, "batches": b.value,
+            "bytes_in_use": u.value}
+
+
+def service_reset_stats():
+    _check(lib().pimul_service_reset_stats())
+
+
+def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
+    """Digits of pi ("31415...") by Chudnovsky with large products on the GPU
+    (crates/pi-core/src/algorithm/chudnovsky.rs:75).  `backend`: address of
+    a pimul_mul_fn-compatible multiply (None = the GPU engine).  Returns
+    (digits_str, info) with phase times and the backend-call histogram."""
+    buf = ctypes.create_string_buffer(digits + 1)
+    ph = (ctypes.c_double * 3)()
+    n = ctypes.c_uint64(0)
+    hist = (ctypes.c_uint64 * 33)()
+    _check(lib().pimul_pi_chudnovsky(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
+                                     ntt_threshold, ph, ctypes.byref(n), hist))
+    info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
+            "ntt_products": n.value, "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
+    return buf.raw[:digits].decode(), info
 
 
 def bbp_hex_digits(positions, stop=None) -> np.ndarray:

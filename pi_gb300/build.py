@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimul.so")
 
-SOURCES = ["engine.cu", "bbp.cu"]
+SOURCES = ["engine.cu", "bbp.cu", "pi_host.cpp"]
 HEADERS = ["gl.cuh", "ntt_kernels.cuh"]
 
 NVCC_FLAGS = [

@@ -9,7 +9,14 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -165,14 +172,44 @@ __device__ __forceinline__ void load_tw512(uint64_t* tw, const Roots& R) {
 // every thread keeps 16 independent global loads in flight.
 constexpr int PER_THREAD = (1 << 13) / 256;
 
+// One product of a batch (or the only product of a plain call): operands,
+// output and its scratch.  Kernels take `const Job* jobs, Job one`: with a
+// device array, blockIdx.y selects the product; with jobs == nullptr the
+// by-value `one` is used (no descriptor upload for single products).
+struct Job {
+  const uint64_t* a;
+  const uint64_t* b;
+  uint64_t* out;
+  uint64_t* A;  // N words: a's spectrum (and the product for a square)
+  uint64_t* B;  // N words: b's spectrum and the product (unused for a square)
+  uint64_t* H;  // high parts of the carry windows
+  uint8_t* aux; // carry-scan flags
+  uint64_t la, lb;
+};
+
+__device__ __forceinline__ Job job_of(const Job* jobs, const Job& one) {
+  if (jobs) return jobs[blockIdx.y];
+  return one;
+}
+__device__ __forceinline__ bool is_square(const Job& J) { return J.a == J.b && J.la == J.lb; }
+// Array a pass works on: 0 = A, 1 = B, 2 = the product array.
+__device__ __forceinline__ uint64_t* job_array(const Job& J, int which) {
+  return which == 0 ? J.A : (which == 1 || !is_square(J)) ? J.B : J.A;
+}
+
 // Forward pass 0 with the limb -> 16-bit coefficient split fused in
 // (crates/bignum/src/ntt.rs:640-665): element (i, j) of the tile is
 // coefficient n = i * 2^S + j0 + j, i.e. 16-bit slice n % 4 of limb n / 4;
-// limbs past nl are zero (the reference's zero tail).
+// limbs past nl are zero (the reference's zero tail).  which = 0: operand a,
+// 1: operand b (squares skip b).
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const uint64_t* __restrict__ limbs, uint64_t nl,
-                                                             uint64_t* __restrict__ data, int L, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT) {
   constexpr int T = TILE_LOG - R;
+  const Job J = job_of(jobs, one);
+  if (which == 1 && is_square(J)) return;
+  const uint64_t* __restrict__ limbs = which ? J.b : J.a;
+  const uint64_t nl = which ? J.lb : J.la;
+  uint64_t* __restrict__ data = which ? J.B : J.A;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
@@ -213,8 +250,11 @@ __global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const uint64_t* __re
 // Middle column pass: 2^(9-R) blocks x 2^R rows x 16 columns; forward pass
 // twiddles w_M^(f*j) after the rounds, inverse ones before.
 template <int R, bool FWD>
-__global__ void __launch_bounds__(PASS_THREADS) k_col_mid(uint64_t* __restrict__ data, int S, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT) {
   constexpr int T = 4, BC = 9 - R;
+  const Job J = job_of(jobs, one);
+  if (FWD && which == 1 && is_square(J)) return;
+  uint64_t* __restrict__ data = job_array(J, which);
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
@@ -268,14 +308,17 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(uint64_t* __restrict__
   }
 }
 
-// Last forward pass (stride 1): 2^(13-R) contiguous blocks of 2^R words.
+// Last forward pass of operand a (stride 1): 2^(13-R) contiguous blocks of
+// 2^R words.  Squares skip it: their last pass is fused into k_mid.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(uint64_t* __restrict__ data, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(const Job* jobs, Job one, Roots RT) {
   constexpr int BC = TILE_LOG - R;
+  const Job J = job_of(jobs, one);
+  if (is_square(J)) return;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
-  uint64_t* base = data + ((uint64_t)blockIdx.x << TILE_LOG);
+  uint64_t* base = J.A + ((uint64_t)blockIdx.x << TILE_LOG);
   load_tw512(tw, RT);
   for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = base[lin];
   __syncthreads();
@@ -286,27 +329,31 @@ __global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(uint64_t* __restrict_
 // Fused middle of the multiply on one contiguous tile: last forward pass of
 // b, pointwise product with the spectrum of a (times N^-1, the inverse's
 // 1/N, crates/bignum/src/ntt.rs:383-390 and 845-853), first inverse pass;
-// the result overwrites b's array.  SQUARE: a's own spectrum is squared.
-template <int R, bool SQUARE>
-__global__ void __launch_bounds__(PASS_THREADS) k_mid(uint64_t* __restrict__ b, const uint64_t* __restrict__ a,
-                                                       uint64_t ninv, Roots RT) {
+// the result overwrites b's array.  A square transforms and squares a's
+// array in place.
+template <int R>
+__global__ void __launch_bounds__(PASS_THREADS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
   constexpr int BC = TILE_LOG - R;
+  const Job J = job_of(jobs, one);
+  const bool sq = is_square(J);
+  uint64_t* __restrict__ c = sq ? J.A : J.B;
+  const uint64_t* __restrict__ a = J.A;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
   const uint64_t off = (uint64_t)blockIdx.x << TILE_LOG;
   load_tw512(tw, RT);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = b[off + lin];
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = c[off + lin];
   __syncthreads();
   tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
   for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
     uint64_t x = sm[spad(lin)];
-    uint64_t y = SQUARE ? x : a[off + lin];
+    uint64_t y = sq ? x : a[off + lin];
     sm[spad(lin)] = gl::mul(gl::mul(x, y), ninv);
   }
   __syncthreads();
   tile_inv_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) b[off + lin] = sm[spad(lin)];
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) c[off + lin] = sm[spad(lin)];
 }
 
 // ---- carry normalisation (crates/bignum/src/ntt.rs:676-791) --------------
@@ -339,15 +386,32 @@ __device__ __forceinline__ Win fold16(const uint64_t* c16, int stride) {
   return r;
 }
 
+constexpr int CARRY_THREADS = 256;  // windows per CTA
+
+__host__ __device__ __forceinline__ uint64_t n_windows(uint64_t la, uint64_t lb) {
+  return (4 * la + 4 * lb - 1 + 15) / 16;
+}
+__host__ __device__ __forceinline__ uint64_t n_chunks(uint64_t nwin) {
+  return (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
+}
+// Carry-scan flag layout inside Job::aux: per warp (A, B) masks, then per
+// chunk the (g, p) byte and the carry-in byte.
+__host__ __device__ __forceinline__ uint64_t aux_bytes_for(uint64_t nwin) {
+  uint64_t nc = n_chunks(nwin);
+  return nc * (CARRY_THREADS / 32) * 8 + 2 * nc + 64;
+}
+
 // Inverse pass 0 (natural order out) fused with the window fold: each tile
 // row holds 2^T consecutive coefficients = 2^(T-4) windows; every window
 // writes its low 4 limbs to the output and its high part to H.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const uint64_t* __restrict__ data, int L,
-                                                                   uint64_t* __restrict__ out, uint64_t nlimbs,
-                                                                   uint64_t* __restrict__ H, uint64_t nwin,
-                                                                   Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
   constexpr int T = TILE_LOG - R;
+  const Job J = job_of(jobs, one);
+  const uint64_t* __restrict__ data = job_array(J, 2);
+  uint64_t* __restrict__ out = J.out;
+  uint64_t* __restrict__ H = J.H;
+  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb);
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
@@ -390,14 +454,17 @@ __global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const uint64_t
   }
 }
 
-constexpr int CARRY_THREADS = 256;  // windows per CTA
-
-// Carry pass 1: s_w = lo_w + hi_(w-1) written back as the output limbs; per
-// window (g, p), per warp the (A, B) masks, per CTA the chunk's carry out
-// for carry in 0 and 1.
-__global__ void __launch_bounds__(CARRY_THREADS)
-k_carry_local(uint64_t* __restrict__ out, uint64_t nlimbs, const uint64_t* __restrict__ H, uint64_t nwin,
-              uint32_t* __restrict__ masks, uint8_t* __restrict__ chunk_gp) {
+// Carry pass 1 (grid.x = chunk, grid.y = product): s_w = lo_w + hi_(w-1)
+// written back as the output limbs; per window (g, p), per warp the (A, B)
+// masks, per CTA the chunk's carry out for carry in 0 and 1.
+__global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, Job one) {
+  const Job J = job_of(jobs, one);
+  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb), nchunk = n_chunks(nwin);
+  if (blockIdx.x >= nchunk) return;  // uniform per CTA
+  uint64_t* __restrict__ out = J.out;
+  const uint64_t* __restrict__ H = J.H;
+  uint32_t* masks = reinterpret_cast<uint32_t*>(J.aux);
+  uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;
   __shared__ uint32_t sA[CARRY_THREADS / 32], sB[CARRY_THREADS / 32];
   const uint64_t w = (uint64_t)blockIdx.x * CARRY_THREADS + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -443,11 +510,15 @@ k_carry_local(uint64_t* __restrict__ out, uint64_t nlimbs, const uint64_t* __res
   }
 }
 
-// Carry pass 2: carry into every chunk.  One CTA; each thread walks a
-// contiguous segment of chunks, the segment results are chained by thread 0.
+// Carry pass 2 (one CTA per product): carry into every chunk.  Each thread
+// walks a contiguous segment of chunks, the segment results are chained by
+// thread 0.
 constexpr int SCAN_THREADS = 1024;
-__global__ void __launch_bounds__(SCAN_THREADS)
-k_carry_scan(const uint8_t* __restrict__ chunk_gp, uint64_t nchunk, uint8_t* __restrict__ chunk_cin) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Job one) {
+  const Job J = job_of(jobs, one);
+  const uint64_t nchunk = n_chunks(n_windows(J.la, J.lb));
+  const uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;
+  uint8_t* chunk_cin = const_cast<uint8_t*>(chunk_gp) + nchunk;
   __shared__ uint8_t seg_g[SCAN_THREADS], seg_p[SCAN_THREADS], seg_cin[SCAN_THREADS];
   const uint64_t per = (nchunk + SCAN_THREADS - 1) / SCAN_THREADS;
   const uint64_t lo = threadIdx.x * per, hi = lo + per < nchunk ? lo + per : nchunk;
@@ -478,9 +549,13 @@ k_carry_scan(const uint8_t* __restrict__ chunk_gp, uint64_t nchunk, uint8_t* __r
 }
 
 // Carry pass 3: add the incoming carry to every window that receives one.
-__global__ void __launch_bounds__(CARRY_THREADS)
-k_carry_apply(uint64_t nwin, uint64_t* __restrict__ out, uint64_t nlimbs, const uint32_t* __restrict__ masks,
-              const uint8_t* __restrict__ chunk_cin) {
+__global__ void __launch_bounds__(CARRY_THREADS) k_carry_apply(const Job* jobs, Job one) {
+  const Job J = job_of(jobs, one);
+  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb), nchunk = n_chunks(nwin);
+  if (blockIdx.x >= nchunk) return;
+  uint64_t* __restrict__ out = J.out;
+  const uint32_t* masks = reinterpret_cast<const uint32_t*>(J.aux);
+  const uint8_t* chunk_cin = J.aux + nchunk * (CARRY_THREADS / 32) * 8 + nchunk;
   const uint64_t w = (uint64_t)blockIdx.x * CARRY_THREADS + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t cin = chunk_cin[blockIdx.x];
@@ -586,13 +661,20 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
   }
 }
 
-__global__ void __launch_bounds__(SMALL_THREADS) k_small_mul(SmallJob job, Roots R) {
+// One CTA per product; with a device job list the CTAs stride over it
+// (a persistent kernel over a size-sorted bucket).
+__global__ void __launch_bounds__(SMALL_THREADS) k_small_mul(const SmallJob* jobs, SmallJob one, uint32_t njobs,
+                                                               Roots R) {
   extern __shared__ uint64_t sm[];
-  const uint32_t n_out = 4 * job.la + 4 * job.lb - 1;
-  int L = 0;
-  while ((1u << L) < n_out) L++;
-  uint32_t N = 1u << L;
-  small_multiply(job, R, sm, sm + spad(N));
+  for (uint32_t k = blockIdx.x; k < njobs; k += gridDim.x) {
+    const SmallJob job = jobs ? jobs[k] : one;
+    const uint32_t n_out = 4 * job.la + 4 * job.lb - 1;
+    int L = 0;
+    while ((1u << L) < n_out) L++;
+    uint32_t N = 1u << L;
+    small_multiply(job, R, sm, sm + spad(N));
+    __syncthreads();
+  }
 }
 
 // ------------------------------------------------------------------ host side
@@ -660,8 +742,7 @@ static cudaError_t set_smem_attrs_r() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd_last<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return e;
 }
 
@@ -718,26 +799,43 @@ struct Plan {
   int r[5];
 };
 
-static Plan make_plan(int L) {
-  Plan p{L, 0, {0, 0, 0, 0, 0}};
+// Pass-count override per L chosen by the autotuner (0 = default).
+static std::atomic<int> g_tuned_np[33];
+// Persistent grid of the one-CTA kernel in a batch: CTAs per SM (autotuned).
+static std::atomic<int> g_small_ctas_per_sm{4};
+
+static int default_np(int L) {
   int np = (L + 8) / 9;
-  if (np < 2) np = 2;
+  return np < 2 ? 2 : np;
+}
+
+static Plan make_plan_np(int L, int np) {
+  Plan p{L, 0, {0, 0, 0, 0, 0}};
   int base = L / np, extra = L % np;
   for (int i = 0; i < np; i++) p.r[i] = base + (i < extra ? 1 : 0);
   p.np = np;
   return p;
 }
 
-// Scratch of one large product.
-struct Scratch {
-  uint64_t* A;     // N words
-  uint64_t* B;     // N words (unused for a square)
-  uint64_t* H;     // high parts of the carry windows, nwin words
-  uint8_t* aux;    // carry-scan flags
-};
+// A plan is valid when every pass radix is 2^6 .. 2^9 (the compiled kernels).
+static bool plan_valid(const Plan& p) {
+  if (p.np < 2 || p.np > 5) return false;
+  for (int i = 0; i < p.np; i++)
+    if (p.r[i] < 6 || p.r[i] > 9) return false;
+  return true;
+}
+
+static Plan make_plan(int L) {
+  int np = (L >= 0 && L <= 32) ? g_tuned_np[L].load(std::memory_order_relaxed) : 0;
+  if (np) {
+    Plan p = make_plan_np(L, np);
+    if (plan_valid(p)) return p;
+  }
+  return make_plan_np(L, default_np(L));
+}
 
 struct Sizes {
-  uint64_t n_out, N, nwin, nchunk, nwarp, aux_bytes;
+  uint64_t n_out, N, nwin, nchunk, aux_bytes;
   int L;
 };
 
@@ -746,13 +844,33 @@ static Sizes sizes_for(uint64_t la, uint64_t lb) {
   z.n_out = 4 * la + 4 * lb - 1;
   z.L = log2_ceil(z.n_out);
   z.N = 1ull << z.L;
-  z.nwin = (z.n_out + 15) / 16;
-  z.nchunk = (z.nwin + CARRY_THREADS - 1) / CARRY_THREADS;
-  z.nwarp = z.nchunk * (CARRY_THREADS / 32);
-  z.aux_bytes = z.nwarp * 8 + z.nchunk * 2 + 64;
+  z.nwin = n_windows(la, lb);
+  z.nchunk = n_chunks(z.nwin);
+  z.aux_bytes = aux_bytes_for(z.nwin);
   return z;
 }
 
+// Scratch bytes of one large product (A, B unless square, H, aux), each
+// piece rounded to 256 bytes.
+static uint64_t round256(uint64_t x) { return (x + 255) & ~255ull; }
+static uint64_t scratch_bytes(uint64_t la, uint64_t lb, bool square) {
+  Sizes z = sizes_for(la, lb);
+  return round256(z.N * 8) * (square ? 1 : 2) + round256(z.nwin * 8) + round256(z.aux_bytes);
+}
+static void carve_scratch(Job& J, uint8_t* base, bool square) {
+  Sizes z = sizes_for(J.la, J.lb);
+  J.A = reinterpret_cast<uint64_t*>(base);
+  base += round256(z.N * 8);
+  if (!square) {
+    J.B = reinterpret_cast<uint64_t*>(base);
+    base += round256(z.N * 8);
+  } else {
+    J.B = nullptr;
+  }
+  J.H = reinterpret_cast<uint64_t*>(base);
+  base += round256(z.nwin * 8);
+  J.aux = base;
+}
 
 // Launch helpers (template dispatch on the pass radix).
 #define PIMUL_DISPATCH_R(r, CALL)          \
@@ -769,71 +887,53 @@ struct Launcher {
   const Roots& R;
 };
 
-static void run_transform_fwd(const Launcher& X, const uint64_t* limbs, uint64_t nl, uint64_t* data,
-                              const Plan& pl, bool last) {
-  const int L = pl.L;
-  const unsigned grid = (unsigned)(1ull << (L - TILE_LOG));
+// All launches of the large-product pipeline for `nj` products sharing the
+// transform length 2^L: the products come from the device array `jobs`
+// (blockIdx.y) or, for nj == 1 and jobs == nullptr, from `one`.
+// max_chunk: largest carry-chunk count among the products.
+static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32_t nj, int L, uint64_t max_chunk) {
+  const Plan pl = make_plan(L);
+  const dim3 grid((unsigned)(1ull << (L - TILE_LOG)), nj);
   const size_t smem = pass_smem_bytes(TILE_LOG);
-  {
-    KTimer kt(K_PACK, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(limbs, nl, data, L, X.R)));
-  }
-  int consumed = pl.r[0];
-  for (int p = 1; p < pl.np - 1; p++) {
-    consumed += pl.r[p];
-    int S = L - consumed;
-    KTimer kt(K_PASS_FWD, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(data, S, X.R)));
-  }
-  if (last) {
-    KTimer kt(K_PASS_FWD, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[pl.np - 1], (k_fwd_last<RR><<<grid, PASS_THREADS, smem, X.st>>>(data, X.R)));
-  }
-}
-
-// out[0 .. la+lb) = a * b for N >= 2^13 using the given scratch.
-static void run_multiply(const Launcher& X, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
-                         uint64_t* d_out, const Scratch& sc, const Sizes& z) {
-  const bool square = d_a == d_b && la == lb;
-  const Plan pl = make_plan(z.L);
-  const unsigned grid = (unsigned)(1ull << (z.L - TILE_LOG));
-  const size_t smem = pass_smem_bytes(TILE_LOG);
-  const uint64_t ninv = hf::pow(hf::pow(2, 191), z.L);  // 2^-L (2^192 = 1)
+  const uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L (2^192 = 1)
   const int rl = pl.r[pl.np - 1];
-  uint64_t* C;
-  if (square) {
-    run_transform_fwd(X, d_a, la, sc.A, pl, false);
-    KTimer kt(K_POINTWISE, X.st, X.stats);
-    PIMUL_DISPATCH_R(rl, (k_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(sc.A, sc.A, ninv, X.R)));
-    C = sc.A;
-  } else {
-    run_transform_fwd(X, d_a, la, sc.A, pl, true);
-    run_transform_fwd(X, d_b, lb, sc.B, pl, false);
-    KTimer kt(K_POINTWISE, X.st, X.stats);
-    PIMUL_DISPATCH_R(rl, (k_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(sc.B, sc.A, ninv, X.R)));
-    C = sc.B;
+  for (int which = 0; which < 2; which++) {
+    {
+      KTimer kt(K_PACK, X.st, X.stats);
+      PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L, X.R)));
+    }
+    int consumed = pl.r[0];
+    for (int p = 1; p < pl.np - 1; p++) {
+      consumed += pl.r[p];
+      KTimer kt(K_PASS_FWD, X.st, X.stats);
+      PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L - consumed, X.R)));
+    }
+    if (which == 0) {
+      KTimer kt(K_PASS_FWD, X.st, X.stats);
+      PIMUL_DISPATCH_R(rl, (k_fwd_last<RR><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, X.R)));
+    }
   }
-  int consumed = z.L - rl;
+  {
+    KTimer kt(K_POINTWISE, X.st, X.stats);
+    PIMUL_DISPATCH_R(rl, (k_mid<RR><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, ninv, X.R)));
+  }
+  int consumed = L - rl;
   for (int p = pl.np - 2; p >= 1; p--) {
-    int S = z.L - consumed;
+    int S = L - consumed;
     consumed -= pl.r[p];
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(C, S, X.R)));
+    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, 2, S, X.R)));
   }
-  const uint64_t nlimbs = la + lb;
   {
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(
-                                  C, z.L, d_out, nlimbs, sc.H, z.nwin, X.R)));
+    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, L, X.R)));
   }
-  uint32_t* masks = reinterpret_cast<uint32_t*>(sc.aux);
-  uint8_t* chunk_gp = sc.aux + z.nwarp * 8;
-  uint8_t* chunk_cin = chunk_gp + z.nchunk;
   {
     KTimer kt(K_CARRY, X.st, X.stats);
-    k_carry_local<<<(unsigned)z.nchunk, CARRY_THREADS, 0, X.st>>>(d_out, nlimbs, sc.H, z.nwin, masks, chunk_gp);
-    k_carry_scan<<<1, SCAN_THREADS, 0, X.st>>>(chunk_gp, z.nchunk, chunk_cin);
-    k_carry_apply<<<(unsigned)z.nchunk, CARRY_THREADS, 0, X.st>>>(z.nwin, d_out, nlimbs, masks, chunk_cin);
+    const dim3 cgrid((unsigned)max_chunk, nj);
+    k_carry_local<<<cgrid, CARRY_THREADS, 0, X.st>>>(jobs, one);
+    k_carry_scan<<<dim3(1, nj), SCAN_THREADS, 0, X.st>>>(jobs, one);
+    k_carry_apply<<<cgrid, CARRY_THREADS, 0, X.st>>>(jobs, one);
   }
   if (X.stats) g_launch[K_CARRY].fetch_add(2, std::memory_order_relaxed);
 }
@@ -850,32 +950,569 @@ static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uin
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
     {
       KTimer kt(K_SMALL, st, true);
-      k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(job, R);
+      k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(nullptr, job, 1, R);
     }
     CU(cudaGetLastError());
     return PIMUL_OK;
   }
-  Scratch sc{nullptr, nullptr, nullptr, nullptr};
-  cudaError_t e = cudaMallocAsync((void**)&sc.A, z.N * 8, g_dev.pool, st);
-  if (e == cudaSuccess && !square) e = cudaMallocAsync((void**)&sc.B, z.N * 8, g_dev.pool, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.H, z.nwin * 8, g_dev.pool, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.aux, z.aux_bytes, g_dev.pool, st);
+  uint8_t* base = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&base, scratch_bytes(la, lb, square), g_dev.pool, st);
   if (e != cudaSuccess) {
-    if (sc.A) cudaFreeAsync(sc.A, st);
-    if (sc.B) cudaFreeAsync(sc.B, st);
-    if (sc.H) cudaFreeAsync(sc.H, st);
     cudaGetLastError();
     return fail(PIMUL_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
   }
+  Job J{d_a, d_b, d_out, nullptr, nullptr, nullptr, nullptr, la, lb};
+  carve_scratch(J, base, square);
   Launcher X{st, true, R};
-  run_multiply(X, d_a, la, d_b, lb, d_out, sc, z);
+  run_large(X, nullptr, J, 1, z.L, z.nchunk);
   cudaError_t le = cudaGetLastError();
-  cudaFreeAsync(sc.A, st);
-  if (sc.B) cudaFreeAsync(sc.B, st);
-  cudaFreeAsync(sc.H, st);
-  cudaFreeAsync(sc.aux, st);
+  cudaFreeAsync(base, st);
   if (le != cudaSuccess) return fail(PIMUL_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
   return PIMUL_OK;
+}
+
+// ------------------------------------------------------------------ batches
+// A batch of independent products on device buffers.  Products are grouped
+// by transform length: lengths up to 2^12 run as one CTA per product in a
+// persistent kernel over a size-sorted list; longer ones run the pass
+// pipeline once per length with one grid row (blockIdx.y) per product.
+struct BatchLayout {
+  std::vector<uint32_t> small;  // job indices, size-sorted descending
+  struct Bucket {
+    int L;
+    std::vector<uint32_t> idx;
+    uint64_t max_chunk;
+  };
+  std::vector<Bucket> large;
+  uint64_t arena_bytes = 0;
+  std::vector<uint64_t> arena_off;  // per job (large only)
+  int small_L = 0;                  // largest L among the small jobs
+};
+
+static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
+  std::vector<int> Ls(n);
+  for (size_t i = 0; i < n; i++) {
+    if (jobs[i].la == 0 || jobs[i].lb == 0) { Ls[i] = -1; continue; }
+    int L = log2_ceil(4 * (uint64_t)jobs[i].la + 4 * (uint64_t)jobs[i].lb - 1);
+    if (L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32 in batch");
+    Ls[i] = L;
+  }
+  B.arena_off.assign(n, 0);
+  std::vector<std::vector<uint32_t>> byL(33);
+  for (size_t i = 0; i < n; i++) {
+    if (Ls[i] < 0) continue;
+    if (Ls[i] <= SMALL_LOG_MAX) {
+      B.small.push_back((uint32_t)i);
+      if (Ls[i] > B.small_L) B.small_L = Ls[i];
+    } else {
+      byL[Ls[i]].push_back((uint32_t)i);
+    }
+  }
+  std::stable_sort(B.small.begin(), B.small.end(), [&](uint32_t x, uint32_t y) {
+    return jobs[x].la + jobs[x].lb > jobs[y].la + jobs[y].lb;
+  });
+  uint64_t off = 0;
+  for (int L = 32; L > SMALL_LOG_MAX; L--) {
+    if (byL[L].empty()) continue;
+    // grid.y is limited to 65535 rows: split big buckets
+    for (size_t s = 0; s < byL[L].size(); s += 65535) {
+      BatchLayout::Bucket bk;
+      bk.L = L;
+      bk.max_chunk = 0;
+      for (size_t k = s; k < byL[L].size() && k < s + 65535; k++) {
+        uint32_t i = byL[L][k];
+        bk.idx.push_back(i);
+        bk.max_chunk = std::max<uint64_t>(bk.max_chunk, n_chunks(n_windows(jobs[i].la, jobs[i].lb)));
+        B.arena_off[i] = off;
+        off += scratch_bytes(jobs[i].la, jobs[i].lb, false);
+      }
+      B.large.push_back(std::move(bk));
+    }
+  }
+  B.arena_bytes = off;
+  return PIMUL_OK;
+}
+
+// Host images of the device descriptors, in launch order: small jobs first,
+// then each large bucket.
+static void fill_descriptors(const pimul_job* jobs, const BatchLayout& B, uint8_t* arena, SmallJob* sd, Job* ld) {
+  size_t k = 0;
+  for (uint32_t i : B.small)
+    sd[k++] = SmallJob{jobs[i].a, jobs[i].b, jobs[i].out, (uint32_t)jobs[i].la, (uint32_t)jobs[i].lb};
+  k = 0;
+  for (const auto& bk : B.large)
+    for (uint32_t i : bk.idx) {
+      Job J{jobs[i].a, jobs[i].b, jobs[i].out, nullptr, nullptr, nullptr, nullptr, jobs[i].la, jobs[i].lb};
+      carve_scratch(J, arena + B.arena_off[i], false);
+      ld[k++] = J;
+    }
+}
+
+static void launch_batch(const Launcher& X, const BatchLayout& B, const SmallJob* d_small, const Job* d_large) {
+  if (!B.small.empty()) {
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_dev.device);
+    uint64_t grid = (uint64_t)sms * (uint64_t)g_small_ctas_per_sm.load();
+    if (grid > B.small.size()) grid = B.small.size();
+    KTimer kt(K_SMALL, X.st, X.stats);
+    k_small_mul<<<(unsigned)grid, SMALL_THREADS, small_smem_bytes(B.small_L), X.st>>>(
+        d_small, SmallJob{}, (uint32_t)B.small.size(), X.R);
+  }
+  size_t off = 0;
+  for (const auto& bk : B.large) {
+    run_large(X, d_large + off, Job{}, (uint32_t)bk.idx.size(), bk.L, bk.max_chunk);
+    off += bk.idx.size();
+  }
+}
+
+static int mul_batch(const pimul_job* jobs, size_t n, cudaStream_t st) {
+  BatchLayout B;
+  int rc = layout_batch(jobs, n, B);
+  if (rc) return rc;
+  const size_t ns = B.small.size();
+  size_t nl = 0;
+  for (const auto& bk : B.large) nl += bk.idx.size();
+  if (ns + nl == 0) return PIMUL_OK;
+  const size_t desc_bytes = round256(ns * sizeof(SmallJob)) + nl * sizeof(Job);
+  uint8_t* dev = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dev, round256(B.arena_bytes) + desc_bytes, g_dev.pool, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("batch scratch allocation: ") + cudaGetErrorString(e));
+  }
+  uint8_t* arena = dev;
+  uint8_t* desc = dev + round256(B.arena_bytes);
+  std::vector<uint8_t> host(desc_bytes);
+  SmallJob* hs = reinterpret_cast<SmallJob*>(host.data());
+  Job* hl = reinterpret_cast<Job*>(host.data() + round256(ns * sizeof(SmallJob)));
+  fill_descriptors(jobs, B, arena, hs, hl);
+  e = cudaMemcpyAsync(desc, host.data(), desc_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    Launcher X{st, true, g_dev.roots};
+    launch_batch(X, B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + round256(ns * sizeof(SmallJob))));
+    e = cudaGetLastError();
+  }
+  // the host image must outlive the copy (pageable source: staged before return)
+  cudaFreeAsync(dev, st);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+// A batch plan: the layout, arena and descriptors of a fixed batch shape,
+// with every launch captured once into a CUDA graph.  Running it writes the
+// new operand pointers into a pinned staging image, and one graph launch
+// copies the descriptors in and runs all kernels.
+struct BatchPlan {
+  std::vector<uint64_t> la, lb;
+  BatchLayout B;
+  uint8_t* dev = nullptr;      // arena + descriptors
+  uint8_t* staging = nullptr;  // pinned host image of the descriptors
+  size_t desc_bytes = 0, ns = 0, nl = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;
+  bool launched = false;
+};
+
+static int plan_create(const size_t* la, const size_t* lb, size_t n, BatchPlan** out) {
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  CU(cudaSetDevice(g_dev.device));
+  auto* P = new BatchPlan();
+  P->la.assign(la, la + n);
+  P->lb.assign(lb, lb + n);
+  // shape-only jobs (distinct dummy pointers: no job is a square)
+  std::vector<pimul_job> shape(n);
+  for (size_t i = 0; i < n; i++) shape[i] = pimul_job{nullptr, la[i], (const uint64_t*)(uintptr_t)(8 + 16 * i), lb[i], nullptr};
+  rc = layout_batch(shape.data(), n, P->B);
+  if (rc) { delete P; return rc; }
+  P->ns = P->B.small.size();
+  for (const auto& bk : P->B.large) P->nl += bk.idx.size();
+  P->desc_bytes = round256(P->ns * sizeof(SmallJob)) + P->nl * sizeof(Job);
+  cudaError_t e = cudaMalloc((void**)&P->dev, round256(P->B.arena_bytes) + P->desc_bytes + 256);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&P->staging, P->desc_bytes + 256);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming);
+  cudaStream_t cs = nullptr;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    uint8_t* desc = P->dev + round256(P->B.arena_bytes);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaMemcpyAsync(desc, P->staging, P->desc_bytes, cudaMemcpyHostToDevice, cs);
+      Launcher X{cs, false, g_dev.roots};
+      launch_batch(X, P->B, reinterpret_cast<SmallJob*>(desc),
+                   reinterpret_cast<Job*>(desc + round256(P->ns * sizeof(SmallJob))));
+      e = cudaStreamEndCapture(cs, &P->graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&P->exec, P->graph, 0);
+  }
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    if (P->graph) cudaGraphDestroy(P->graph);
+    if (P->dev) cudaFree(P->dev);
+    if (P->staging) cudaFreeHost(P->staging);
+    if (P->done) cudaEventDestroy(P->done);
+    delete P;
+    return fail(e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA,
+                std::string("batch plan: ") + cudaGetErrorString(e));
+  }
+  *out = P;
+  return PIMUL_OK;
+}
+
+static int plan_run(BatchPlan* P, const pimul_job* jobs, size_t n, cudaStream_t st) {
+  if (n != P->la.size()) return fail(PIMUL_EINVAL, "batch size differs from the plan");
+  for (size_t i = 0; i < n; i++)
+    if (jobs[i].la != P->la[i] || jobs[i].lb != P->lb[i]) return fail(PIMUL_EINVAL, "job sizes differ from the plan");
+  // the previous run's descriptor copy must have read the staging image
+  if (P->launched) CU(cudaEventSynchronize(P->done));
+  SmallJob* hs = reinterpret_cast<SmallJob*>(P->staging);
+  Job* hl = reinterpret_cast<Job*>(P->staging + round256(P->ns * sizeof(SmallJob)));
+  fill_descriptors(jobs, P->B, P->dev, hs, hl);
+  CU(cudaGraphLaunch(P->exec, st));
+  CU(cudaEventRecord(P->done, st));
+  P->launched = true;
+  return PIMUL_OK;
+}
+
+static void plan_destroy(BatchPlan* P) {
+  if (!P) return;
+  if (P->launched) cudaEventSynchronize(P->done);
+  if (P->exec) cudaGraphExecDestroy(P->exec);
+  if (P->graph) cudaGraphDestroy(P->graph);
+  if (P->dev) cudaFree(P->dev);
+  if (P->staging) cudaFreeHost(P->staging);
+  if (P->done) cudaEventDestroy(P->done);
+  delete P;
+}
+
+// ------------------------------------------------------------------ autotuner
+// Times the candidate pass splits for each length in [Lmin, Lmax] on a
+// batch of `reps` synthetic products (device-resident), keeps the fastest,
+// and tunes the one-CTA kernel's persistent grid on a batch of small
+// products.  The choice only changes the schedule; products are identical.
+static int autotune(int Lmin, int Lmax, int reps, char* report, size_t cap) {
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  cudaStream_t st;
+  rc = get_stream(&st);
+  if (rc) return rc;
+  std::string rep = "{";
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  auto time_batch = [&](std::vector<pimul_job>& js, float* ms_out) -> int {
+    for (int w = 0; w < 2; w++) {
+      int r2 = mul_batch(js.data(), js.size(), st);
+      if (r2) return r2;
+    }
+    cudaEventRecord(e0, st);
+    for (int w = 0; w < 3; w++) {
+      int r2 = mul_batch(js.data(), js.size(), st);
+      if (r2) return r2;
+    }
+    cudaEventRecord(e1, st);
+    CU(cudaEventSynchronize(e1));
+    CU(cudaEventElapsedTime(ms_out, e0, e1));
+    return PIMUL_OK;
+  };
+  // operands: one buffer of random-ish limbs, reused by every synthetic job
+  // large lengths read 2 * max_limbs input words and write reps * 2 * max_limbs;
+  // the small-kernel batch reads 1024 words and writes 4096 * 1024
+  const uint64_t max_limbs = Lmax >= 3 ? (1ull << (Lmax - 3)) : 1;
+  const uint64_t in_words = std::max<uint64_t>(2 * max_limbs, 1024);
+  const uint64_t out_words = std::max<uint64_t>((uint64_t)reps * 2 * max_limbs, 4096ull * 1024);
+  uint64_t* d_in = nullptr;
+  uint64_t* d_out = nullptr;
+  CU(cudaMallocAsync((void**)&d_in, in_words * 8, g_dev.pool, st));
+  CU(cudaMallocAsync((void**)&d_out, out_words * 8, g_dev.pool, st));
+  CU(cudaMemsetAsync(d_in, 0xA5, in_words * 8, st));
+  bool first = true;
+  for (int L = std::max(Lmin, SMALL_LOG_MAX + 1); L <= Lmax && L <= 32; L++) {
+    uint64_t limbs = (1ull << (L - 3)) - 1;  // la = lb: 4(la+lb) - 1 < 2^L
+    std::vector<pimul_job> js(reps);
+    for (int k = 0; k < reps; k++)
+      js[k] = pimul_job{d_in, limbs, d_in + limbs, limbs, d_out + (uint64_t)k * 2 * limbs};
+    int best_np = 0;
+    float best = 1e30f;
+    for (int np = 2; np <= 5; np++) {
+      if (!plan_valid(make_plan_np(L, np))) continue;
+      g_tuned_np[L].store(np);
+      float ms = 0;
+      rc = time_batch(js, &ms);
+      if (rc) break;
+      if (ms < best) { best = ms; best_np = np; }
+    }
+    if (rc) break;
+    g_tuned_np[L].store(best_np);
+    char buf[96];
+    snprintf(buf, sizeof buf, "%s\"np_%d\": %d", first ? "" : ", ", L, best_np);
+    rep += buf;
+    first = false;
+  }
+  if (!rc && Lmin <= SMALL_LOG_MAX) {
+    // small kernel: CTAs per SM for a batch of 4096 products of 16..512 limbs
+    std::vector<pimul_job> js(4096);
+    for (int k = 0; k < 4096; k++) {
+      uint64_t l = 16 + (k * 37) % 497;
+      js[k] = pimul_job{d_in, l, d_in + l, l, d_out + (uint64_t)k * 1024};
+    }
+    int best_c = 4;
+    float best = 1e30f;
+    for (int c : {1, 2, 3, 4, 6, 8}) {
+      g_small_ctas_per_sm.store(c);
+      float ms = 0;
+      rc = time_batch(js, &ms);
+      if (rc) break;
+      if (ms < best) { best = ms; best_c = c; }
+    }
+    g_small_ctas_per_sm.store(best_c);
+    char buf[96];
+    snprintf(buf, sizeof buf, "%s\"small_ctas_per_sm\": %d", first ? "" : ", ", best_c);
+    rep += buf;
+  }
+  rep += "}";
+  cudaFreeAsync(d_in, st);
+  cudaFreeAsync(d_out, st);
+  cudaStreamSynchronize(st);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (report && cap) {
+    strncpy(report, rep.c_str(), cap - 1);
+    report[cap - 1] = 0;
+  }
+  return rc;
+}
+
+// ------------------------------------------------------------------ service
+// Served form: device-resident integers (handles) and an asynchronous
+// multiply service.  submit() queues a request and returns its result handle
+// at once; the handle can feed later requests before it is computed
+// (dependencies are CUDA events, never a host round trip).  A service thread
+// admits queued requests while their memory fits the HBM budget, launches
+// each admitted group as one batch on one of several streams (continuous
+// batching: new requests join as earlier ones complete and release memory,
+// and groups on different streams overlap on the device), and records every
+// request's latency from submit to completion.
+struct SvcHandle {
+  uint64_t* d = nullptr;
+  uint64_t limbs = 0;        // stored length (a product stores la + lb limbs)
+  cudaEvent_t ready = nullptr;  // recorded after the producing batch (or upload)
+  bool pending = false;      // produced by a request not yet launched
+  int64_t producer = -1;     // ticket of the producing request
+  bool freed = false;
+  uint64_t bytes = 0;
+  int readers = 0;           // queued or running requests that read this handle
+};
+
+struct SvcRequest {
+  uint64_t ticket;
+  int op;  // 0 multiply, 1 square
+  uint64_t a, b, out;  // handle ids
+  double t_submit;
+  double t_done = 0;
+  uint64_t scratch = 0;
+  int state = 0;  // 0 queued, 1 launched, 2 done, 3 cancelled
+};
+
+struct SvcBatch {
+  cudaEvent_t done;
+  std::vector<uint64_t> tickets;
+  uint64_t scratch = 0;
+  int stream = 0;
+};
+
+struct Service {
+  std::mutex mu;
+  std::condition_variable cv;       // wakes the service thread
+  std::condition_variable done_cv;  // wakes waiters
+  std::thread th;
+  bool running = false, stop = false;
+  uint64_t budget = 120ull << 30;
+  uint64_t in_use = 0;  // handle bytes + scratch of launched requests
+  uint64_t next_handle = 1, next_ticket = 1;
+  std::unordered_map<uint64_t, SvcHandle> handles;
+  std::unordered_map<uint64_t, SvcRequest> requests;
+  std::deque<uint64_t> queue;
+  std::vector<SvcBatch> inflight;
+  std::vector<cudaStream_t> streams;
+  std::vector<int> stream_busy;
+  std::vector<double> latencies;  // seconds, completed requests
+  uint64_t completed = 0, batches = 0;
+  int max_batch = 4096;
+};
+// Heap-allocated and never destroyed: its thread is joined by an atexit
+// handler (registered after the CUDA runtime's, so it runs first).
+static Service& svc_obj() {
+  static Service* s = new Service();
+  return *s;
+}
+#define g_svc (svc_obj())
+
+static void svc_atexit() {
+  std::unique_lock<std::mutex> lk(g_svc.mu);
+  if (!g_svc.running) return;
+  g_svc.stop = true;
+  g_svc.cv.notify_all();
+  lk.unlock();
+  if (g_svc.th.joinable()) g_svc.th.join();
+  lk.lock();
+  g_svc.running = false;
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static void svc_loop();
+
+static int svc_start() {
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  if (g_svc.running) return PIMUL_OK;
+  CU(cudaSetDevice(g_dev.device));
+  if (g_svc.streams.empty()) {
+    for (int i = 0; i < 4; i++) {
+      cudaStream_t s;
+      CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      g_svc.streams.push_back(s);
+      g_svc.stream_busy.push_back(0);
+    }
+  }
+  g_svc.stop = false;
+  g_svc.running = true;
+  g_svc.th = std::thread(svc_loop);
+  static bool registered = (std::atexit(svc_atexit), true);
+  (void)registered;
+  return PIMUL_OK;
+}
+
+// One iteration's worth of admission: FIFO, stop at the first request whose
+// inputs are not launched yet (its producer is still queued) or that does
+// not fit the budget.
+static void svc_admit(std::unique_lock<std::mutex>& lk) {
+  int si = -1;
+  for (size_t i = 0; i < g_svc.streams.size(); i++)
+    if (!g_svc.stream_busy[i]) { si = (int)i; break; }
+  if (si < 0 || g_svc.queue.empty()) return;
+  std::vector<uint64_t> take;
+  uint64_t add = 0;
+  while (!g_svc.queue.empty() && (int)take.size() < g_svc.max_batch) {
+    uint64_t t = g_svc.queue.front();
+    SvcRequest& r = g_svc.requests[t];
+    SvcHandle& A = g_svc.handles[r.a];
+    SvcHandle& B = g_svc.handles[r.b];
+    bool inputs_launched = !A.pending && !B.pending;
+    if (!inputs_launched) {
+      // a producer inside this same group is fine only if launched before:
+      // keep it simple and start a new group at that point
+      break;
+    }
+    if (g_svc.in_use + add + r.scratch > g_svc.budget && !(take.empty() && g_svc.inflight.empty())) break;
+    take.push_back(t);
+    add += r.scratch;
+    g_svc.queue.pop_front();
+  }
+  if (take.empty()) return;
+  cudaStream_t st = g_svc.streams[si];
+  std::vector<pimul_job> jobs;
+  jobs.reserve(take.size());
+  for (uint64_t t : take) {
+    SvcRequest& r = g_svc.requests[t];
+    SvcHandle& A = g_svc.handles[r.a];
+    SvcHandle& B = g_svc.handles[r.b];
+    SvcHandle& O = g_svc.handles[r.out];
+    if (A.ready) cudaStreamWaitEvent(st, A.ready, 0);
+    if (r.op == 0 && B.ready) cudaStreamWaitEvent(st, B.ready, 0);
+    if (O.ready) cudaStreamWaitEvent(st, O.ready, 0);  // result buffer allocated
+    const uint64_t* pa = A.d;
+    const uint64_t* pb = r.op == 1 ? A.d : B.d;
+    uint64_t lb = r.op == 1 ? A.limbs : B.limbs;
+    jobs.push_back(pimul_job{pa, A.limbs, pb, lb, O.d});
+    r.state = 1;
+  }
+  SvcBatch bt;
+  bt.stream = si;
+  bt.scratch = add;
+  bt.tickets = take;
+  g_svc.in_use += add;
+  lk.unlock();
+  int rc = mul_batch(jobs.data(), jobs.size(), st);
+  cudaEventCreateWithFlags(&bt.done, cudaEventDisableTiming);
+  cudaEventRecord(bt.done, st);
+  lk.lock();
+  for (uint64_t t : take) {
+    SvcRequest& r = g_svc.requests[t];
+    SvcHandle& O = g_svc.handles[r.out];
+    cudaEvent_t e;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    cudaEventRecord(e, st);
+    if (O.ready) cudaEventDestroy(O.ready);
+    O.ready = e;
+    O.pending = false;
+    if (rc) r.state = 3;
+  }
+  g_svc.stream_busy[si] = 1;
+  g_svc.inflight.push_back(std::move(bt));
+  g_svc.batches++;
+}
+
+static void svc_reap(std::unique_lock<std::mutex>& lk) {
+  for (size_t i = 0; i < g_svc.inflight.size();) {
+    SvcBatch& bt = g_svc.inflight[i];
+    if (cudaEventQuery(bt.done) == cudaSuccess) {
+      double t = now_s();
+      for (uint64_t tk : bt.tickets) {
+        SvcRequest& r = g_svc.requests[tk];
+        if (r.state != 3) r.state = 2;
+        r.t_done = t;
+        auto ia = g_svc.handles.find(r.a);
+        if (ia != g_svc.handles.end()) ia->second.readers--;
+        if (r.b != r.a) {
+          auto ib = g_svc.handles.find(r.b);
+          if (ib != g_svc.handles.end()) ib->second.readers--;
+        }
+        g_svc.latencies.push_back(t - r.t_submit);
+        g_svc.completed++;
+      }
+      g_svc.in_use -= bt.scratch;
+      g_svc.stream_busy[bt.stream] = 0;
+      cudaEventDestroy(bt.done);
+      g_svc.inflight.erase(g_svc.inflight.begin() + i);
+      g_svc.done_cv.notify_all();
+    } else {
+      i++;
+    }
+  }
+}
+
+static void svc_loop() {
+  cudaSetDevice(g_dev.device);
+  std::unique_lock<std::mutex> lk(g_svc.mu);
+  while (!g_svc.stop) {
+    svc_reap(lk);
+    svc_admit(lk);
+    if (g_svc.inflight.empty() && g_svc.queue.empty()) {
+      g_svc.cv.wait_for(lk, std::chrono::milliseconds(50));
+    } else {
+      // bounded poll: completions are checked every 20 us while work is in flight
+      g_svc.cv.wait_for(lk, std::chrono::microseconds(20));
+    }
+  }
+}
+
+static uint64_t svc_new_handle(uint64_t limbs, uint64_t* d, bool pending, uint64_t bytes) {
+  uint64_t id = g_svc.next_handle++;
+  SvcHandle h;
+  h.d = d;
+  h.limbs = limbs;
+  h.pending = pending;
+  h.bytes = bytes;
+  g_svc.handles[id] = h;
+  return id;
 }
 
 }  // namespace pimul
@@ -892,6 +1529,17 @@ const char* pimul_last_error(void) { return t_err.c_str(); }
 int pimul_init(int device) { return ensure_init(device); }
 
 int pimul_shutdown(void) {
+  {
+    std::unique_lock<std::mutex> sl(g_svc.mu);
+    if (g_svc.running) {
+      g_svc.stop = true;
+      g_svc.cv.notify_all();
+      sl.unlock();
+      if (g_svc.th.joinable()) g_svc.th.join();
+      sl.lock();
+      g_svc.running = false;
+    }
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_dev.ready) return PIMUL_OK;
   cudaSetDevice(g_dev.device);
@@ -944,6 +1592,252 @@ int pimul_sync(void) {
   int rc = get_stream(&st);
   if (rc) return rc;
   CU(cudaStreamSynchronize(st));
+  return PIMUL_OK;
+}
+
+int pimul_mul_batch(const pimul_job* jobs, size_t n, void* stream) {
+  if (n && !jobs) return fail(PIMUL_EINVAL, "null job list");
+  for (size_t i = 0; i < n; i++)
+    if (jobs[i].la && jobs[i].lb && (!jobs[i].a || !jobs[i].b || !jobs[i].out))
+      return fail(PIMUL_EINVAL, "null device pointer in batch");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  return mul_batch(jobs, n, st);
+}
+
+int pimul_batch_plan_create(const size_t* la, const size_t* lb, size_t n, pimul_batch_plan** plan) {
+  if (!plan || (n && (!la || !lb))) return fail(PIMUL_EINVAL, "null argument");
+  BatchPlan* P = nullptr;
+  int rc = plan_create(la, lb, n, &P);
+  if (rc) return rc;
+  *plan = reinterpret_cast<pimul_batch_plan*>(P);
+  return PIMUL_OK;
+}
+
+int pimul_batch_plan_run(pimul_batch_plan* plan, const pimul_job* jobs, size_t n, void* stream) {
+  if (!plan || (n && !jobs)) return fail(PIMUL_EINVAL, "null argument");
+  for (size_t i = 0; i < n; i++)
+    if (jobs[i].la && jobs[i].lb && (!jobs[i].a || !jobs[i].b || !jobs[i].out))
+      return fail(PIMUL_EINVAL, "null device pointer in batch");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  return plan_run(reinterpret_cast<BatchPlan*>(plan), jobs, n, st);
+}
+
+int pimul_batch_plan_destroy(pimul_batch_plan* plan) {
+  plan_destroy(reinterpret_cast<BatchPlan*>(plan));
+  return PIMUL_OK;
+}
+
+int pimul_autotune(int log_n_min, int log_n_max, int reps, char* report, size_t report_cap) {
+  if (log_n_min < 1 || log_n_max > 28 || log_n_min > log_n_max || reps < 1)
+    return fail(PIMUL_EINVAL, "autotune range must lie in [1, 28] and reps >= 1");
+  return autotune(log_n_min, log_n_max, reps, report, report_cap);
+}
+
+int pimul_tuning_set(int log_n, int passes, int small_ctas_per_sm) {
+  if (log_n >= 0 && log_n <= 32) {
+    if (passes && !plan_valid(make_plan_np(log_n, passes))) return fail(PIMUL_EINVAL, "no kernels for that split");
+    g_tuned_np[log_n].store(passes);
+  }
+  if (small_ctas_per_sm > 0) g_small_ctas_per_sm.store(small_ctas_per_sm);
+  return PIMUL_OK;
+}
+
+int pimul_set_budget(uint64_t bytes) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  g_svc.budget = bytes;
+  return PIMUL_OK;
+}
+
+int pimul_upload(const uint64_t* host, size_t n, uint64_t* handle) {
+  if (!handle || (n && !host)) return fail(PIMUL_EINVAL, "null argument");
+  int rc = svc_start();
+  if (rc) return rc;
+  uint64_t bytes = round256(std::max<uint64_t>(n, 1) * 8);
+  {
+    std::lock_guard<std::mutex> lk(g_svc.mu);
+    if (g_svc.in_use + bytes > g_svc.budget) return fail(PIMUL_ENOMEM, "upload exceeds the HBM budget");
+    g_svc.in_use += bytes;
+  }
+  cudaStream_t st;
+  rc = get_stream(&st);
+  if (rc) return rc;
+  uint64_t* d = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&d, bytes, g_dev.pool, st);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(d, host, n * 8, cudaMemcpyHostToDevice, st);
+  cudaEvent_t ev = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ev, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host buffer may be reused on return
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  if (e != cudaSuccess) {
+    g_svc.in_use -= bytes;
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("upload: ") + cudaGetErrorString(e));
+  }
+  uint64_t id = svc_new_handle(n, d, false, bytes);
+  g_svc.handles[id].ready = ev;
+  *handle = id;
+  return PIMUL_OK;
+}
+
+int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t* ticket) {
+  if (!out_handle || !ticket || (op != PIMUL_OP_MUL && op != PIMUL_OP_SQR)) return fail(PIMUL_EINVAL, "bad argument");
+  int rc = svc_start();
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  auto ia = g_svc.handles.find(a);
+  auto ib = g_svc.handles.find(op == PIMUL_OP_SQR ? a : b);
+  if (ia == g_svc.handles.end() || ib == g_svc.handles.end() || ia->second.freed || ib->second.freed)
+    return fail(PIMUL_ENOTFOUND, "unknown or freed handle");
+  uint64_t la = ia->second.limbs, lb = ib->second.limbs;
+  uint64_t outl = la + lb;
+  uint64_t obytes = round256(std::max<uint64_t>(outl, 1) * 8);
+  uint64_t scratch = (la && lb && sizes_for(la, lb).L > SMALL_LOG_MAX) ? scratch_bytes(la, lb, false) : 0;
+  if (la && lb && sizes_for(la, lb).L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
+  if (obytes + scratch > g_svc.budget) return fail(PIMUL_ENOMEM, "request larger than the HBM budget");
+  uint64_t* d = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync((void**)&d, obytes, g_dev.pool, g_svc.streams[0]);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, obytes, g_svc.streams[0]);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("result allocation: ") + cudaGetErrorString(e));
+  }
+  // the result buffer must exist before any batch stream writes it
+  cudaEvent_t alloc_ev;
+  cudaEventCreateWithFlags(&alloc_ev, cudaEventDisableTiming);
+  cudaEventRecord(alloc_ev, g_svc.streams[0]);
+  g_svc.in_use += obytes;
+  uint64_t oid = svc_new_handle(outl, d, true, obytes);
+  g_svc.handles[oid].ready = alloc_ev;
+  uint64_t t = g_svc.next_ticket++;
+  SvcRequest r;
+  r.ticket = t;
+  r.op = op == PIMUL_OP_SQR ? 1 : 0;
+  r.a = a;
+  r.b = op == PIMUL_OP_SQR ? a : b;
+  r.out = oid;
+  r.t_submit = now_s();
+  r.scratch = scratch;
+  g_svc.handles[oid].producer = (int64_t)t;
+  ia->second.readers++;
+  if (r.b != r.a) g_svc.handles[r.b].readers++;
+  g_svc.requests[t] = r;
+  g_svc.queue.push_back(t);
+  *out_handle = oid;
+  *ticket = t;
+  g_svc.cv.notify_one();
+  return PIMUL_OK;
+}
+
+int pimul_wait(uint64_t ticket, int64_t timeout_us) {
+  std::unique_lock<std::mutex> lk(g_svc.mu);
+  auto it = g_svc.requests.find(ticket);
+  if (it == g_svc.requests.end()) return fail(PIMUL_ENOTFOUND, "unknown ticket");
+  SvcRequest* rp = &it->second;  // element pointers survive rehashing
+  auto pred = [&] { return rp->state >= 2; };
+  if (timeout_us < 0) {
+    g_svc.done_cv.wait(lk, pred);
+  } else if (!g_svc.done_cv.wait_for(lk, std::chrono::microseconds(timeout_us), pred)) {
+    return fail(PIMUL_ETIMEDOUT, "request not finished within the timeout");
+  }
+  return rp->state == 3 ? fail(PIMUL_ECUDA, "request failed") : PIMUL_OK;
+}
+
+int pimul_handle_size(uint64_t handle, size_t* limbs) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  auto it = g_svc.handles.find(handle);
+  if (it == g_svc.handles.end() || it->second.freed || !limbs) return fail(PIMUL_ENOTFOUND, "unknown handle");
+  *limbs = it->second.limbs;
+  return PIMUL_OK;
+}
+
+int pimul_download(uint64_t handle, uint64_t* host, size_t cap, size_t* len) {
+  if (!len) return fail(PIMUL_EINVAL, "null len");
+  uint64_t* d;
+  uint64_t n;
+  cudaEvent_t ready;
+  int64_t producer;
+  {
+    std::lock_guard<std::mutex> lk(g_svc.mu);
+    auto it = g_svc.handles.find(handle);
+    if (it == g_svc.handles.end() || it->second.freed) return fail(PIMUL_ENOTFOUND, "unknown handle");
+    d = it->second.d;
+    n = it->second.limbs;
+    producer = it->second.producer;
+  }
+  if (producer >= 0) {
+    int rc = pimul_wait((uint64_t)producer, -1);
+    if (rc) return rc;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_svc.mu);
+    ready = g_svc.handles[handle].ready;
+  }
+  if (cap < n) return fail(PIMUL_EINVAL, "capacity below the stored length");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (ready) CU(cudaStreamWaitEvent(st, ready, 0));
+  if (n) CU(cudaMemcpyAsync(host, d, n * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  size_t m = n;
+  while (m && host[m - 1] == 0) m--;
+  *len = m;
+  return PIMUL_OK;
+}
+
+int pimul_free(uint64_t handle) {
+  std::unique_lock<std::mutex> lk(g_svc.mu);
+  auto it = g_svc.handles.find(handle);
+  if (it == g_svc.handles.end() || it->second.freed) return fail(PIMUL_ENOTFOUND, "unknown or already freed handle");
+  int64_t producer = it->second.producer;
+  lk.unlock();
+  if (producer >= 0) pimul_wait((uint64_t)producer, -1);
+  lk.lock();
+  // requests that read the handle must finish first
+  g_svc.done_cv.wait(lk, [&] {
+    auto f = g_svc.handles.find(handle);
+    return f == g_svc.handles.end() || f->second.readers <= 0;
+  });
+  auto f = g_svc.handles.find(handle);
+  if (f == g_svc.handles.end()) return fail(PIMUL_ENOTFOUND, "handle freed concurrently");
+  SvcHandle& h = f->second;
+  if (h.ready) {
+    cudaStreamWaitEvent(g_svc.streams[0], h.ready, 0);
+    cudaEventDestroy(h.ready);
+  }
+  cudaFreeAsync(h.d, g_svc.streams[0]);
+  g_svc.in_use -= h.bytes;
+  h.freed = true;
+  h.d = nullptr;
+  g_svc.handles.erase(handle);
+  return PIMUL_OK;
+}
+
+int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uint64_t* batches, uint64_t* in_use) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  std::vector<double> v = g_svc.latencies;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double q) { return v.empty() ? 0.0 : 1e3 * v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };
+  if (p50_ms) *p50_ms = pct(0.50);
+  if (p99_ms) *p99_ms = pct(0.99);
+  if (completed) *completed = g_svc.completed;
+  if (batches) *batches = g_svc.batches;
+  if (in_use) *in_use = g_svc.in_use;
+  return PIMUL_OK;
+}
+
+int pimul_service_reset_stats(void) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  g_svc.latencies.clear();
+  g_svc.completed = 0;
+  g_svc.batches = 0;
   return PIMUL_OK;
 }
 
@@ -1030,6 +1924,8 @@ constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;
 constexpr uint64_t NOALLOC_WIN_MAX = NOALLOC_N_MAX / 16;
 constexpr uint64_t NOALLOC_CHUNK_MAX = (NOALLOC_WIN_MAX + CARRY_THREADS - 1) / CARRY_THREADS;
 constexpr uint64_t NOALLOC_AUX_WORDS = (NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64) / 8 + 1;
+static_assert(NOALLOC_AUX_WORDS * 8 >= NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64,
+              "no-alloc carry flags must fit");
 
 static __device__ __align__(256) uint64_t g_noalloc_scratch[2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX + NOALLOC_AUX_WORDS];
 static __device__ __align__(256) uint64_t g_noalloc_roots[ROOT_WORDS];
@@ -1076,17 +1972,18 @@ static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* 
   const Roots& R = nd->roots;
   if (z.L <= SMALL_LOG_MAX) {  // whole product in one CTA's shared memory: no scratch
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
-    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(job, R);
+    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(nullptr, job, 1, R);
     CU(cudaGetLastError());
     return PIMUL_OK;
   }
-  Scratch sc;
-  sc.A = nd->scratch;
-  sc.B = nd->scratch + NOALLOC_N_MAX;
-  sc.H = nd->scratch + 2 * NOALLOC_N_MAX;
-  sc.aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX);
+  const bool square = d_a == d_b && la == lb;
+  Job J{d_a, d_b, d_out, nullptr, nullptr, nullptr, nullptr, la, lb};
+  J.A = nd->scratch;
+  J.B = square ? nullptr : nd->scratch + NOALLOC_N_MAX;
+  J.H = nd->scratch + 2 * NOALLOC_N_MAX;
+  J.aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX);
   Launcher X{st, false, R};  // no statistics hook: its event timing would create CUDA events
-  run_multiply(X, d_a, la, d_b, lb, d_out, sc, z);
+  run_large(X, nullptr, J, 1, z.L, z.nchunk);
   CU(cudaGetLastError());
   return PIMUL_OK;
 }

@@ -1,0 +1,834 @@
+// Host side above the C ABI: the reference's pi pipeline restated in C++,
+// with every large product routed through the GPU multiply.
+//
+// This is the caller of the drop-in (crates/bignum/src/integer.rs:445
+// mul_mag -> ntt.rs:806 mul_mag_ntt) in the three places pi-core uses it:
+// Chudnovsky binary splitting, the final assembly's Newton reciprocal and
+// square root, and the decimal conversion's Newton divisions.  It mirrors
+// the reference's algorithms and thresholds:
+//   * mul_mag dispatch: schoolbook below 32 limbs, Karatsuba below the NTT
+//     threshold (8192 limbs of the smaller operand), else the NTT multiply
+//     (crates/bignum/src/integer.rs:445-608, config.rs:94-127);
+//   * Float: sign * mantissa * 2^exp, round-half-up to prec bits
+//     (crates/bignum/src/float.rs:524-569), precision-doubling Newton for
+//     the reciprocal (float.rs:417-474) and the square root (float.rs:85-174);
+//   * Integer division: Knuth D below 64 limbs, Newton reciprocal above
+//     (integer.rs:702-827, 1031-1083); decimal conversion by divide and
+//     conquer on powers of ten (integer.rs:892-983);
+//   * Chudnovsky: n_terms = ceil(D / 14.1816...) + 8, binary splitting without
+//     the root P, pi = 426880 sqrt(10005) Q / (A Q + T), digits by scaling
+//     with 10^(D-1) and truncating (crates/pi-core/src/algorithm/
+//     chudnovsky.rs:75-413, util.rs:25-83, precision.rs:45-70).
+// The multiply backend is pluggable (C ABI pimul_pi_chudnovsky): the GPU
+// engine by default, or any function with pimul_mul's signature.
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/pimul.h"
+
+namespace pihost {
+
+typedef unsigned __int128 u128;
+using Limbs = std::vector<uint64_t>;
+
+// ------------------------------------------------------------------ config
+static size_t g_karatsuba_threshold = 32;   // config.rs:101
+static size_t g_ntt_threshold = 8192;       // config.rs:103
+static size_t g_newton_div_threshold = 64;  // config.rs:104
+static size_t g_to_string_dc_threshold = 32;  // config.rs:105
+static const uint64_t PARALLEL_SPLIT = 64;  // pi-core config.rs:61
+
+typedef int (*mul_fn)(const uint64_t*, size_t, const uint64_t*, size_t, uint64_t*, size_t, size_t*);
+static mul_fn g_backend = nullptr;
+static std::atomic<uint64_t> g_ntt_calls{0};
+static std::atomic<uint64_t> g_ntt_hist[33];
+static std::atomic<int> g_error{0};
+static std::string g_errmsg;
+
+// ------------------------------------------------------------------ magnitudes
+static void trim(Limbs& a) {
+  while (!a.empty() && a.back() == 0) a.pop_back();
+}
+
+static uint64_t bits_of(const Limbs& a) {
+  if (a.empty()) return 0;
+  return (a.size() - 1) * 64 + (64 - __builtin_clzll(a.back()));
+}
+
+static int cmp_mag(const Limbs& a, const Limbs& b) {
+  if (a.size() != b.size()) return a.size() < b.size() ? -1 : 1;
+  for (size_t i = a.size(); i-- > 0;)
+    if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+  return 0;
+}
+
+static Limbs add_mag(const Limbs& a, const Limbs& b) {  // integer.rs:351-365
+  const Limbs& L = a.size() >= b.size() ? a : b;
+  const Limbs& S = a.size() >= b.size() ? b : a;
+  Limbs out(L.size() + 1);
+  u128 c = 0;
+  for (size_t i = 0; i < L.size(); i++) {
+    c += (u128)L[i] + (i < S.size() ? S[i] : 0);
+    out[i] = (uint64_t)c;
+    c >>= 64;
+  }
+  out[L.size()] = (uint64_t)c;
+  trim(out);
+  return out;
+}
+
+static Limbs sub_mag(const Limbs& a, const Limbs& b) {  // a >= b, integer.rs:368-389
+  Limbs out(a.size());
+  uint64_t borrow = 0;
+  for (size_t i = 0; i < a.size(); i++) {
+    uint64_t bi = i < b.size() ? b[i] : 0;
+    uint64_t d = a[i] - bi - borrow;
+    borrow = (a[i] < bi) || (a[i] - bi < borrow);
+    out[i] = d;
+  }
+  trim(out);
+  return out;
+}
+
+static Limbs shl_mag(const Limbs& a, uint64_t s) {  // integer.rs:1097-1125
+  if (a.empty()) return {};
+  size_t w = s / 64, r = s % 64;
+  Limbs out(a.size() + w + 1, 0);
+  for (size_t i = 0; i < a.size(); i++) {
+    out[i + w] |= a[i] << r;
+    if (r) out[i + w + 1] |= a[i] >> (64 - r);
+  }
+  trim(out);
+  return out;
+}
+
+static Limbs shr_mag(const Limbs& a, uint64_t s) {  // integer.rs:1127-1155
+  size_t w = s / 64, r = s % 64;
+  if (w >= a.size()) return {};
+  Limbs out(a.size() - w);
+  for (size_t i = 0; i < out.size(); i++) {
+    uint64_t lo = a[i + w] >> r;
+    uint64_t hi = (r && i + w + 1 < a.size()) ? a[i + w + 1] << (64 - r) : 0;
+    out[i] = lo | hi;
+  }
+  trim(out);
+  return out;
+}
+
+static bool has_low_bits(const Limbs& a, uint64_t n) {  // float.rs:615-634
+  if (n == 0 || a.empty()) return false;
+  size_t full = n / 64;
+  for (size_t i = 0; i < full && i < a.size(); i++)
+    if (a[i]) return true;
+  unsigned r = n % 64;
+  if (r && full < a.size() && (a[full] & ((1ull << r) - 1))) return true;
+  return false;
+}
+
+static uint64_t bit_at(const Limbs& a, uint64_t i) {
+  size_t l = i / 64;
+  return l < a.size() ? (a[l] >> (i % 64)) & 1 : 0;
+}
+
+// ------------------------------------------------------------------ multiply
+static Limbs mul_schoolbook(const Limbs& a, const Limbs& b) {  // integer.rs:492-520
+  if (a.empty() || b.empty()) return {};
+  Limbs out(a.size() + b.size(), 0);
+  for (size_t i = 0; i < a.size(); i++) {
+    u128 carry = 0;
+    for (size_t j = 0; j < b.size(); j++) {
+      u128 cur = (u128)out[i + j] + (u128)a[i] * b[j] + carry;
+      out[i + j] = (uint64_t)cur;
+      carry = cur >> 64;
+    }
+    size_t k = i + b.size();
+    while (carry) {
+      u128 cur = (u128)out[k] + carry;
+      out[k] = (uint64_t)cur;
+      carry = cur >> 64;
+      k++;
+    }
+  }
+  trim(out);
+  return out;
+}
+
+static Limbs mul_mag(const Limbs& a, const Limbs& b);
+
+static void add_at(Limbs& d, const Limbs& s, size_t off) {  // integer.rs:612-635
+  if (s.empty()) return;
+  if (d.size() < off + s.size()) d.resize(off + s.size(), 0);
+  u128 c = 0;
+  for (size_t i = 0; i < s.size(); i++) {
+    c += (u128)d[off + i] + s[i];
+    d[off + i] = (uint64_t)c;
+    c >>= 64;
+  }
+  for (size_t k = off + s.size(); c; k++) {
+    if (k >= d.size()) d.push_back(0);
+    c += d[k];
+    d[k] = (uint64_t)c;
+    c >>= 64;
+  }
+}
+
+static Limbs mul_karatsuba(const Limbs& a, const Limbs& b) {  // integer.rs:552-608
+  size_t n = std::max(a.size(), b.size()), m = n / 2;
+  Limbs alo(a.begin(), a.begin() + std::min(m, a.size())), ahi(a.begin() + std::min(m, a.size()), a.end());
+  Limbs blo(b.begin(), b.begin() + std::min(m, b.size())), bhi(b.begin() + std::min(m, b.size()), b.end());
+  Limbs z0 = mul_mag(alo, blo);
+  Limbs z2 = mul_mag(ahi, bhi);
+  Limbs as = alo, bs = blo;
+  trim(as);
+  trim(bs);
+  Limbs ah = ahi, bh = bhi;
+  trim(ah);
+  trim(bh);
+  Limbs z1 = mul_mag(add_mag(as, ah), add_mag(bs, bh));
+  Limbs z02 = add_mag(z0, z2);
+  z1 = sub_mag(z1, z02);
+  Limbs out(a.size() + b.size() + 1, 0);
+  add_at(out, z0, 0);
+  add_at(out, z1, m);
+  add_at(out, z2, 2 * m);
+  trim(out);
+  return out;
+}
+
+static Limbs mul_ntt(const Limbs& a, const Limbs& b) {
+  Limbs out(a.size() + b.size());
+  size_t n = 0;
+  int rc = g_backend ? g_backend(a.data(), a.size(), b.data(), b.size(), out.data(), out.size(), &n)
+                     : pimul_mul(a.data(), a.size(), b.data(), b.size(), out.data(), out.size(), &n);
+  if (rc) {
+    g_error.store(rc);
+    return {};
+  }
+  uint64_t L = 0;
+  while ((1ull << L) < 4 * (a.size() + b.size()) - 1) L++;
+  g_ntt_calls.fetch_add(1, std::memory_order_relaxed);
+  g_ntt_hist[L].fetch_add(1, std::memory_order_relaxed);
+  out.resize(n);
+  return out;
+}
+
+// integer.rs:460-486 (with the 2^32-coefficient cap of integer.rs:445-453)
+static Limbs mul_mag(const Limbs& a0, const Limbs& b0) {
+  if (a0.empty() || b0.empty()) return {};
+  size_t smaller = std::min(a0.size(), b0.size());
+  bool fits = (a0.size() + b0.size()) * 4 <= (1ull << 32);
+  if (fits && smaller >= g_ntt_threshold) return mul_ntt(a0, b0);
+  if (smaller < g_karatsuba_threshold) return mul_schoolbook(a0, b0);
+  return mul_karatsuba(a0, b0);
+}
+
+static Limbs mul_small(const Limbs& a, uint64_t s) {
+  if (a.empty() || s == 0) return {};
+  Limbs out(a.size() + 1);
+  u128 c = 0;
+  for (size_t i = 0; i < a.size(); i++) {
+    c += (u128)a[i] * s;
+    out[i] = (uint64_t)c;
+    c >>= 64;
+  }
+  out[a.size()] = (uint64_t)c;
+  trim(out);
+  return out;
+}
+
+// ------------------------------------------------------------------ Integer
+struct Int {
+  Limbs m;
+  bool neg = false;
+  Int() {}
+  explicit Int(uint64_t v) {
+    if (v) m.push_back(v);
+  }
+  Int(Limbs l, bool n) : m(std::move(l)), neg(n) {
+    trim(m);
+    if (m.empty()) neg = false;
+  }
+  bool zero() const { return m.empty(); }
+};
+
+static Int add(const Int& a, const Int& b) {  // integer.rs:391-421
+  if (a.neg == b.neg) return Int(add_mag(a.m, b.m), a.neg);
+  int c = cmp_mag(a.m, b.m);
+  if (c == 0) return Int();
+  if (c > 0) return Int(sub_mag(a.m, b.m), a.neg);
+  return Int(sub_mag(b.m, a.m), b.neg);
+}
+static Int neg(Int a) {
+  if (!a.zero()) a.neg = !a.neg;
+  return a;
+}
+static Int sub(const Int& a, const Int& b) { return add(a, neg(b)); }
+static Int mul(const Int& a, const Int& b) {  // integer.rs:637-643
+  return Int(mul_mag(a.m, b.m), a.neg != b.neg);
+}
+static Int mulu(const Int& a, uint64_t s) { return Int(mul_small(a.m, s), a.neg); }
+
+// Knuth algorithm D (integer.rs:702-827), magnitudes, b nonzero.
+static void divrem_knuth(const Limbs& a, const Limbs& b, Limbs& q, Limbs& r) {
+  if (cmp_mag(a, b) < 0) {
+    q.clear();
+    r = a;
+    return;
+  }
+  if (b.size() == 1) {
+    q.assign(a.size(), 0);
+    u128 rem = 0;
+    for (size_t i = a.size(); i-- > 0;) {
+      u128 cur = (rem << 64) | a[i];
+      q[i] = (uint64_t)(cur / b[0]);
+      rem = cur % b[0];
+    }
+    trim(q);
+    r.clear();
+    if (rem) r.push_back((uint64_t)rem);
+    return;
+  }
+  size_t n = b.size(), m = a.size() - n;
+  int d = __builtin_clzll(b[n - 1]);
+  Limbs v = d ? shl_mag(b, d) : b;
+  Limbs u = d ? shl_mag(a, d) : a;
+  u.resize(a.size() + 1, 0);
+  uint64_t vt = v[n - 1], vn = v[n - 2];
+  q.assign(m + 1, 0);
+  for (size_t j = m + 1; j-- > 0;) {
+    u128 num = ((u128)u[j + n] << 64) | u[j + n - 1];
+    u128 qhat, rhat;
+    if (u[j + n] >= vt) {
+      qhat = UINT64_MAX;
+      rhat = num - qhat * vt;
+    } else {
+      qhat = num / vt;
+      rhat = num % vt;
+    }
+    while (rhat < ((u128)1 << 64)) {
+      if ((u128)(uint64_t)qhat * vn <= ((rhat << 64) | u[j + n - 2])) break;
+      qhat--;
+      rhat += vt;
+    }
+    // u[j..j+n] -= qhat * v
+    u128 carry = 0;
+    int64_t borrow = 0;
+    for (size_t i = 0; i < n; i++) {
+      u128 p = (u128)(uint64_t)qhat * v[i] + carry;
+      carry = p >> 64;
+      __int128 t = (__int128)u[i + j] - (uint64_t)p - borrow;
+      borrow = t < 0;
+      u[i + j] = (uint64_t)t;
+    }
+    __int128 t = (__int128)u[j + n] - (__int128)carry - borrow;
+    u[j + n] = (uint64_t)t;
+    if (t < 0) {  // add back
+      qhat--;
+      u128 c = 0;
+      for (size_t i = 0; i < n; i++) {
+        c += (u128)u[i + j] + v[i];
+        u[i + j] = (uint64_t)c;
+        c >>= 64;
+      }
+      u[j + n] += (uint64_t)c;
+    }
+    q[j] = (uint64_t)qhat;
+  }
+  u.resize(n);
+  r = d ? shr_mag(u, d) : u;
+  trim(r);
+  trim(q);
+}
+
+// ------------------------------------------------------------------ Float
+struct Flt {
+  uint64_t prec = 64;
+  bool sign = false;
+  Limbs mant;
+  int64_t exp = 0;
+  bool zero() const { return mant.empty(); }
+};
+
+static void round_to_prec(Flt& f) {  // float.rs:524-569 (round half up)
+  if (f.mant.empty()) {
+    f.sign = false;
+    f.exp = 0;
+    return;
+  }
+  uint64_t b = bits_of(f.mant);
+  if (b <= f.prec) return;
+  uint64_t drop = b - f.prec;
+  uint64_t rb = bit_at(f.mant, drop - 1);
+  Limbs nl = shr_mag(f.mant, drop);
+  if (rb) nl = add_mag(nl, Limbs{1});
+  f.mant = nl;
+  f.exp += (int64_t)drop;
+  uint64_t nb = bits_of(f.mant);
+  if (nb > f.prec) {
+    uint64_t extra = nb - f.prec;
+    f.mant = shr_mag(f.mant, extra);
+    f.exp += (int64_t)extra;
+  }
+}
+
+static Flt flt_from_u64(uint64_t v, uint64_t prec) {
+  Flt f;
+  f.prec = prec;
+  if (v) f.mant.push_back(v);
+  round_to_prec(f);
+  return f;
+}
+
+static Flt flt_from_int(const Int& v) {  // float.rs From<Integer>
+  Flt f;
+  f.sign = v.neg;
+  f.mant = v.m;
+  f.prec = std::max<uint64_t>(bits_of(v.m), 64);
+  return f;
+}
+
+static Flt flt_from_f64(double v, uint64_t prec) {  // float.rs:571-593
+  Flt f;
+  f.prec = prec;
+  if (v == 0.0) return f;
+  uint64_t bits;
+  memcpy(&bits, &v, 8);
+  f.sign = (bits >> 63) & 1;
+  int64_t raw_exp = (bits >> 52) & 0x7FF;
+  uint64_t raw = bits & ((1ull << 52) - 1);
+  uint64_t mu;
+  if (raw_exp == 0) {
+    mu = raw;
+    f.exp = -1074;
+  } else {
+    mu = raw | (1ull << 52);
+    f.exp = raw_exp - 1023 - 52;
+  }
+  f.mant = Limbs{mu};
+  trim(f.mant);
+  round_to_prec(f);
+  return f;
+}
+
+static void to_f64_with_exp(const Limbs& a, double& m, int64_t& e) {  // integer.rs:187-215
+  uint64_t tb = bits_of(a);
+  if (tb <= 53) {
+    uint64_t v = a.empty() ? 0 : a[0];
+    int64_t x = (int64_t)tb - 1;
+    m = (double)v * std::ldexp(1.0, -(int)x);
+    e = x;
+  } else {
+    uint64_t drop = tb - 53;
+    Limbs t = shr_mag(a, drop);
+    uint64_t top = t.empty() ? 0 : t[0];
+    m = (double)top * std::ldexp(1.0, -52);
+    e = (int64_t)drop + 52;
+  }
+}
+
+static Flt truncated_to_prec(const Flt& s, uint64_t prec) {  // float.rs:485-518
+  Flt out;
+  out.prec = prec;
+  if (s.zero()) return out;
+  if (bits_of(s.mant) <= prec) {
+    out = s;
+    out.prec = prec;
+    return out;
+  }
+  size_t keep = (prec + 64) / 64 + 1;
+  if (keep >= s.mant.size()) {
+    out = s;
+    out.prec = prec;
+    round_to_prec(out);
+    return out;
+  }
+  size_t drop = s.mant.size() - keep;
+  out.sign = s.sign;
+  out.mant.assign(s.mant.begin() + drop, s.mant.end());
+  out.exp = s.exp + (int64_t)drop * 64;
+  round_to_prec(out);
+  return out;
+}
+
+static Flt mul_at_prec(const Flt& a, const Flt& b, uint64_t prec) {  // float.rs:331-344
+  Flt out;
+  out.prec = prec;
+  if (a.zero() || b.zero()) return out;
+  out.mant = mul_mag(a.mant, b.mant);
+  out.exp = a.exp + b.exp;
+  out.sign = a.sign != b.sign;
+  round_to_prec(out);
+  return out;
+}
+
+static Flt add_at_prec(const Flt& a, const Flt& b, uint64_t prec) {  // float.rs:284-323
+  if (a.zero()) {
+    Flt r = b;
+    r.prec = prec;
+    round_to_prec(r);
+    return r;
+  }
+  if (b.zero()) {
+    Flt r = a;
+    r.prec = prec;
+    round_to_prec(r);
+    return r;
+  }
+  Limbs am = a.mant, bm = b.mant;
+  int64_t ae = a.exp, be = b.exp;
+  if (ae > be) {
+    am = shl_mag(am, (uint64_t)(ae - be));
+    ae = be;
+  } else if (be > ae) {
+    bm = shl_mag(bm, (uint64_t)(be - ae));
+  }
+  Int s = add(Int(am, a.sign), Int(bm, b.sign));
+  Flt out;
+  out.prec = prec;
+  out.sign = s.neg;
+  out.mant = s.m;
+  out.exp = ae;
+  round_to_prec(out);
+  return out;
+}
+
+static Flt sub_at_prec(const Flt& a, const Flt& b, uint64_t prec) {
+  Flt nb = b;
+  if (!nb.zero()) nb.sign = !nb.sign;
+  return add_at_prec(a, nb, prec);
+}
+
+// Newton reciprocal with precision doubling and one extra iteration at
+// the cap (float.rs:417-474).
+static Flt reciprocal_at_prec(const Flt& self, uint64_t target) {
+  Flt mag = self;
+  mag.sign = false;
+  double m;
+  int64_t e;
+  to_f64_with_exp(mag.mant, m, e);
+  Flt x = flt_from_f64(1.0 / m, 64);
+  x.exp += -(e + mag.exp);
+  round_to_prec(x);
+  uint64_t cur = 64;
+  int full = 0;
+  while (true) {
+    cur = std::min(cur * 2, target + 16);
+    Flt b = truncated_to_prec(mag, cur);
+    x.prec = cur;
+    round_to_prec(x);
+    Flt bx = mul_at_prec(b, x, cur + 8);
+    Flt two = flt_from_f64(2.0, cur + 8);
+    Flt t = sub_at_prec(two, bx, cur + 8);
+    x = mul_at_prec(x, t, cur);
+    if (cur >= target + 16 && ++full >= 2) break;
+  }
+  x.prec = target;
+  round_to_prec(x);
+  x.sign = self.sign;
+  return x;
+}
+
+static Flt div_at_prec(const Flt& a, const Flt& b, uint64_t prec) {  // float.rs:360-373
+  if (a.zero()) {
+    Flt z;
+    z.prec = prec;
+    return z;
+  }
+  Flt r = reciprocal_at_prec(b, prec + 16);
+  return mul_at_prec(a, r, prec);
+}
+
+// Newton square root with precision doubling (float.rs:85-174).
+static void sqrt_mut(Flt& self) {
+  if (self.zero()) return;
+  uint64_t target = self.prec;
+  double m;
+  int64_t e;
+  to_f64_with_exp(self.mant, m, e);
+  int64_t tot = e + self.exp;
+  int64_t half = tot >= 0 ? tot / 2 : -((-tot + 1) / 2);
+  int64_t left = tot - 2 * half;
+  double mc = left == 0 ? m : m * 2.0;
+  uint64_t cur = 64;
+  Flt x = flt_from_f64(std::sqrt(mc), cur);
+  x.exp += half;
+  round_to_prec(x);
+  int full = 0;
+  while (true) {
+    cur = std::min(cur * 2, target + 16);
+    Flt n = truncated_to_prec(self, cur);
+    x.prec = cur;
+    round_to_prec(x);
+    Flt d = div_at_prec(n, x, cur + 8);
+    Flt s = add_at_prec(x, d, cur + 8);
+    s.exp -= 1;
+    s.prec = cur;
+    round_to_prec(s);
+    x = s;
+    if (cur >= target + 16 && ++full >= 2) break;
+  }
+  x.prec = target;
+  round_to_prec(x);
+  self = x;
+}
+
+static Flt pow_int(const Flt& base0, const Int& ex) {  // float.rs:246-270
+  uint64_t prec = base0.prec;
+  Flt result = flt_from_u64(1, prec);
+  if (ex.zero()) return result;
+  Flt base = base0;
+  uint64_t nb = bits_of(ex.m);
+  for (uint64_t i = 0; i < nb; i++) {
+    if (bit_at(ex.m, i)) result = mul_at_prec(result, base, prec);
+    if (i + 1 < nb) base = mul_at_prec(base, base, prec);
+  }
+  return result;
+}
+
+static Int to_integer_down(const Flt& f) {  // float.rs:199-241 (non-negative use)
+  if (f.zero()) return Int();
+  if (f.exp >= 0) return Int(f.exp ? shl_mag(f.mant, (uint64_t)f.exp) : f.mant, f.sign);
+  uint64_t s = (uint64_t)(-f.exp);
+  Limbs t = shr_mag(f.mant, s);
+  bool low = has_low_bits(f.mant, s);
+  Int r(t, false);
+  if (f.sign && (!r.zero() || low)) {
+    if (low) r = add(r, Int(1));
+    r.neg = !r.zero();
+  }
+  return r;
+}
+
+// ------------------------------------------------------------------ division
+static void divrem(const Int& a, const Int& b, Int& q, Int& r);
+
+static void divrem_newton(const Int& a, const Int& b, Int& q, Int& r) {  // integer.rs:1031-1083
+  uint64_t ab = bits_of(a.m), bb = bits_of(b.m);
+  uint64_t qb = ab - bb + 1, prec = qb + 64;
+  Flt recip = reciprocal_at_prec(flt_from_int(b), prec);
+  Flt at = truncated_to_prec(flt_from_int(a), prec);
+  Flt qf = mul_at_prec(at, recip, prec);
+  q = to_integer_down(qf);
+  r = sub(a, mul(q, b));
+  while (r.neg && !r.zero()) {
+    q = sub(q, Int(1));
+    r = add(r, b);
+  }
+  while (!r.neg && cmp_mag(r.m, b.m) >= 0) {
+    q = add(q, Int(1));
+    r = sub(r, b);
+  }
+}
+
+static void divrem(const Int& a, const Int& b, Int& q, Int& r) {  // integer.rs:1004-1029
+  if (b.m.size() >= g_newton_div_threshold && a.m.size() >= g_newton_div_threshold && cmp_mag(a.m, b.m) >= 0) {
+    divrem_newton(a, b, q, r);
+    return;
+  }
+  Limbs ql, rl;
+  divrem_knuth(a.m, b.m, ql, rl);
+  q = Int(ql, false);
+  r = Int(rl, false);
+}
+
+static Int pow_u(uint64_t base, uint64_t e) {  // integer.rs:68-82
+  Int result(1), b(base);
+  while (e) {
+    if (e & 1) result = mul(result, b);
+    e >>= 1;
+    if (e) b = mul(b, b);
+  }
+  return result;
+}
+
+// ------------------------------------------------------------------ decimal
+static const uint64_t DEC_CHUNK = 10000000000000000000ull;  // 10^19 (integer.rs:887-888)
+
+static std::string decimal_naive(Limbs mag) {  // integer.rs:968-983
+  std::vector<uint64_t> chunks;
+  while (!mag.empty()) {
+    u128 rem = 0;
+    for (size_t i = mag.size(); i-- > 0;) {
+      u128 cur = (rem << 64) | mag[i];
+      mag[i] = (uint64_t)(cur / DEC_CHUNK);
+      rem = cur % DEC_CHUNK;
+    }
+    trim(mag);
+    chunks.push_back((uint64_t)rem);
+  }
+  std::string out = std::to_string(chunks.back());
+  char buf[32];
+  for (size_t i = chunks.size() - 1; i-- > 0;) {
+    snprintf(buf, sizeof buf, "%019llu", (unsigned long long)chunks[i]);
+    out += buf;
+  }
+  return out;
+}
+
+static uint64_t dec_estimate(uint64_t bits) { return (uint64_t)std::ceil((double)bits * 0.301029995663981); }
+
+static std::string to_decimal_padded(const Int& n, size_t want);
+
+static std::string to_decimal_top(const Int& n) {  // integer.rs:892-930
+  if (n.m.size() <= g_to_string_dc_threshold) return decimal_naive(n.m);
+  uint64_t m = dec_estimate(bits_of(n.m)) / 2;
+  if (m == 0) return decimal_naive(n.m);
+  Int sp = pow_u(10, m), hi, lo;
+  divrem(n, sp, hi, lo);
+  std::string hs, ls;
+  if (n.m.size() >= 4096) {
+    std::thread t([&] { ls = to_decimal_padded(lo, m); });
+    hs = to_decimal_top(hi);
+    t.join();
+  } else {
+    hs = to_decimal_top(hi);
+    ls = to_decimal_padded(lo, m);
+  }
+  return hs + ls;
+}
+
+static std::string to_decimal_padded(const Int& n, size_t want) {  // integer.rs:932-964
+  if (n.zero()) return std::string(want, '0');
+  if (n.m.size() <= g_to_string_dc_threshold) {
+    std::string s = decimal_naive(n.m);
+    return std::string(want - s.size(), '0') + s;
+  }
+  size_t m = want / 2;
+  Int sp = pow_u(10, m), hi, lo;
+  divrem(n, sp, hi, lo);
+  std::string hs, ls;
+  if (n.m.size() >= 4096) {
+    std::thread t([&] { ls = to_decimal_padded(lo, m); });
+    hs = to_decimal_padded(hi, want - m);
+    t.join();
+  } else {
+    hs = to_decimal_padded(hi, want - m);
+    ls = to_decimal_padded(lo, m);
+  }
+  return hs + ls;
+}
+
+// ------------------------------------------------------------------ Chudnovsky
+static const uint64_t CH_A = 13591409, CH_B = 545140134;  // chudnovsky.rs:57-58
+static const uint64_t C3_OVER_24 = 10939058860032000ull;  // chudnovsky.rs:61
+static const double DIGITS_PER_TERM = 14.181647462725478;  // chudnovsky.rs:50
+static const uint64_t SAFETY_TERMS = 8;                    // chudnovsky.rs:55
+
+struct PQT {
+  Int p, q, t;
+};
+
+// chudnovsky.rs:377-413 (rayon::join on subtrees of >= 64 terms becomes a
+// host thread for the top levels)
+static PQT split(uint64_t a, uint64_t b, int depth) {
+  if (b - a == 1) {
+    Int k(a);
+    Int f1 = sub(mulu(k, 6), Int(5)), f2 = sub(mulu(k, 6), Int(1)), f3 = sub(mulu(k, 2), Int(1));
+    Int p = neg(mul(mul(f1, f2), f3));
+    Int q = mul(Int(C3_OVER_24), mul(mul(k, k), k));
+    Int t = mul(p, add(Int(CH_A), mulu(k, CH_B)));
+    return PQT{p, q, t};
+  }
+  uint64_t m = (a + b) / 2;
+  PQT L, R;
+  if (b - a >= PARALLEL_SPLIT && depth < 4) {
+    std::thread th([&] { R = split(m, b, depth + 1); });
+    L = split(a, m, depth + 1);
+    th.join();
+  } else {
+    L = split(a, m, depth);
+    R = split(m, b, depth);
+  }
+  PQT o;
+  o.t = add(mul(L.t, R.q), mul(L.p, R.t));
+  o.p = mul(L.p, R.p);
+  o.q = mul(L.q, R.q);
+  return o;
+}
+
+// Root without P (chudnovsky.rs:339-369).
+static void split_root(uint64_t a, uint64_t b, Int& q, Int& t) {
+  if (b - a == 1) {
+    PQT x = split(a, b, 0);
+    q = x.q;
+    t = x.t;
+    return;
+  }
+  uint64_t m = (a + b) / 2;
+  PQT L, R;
+  std::thread th([&] { R = split(m, b, 1); });
+  L = split(a, m, 1);
+  th.join();
+  t = add(mul(L.t, R.q), mul(L.p, R.t));
+  q = mul(L.q, R.q);
+}
+
+static double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace pihost
+
+using namespace pihost;
+
+// Digits of pi by Chudnovsky (crates/pi-core/src/algorithm/chudnovsky.rs:75-235):
+// writes `digits` characters ("31415...", no decimal point) to out.
+// phase_ms (optional, 3 entries): binary splitting, final assembly,
+// decimal conversion.  backend NULL = the GPU engine (pimul_mul).
+extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                   uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products,
+                                   uint64_t* ntt_hist33) {
+  if (digits == 0) return PIMUL_OK;
+  if (!out || cap < digits) return PIMUL_EINVAL;
+  g_backend = reinterpret_cast<mul_fn>(backend);
+  g_ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
+  g_ntt_calls.store(0);
+  for (auto& h : g_ntt_hist) h.store(0);
+  g_error.store(0);
+  // precision.rs:64: bits = ceil(D log2 10) + 256
+  const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
+  const uint64_t n_terms = (uint64_t)std::ceil((double)digits / DIGITS_PER_TERM) + SAFETY_TERMS;
+  double t0 = now_ms();
+  // sqrt(10005) * 426880 runs beside the binary splitting (chudnovsky.rs:118-126)
+  Flt sq;
+  std::thread sqrt_th([&] {
+    Flt p = flt_from_u64(10005, prec);
+    sqrt_mut(p);
+    sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
+  });
+  Int q, t;
+  split_root(1, n_terms + 1, q, t);
+  double t1 = now_ms();
+  // final assembly (chudnovsky.rs:146-204)
+  Int denom = add(mul(Int(CH_A), q), t);
+  Flt denf = flt_from_int(denom);
+  sqrt_th.join();
+  Flt recip = reciprocal_at_prec(denf, prec + 16);
+  Flt num = mul_at_prec(sq, flt_from_int(q), sq.prec);
+  Flt pi = mul_at_prec(num, recip, prec);
+  double t2 = now_ms();
+  // decimal conversion (util.rs:25-83)
+  Flt scale = pow_int(flt_from_u64(10, pi.prec), Int(digits - 1));
+  pi = mul_at_prec(pi, scale, pi.prec);
+  Int ip = to_integer_down(pi);
+  std::string s = to_decimal_top(ip);
+  double t3 = now_ms();
+  if (g_error.load()) return g_error.load();
+  if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
+  memcpy(out, s.data(), digits);
+  if (phase_ms) {
+    phase_ms[0] = t1 - t0;
+    phase_ms[1] = t2 - t1;
+    phase_ms[2] = t3 - t2;
+  }
+  if (ntt_products) *ntt_products = g_ntt_calls.load();
+  if (ntt_hist33)
+    for (int i = 0; i < 33; i++) ntt_hist33[i] = g_ntt_hist[i].load();
+  return PIMUL_OK;
+}

@@ -1,0 +1,34 @@
+"""Configuration 1: Chudnovsky pi with every product above the reference's
+NTT threshold going through the GPU multiply (one call per product); digits
+must equal the independent mpmath digits and the same pipeline with the CPU
+multiply (the reference's CPU path)."""
+import hashlib
+import json
+import os
+
+import pytest
+
+import oracle as O
+import pi_gb300 as pm
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_1e5_digits_lowered_threshold():
+    with open(os.path.join(HERE, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    s, info = pm.pi_chudnovsky(100_000, ntt_threshold=512)
+    assert s == ref
+    assert info["ntt_products"] > 50
+
+
+def test_1e6_digits_reference_threshold():
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, info = pm.pi_chudnovsky(1_000_000)
+    assert info["ntt_products"] > 0
+    assert s[-20:] == want["last20"]
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+    cpu, _ = pm.pi_chudnovsky(1_000_000, backend=O.mul_abi_pointer())
+    assert cpu == s
