@@ -193,6 +193,17 @@ typedef int (*pimul_mul_fn)(const uint64_t* a, size_t la, const uint64_t* b, siz
 int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
                         double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33);
 
+/*
+ * Digits of pi by the Gauss-Legendre AGM, same conventions as
+ * pimul_pi_chudnovsky (phase_ms: iterations + final assembly, unused,
+ * decimal conversion).
+ *
+ * Replaces: crates/pi-core/src/algorithm/gauss_legendre.rs:61
+ * GaussLegendre::compute with util.rs:25 write_decimal_digits.
+ */
+int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
+                            double* phase_ms, uint64_t* ntt_products);
+
 /* Transform plan for a product: N and the number of HBM passes per transform.
  * Mirrors the sizing of crates/bignum/src/ntt.rs:810-813. */
 int pimul_plan(size_t la, size_t lb, uint64_t* n_transform, int* passes);

@@ -26,7 +26,7 @@ __all__ = [
     "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device",
     "plan", "sync", "bbp_hex_digits", "mul_batch", "BatchPlan", "autotune",
     "tuning_apply", "PimulJob", "set_budget", "upload", "submit", "wait", "download", "free",
-    "handle_size", "pi_chudnovsky", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
+    "handle_size", "pi_chudnovsky", "pi_gauss_legendre", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
 ]
 
 LIB_PATH = _build.LIB
@@ -83,6 +83,8 @@ def load(build_if_stale: bool = True):
     L.pimul_pi_chudnovsky.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
                                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_pi_gauss_legendre.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
     L.pimul_bbp_last_error.restype = ctypes.c_char_p
     _lib = L
@@ -301,6 +303,18 @@ def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
     return buf.raw[:digits].decode(), info
+
+
+def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0):
+    """Digits of pi by the Gauss-Legendre AGM
+    (crates/pi-core/src/algorithm/gauss_legendre.rs:61)."""
+    buf = ctypes.create_string_buffer(digits + 1)
+    ph = (ctypes.c_double * 3)()
+    n = ctypes.c_uint64(0)
+    _check(lib().pimul_pi_gauss_legendre(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
+                                         ntt_threshold, ph, ctypes.byref(n)))
+    return buf.raw[:digits].decode(), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
+                                       "ntt_products": n.value}
 
 
 def bbp_hex_digits(positions, stop=None) -> np.ndarray:

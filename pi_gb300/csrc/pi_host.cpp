@@ -773,9 +773,88 @@ static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Float from an f64 at prec (Float::with_val_64(prec, f64)).
+static Flt flt_f64_prec(double v, uint64_t prec) {
+  Flt f = flt_from_f64(v, 64);
+  f.prec = prec;
+  round_to_prec(f);
+  return f;
+}
+
+// Gauss-Legendre AGM (crates/pi-core/src/algorithm/gauss_legendre.rs:61-151):
+// iterations = ceil(log2 prec) + 2; per iteration a' = (a+b)/2,
+// b' = sqrt(a b), t -= p (a - a')^2, p <<= 1; pi = (a+b)^2 / t / 4.
+static Flt gauss_legendre(uint64_t prec) {
+  const uint32_t iters = (uint32_t)std::ceil(std::log2((double)prec)) + 2;
+  Flt a = flt_from_u64(1, prec);
+  Flt b = flt_f64_prec(0.5, prec);
+  sqrt_mut(b);
+  Flt t = flt_f64_prec(0.25, prec);
+  Int p(1);
+  for (uint32_t it = 0; it < iters; it++) {
+    Flt an = add_at_prec(a, b, prec);
+    an = div_at_prec(an, flt_from_u64(2, 64), prec);
+    Flt bn = mul_at_prec(a, b, prec);
+    sqrt_mut(bn);
+    Flt diff = sub_at_prec(a, an, prec);
+    Flt dsq = mul_at_prec(diff, diff, prec);
+    dsq = mul_at_prec(dsq, flt_from_int(p), prec);
+    t = sub_at_prec(t, dsq, prec);
+    a = an;
+    b = bn;
+    p = Int(shl_mag(p.m, 1), false);
+  }
+  Flt pi = add_at_prec(a, b, prec);
+  Flt sq = pi;  // square_mut: mantissa^2, exp doubled, rounded to prec
+  sq.mant = mul_mag(pi.mant, pi.mant);
+  sq.exp = 2 * pi.exp;
+  sq.sign = false;
+  round_to_prec(sq);
+  sq = div_at_prec(sq, t, prec);
+  return div_at_prec(sq, flt_from_u64(4, 64), prec);
+}
+
 }  // namespace pihost
 
 using namespace pihost;
+
+static int finish_digits(Flt pi, uint64_t digits, char* out, double* t_phase) {
+  double t0 = now_ms();
+  Flt scale = pow_int(flt_from_u64(10, pi.prec), Int(digits - 1));
+  pi = mul_at_prec(pi, scale, pi.prec);
+  Int ip = to_integer_down(pi);
+  std::string s = to_decimal_top(ip);
+  if (t_phase) *t_phase = now_ms() - t0;
+  if (g_error.load()) return g_error.load();
+  if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
+  memcpy(out, s.data(), digits);
+  return PIMUL_OK;
+}
+
+// Digits of pi by Gauss-Legendre (see pimul.h).
+extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                       uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products) {
+  if (digits == 0) return PIMUL_OK;
+  if (!out || cap < digits) return PIMUL_EINVAL;
+  g_backend = reinterpret_cast<mul_fn>(backend);
+  g_ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
+  g_ntt_calls.store(0);
+  for (auto& h : g_ntt_hist) h.store(0);
+  g_error.store(0);
+  const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
+  double t0 = now_ms();
+  Flt pi = gauss_legendre(prec);
+  double t1 = now_ms();
+  double tdc = 0;
+  int rc = finish_digits(pi, digits, out, &tdc);
+  if (phase_ms) {
+    phase_ms[0] = t1 - t0;
+    phase_ms[1] = 0;
+    phase_ms[2] = tdc;
+  }
+  if (ntt_products) *ntt_products = g_ntt_calls.load();
+  return rc;
+}
 
 // Digits of pi by Chudnovsky (crates/pi-core/src/algorithm/chudnovsky.rs:75-235):
 // writes `digits` characters ("31415...", no decimal point) to out.

@@ -32,3 +32,11 @@ def test_1e6_digits_reference_threshold():
     assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
     cpu, _ = pm.pi_chudnovsky(1_000_000, backend=O.mul_abi_pointer())
     assert cpu == s
+
+
+def test_gauss_legendre_1e5_equals_chudnovsky():
+    # the reference's own acceptance check: both algorithms byte-identical
+    g, info = pm.pi_gauss_legendre(100_000, ntt_threshold=512)
+    c, _ = pm.pi_chudnovsky(100_000, ntt_threshold=512)
+    assert g == c
+    assert info["ntt_products"] > 0

@@ -28,3 +28,9 @@ def test_digits_vs_mpmath(digits, thr):
     assert s == ref_digits()[:digits]
     if thr:
         assert info["ntt_products"] > 0  # the backend saw the large products
+
+
+@pytest.mark.parametrize("digits,thr", [(1, 0), (100, 0), (3000, 64), (20000, 256)])
+def test_gauss_legendre_vs_mpmath(digits, thr):
+    s, info = pm.pi_gauss_legendre(digits, backend=O.mul_abi_pointer(), ntt_threshold=thr)
+    assert s == ref_digits()[:digits]
