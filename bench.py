@@ -592,6 +592,14 @@ def run_pi(args):
     import pi_gb300 as pm
     pm.init(0)
     D = args.digits
+    other_same = None
+    if args.algorithm == "both":
+        t0 = time.perf_counter()
+        g, _ = pm.pi_gauss_legendre(D)
+        gl_wall = time.perf_counter() - t0
+        args.algorithm = "chudnovsky"
+        args.gl_wall = gl_wall
+        args.gl_digits = g
     run = pm.pi_gauss_legendre if args.algorithm == "gl" else pm.pi_chudnovsky
     run(min(D, 100_000))  # warm-up (tables, pools, kernels)
     t0 = time.perf_counter()
@@ -610,6 +618,8 @@ def run_pi(args):
                "sample": f"the same {D}-digit run with the C restatement of mul_mag_ntt "
                          "(crates/bignum/src/ntt.rs:806-865) as the multiply",
                "phases_ms": {k: round(v, 1) for k, v in cinfo.items() if k.endswith("_ms")}}
+    if getattr(args, "gl_digits", None) is not None:
+        other_same = args.gl_digits == s
     golden = None
     path = os.path.join(ROOT, "tests", "golden", "pi_digits_hashes.json")
     if os.path.exists(path):
@@ -628,8 +638,53 @@ def run_pi(args):
         "phases_ms": {k: round(v, 1) for k, v in info.items() if k.endswith("_ms")},
         "gpu_products": info["ntt_products"], "gpu_products_by_length": info.get("ntt_hist"),
         "digits_match_cpu_run": same, "digits_match_mpmath_sha256": golden,
+        "gauss_legendre": None if other_same is None else {"wall_s": round(args.gl_wall, 3),
+                                                           "digits_identical_to_chudnovsky": other_same},
+        "sha256": hashlib.sha256(s.encode()).hexdigest(),
         "last_digits": s[-20:], "cpu_baseline": cpu,
     }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- BBP
+def run_bbp(args):
+    """Config 5's spot checks: batched BBP hex digits at seeded positions
+    uniform in [0, max_pos); positions/s and modular multiplies/s.  The CPU
+    oracle times a smaller seeded subsample (scaled linearly in n)."""
+    import pi_gb300 as pm
+    rng = np.random.default_rng(2025)
+    pos = rng.integers(0, int(args.max_pos), size=args.positions, dtype=np.uint64)
+    pm.bbp_hex_digits(np.arange(64, dtype=np.uint64))  # warm-up
+    t0 = time.perf_counter()
+    d = pm.bbp_hex_digits(pos)
+    dt = time.perf_counter() - t0
+    terms = 4.0 * float((pos.astype(np.float64) + 1).sum())
+    line = {
+        "metric": "BBP hex-digit spot checks (positions/s)", "baseline_metric": BASELINE_METRIC,
+        "value": round(args.positions / dt, 3), "unit": "positions/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": round(1e3 * dt, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64+f64", "data": f"seeded positions uniform in [0, {int(args.max_pos)})",
+        "config": {"workload": f"{args.positions} positions in one batched launch"},
+        "terms_per_s": round(terms / dt, 1),
+        "extrapolated_65536_positions_s": round(dt * 65536 / args.positions, 1),
+        "first_digits": [f"{int(x):08x}" for x in d[:4]],
+    }
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        sub = pos[: args.cpu_positions]
+        scale = float(args.cpu_depth) / float(max(1, sub.mean()))
+        sub = np.maximum((sub.astype(np.float64) * scale).astype(np.uint64), 1)
+        t1 = time.perf_counter()
+        cd = oracle.bbp_batch(sub)
+        ct = time.perf_counter() - t1
+        gd = pm.bbp_hex_digits(sub)
+        cterms = 4.0 * float((sub.astype(np.float64) + 1).sum())
+        line["cpu_baseline"] = {"value": round(cterms / ct, 1), "unit": "terms/s", "cores": oracle.max_threads(),
+                                "kind": "port",
+                                "sample": f"{sub.size} positions scaled to mean depth {args.cpu_depth} "
+                                          "(C restatement of crates/pi-core/src/bbp.rs:52-140, OpenMP)",
+                                "gpu_matches_cpu": bool(np.array_equal(cd, gd))}
     print(json.dumps(line), flush=True)
 
 
@@ -707,8 +762,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-API leg (profiling runs)")
     ap.add_argument("--digits", type=int, default=1_000_000)
-    ap.add_argument("--algorithm", choices=["chudnovsky", "gl"], default="chudnovsky")
-    ap.add_argument("--workload", choices=["mul", "batch", "served", "pi"], default="mul",
+    ap.add_argument("--algorithm", choices=["chudnovsky", "gl", "both"], default="chudnovsky")
+    ap.add_argument("--positions", type=int, default=256)
+    ap.add_argument("--max-pos", type=float, default=8e8)
+    ap.add_argument("--cpu-positions", type=int, default=16)
+    ap.add_argument("--cpu-depth", type=float, default=2e6)
+    ap.add_argument("--workload", choices=["mul", "batch", "served", "pi", "bbp"], default="mul",
                     help="mul: the 2^30-bit product (headline); batch: 4096 uneven products; "
                          "served: Poisson request stream through the multiply service")
     ap.add_argument("--requests", type=int, default=1000)
@@ -729,6 +788,8 @@ def main():
         run_served(args)
     elif args.workload == "pi":
         run_pi(args)
+    elif args.workload == "bbp":
+        run_bbp(args)
     else:
         run_gpu(args)
 

@@ -145,9 +145,10 @@ int pimul_tuning_set(int log_n, int passes, int small_ctas_per_sm);
  * round trip).  A service thread admits queued requests in order while
  * their result and scratch memory fit the HBM budget (pimul_set_budget,
  * default 120 GiB; handles count against it until freed), launches each
- * admitted group as one batch on one of four streams, and releases the
- * scratch when the group completes; requests that arrive meanwhile join the
- * next group (continuous batching).  pimul_wait blocks until a ticket's
+ * admitted group as one batch, and releases the scratch when the group
+ * completes; requests that arrive meanwhile join the next group (continuous
+ * batching).  Groups of small requests run on four streams; a request with a
+ * transform of 2^20 or more forms its own group on a high-priority stream.  pimul_wait blocks until a ticket's
  * product is done (timeout_us < 0: no limit) or returns PIMUL_ETIMEDOUT.
  * pimul_free waits for the handle's producer and readers.  A result handle
  * stores la + lb limbs; pimul_download returns the trimmed value.

@@ -1375,9 +1375,14 @@ static int svc_start() {
   if (g_svc.running) return PIMUL_OK;
   CU(cudaSetDevice(g_dev.device));
   if (g_svc.streams.empty()) {
-    for (int i = 0; i < 4; i++) {
+    // stream 0: highest priority, reserved for large requests (one per
+    // group) so they run at near-solo speed; streams 1-4 carry batched
+    // groups of smaller requests
+    int lo = 0, hi = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int i = 0; i < 5; i++) {
       cudaStream_t s;
-      CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      CU(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, i == 0 ? hi : lo));
       g_svc.streams.push_back(s);
       g_svc.stream_busy.push_back(0);
     }
@@ -1393,16 +1398,33 @@ static int svc_start() {
 // One iteration's worth of admission: FIFO, stop at the first request whose
 // inputs are not launched yet (its producer is still queued) or that does
 // not fit the budget.
+// Transform length (log2) of a queued request.
+static int svc_req_L(const SvcRequest& r) {
+  uint64_t la = g_svc.handles[r.a].limbs, lb = g_svc.handles[r.b].limbs;
+  if (!la || !lb) return 0;
+  return log2_ceil(4 * la + 4 * lb - 1);
+}
+
+static const int SVC_BIG_L = 20;  // transforms of 2^20 and longer run alone
+
 static void svc_admit(std::unique_lock<std::mutex>& lk) {
+  if (g_svc.queue.empty()) return;
+  const bool big_head = svc_req_L(g_svc.requests[g_svc.queue.front()]) >= SVC_BIG_L;
   int si = -1;
-  for (size_t i = 0; i < g_svc.streams.size(); i++)
-    if (!g_svc.stream_busy[i]) { si = (int)i; break; }
-  if (si < 0 || g_svc.queue.empty()) return;
+  if (big_head) {
+    if (!g_svc.stream_busy[0]) si = 0;
+  } else {
+    for (size_t i = 1; i < g_svc.streams.size(); i++)
+      if (!g_svc.stream_busy[i]) { si = (int)i; break; }
+  }
+  if (si < 0) return;
   std::vector<uint64_t> take;
   uint64_t add = 0;
   while (!g_svc.queue.empty() && (int)take.size() < g_svc.max_batch) {
     uint64_t t = g_svc.queue.front();
     SvcRequest& r = g_svc.requests[t];
+    const bool big = svc_req_L(r) >= SVC_BIG_L;
+    if (big != big_head || (big && !take.empty())) break;  // a big request forms its own group
     SvcHandle& A = g_svc.handles[r.a];
     SvcHandle& B = g_svc.handles[r.b];
     bool inputs_launched = !A.pending && !B.pending;

@@ -1,7 +1,8 @@
 """Pi digit fixtures computed with mpmath (an independent arbitrary-precision
 implementation):
   tests/golden/pi_digits_100k.txt   first 100,000 digits ("31415...", no point)
-  tests/golden/pi_digits_hashes.json SHA-256 and last 20 of the first 10^6 digits
+  tests/golden/pi_digits_hashes.json SHA-256 and last 20 of the first 10^6 and
+                                     10^7 digits (10^7 takes about 10 minutes)
 Run: python tests/golden/make_pi_digits.py"""
 import hashlib
 import json
@@ -22,7 +23,7 @@ def main():
     with open(os.path.join(HERE, "pi_digits_100k.txt"), "w") as f:
         f.write(s + "\n")
     out = {}
-    for n in (1_000_000,):
+    for n in (1_000_000, 10_000_000):
         d = digits(n)
         out[str(n)] = {"sha256": hashlib.sha256(d.encode()).hexdigest(), "last20": d[-20:]}
     with open(os.path.join(HERE, "pi_digits_hashes.json"), "w") as f:

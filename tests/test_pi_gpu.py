@@ -40,3 +40,12 @@ def test_gauss_legendre_1e5_equals_chudnovsky():
     c, _ = pm.pi_chudnovsky(100_000, ntt_threshold=512)
     assert g == c
     assert info["ntt_products"] > 0
+
+
+def test_1e7_digits_against_mpmath():
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["10000000"]
+    s, info = pm.pi_chudnovsky(10_000_000)
+    assert info["ntt_products"] > 100
+    assert s[-20:] == want["last20"]
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
