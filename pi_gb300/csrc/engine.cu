@@ -152,14 +152,22 @@ static uint64_t find_rho() {
 }
 
 // ------------------------------------------------------------------ kernels
-// Geometry of the HBM passes.  All pass tiles hold 2^13 words (64 KiB plus
-// padding) and are processed by 256 threads:
-//   first pass (p = 0):   2^R rows x 2^(13-R) columns of the single block
-//   middle passes:        2^(9-R) blocks x 2^R rows x 16 columns
-//   last pass (S = 1):    2^(13-R) contiguous blocks of 2^R words
-// Column tiles read 128-byte (or wider) row segments.
+// Geometry of the HBM passes.  Pass tiles hold 2^12 words (32 KiB plus
+// padding, so that five CTAs share an SM) and are processed by 256 threads:
+//   first pass (p = 0):   2^R rows x 2^(12-R) columns of the single block
+//   middle passes:        2^(9-R) blocks x 2^R rows x 8 columns
+//   last pass (S = 1):    2^(12-R) contiguous blocks of 2^R words
+// Column tiles read 64-byte (or wider) row segments.  The inverse first pass,
+// which folds 16-coefficient carry windows out of its rows, uses 2^13-word
+// tiles (rows of at least 16 consecutive coefficients).
 constexpr int PASS_THREADS = 256;
-constexpr int TILE_LOG = 13;
+constexpr int TILE_LOG = 12;
+constexpr int CARRY_TILE_LOG = 13;
+// Resident CTAs per SM the pass kernels are register-limited for.
+#ifndef PIMUL_PASS_MIN_CTAS
+#define PIMUL_PASS_MIN_CTAS 5
+#endif
+constexpr int PASS_MIN_CTAS = PIMUL_PASS_MIN_CTAS;
 
 static inline size_t pass_smem_bytes(int tile_log) { return ((size_t)1 << tile_log) * 17 / 16 * 8 + 512 * 8; }
 
@@ -168,9 +176,10 @@ __device__ __forceinline__ void load_tw512(uint64_t* tw, const Roots& R) {
   for (int t = threadIdx.x; t < 512; t += blockDim.x) tw[t] = __ldg(R.lvl + 512 + t);
 }
 
-// Elements per thread in a 2^13-word tile, processed in groups of 8 so that
-// every thread keeps 16 independent global loads in flight.
-constexpr int PER_THREAD = (1 << 13) / 256;
+// Elements per thread in a pass tile, processed in groups of 8 so that
+// every thread keeps 8 independent global loads in flight.
+constexpr int PER_THREAD = (1 << TILE_LOG) / PASS_THREADS;
+constexpr int PER_THREAD_CARRY = (1 << CARRY_TILE_LOG) / PASS_THREADS;
 
 // One product of a batch (or the only product of a plain call): operands,
 // output and its scratch.  Kernels take `const Job* jobs, Job one`: with a
@@ -203,7 +212,7 @@ __device__ __forceinline__ uint64_t* job_array(const Job& J, int which) {
 // limbs past nl are zero (the reference's zero tail).  which = 0: operand a,
 // 1: operand b (squares skip b).
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT) {
   constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   if (which == 1 && is_square(J)) return;
@@ -247,11 +256,12 @@ __global__ void __launch_bounds__(PASS_THREADS) k_fwd_first(const Job* jobs, Job
   }
 }
 
-// Middle column pass: 2^(9-R) blocks x 2^R rows x 16 columns; forward pass
+// Middle column pass: 2^(9-R) blocks x 2^R rows x 2^T columns; forward pass
 // twiddles w_M^(f*j) after the rounds, inverse ones before.
 template <int R, bool FWD>
-__global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT) {
-  constexpr int T = 4, BC = 9 - R;
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT) {
+  constexpr int T = TILE_LOG - 9, BC = 9 - R;
+  constexpr uint32_t TM = (1u << T) - 1;
   const Job J = job_of(jobs, one);
   if (FWD && which == 1 && is_square(J)) return;
   uint64_t* __restrict__ data = job_array(J, which);
@@ -264,7 +274,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job o
   const uint64_t j0 = ct << T;
   load_tw512(tw, RT);
   auto gaddr = [&](uint32_t lin) {
-    uint32_t j = lin & 15, i = (lin >> 4) & ((1u << R) - 1), blk = lin >> (4 + R);
+    uint32_t j = lin & TM, i = (lin >> T) & ((1u << R) - 1), blk = lin >> (T + R);
     return ((b0 + blk) << mlog) + ((uint64_t)i << S) + j0 + j;
   };
 #pragma unroll 1
@@ -276,8 +286,8 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job o
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         uint32_t lin = (g + q) * PASS_THREADS + tid;
-        uint32_t i = (lin >> 4) & ((1u << R) - 1);
-        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), true);
+        uint32_t i = (lin >> T) & ((1u << R) - 1);
+        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & TM)), true);
       }
 #pragma unroll
       for (int q = 0; q < 8; q++) v8[q] = gl::mul(v8[q], t8[q]);
@@ -295,8 +305,8 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job o
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         uint32_t lin = (g + q) * PASS_THREADS + tid;
-        uint32_t i = (lin >> 4) & ((1u << R) - 1);
-        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & 15)), false);
+        uint32_t i = (lin >> T) & ((1u << R) - 1);
+        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & TM)), false);
       }
     }
 #pragma unroll
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_col_mid(const Job* jobs, Job o
 // Last forward pass of operand a (stride 1): 2^(13-R) contiguous blocks of
 // 2^R words.  Squares skip it: their last pass is fused into k_mid.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(const Job* jobs, Job one, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const Job* jobs, Job one, Roots RT) {
   constexpr int BC = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   if (is_square(J)) return;
@@ -332,7 +342,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_fwd_last(const Job* jobs, Job 
 // the result overwrites b's array.  A square transforms and squares a's
 // array in place.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
   constexpr int BC = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   const bool sq = is_square(J);
@@ -406,20 +416,20 @@ __host__ __device__ __forceinline__ uint64_t aux_bytes_for(uint64_t nwin) {
 // writes its low 4 limbs to the output and its high part to H.
 template <int R>
 __global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
-  constexpr int T = TILE_LOG - R;
+  constexpr int T = CARRY_TILE_LOG - R;
   const Job J = job_of(jobs, one);
   const uint64_t* __restrict__ data = job_array(J, 2);
   uint64_t* __restrict__ out = J.out;
   uint64_t* __restrict__ H = J.H;
   const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb);
   extern __shared__ uint64_t sm[];
-  uint64_t* tw = sm + spad(1u << TILE_LOG);
+  uint64_t* tw = sm + spad(1u << CARRY_TILE_LOG);
   const int tid = threadIdx.x;
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
   load_tw512(tw, RT);
 #pragma unroll 1
-  for (int g = 0; g < PER_THREAD; g += 8) {
+  for (int g = 0; g < PER_THREAD_CARRY; g += 8) {
     uint64_t v8[8], t8[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -438,7 +448,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const Job* job
   }
   __syncthreads();
   tile_inv_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t q = tid; q < (1u << (TILE_LOG - 4)); q += PASS_THREADS) {
+  for (uint32_t q = tid; q < (1u << (CARRY_TILE_LOG - 4)); q += PASS_THREADS) {
     uint32_t i = q >> (T - 4), k = q & ((1u << (T - 4)) - 1);
     uint64_t w = ((((uint64_t)i << S) + j0) >> 4) + k;
     if (w >= nwin) continue;
@@ -737,7 +747,8 @@ static cudaError_t set_smem_attrs_r() {
   if (R >= 7) {
     e = cudaFuncSetAttribute(k_fwd_first<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_inv_first_carry<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      e = cudaFuncSetAttribute(k_inv_first_carry<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pass_smem_bytes(CARRY_TILE_LOG));
   }
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -817,9 +828,10 @@ static Plan make_plan_np(int L, int np) {
   return p;
 }
 
-// A plan is valid when every pass radix is 2^6 .. 2^9 (the compiled kernels).
+// A plan is valid when every pass radix is 2^6 .. 2^9 and the first one at
+// least 2^7 (the compiled kernels).
 static bool plan_valid(const Plan& p) {
-  if (p.np < 2 || p.np > 5) return false;
+  if (p.np < 2 || p.np > 5 || p.r[0] < 7) return false;
   for (int i = 0; i < p.np; i++)
     if (p.r[i] < 6 || p.r[i] > 9) return false;
   return true;
@@ -894,6 +906,7 @@ struct Launcher {
 static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32_t nj, int L, uint64_t max_chunk) {
   const Plan pl = make_plan(L);
   const dim3 grid((unsigned)(1ull << (L - TILE_LOG)), nj);
+  const dim3 cgrid_first((unsigned)(1ull << (L - CARRY_TILE_LOG)), nj);
   const size_t smem = pass_smem_bytes(TILE_LOG);
   const uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L (2^192 = 1)
   const int rl = pl.r[pl.np - 1];
@@ -926,7 +939,8 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
   }
   {
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, L, X.R)));
+    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<cgrid_first, PASS_THREADS,
+                                                                       pass_smem_bytes(CARRY_TILE_LOG), X.st>>>(jobs, one, L, X.R)));
   }
   {
     KTimer kt(K_CARRY, X.st, X.stats);

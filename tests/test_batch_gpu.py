@@ -100,13 +100,28 @@ def test_autotune_keeps_products_exact():
     torch.cuda.synchronize()
     for (da, db, o), r in zip(jobs, _plain(jobs)):
         assert torch.equal(o, r)
-    # a forced 3-pass split of a 2^18 transform gives the same bits
-    pm.tuning_apply({"np_18": 3})
-    jobs, _ = _make([[30000, 25000]], 11)
-    pm.mul_batch(jobs)
-    torch.cuda.synchronize()
-    assert torch.equal(jobs[0][2], _plain(jobs)[0])
-    pm.tuning_apply({"np_18": 0})
+    # a split with no compiled first-pass kernel (2^6 x 2^6 x 2^6) is refused
+    with pytest.raises(pm.PimulError):
+        pm.tuning_apply({"np_18": 3})
+
+
+def test_forced_four_pass_split_matches_oracle():
+    # 2^25 transform: default 2^9 x 2^8 x 2^8, forced 2^7 x 2^6 x 2^6 x 2^6
+    # (two middle column passes); both must give the oracle's product
+    rng = np.random.default_rng(12)
+    a = rng.integers(0, 2**63, 3_000_000, dtype=np.uint64) | np.uint64(1)
+    b = rng.integers(0, 2**63, 2_900_000, dtype=np.uint64) | np.uint64(1)
+    assert pm.plan(a.size, b.size) == (1 << 25, 3)
+    want = O.mul_mag(a, b)
+    pm.tuning_apply({"np_25": 4})
+    try:
+        assert pm.plan(a.size, b.size) == (1 << 25, 4)
+        got4 = pm.mul_mag_ntt(a, b)
+    finally:
+        pm.tuning_apply({"np_25": 0})
+    got3 = pm.mul_mag_ntt(a, b)
+    assert np.array_equal(got3, want)
+    assert np.array_equal(got4, want)
 
 
 def test_empty_batch_and_zero_lengths():
