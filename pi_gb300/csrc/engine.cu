@@ -673,7 +673,7 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
 
 // One CTA per product; with a device job list the CTAs stride over it
 // (a persistent kernel over a size-sorted bucket).
-__global__ void __launch_bounds__(SMALL_THREADS) k_small_mul(const SmallJob* jobs, SmallJob one, uint32_t njobs,
+__global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* jobs, SmallJob one, uint32_t njobs,
                                                                Roots R) {
   extern __shared__ uint64_t sm[];
   for (uint32_t k = blockIdx.x; k < njobs; k += gridDim.x) {

@@ -65,26 +65,29 @@ __device__ __forceinline__ uint64_t canon(uint64_t x) { return x >= P ? x - P : 
 
 __device__ __forceinline__ uint64_t neg(uint64_t a) { return sub(0, a); }
 
-// 128-bit value (x3 x2 x1 x0) -> weak 64-bit:  (x1:x0) - x3 + x2 * (2^32 - 1).
+// 128-bit value (x3 x2 x1 x0) -> weak 64-bit:  (x1:x0) + x2 * (2^32 - 1) - x3.
+// u = x2 * (2^32 - 1) comes from one wide multiply; the sum's net carry
+// k in {-1, 0, 1} is worth k * 2^64 = k * EPS, and adding that cannot carry
+// again (|k * EPS| is far from both ends of the 64-bit range).
 __device__ __forceinline__ uint64_t reduce_words(uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3) {
+  uint64_t u;
+  asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(r2));
   uint32_t z0, z1;
-  asm("{\n\t.reg .u32 t0, t1, b, u0, u1, c;\n\t"
-      "sub.cc.u32 t0, %2, %5;\n\t"      // t = (x1:x0) - x3
-      "subc.cc.u32 t1, %3, 0;\n\t"
-      "subc.u32 b, 0, 0;\n\t"           // borrow mask: -2^64 = -EPS
-      "sub.cc.u32 t0, t0, b;\n\t"       // cannot borrow again
-      "subc.u32 t1, t1, 0;\n\t"
-      "sub.cc.u32 u0, 0, %4;\n\t"       // u = x2 * (2^32 - 1)
-      "subc.u32 u1, %4, 0;\n\t"
-      "add.cc.u32 t0, t0, u0;\n\t"      // t + u
-      "addc.cc.u32 t1, t1, u1;\n\t"
-      "addc.u32 c, 0, 0;\n\t"
-      "neg.s32 c, c;\n\t"               // carry: +2^64 = +EPS (cannot carry again)
-      "add.cc.u32 %0, t0, c;\n\t"
-      "addc.u32 %1, t1, 0;\n\t"
+  asm("{\n\t.reg .u32 k, nk, hk, u0, u1;\n\t"
+      "mov.b64 {u0, u1}, %6;\n\t"
+      "add.cc.u32 %0, %2, u0;\n\t"
+      "addc.cc.u32 %1, %3, u1;\n\t"
+      "addc.u32 k, 0, 0;\n\t"
+      "sub.cc.u32 %0, %0, %5;\n\t"
+      "subc.cc.u32 %1, %1, 0;\n\t"
+      "subc.u32 k, k, 0;\n\t"
+      "neg.s32 nk, k;\n\t"           // k * EPS = (k >> 31 : -k) for k in {-1, 0, 1}
+      "shr.s32 hk, k, 31;\n\t"
+      "add.cc.u32 %0, %0, nk;\n\t"
+      "addc.u32 %1, %1, hk;\n\t"
       "}"
-      : "=r"(z0), "=r"(z1)
-      : "r"(r0), "r"(r1), "r"(r2), "r"(r3));
+      : "=&r"(z0), "=&r"(z1)
+      : "r"(r0), "r"(r1), "r"(r2), "r"(r3), "l"(u));
   return mk64(z0, z1);
 }
 
@@ -136,6 +139,136 @@ __device__ __forceinline__ uint64_t shl(uint64_t x) {
     uint64_t yl = T ? (x << T) : x;
     uint64_t yh = T ? (x >> (64 - T)) : 0;  // < 2^32
     return sub(reduce128(0, yl), yh << 32);
+  }
+}
+
+// ------------------------------------------------------------ lazy values
+// Inside the radix-8 / radix-4 butterflies values are carried "lazy": a
+// 64-bit word plus a small signed count k of 2^64 overflows,
+//   value = l + h 2^32 + k 2^64   (= l + h 2^32 + k EPS  mod p).
+// Adding or subtracting two lazy values is one 96-bit add (three carry-chain
+// instructions) with no modular fix-up; fold() turns a lazy value back into a
+// weak 64-bit word once, at the end of the butterfly network.
+struct Lz {
+  uint32_t l, h;
+  int32_t k;
+};
+
+__device__ __forceinline__ Lz lz(uint64_t x) { return Lz{lo32(x), hi32(x), 0}; }
+
+__device__ __forceinline__ Lz lz_add(Lz x, Lz y) {
+  Lz z;
+  asm("add.cc.u32 %0, %3, %6;\n\taddc.cc.u32 %1, %4, %7;\n\taddc.u32 %2, %5, %8;"
+      : "=r"(z.l), "=r"(z.h), "=r"(z.k)
+      : "r"(x.l), "r"(x.h), "r"(x.k), "r"(y.l), "r"(y.h), "r"(y.k));
+  return z;
+}
+
+__device__ __forceinline__ Lz lz_sub(Lz x, Lz y) {
+  Lz z;
+  asm("sub.cc.u32 %0, %3, %6;\n\tsubc.cc.u32 %1, %4, %7;\n\tsubc.u32 %2, %5, %8;"
+      : "=r"(z.l), "=r"(z.h), "=r"(z.k)
+      : "r"(x.l), "r"(x.h), "r"(x.k), "r"(y.l), "r"(y.h), "r"(y.k));
+  return z;
+}
+
+// (h:l) + w * EPS for a signed |w| < 2^31 -> weak 64-bit.  As a 96-bit
+// signed sum, (h:l) - w + w 2^32 has top word c in {-1, 0, 1}; c * EPS is
+// added back as in reduce_words.
+__device__ __forceinline__ uint64_t fold_words(uint32_t l, uint32_t h, int32_t w) {
+  uint32_t z0, z1;
+  asm("{\n\t.reg .u32 wh, c, nc, hc;\n\t"
+      "shr.s32 wh, %4, 31;\n\t"
+      "sub.cc.u32 %0, %2, %4;\n\t"
+      "subc.cc.u32 %1, %3, wh;\n\t"
+      "subc.u32 c, 0, wh;\n\t"
+      "add.cc.u32 %1, %1, %4;\n\t"
+      "addc.u32 c, c, wh;\n\t"
+      "neg.s32 nc, c;\n\t"
+      "shr.s32 hc, c, 31;\n\t"
+      "add.cc.u32 %0, %0, nc;\n\t"
+      "addc.u32 %1, %1, hc;\n\t"
+      "}"
+      : "=&r"(z0), "=&r"(z1)
+      : "r"(l), "r"(h), "r"(w));
+  return mk64(z0, z1);
+}
+
+__device__ __forceinline__ uint64_t fold(Lz x) { return fold_words(x.l, x.h, x.k); }
+
+// a * b as a lazy value with k in {-1, 0}: with u = x2 EPS + (EPS - x3)
+// (which cannot overflow 64 bits), a b = (x1:x0) + u - EPS and -EPS = -2^64.
+__device__ __forceinline__ Lz lz_mul(uint64_t a, uint64_t b) {
+  uint32_t r0, r1, r2, r3;
+  mul128(a, b, r0, r1, r2, r3);
+  uint64_t u;
+  asm("mad.wide.u32 %0, %1, 0xFFFFFFFF, %2;" : "=l"(u) : "r"(r2), "l"((uint64_t)(~r3)));
+  Lz z;
+  asm("add.cc.u32 %0, %3, %5;\n\taddc.cc.u32 %1, %4, %6;\n\taddc.u32 %2, 0xFFFFFFFF, 0;"
+      : "=r"(z.l), "=r"(z.h), "=r"(z.k)
+      : "r"(r0), "r"(r1), "r"(lo32(u)), "r"(hi32(u)));
+  return z;
+}
+
+// x * 2^S for S in {24, 48, 72} on a lazy value with |k| < 2^6 -> weak.
+template <int S>
+__device__ __forceinline__ uint64_t lz_shl(Lz x) {
+  static_assert(S == 24 || S == 48 || S == 72, "lazy shifts are 24, 48 or 72 bits");
+  if constexpr (S == 24) {
+    // (h:l) 2^24 = (w2:w1:w0), w2 < 2^24; k 2^88 adds k 2^24 to w2
+    uint32_t w0 = x.l << 24;
+    uint32_t w1 = __funnelshift_l(x.l, x.h, 24);
+    int32_t w2 = (int32_t)(x.h >> 8) + (int32_t)((uint32_t)x.k << 24);
+    return fold_words(w0, w1, w2);
+  } else if constexpr (S == 48) {
+    // (h:l) 2^48 = words (0, l << 16, w2, h >> 16) and k 2^112 = -k 2^16 (2^96 = -1):
+    // value = (w1:0) + w2 EPS - w3 with w3 = (h >> 16) + k 2^16
+    uint32_t w1 = x.l << 16;
+    uint32_t w2 = __funnelshift_l(x.l, x.h, 16);
+    int32_t w3 = (int32_t)(x.h >> 16) + (int32_t)((uint32_t)x.k << 16);
+    uint64_t u;
+    asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(w2));
+    uint32_t z0, z1;
+    asm("{\n\t.reg .u32 k, nk, hk, u0, u1, w3h;\n\t"
+        "mov.b64 {u0, u1}, %4;\n\t"
+        "shr.s32 w3h, %3, 31;\n\t"
+        "sub.cc.u32 %0, 0, %3;\n\t"
+        "subc.cc.u32 %1, %2, w3h;\n\t"
+        "subc.u32 k, 0, w3h;\n\t"
+        "add.cc.u32 %0, %0, u0;\n\t"
+        "addc.cc.u32 %1, %1, u1;\n\t"
+        "addc.u32 k, k, 0;\n\t"
+        "neg.s32 nk, k;\n\t"
+        "shr.s32 hk, k, 31;\n\t"
+        "add.cc.u32 %0, %0, nk;\n\t"
+        "addc.u32 %1, %1, hk;\n\t"
+        "}"
+        : "=&r"(z0), "=&r"(z1)
+        : "r"(w1), "r"(w3), "l"(u));
+    return mk64(z0, z1);
+  } else {
+    // y = (h:l) 2^8 = (y2:y1:y0); y 2^64 = y0 EPS - y1 - y2 2^32 (2^128 = -2^32)
+    // and k 2^136 = -k 2^40: value = y0 EPS - ((y2 + k 2^8) : y1)
+    uint32_t y0 = x.l << 8;
+    uint32_t y1 = __funnelshift_l(x.l, x.h, 8);
+    int32_t y2 = (int32_t)(x.h >> 24) + (int32_t)((uint32_t)x.k << 8);
+    uint64_t u;
+    asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(y0));
+    uint32_t z0, z1;
+    asm("{\n\t.reg .u32 k, nk, hk, u0, u1, y2h;\n\t"
+        "mov.b64 {u0, u1}, %4;\n\t"
+        "shr.s32 y2h, %3, 31;\n\t"
+        "sub.cc.u32 %0, u0, %2;\n\t"
+        "subc.cc.u32 %1, u1, %3;\n\t"
+        "subc.u32 k, 0, y2h;\n\t"
+        "neg.s32 nk, k;\n\t"
+        "shr.s32 hk, k, 31;\n\t"
+        "add.cc.u32 %0, %0, nk;\n\t"
+        "addc.u32 %1, %1, hk;\n\t"
+        "}"
+        : "=&r"(z0), "=&r"(z1)
+        : "r"(y1), "r"(y2), "l"(u));
+    return mk64(z0, z1);
   }
 }
 

@@ -62,16 +62,6 @@ __device__ __forceinline__ uint64_t round_tw(const Roots& R, int mlog, uint32_t 
 // Shared-memory index with one pad word per 16 to spread 8-byte banks.
 __device__ __forceinline__ uint32_t spad(uint32_t lin) { return lin + (lin >> 4); }
 
-template <int B>
-__device__ __forceinline__ void reg_bitrev(uint64_t* v) {
-  if constexpr (B == 2) {
-    uint64_t t = v[1]; v[1] = v[2]; v[2] = t;
-  } else if constexpr (B == 3) {
-    uint64_t t = v[1]; v[1] = v[4]; v[4] = t;
-    t = v[3]; v[3] = v[6]; v[6] = t;
-  }
-}
-
 // DIF radix-2 butterfly with a constant shift twiddle 2^S (S = 0: none).
 template <int S>
 __device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
@@ -80,69 +70,95 @@ __device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
   b = gl::shl<S>(gl::sub(u, w));
 }
 
-// DIT radix-2 butterfly with the inverse shift twiddle 2^(-S) = 2^(192-S).
-template <int S>
-__device__ __forceinline__ void bfly_dit(uint64_t& a, uint64_t& b) {
-  uint64_t u = a, w = (S == 0) ? b : gl::shl<(192 - S) % 192>(b);
-  a = gl::add(u, w);
-  b = gl::sub(u, w);
-}
-
 // Forward DFT of 2^B values in registers: v[k] <- sum_m v[m] w^(m k), with
 // w = 2^(192 / 2^B) (the 8th root of unity is 2^24).  Natural-order output.
+// Radix 4 and 8 run on lazy values (see gl.cuh) and fold once at the end.
 template <int B>
 __device__ __forceinline__ void dft_fwd(uint64_t* v) {
+  using namespace gl;
   if constexpr (B == 1) {
     bfly_dif<0>(v[0], v[1]);
   } else if constexpr (B == 2) {
-    bfly_dif<0>(v[0], v[2]);
-    bfly_dif<48>(v[1], v[3]);
-    bfly_dif<0>(v[0], v[1]);
-    bfly_dif<0>(v[2], v[3]);
+    Lz a0 = lz_add(lz(v[0]), lz(v[2])), c = lz_sub(lz(v[0]), lz(v[2]));
+    Lz a1 = lz_add(lz(v[1]), lz(v[3]));
+    Lz d = lz(lz_shl<48>(lz_sub(lz(v[1]), lz(v[3]))));
+    v[0] = fold(lz_add(a0, a1));
+    v[1] = fold(lz_add(c, d));
+    v[2] = fold(lz_sub(a0, a1));
+    v[3] = fold(lz_sub(c, d));
   } else {
     static_assert(B == 3, "radix 2, 4 or 8");
-    bfly_dif<0>(v[0], v[4]);
-    bfly_dif<24>(v[1], v[5]);
-    bfly_dif<48>(v[2], v[6]);
-    bfly_dif<72>(v[3], v[7]);
-    bfly_dif<0>(v[0], v[2]);
-    bfly_dif<48>(v[1], v[3]);
-    bfly_dif<0>(v[4], v[6]);
-    bfly_dif<48>(v[5], v[7]);
-    bfly_dif<0>(v[0], v[1]);
-    bfly_dif<0>(v[2], v[3]);
-    bfly_dif<0>(v[4], v[5]);
-    bfly_dif<0>(v[6], v[7]);
+    // stage 1: x_k +- x_(k+4), differences times w^k = 2^(24k)
+    Lz a0 = lz_add(lz(v[0]), lz(v[4])), d0 = lz_sub(lz(v[0]), lz(v[4]));
+    Lz a1 = lz_add(lz(v[1]), lz(v[5])), d1 = lz_sub(lz(v[1]), lz(v[5]));
+    Lz a2 = lz_add(lz(v[2]), lz(v[6])), d2 = lz_sub(lz(v[2]), lz(v[6]));
+    Lz a3 = lz_add(lz(v[3]), lz(v[7])), d3 = lz_sub(lz(v[3]), lz(v[7]));
+    Lz b1 = lz(lz_shl<24>(d1)), b2 = lz(lz_shl<48>(d2)), b3 = lz(lz_shl<72>(d3));
+    // stage 2: radix-4 halves, the odd difference times w^2 = 2^48
+    Lz c0 = lz_add(a0, a2), c2 = lz_sub(a0, a2);
+    Lz c1 = lz_add(a1, a3), c3 = lz(lz_shl<48>(lz_sub(a1, a3)));
+    Lz e0 = lz_add(d0, b2), e2 = lz_sub(d0, b2);
+    Lz e1 = lz_add(b1, b3), e3 = lz(lz_shl<48>(lz_sub(b1, b3)));
+    // stage 3 with the output bit reversal folded into the stores
+    v[0] = fold(lz_add(c0, c1));
+    v[4] = fold(lz_sub(c0, c1));
+    v[2] = fold(lz_add(c2, c3));
+    v[6] = fold(lz_sub(c2, c3));
+    v[1] = fold(lz_add(e0, e1));
+    v[5] = fold(lz_sub(e0, e1));
+    v[3] = fold(lz_add(e2, e3));
+    v[7] = fold(lz_sub(e2, e3));
   }
-  reg_bitrev<B>(v);
 }
 
-// Unscaled inverse of dft_fwd: v[m] <- sum_k v[k] w^(-m k)  (= 2^B * x[m]).
+// Unscaled inverse of dft_fwd on lazy inputs (|k| <= 1, e.g. twiddle
+// products from lz_mul): v[m] <- sum_k x[k] w^(-m k)  (= 2^B * original).
+// w^-s = -w^(96 - s): the DIT butterfly u +- w^-s b becomes u -+ 2^(96-s) b.
 template <int B>
-__device__ __forceinline__ void dft_inv(uint64_t* v) {
-  reg_bitrev<B>(v);
+__device__ __forceinline__ void dft_inv_lz(const gl::Lz* x, uint64_t* v) {
+  using namespace gl;
   if constexpr (B == 1) {
-    bfly_dit<0>(v[0], v[1]);
+    v[0] = fold(lz_add(x[0], x[1]));
+    v[1] = fold(lz_sub(x[0], x[1]));
   } else if constexpr (B == 2) {
-    bfly_dit<0>(v[0], v[1]);
-    bfly_dit<0>(v[2], v[3]);
-    bfly_dit<0>(v[0], v[2]);
-    bfly_dit<48>(v[1], v[3]);
+    // inputs in bit-reversed order (x0, x2, x1, x3)
+    Lz s = lz_add(x[0], x[2]), d = lz_sub(x[0], x[2]);
+    Lz t = lz_add(x[1], x[3]);
+    Lz e = lz(lz_shl<48>(lz_sub(x[1], x[3])));
+    v[0] = fold(lz_add(s, t));
+    v[2] = fold(lz_sub(s, t));
+    v[1] = fold(lz_sub(d, e));
+    v[3] = fold(lz_add(d, e));
   } else {
     static_assert(B == 3, "radix 2, 4 or 8");
-    bfly_dit<0>(v[0], v[1]);
-    bfly_dit<0>(v[2], v[3]);
-    bfly_dit<0>(v[4], v[5]);
-    bfly_dit<0>(v[6], v[7]);
-    bfly_dit<0>(v[0], v[2]);
-    bfly_dit<48>(v[1], v[3]);
-    bfly_dit<0>(v[4], v[6]);
-    bfly_dit<48>(v[5], v[7]);
-    bfly_dit<0>(v[0], v[4]);
-    bfly_dit<24>(v[1], v[5]);
-    bfly_dit<48>(v[2], v[6]);
-    bfly_dit<72>(v[3], v[7]);
+    // inputs in bit-reversed order (x0, x4, x2, x6, x1, x5, x3, x7)
+    Lz s01 = lz_add(x[0], x[4]), d01 = lz_sub(x[0], x[4]);
+    Lz s23 = lz_add(x[2], x[6]), d23 = lz_sub(x[2], x[6]);
+    Lz s45 = lz_add(x[1], x[5]), d45 = lz_sub(x[1], x[5]);
+    Lz s67 = lz_add(x[3], x[7]), d67 = lz_sub(x[3], x[7]);
+    Lz t23 = lz(lz_shl<48>(d23)), t67 = lz(lz_shl<48>(d67));
+    Lz v0 = lz_add(s01, s23), v2 = lz_sub(s01, s23);
+    Lz v1 = lz_sub(d01, t23), v3 = lz_add(d01, t23);
+    Lz v4 = lz_add(s45, s67), v6 = lz_sub(s45, s67);
+    Lz v5 = lz_sub(d45, t67), v7 = lz_add(d45, t67);
+    Lz t5 = lz(lz_shl<72>(v5)), t6 = lz(lz_shl<48>(v6)), t7 = lz(lz_shl<24>(v7));
+    v[0] = fold(lz_add(v0, v4));
+    v[4] = fold(lz_sub(v0, v4));
+    v[1] = fold(lz_sub(v1, t5));
+    v[5] = fold(lz_add(v1, t5));
+    v[2] = fold(lz_sub(v2, t6));
+    v[6] = fold(lz_add(v2, t6));
+    v[3] = fold(lz_sub(v3, t7));
+    v[7] = fold(lz_add(v3, t7));
   }
+}
+
+template <int B>
+__device__ __forceinline__ void dft_inv(uint64_t* v) {
+  gl::Lz x[1 << B];
+#pragma unroll
+  for (int k = 0; k < (1 << B); k++) x[k] = gl::lz(v[k]);
+  dft_inv_lz<B>(x, v);
 }
 
 // ---------------------------------------------------------------- rounds
@@ -219,13 +235,19 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
     const uint32_t jp = rest & ((1u << SLOG) - 1);
     const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
     uint64_t v[1 << B];
+    gl::Lz x[1 << B];
 #pragma unroll
     for (int k = 0; k < (1 << B); k++) v[k] = sm[spad(((row0 + (k << SLOG)) << T) | j)];
-    if constexpr (SLOG > 0) {
+    x[0] = gl::lz(v[0]);
 #pragma unroll
-      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
+    for (int k = 1; k < (1 << B); k++) {
+      if constexpr (SLOG > 0) {
+        x[k] = gl::lz_mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
+      } else {
+        x[k] = gl::lz(v[k]);
+      }
     }
-    dft_inv<B>(v);
+    dft_inv_lz<B>(x, v);
 #pragma unroll
     for (int m = 0; m < (1 << B); m++) sm[spad(((row0 + (m << SLOG)) << T) | j)] = v[m];
   }
@@ -307,13 +329,14 @@ __device__ __forceinline__ void round_inv(uint64_t* sm, TileGeom g, int mlog, co
     uint32_t jp = rest & smask;
     uint32_t row0 = ((rest >> slog) << mlog) + jp;
     uint64_t v[1 << B];
+    gl::Lz x[1 << B];
 #pragma unroll
     for (int k = 0; k < (1 << B); k++) v[k] = sm[spad(((row0 + (k << slog)) << g.t) | j)];
-    if (slog > 0) {
+    x[0] = gl::lz(v[0]);
 #pragma unroll
-      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], round_tw(R, mlog, k * jp, true));
-    }
-    dft_inv<B>(v);
+    for (int k = 1; k < (1 << B); k++)
+      x[k] = slog > 0 ? gl::lz_mul(v[k], round_tw(R, mlog, k * jp, true)) : gl::lz(v[k]);
+    dft_inv_lz<B>(x, v);
 #pragma unroll
     for (int m = 0; m < (1 << B); m++) sm[spad(((row0 + (m << slog)) << g.t) | j)] = v[m];
   }
