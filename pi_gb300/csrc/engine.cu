@@ -157,12 +157,10 @@ static uint64_t find_rho() {
 //   first pass (p = 0):   2^R rows x 2^(12-R) columns of the single block
 //   middle passes:        2^(9-R) blocks x 2^R rows x 8 columns
 //   last pass (S = 1):    2^(12-R) contiguous blocks of 2^R words
-// Column tiles read 64-byte (or wider) row segments.  The inverse first pass,
-// which folds 16-coefficient carry windows out of its rows, uses 2^13-word
-// tiles (rows of at least 16 consecutive coefficients).
+// Column tiles read 64-byte (or wider) row segments; first-pass rows hold at
+// least 8 consecutive coefficients, one carry window.
 constexpr int PASS_THREADS = 256;
 constexpr int TILE_LOG = 12;
-constexpr int CARRY_TILE_LOG = 13;
 // Resident CTAs per SM the pass kernels are register-limited for.
 #ifndef PIMUL_PASS_MIN_CTAS
 #define PIMUL_PASS_MIN_CTAS 5
@@ -179,7 +177,6 @@ __device__ __forceinline__ void load_tw512(uint64_t* tw, const Roots& R) {
 // Elements per thread in a pass tile, processed in groups of 8 so that
 // every thread keeps 8 independent global loads in flight.
 constexpr int PER_THREAD = (1 << TILE_LOG) / PASS_THREADS;
-constexpr int PER_THREAD_CARRY = (1 << CARRY_TILE_LOG) / PASS_THREADS;
 
 // One product of a batch (or the only product of a plain call): operands,
 // output and its scratch.  Kernels take `const Job* jobs, Job one`: with a
@@ -367,21 +364,43 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
 }
 
 // ---- carry normalisation (crates/bignum/src/ntt.rs:676-791) --------------
-// Coefficients are grouped in windows of 16 (= 4 limbs).  Window w has value
-// V_w = sum_t c[16w+t] 2^(16t) = lo_w + hi_w 2^256.  The product is
-// sum_w (lo_w + hi_(w-1)) 2^(256w); s_w = lo_w + hi_(w-1) may carry one bit
-// (g_w) into window w+1, which a run of all-ones windows (p_w) propagates.
-// Carries are resolved with a carry-lookahead scan over (g, p) bit vectors:
-// with A = g|p and B = g, the carry into each window is bit w of
+// Coefficients are grouped in windows of 8 (= 2 limbs).  Window w has value
+// V_w = sum_t c[8w+t] 2^(16t) = lo_w + hi_w 2^128 (hi_w < 2^49).  The
+// product is sum_w (lo_w + hi_(w-1)) 2^(128w); s_w = lo_w + hi_(w-1) may
+// carry one bit (g_w) into window w+1, which a run of all-ones windows (p_w)
+// propagates.  Carries are resolved with a carry-lookahead scan over (g, p)
+// bit vectors: with A = g|p and B = g, the carry into each window is bit w of
 // (A + B + cin) ^ A ^ B.
+constexpr int WIN_COEFFS = 8;
+constexpr int WIN_LIMBS = 2;
 
+struct Win2 {
+  uint64_t l[2];
+  uint64_t hi;
+};
+
+// Window value from 8 canonical coefficients (u128 accumulator, as the
+// reference's unpack loop, ntt.rs:694-707).
+__device__ __forceinline__ Win2 fold8(const uint64_t* c8) {
+  Win2 r;
+  unsigned __int128 acc = 0;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc += (unsigned __int128)c8[4 * k + q] << (16 * q);
+    r.l[k] = (uint64_t)acc;
+    acc >>= 64;
+  }
+  r.hi = (uint64_t)acc;
+  return r;
+}
+
+// 16-coefficient windows of the one-CTA multiply (its own carry chain).
 struct Win {
   uint64_t l[4];
   uint64_t hi;
 };
 
-// Window value from 16 canonical coefficients (u128 accumulator, as the
-// reference's unpack loop, ntt.rs:694-707).
 __device__ __forceinline__ Win fold16(const uint64_t* c16, int stride) {
   Win r;
   unsigned __int128 acc = 0;
@@ -399,7 +418,7 @@ __device__ __forceinline__ Win fold16(const uint64_t* c16, int stride) {
 constexpr int CARRY_THREADS = 256;  // windows per CTA
 
 __host__ __device__ __forceinline__ uint64_t n_windows(uint64_t la, uint64_t lb) {
-  return (4 * la + 4 * lb - 1 + 15) / 16;
+  return (4 * la + 4 * lb - 1 + WIN_COEFFS - 1) / WIN_COEFFS;
 }
 __host__ __device__ __forceinline__ uint64_t n_chunks(uint64_t nwin) {
   return (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
@@ -412,24 +431,24 @@ __host__ __device__ __forceinline__ uint64_t aux_bytes_for(uint64_t nwin) {
 }
 
 // Inverse pass 0 (natural order out) fused with the window fold: each tile
-// row holds 2^T consecutive coefficients = 2^(T-4) windows; every window
-// writes its low 4 limbs to the output and its high part to H.
+// row holds 2^T consecutive coefficients = 2^(T-3) windows; every window
+// writes its low 2 limbs to the output and its high part to H.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
-  constexpr int T = CARRY_TILE_LOG - R;
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
+  constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   const uint64_t* __restrict__ data = job_array(J, 2);
   uint64_t* __restrict__ out = J.out;
   uint64_t* __restrict__ H = J.H;
   const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb);
   extern __shared__ uint64_t sm[];
-  uint64_t* tw = sm + spad(1u << CARRY_TILE_LOG);
+  uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
   load_tw512(tw, RT);
 #pragma unroll 1
-  for (int g = 0; g < PER_THREAD_CARRY; g += 8) {
+  for (int g = 0; g < PER_THREAD; g += 8) {
     uint64_t v8[8], t8[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -448,18 +467,18 @@ __global__ void __launch_bounds__(PASS_THREADS) k_inv_first_carry(const Job* job
   }
   __syncthreads();
   tile_inv_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t q = tid; q < (1u << (CARRY_TILE_LOG - 4)); q += PASS_THREADS) {
-    uint32_t i = q >> (T - 4), k = q & ((1u << (T - 4)) - 1);
-    uint64_t w = ((((uint64_t)i << S) + j0) >> 4) + k;
+  for (uint32_t q = tid; q < (1u << (TILE_LOG - 3)); q += PASS_THREADS) {
+    uint32_t i = q >> (T - 3), k = q & ((1u << (T - 3)) - 1);
+    uint64_t w = ((((uint64_t)i << S) + j0) >> 3) + k;
     if (w >= nwin) continue;
-    uint64_t c[16];
-    uint32_t b = (i << T) + 16 * k;
+    uint64_t c[8];
+    uint32_t b = (i << T) + 8 * k;
 #pragma unroll
-    for (int t = 0; t < 16; t++) c[t] = gl::canon(sm[spad(b + t)]);
-    Win v = fold16(c, 1);
+    for (int t = 0; t < 8; t++) c[t] = gl::canon(sm[spad(b + t)]);
+    Win2 v = fold8(c);
 #pragma unroll
-    for (int t = 0; t < 4; t++)
-      if (4 * w + t < nlimbs) out[4 * w + t] = v.l[t];
+    for (int t = 0; t < 2; t++)
+      if (2 * w + t < nlimbs) out[2 * w + t] = v.l[t];
     H[w] = v.hi;
   }
 }
@@ -480,23 +499,17 @@ __global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   bool g = false, p = false;
   if (w < nwin) {
-    uint64_t base = 4 * w;
+    uint64_t base = WIN_LIMBS * w;
     uint64_t l0 = base + 0 < nlimbs ? out[base + 0] : 0;
     uint64_t l1 = base + 1 < nlimbs ? out[base + 1] : 0;
-    uint64_t l2 = base + 2 < nlimbs ? out[base + 2] : 0;
-    uint64_t l3 = base + 3 < nlimbs ? out[base + 3] : 0;
     uint64_t hprev = w > 0 ? H[w - 1] : 0;
     uint64_t s0 = l0 + hprev;
     uint64_t c = s0 < hprev;
     uint64_t s1 = l1 + c;  c = c && s1 == 0;
-    uint64_t s2 = l2 + c;  c = c && s2 == 0;
-    uint64_t s3 = l3 + c;  c = c && s3 == 0;
     g = c != 0;
-    p = (s0 & s1 & s2 & s3) == ~0ull;
+    p = (s0 & s1) == ~0ull;
     if (base + 0 < nlimbs) out[base + 0] = s0;
     if (base + 1 < nlimbs) out[base + 1] = s1;
-    if (base + 2 < nlimbs) out[base + 2] = s2;
-    if (base + 3 < nlimbs) out[base + 3] = s3;
   }
   uint32_t A = __ballot_sync(0xFFFFFFFFu, g || p);
   uint32_t Bm = __ballot_sync(0xFFFFFFFFu, g);
@@ -577,8 +590,8 @@ __global__ void __launch_bounds__(CARRY_THREADS) k_carry_apply(const Job* jobs, 
   uint32_t A = masks[2 * (wbase + warp)], Bm = masks[2 * (wbase + warp) + 1];
   uint32_t carries = (A + Bm + cin) ^ A ^ Bm;
   if (w < nwin && ((carries >> lane) & 1)) {
-    uint64_t base = 4 * w;
-    for (int k = 0; k < 4 && base + k < nlimbs; k++) {
+    uint64_t base = WIN_LIMBS * w;
+    for (int k = 0; k < WIN_LIMBS && base + k < nlimbs; k++) {
       if (++out[base + k] != 0) break;
     }
   }
@@ -747,8 +760,7 @@ static cudaError_t set_smem_attrs_r() {
   if (R >= 7) {
     e = cudaFuncSetAttribute(k_fwd_first<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_inv_first_carry<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)pass_smem_bytes(CARRY_TILE_LOG));
+      e = cudaFuncSetAttribute(k_inv_first_carry<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   }
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -906,7 +918,6 @@ struct Launcher {
 static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32_t nj, int L, uint64_t max_chunk) {
   const Plan pl = make_plan(L);
   const dim3 grid((unsigned)(1ull << (L - TILE_LOG)), nj);
-  const dim3 cgrid_first((unsigned)(1ull << (L - CARRY_TILE_LOG)), nj);
   const size_t smem = pass_smem_bytes(TILE_LOG);
   const uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L (2^192 = 1)
   const int rl = pl.r[pl.np - 1];
@@ -939,8 +950,7 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
   }
   {
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<cgrid_first, PASS_THREADS,
-                                                                       pass_smem_bytes(CARRY_TILE_LOG), X.st>>>(jobs, one, L, X.R)));
+    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, L, X.R)));
   }
   {
     KTimer kt(K_CARRY, X.st, X.stats);
@@ -1943,7 +1953,7 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //  * scratch holds two transform arrays of at most 2^20 words plus the carry
 //    windows and scan flags: la + lb <= 262144 limbs (transform length
 //    N <= 2^20); larger products are rejected with PIMUL_EINVAL.  The
-//    scratch (16.5 MiB) and this path's own root tables (17 MiB) stay
+//    scratch (17 MiB) and this path's own root tables (17 MiB) stay
 //    resident on every GPU that loads this library, until the process exits.
 //  * every call uses the same array, and the array keeps the previous call's
 //    contents; the kernels overwrite every scratch word before reading it,
@@ -1957,7 +1967,7 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 namespace pimul {
 constexpr int NOALLOC_LOG_MAX = 20;
 constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;
-constexpr uint64_t NOALLOC_WIN_MAX = NOALLOC_N_MAX / 16;
+constexpr uint64_t NOALLOC_WIN_MAX = NOALLOC_N_MAX / WIN_COEFFS;
 constexpr uint64_t NOALLOC_CHUNK_MAX = (NOALLOC_WIN_MAX + CARRY_THREADS - 1) / CARRY_THREADS;
 constexpr uint64_t NOALLOC_AUX_WORDS = (NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64) / 8 + 1;
 static_assert(NOALLOC_AUX_WORDS * 8 >= NOALLOC_CHUNK_MAX * (CARRY_THREADS / 32) * 8 + 2 * NOALLOC_CHUNK_MAX + 64,
