@@ -602,9 +602,25 @@ def run_pi(args):
         args.gl_digits = g
     run = pm.pi_gauss_legendre if args.algorithm == "gl" else pm.pi_chudnovsky
     run(min(D, 100_000))  # warm-up (tables, pools, kernels)
-    t0 = time.perf_counter()
-    s, info = run(D)
-    wall = time.perf_counter() - t0
+    batched = None
+    if args.algorithm == "chudnovsky" and args.pi_mode in ("batched", "both"):
+        pm.pi_chudnovsky_batched(min(D, 100_000), args.leaf_terms)
+        t0 = time.perf_counter()
+        sb, binfo = pm.pi_chudnovsky_batched(D, args.leaf_terms)
+        bwall = time.perf_counter() - t0
+        batched = {"wall_s": round(bwall, 3), "leaf_terms": args.leaf_terms or 64,
+                   "phases_ms": {k: round(v, 1) for k, v in binfo.items() if k.endswith("_ms")},
+                   "gpu_products": binfo["ntt_products"], "batched_levels": binfo["batched_levels"],
+                   "sha256": hashlib.sha256(sb.encode()).hexdigest()}
+    if batched is not None and args.pi_mode == "batched":
+        s, info, wall = sb, binfo, bwall
+    else:
+        t0 = time.perf_counter()
+        s, info = run(D)
+        wall = time.perf_counter() - t0
+    if batched is not None and args.pi_mode == "both":
+        batched["digits_identical_to_plain"] = sb == s
+        batched["speedup_vs_plain"] = round(wall / bwall, 3)
     cpu = None
     same = None
     if not args.no_cpu_baseline:
@@ -634,10 +650,15 @@ def run_pi(args):
         "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "deterministic (no random input)",
         "config": {"workload": f"{'Gauss-Legendre AGM' if args.algorithm == 'gl' else 'Chudnovsky binary splitting'}"
-                               f" for pi to {D} decimal digits, products >= 8192 limbs on the GPU (one call per product)"},
+                               f" for pi to {D} decimal digits, "
+                               + ("binary splitting level by level through the batched GPU multiply, "
+                                  "other products >= 8192 limbs one call each"
+                                  if args.pi_mode == "batched" and args.algorithm == "chudnovsky" else
+                                  "products >= 8192 limbs on the GPU (one call per product)")},
         "phases_ms": {k: round(v, 1) for k, v in info.items() if k.endswith("_ms")},
         "gpu_products": info["ntt_products"], "gpu_products_by_length": info.get("ntt_hist"),
         "digits_match_cpu_run": same, "digits_match_mpmath_sha256": golden,
+        "batched_binary_splitting": batched,
         "gauss_legendre": None if other_same is None else {"wall_s": round(args.gl_wall, 3),
                                                            "digits_identical_to_chudnovsky": other_same},
         "sha256": hashlib.sha256(s.encode()).hexdigest(),
@@ -763,6 +784,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-API leg (profiling runs)")
     ap.add_argument("--digits", type=int, default=1_000_000)
     ap.add_argument("--algorithm", choices=["chudnovsky", "gl", "both"], default="chudnovsky")
+    ap.add_argument("--pi-mode", choices=["plain", "batched", "both"], default="both",
+                    help="Chudnovsky binary splitting: one GPU call per product, level-batched, or both")
+    ap.add_argument("--leaf-terms", type=int, default=0, help="terms per host-split leaf (0 = 64)")
     ap.add_argument("--positions", type=int, default=256)
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)

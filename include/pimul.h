@@ -195,6 +195,37 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
                         double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33);
 
 /*
+ * Batched form of pimul_pi_chudnovsky: the binary splitting runs level by
+ * level, each level's independent products (T_L Q_R, P_L T_R, P_L P_R,
+ * Q_L Q_R for every neighbouring pair) in one pimul_mul_batch call, from
+ * leaves of leaf_terms terms (0 = 64) split on host threads.  The final
+ * assembly and decimal conversion are pimul_pi_chudnovsky's (GPU multiply
+ * at the reference's NTT threshold).  Optional outputs: phase_ms[3] as
+ * above; gpu_products = products sent to the GPU (batched and plain);
+ * levels = batched levels; ntt_hist33[L] = products with transform 2^L.
+ * The digits are identical to pimul_pi_chudnovsky's.
+ *
+ * Replaces: crates/pi-core/src/algorithm/chudnovsky.rs:75 Chudnovsky::compute,
+ * whose binary splitting (chudnovsky.rs:377-413) issues each level's
+ * products as independent rayon tasks.
+ */
+int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms, double* phase_ms,
+                                uint64_t* gpu_products, uint64_t* levels, uint64_t* ntt_hist33);
+
+/*
+ * Decimal string of the non-negative integer limbs[0..n) (little-endian u64,
+ * "0" for n == 0 or zero), without a terminator.  *len receives the length;
+ * a NULL or short `out` returns PIMUL_EINVAL after setting *len.  batched = 0:
+ * the reference's recursive divide and conquer (large products one GPU call
+ * each); batched != 0: level by level on powers 10^(19 2^k) with each
+ * level's products in one pimul_mul_batch call.  Both give the same string.
+ *
+ * Replaces: crates/bignum/src/integer.rs:892 Integer::to_string (the divide
+ * and conquer of integer.rs:892-983).
+ */
+int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size_t cap, size_t* len, int batched);
+
+/*
  * Digits of pi by the Gauss-Legendre AGM, same conventions as
  * pimul_pi_chudnovsky (phase_ms: iterations + final assembly, unused,
  * decimal conversion).

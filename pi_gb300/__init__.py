@@ -83,6 +83,10 @@ def load(build_if_stale: bool = True):
     L.pimul_pi_chudnovsky.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
                                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_pi_chudnovsky_batched.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_uint64,
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_to_decimal.argtypes = [_u64p, _sz, ctypes.c_char_p, _sz, ctypes.POINTER(_sz), ctypes.c_int]
     L.pimul_pi_gauss_legendre.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
@@ -303,6 +307,37 @@ def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
     return buf.raw[:digits].decode(), info
+
+
+def pi_chudnovsky_batched(digits: int, leaf_terms: int = 0):
+    """Digits of pi by Chudnovsky with the binary splitting run level by level
+    through the batched GPU multiply (pimul_pi_chudnovsky_batched); same
+    digits as pi_chudnovsky.  Returns (digits_str, info)."""
+    buf = ctypes.create_string_buffer(digits + 1)
+    ph = (ctypes.c_double * 3)()
+    n = ctypes.c_uint64(0)
+    lv = ctypes.c_uint64(0)
+    hist = (ctypes.c_uint64 * 33)()
+    _check(lib().pimul_pi_chudnovsky_batched(digits, buf, digits + 1, leaf_terms, ph, ctypes.byref(n),
+                                             ctypes.byref(lv), hist))
+    info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
+            "ntt_products": n.value, "batched_levels": lv.value,
+            "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
+    return buf.raw[:digits].decode(), info
+
+
+def to_decimal(limbs, batched: bool = True) -> str:
+    """Decimal string of a non-negative integer given as u64 limbs
+    (pimul_to_decimal; crates/bignum/src/integer.rs:892)."""
+    a = _limbs(limbs)
+    n = _sz(0)
+    rc = lib().pimul_to_decimal(a.ctypes.data_as(_u64p), a.size, None, 0, ctypes.byref(n), int(batched))
+    if n.value == 0:  # the length query itself failed
+        _check(rc)
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib().pimul_to_decimal(a.ctypes.data_as(_u64p), a.size, buf, n.value + 1, ctypes.byref(n),
+                                  int(batched)))
+    return buf.raw[: n.value].decode()
 
 
 def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0):

@@ -21,14 +21,19 @@
 //     chudnovsky.rs:75-413, util.rs:25-83, precision.rs:45-70).
 // The multiply backend is pluggable (C ABI pimul_pi_chudnovsky): the GPU
 // engine by default, or any function with pimul_mul's signature.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <functional>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "../../include/pimul.h"
 
@@ -814,6 +819,279 @@ static Flt gauss_legendre(uint64_t prec) {
   return div_at_prec(sq, flt_from_u64(4, 64), prec);
 }
 
+// ------------------------------------------------- batched binary splitting
+// Level-synchronous form of the binary splitting above (the device-batched
+// drive of chudnovsky.rs:377-413): leaves of `leaf` terms are split on host
+// threads, then every level merges neighbouring pairs,
+//   P = P_L P_R,   Q = Q_L Q_R,   T = T_L Q_R + P_L T_R,
+// with all of the level's products in one pimul_mul_batch call (operands
+// staged through one pinned buffer, one copy each way) and T's sum on host
+// threads.  The merge is associative, so the root (Q, T) is exactly the
+// recursive split's, whatever the bracketing.
+
+static void parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn) {
+  const size_t nt = std::max(1u, std::thread::hardware_concurrency());
+  if (n <= 1 || nt == 1) {
+    fn(0, n);
+    return;
+  }
+  const size_t parts = std::min(n, nt);
+  const size_t per = (n + parts - 1) / parts;
+  std::vector<std::thread> th;
+  for (size_t i = 1; i < parts; i++) {
+    size_t lo = i * per, hi = std::min(n, lo + per);
+    if (lo < hi) th.emplace_back(fn, lo, hi);
+  }
+  fn(0, std::min(n, per));
+  for (auto& t : th) t.join();
+}
+
+// Pinned host staging, a device buffer and a stream, grown on demand.
+struct LevelStaging {
+  cudaStream_t st = nullptr;
+  uint64_t* h = nullptr;
+  size_t h_words = 0;
+  uint64_t* d = nullptr;
+  size_t d_words = 0;
+  ~LevelStaging() {
+    if (h) cudaFreeHost(h);
+    if (d) cudaFree(d);
+    if (st) cudaStreamDestroy(st);
+  }
+  int init() {
+    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+    return PIMUL_OK;
+  }
+  int host(size_t w) {
+    if (w <= h_words) return PIMUL_OK;
+    if (h) cudaFreeHost(h);
+    h = nullptr;
+    size_t n = std::max(w, h_words + h_words / 2);
+    if (cudaHostAlloc((void**)&h, std::max<size_t>(n, 1) * 8, cudaHostAllocDefault) != cudaSuccess) {
+      h_words = 0;
+      return PIMUL_ENOMEM;
+    }
+    h_words = n;
+    return PIMUL_OK;
+  }
+  int dev(size_t w) {
+    if (w <= d_words) return PIMUL_OK;
+    if (d) cudaFree(d);
+    d = nullptr;
+    size_t n = std::max(w, d_words + d_words / 2);
+    if (cudaMalloc((void**)&d, std::max<size_t>(n, 1) * 8) != cudaSuccess) {
+      d_words = 0;
+      return PIMUL_ENOMEM;
+    }
+    d_words = n;
+    return PIMUL_OK;
+  }
+};
+
+static std::atomic<uint64_t> g_batch_levels{0};
+
+// Products a[i] * b[i] of magnitudes.  Those whose smaller operand has at
+// least gpu_min limbs go to the GPU in one pimul_mul_batch call: operands
+// deduplicated by address and staged through one pinned buffer (one copy
+// each way); the rest run on host threads through mul_mag.
+static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const Limbs*>& B,
+                     std::vector<Limbs>& out, LevelStaging& S, size_t gpu_min) {
+  const size_t n = A.size();
+  out.assign(n, Limbs());
+  std::vector<size_t> gi, ci;
+  for (size_t i = 0; i < n; i++) {
+    size_t la = A[i]->size(), lb = B[i]->size();
+    if (!la || !lb) continue;
+    bool fits = 4 * (la + lb) <= (1ull << 32);
+    (fits && std::min(la, lb) >= gpu_min ? gi : ci).push_back(i);
+  }
+  if (!gi.empty()) {
+    std::unordered_map<const Limbs*, size_t> off;
+    std::vector<const Limbs*> uniq;
+    std::vector<size_t> uoff, ooff(gi.size() + 1);
+    size_t in_w = 0, out_w = 0;
+    for (size_t g = 0; g < gi.size(); g++) {
+      for (const Limbs* x : {A[gi[g]], B[gi[g]]}) {
+        if (off.emplace(x, in_w).second) {
+          uniq.push_back(x);
+          uoff.push_back(in_w);
+          in_w += x->size();
+        }
+      }
+      ooff[g] = out_w;
+      out_w += A[gi[g]]->size() + B[gi[g]]->size();
+    }
+    ooff[gi.size()] = out_w;
+    int rc = S.host(std::max(in_w, out_w));
+    if (!rc) rc = S.dev(in_w + out_w);
+    if (rc) return rc;
+    parallel_for(uniq.size(), [&](size_t lo, size_t hi) {
+      for (size_t u = lo; u < hi; u++) memcpy(S.h + uoff[u], uniq[u]->data(), uniq[u]->size() * 8);
+    });
+    uint64_t* d_in = S.d;
+    uint64_t* d_out = S.d + in_w;
+    std::vector<pimul_job> jobs(gi.size());
+    for (size_t g = 0; g < gi.size(); g++) {
+      const Limbs* a = A[gi[g]];
+      const Limbs* b = B[gi[g]];
+      jobs[g] = pimul_job{d_in + off[a], a->size(), d_in + off[b], b->size(), d_out + ooff[g]};
+      uint64_t L2 = 0;
+      while ((1ull << L2) < 4 * (a->size() + b->size()) - 1) L2++;
+      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+    }
+    g_ntt_calls.fetch_add(gi.size(), std::memory_order_relaxed);
+    if (cudaMemcpyAsync(d_in, S.h, in_w * 8, cudaMemcpyHostToDevice, S.st) != cudaSuccess) return PIMUL_ECUDA;
+    rc = pimul_mul_batch(jobs.data(), jobs.size(), S.st);
+    if (rc) return rc;
+    if (cudaMemcpyAsync(S.h, d_out, out_w * 8, cudaMemcpyDeviceToHost, S.st) != cudaSuccess) return PIMUL_ECUDA;
+    if (cudaStreamSynchronize(S.st) != cudaSuccess) return PIMUL_ECUDA;
+    parallel_for(gi.size(), [&](size_t lo, size_t hi) {
+      for (size_t g = lo; g < hi; g++) {
+        Limbs r(S.h + ooff[g], S.h + ooff[g + 1]);
+        trim(r);
+        out[gi[g]] = std::move(r);
+      }
+    });
+  }
+  parallel_for(ci.size(), [&](size_t lo, size_t hi) {
+    for (size_t c = lo; c < hi; c++) out[ci[c]] = mul_mag(*A[ci[c]], *B[ci[c]]);
+  });
+  return g_error.load();
+}
+
+// One level: nodes[2i], nodes[2i+1] -> next[i]; an odd last node moves up as
+// it is.  At the root level (one pair) P is not needed.
+static int merge_level(std::vector<PQT>& nodes, LevelStaging& S) {
+  const size_t np = nodes.size() / 2;
+  const bool need_p = nodes.size() > 2;
+  const int per = need_p ? 4 : 3;
+  std::vector<const Limbs*> A, B;
+  A.reserve(np * per);
+  B.reserve(np * per);
+  for (size_t i = 0; i < np; i++) {
+    const PQT& L = nodes[2 * i];
+    const PQT& R = nodes[2 * i + 1];
+    A.push_back(&L.t.m), B.push_back(&R.q.m);  // T_L Q_R
+    A.push_back(&L.p.m), B.push_back(&R.t.m);  // P_L T_R
+    A.push_back(&L.q.m), B.push_back(&R.q.m);  // Q_L Q_R
+    if (need_p) A.push_back(&L.p.m), B.push_back(&R.p.m);  // P_L P_R
+  }
+  std::vector<Limbs> prod;
+  int rc = batch_mul(A, B, prod, S, 1);
+  if (rc) return rc;
+  std::vector<PQT> next(np + (nodes.size() & 1));
+  parallel_for(np, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; i++) {
+      const PQT& L = nodes[2 * i];
+      const PQT& R = nodes[2 * i + 1];
+      Limbs* pr = &prod[per * i];
+      PQT o;
+      o.t = add(Int(std::move(pr[0]), L.t.neg), Int(std::move(pr[1]), L.p.neg != R.t.neg));
+      o.q = Int(std::move(pr[2]), false);
+      if (need_p) o.p = Int(std::move(pr[3]), L.p.neg != R.p.neg);
+      next[i] = std::move(o);
+    }
+  });
+  if (nodes.size() & 1) next[np] = std::move(nodes.back());
+  nodes.swap(next);
+  g_batch_levels.fetch_add(1, std::memory_order_relaxed);
+  return PIMUL_OK;
+}
+
+static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
+  const uint64_t nleaf = (b - a + leaf - 1) / leaf;
+  std::vector<PQT> nodes(nleaf);
+  parallel_for(nleaf, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; i++) nodes[i] = split(a + i * leaf, std::min(b, a + (i + 1) * leaf), 4);
+  });
+  LevelStaging S;
+  int rc = S.init();
+  while (!rc && nodes.size() > 1) rc = merge_level(nodes, S);
+  if (rc) return rc;
+  q = std::move(nodes[0].q);
+  t = std::move(nodes[0].t);
+  return PIMUL_OK;
+}
+
+// ------------------------------------------------ batched decimal conversion
+// Level-synchronous divide and conquer on C = 10^19: with P_k = C^(2^k),
+// every node of level k (a value below P_k^2) splits into (q, r) = divmod by
+// P_k, high half first.  All nodes of a level share P_k and one reciprocal
+// V_k ~ 2^s / P_k (s = 2 bits(P_k) + 64), so floor(N V_k / 2^s) is within
+// one of the quotient; both products of the level (N V_k, then q P_k) go
+// through batch_mul.  Nodes below P_kmin are printed on host threads
+// (19 * 2^kmin digits each, zero-padded).  An integer has one decimal
+// string, so the output equals the reference's conversion
+// (crates/bignum/src/integer.rs:892-983).
+static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S) {
+  if (X.m.size() <= 256) {
+    outs = to_decimal_top(X);
+    return g_error.load();
+  }
+  const uint64_t ndig = dec_estimate(bits_of(X.m)) + 1;
+  const uint64_t nch = (ndig + 18) / 19;
+  int K = 0;
+  while ((1ull << K) < nch) K++;
+  const int kmin = std::min(K, 5);
+  std::vector<Int> P(K);
+  P[0] = Int(DEC_CHUNK);
+  for (int k = 1; k < K; k++) P[k] = mul(P[k - 1], P[k - 1]);
+  std::vector<Int> nodes{X};
+  for (int k = K - 1; k >= kmin; k--) {
+    const uint64_t b = bits_of(P[k].m);
+    const uint64_t sh = 2 * b + 64;
+    Flt r = reciprocal_at_prec(flt_from_int(P[k]), b + 128);
+    r.exp += (int64_t)sh;
+    const Int V = to_integer_down(r);
+    const size_t n = nodes.size();
+    std::vector<const Limbs*> A(n), B(n, &V.m);
+    for (size_t i = 0; i < n; i++) A[i] = &nodes[i].m;
+    std::vector<Limbs> nv;
+    int rc = batch_mul(A, B, nv, S, 32);
+    if (rc) return rc;
+    std::vector<Int> q(n);
+    parallel_for(n, [&](size_t lo, size_t hi) {
+      for (size_t i = lo; i < hi; i++) q[i] = Int(shr_mag(nv[i], sh), false);
+    });
+    nv.clear();
+    std::vector<const Limbs*> Aq(n), Bp(n, &P[k].m);
+    for (size_t i = 0; i < n; i++) Aq[i] = &q[i].m;
+    std::vector<Limbs> qp;
+    rc = batch_mul(Aq, Bp, qp, S, 32);
+    if (rc) return rc;
+    std::vector<Int> next(2 * n);
+    parallel_for(n, [&](size_t lo, size_t hi) {
+      for (size_t i = lo; i < hi; i++) {
+        Int qi = std::move(q[i]);
+        Int ri = sub(nodes[i], Int(std::move(qp[i]), false));
+        while (ri.neg) {
+          qi = sub(qi, Int(1));
+          ri = add(ri, P[k]);
+        }
+        while (cmp_mag(ri.m, P[k].m) >= 0) {
+          qi = add(qi, Int(1));
+          ri = sub(ri, P[k]);
+        }
+        next[2 * i] = std::move(qi);
+        next[2 * i + 1] = std::move(ri);
+      }
+    });
+    nodes.swap(next);
+  }
+  const size_t per = (size_t)19 << kmin;
+  std::string all(per * nodes.size(), '0');
+  parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; i++) {
+      if (nodes[i].zero()) continue;
+      std::string d = decimal_naive(nodes[i].m);
+      memcpy(&all[i * per + per - d.size()], d.data(), d.size());
+    }
+  });
+  size_t nz = all.find_first_not_of('0');
+  outs = nz == std::string::npos ? std::string("0") : all.substr(nz);
+  return g_error.load();
+}
+
 }  // namespace pihost
 
 using namespace pihost;
@@ -860,14 +1138,14 @@ extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, p
 // writes `digits` characters ("31415...", no decimal point) to out.
 // phase_ms (optional, 3 entries): binary splitting, final assembly,
 // decimal conversion.  backend NULL = the GPU engine (pimul_mul).
-extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
-                                   uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products,
-                                   uint64_t* ntt_hist33) {
+static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
+                      uint64_t leaf_terms, double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33) {
   if (digits == 0) return PIMUL_OK;
   if (!out || cap < digits) return PIMUL_EINVAL;
   g_backend = reinterpret_cast<mul_fn>(backend);
   g_ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
   g_ntt_calls.store(0);
+  g_batch_levels.store(0);
   for (auto& h : g_ntt_hist) h.store(0);
   g_error.store(0);
   // precision.rs:64: bits = ceil(D log2 10) + 256
@@ -882,7 +1160,15 @@ extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul
     sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
   });
   Int q, t;
-  split_root(1, n_terms + 1, q, t);
+  int brc = PIMUL_OK;
+  if (leaf_terms)
+    brc = split_root_batched(1, n_terms + 1, leaf_terms, q, t);
+  else
+    split_root(1, n_terms + 1, q, t);
+  if (brc) {
+    sqrt_th.join();
+    return brc;
+  }
   double t1 = now_ms();
   // final assembly (chudnovsky.rs:146-204)
   Int denom = add(mul(Int(CH_A), q), t);
@@ -896,7 +1182,15 @@ extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul
   Flt scale = pow_int(flt_from_u64(10, pi.prec), Int(digits - 1));
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
-  std::string s = to_decimal_top(ip);
+  std::string s;
+  if (leaf_terms) {
+    LevelStaging S;
+    int crc = S.init();
+    if (!crc) crc = to_decimal_batched(ip, s, S);
+    if (crc) return crc;
+  } else {
+    s = to_decimal_top(ip);
+  }
   double t3 = now_ms();
   if (g_error.load()) return g_error.load();
   if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
@@ -910,4 +1204,47 @@ extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul
   if (ntt_hist33)
     for (int i = 0; i < 33; i++) ntt_hist33[i] = g_ntt_hist[i].load();
   return PIMUL_OK;
+}
+
+extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                   uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products,
+                                   uint64_t* ntt_hist33) {
+  return chudnovsky(digits, out, cap, backend, ntt_threshold, 0, phase_ms, ntt_products, ntt_hist33);
+}
+
+// Decimal string of a non-negative integer (see pimul.h).
+extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size_t cap, size_t* len,
+                                int batched) {
+  if (!len || (n && !limbs)) return PIMUL_EINVAL;
+  g_backend = nullptr;
+  g_ntt_threshold = 8192;
+  g_error.store(0);
+  Int x(Limbs(limbs, limbs + n), false);
+  std::string s;
+  if (x.zero()) {
+    s = "0";
+  } else if (batched) {
+    LevelStaging S;
+    int rc = S.init();
+    if (!rc) rc = to_decimal_batched(x, s, S);
+    if (rc) return rc;
+  } else {
+    s = to_decimal_top(x);
+    if (g_error.load()) return g_error.load();
+  }
+  *len = s.size();
+  if (!out || cap < s.size()) return PIMUL_EINVAL;
+  memcpy(out, s.data(), s.size());
+  return PIMUL_OK;
+}
+
+// Batched form (see pimul.h): binary splitting level by level through
+// pimul_mul_batch, everything after it as in pimul_pi_chudnovsky.
+extern "C" int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms,
+                                           double* phase_ms, uint64_t* gpu_products, uint64_t* levels,
+                                           uint64_t* ntt_hist33) {
+  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : 64, phase_ms, gpu_products,
+                      ntt_hist33);
+  if (levels) *levels = g_batch_levels.load();
+  return rc;
 }

@@ -49,3 +49,22 @@ def test_1e7_digits_against_mpmath():
     assert info["ntt_products"] > 100
     assert s[-20:] == want["last20"]
     assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+
+
+@pytest.mark.parametrize("leaf", [7, 64])
+def test_batched_binary_splitting_1e5(leaf):
+    # level-batched splitting (odd node counts at some levels for leaf 7)
+    with open(os.path.join(HERE, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    s, info = pm.pi_chudnovsky_batched(100_000, leaf)
+    assert s == ref
+    assert info["batched_levels"] > 5 and info["ntt_products"] > 100
+
+
+def test_batched_binary_splitting_1e6_matches_mpmath_and_plain():
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, info = pm.pi_chudnovsky_batched(1_000_000)
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+    plain, _ = pm.pi_chudnovsky(1_000_000)
+    assert plain == s
