@@ -593,14 +593,20 @@ def run_pi(args):
     pm.init(0)
     D = args.digits
     other_same = None
+    gl_backend = pm.served_backend() if args.gl_backend == "served" else None
+
+    def gl_run(d, **kw):
+        return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend))
+
     if args.algorithm == "both":
+        gl_run(min(D, 100_000))
         t0 = time.perf_counter()
-        g, _ = pm.pi_gauss_legendre(D)
+        g, _ = gl_run(D)
         gl_wall = time.perf_counter() - t0
         args.algorithm = "chudnovsky"
         args.gl_wall = gl_wall
         args.gl_digits = g
-    run = pm.pi_gauss_legendre if args.algorithm == "gl" else pm.pi_chudnovsky
+    run = gl_run if args.algorithm == "gl" else pm.pi_chudnovsky
     run(min(D, 100_000))  # warm-up (tables, pools, kernels)
     batched = None
     if args.algorithm == "chudnovsky" and args.pi_mode in ("batched", "both"):
@@ -660,6 +666,7 @@ def run_pi(args):
         "digits_match_cpu_run": same, "digits_match_mpmath_sha256": golden,
         "batched_binary_splitting": batched,
         "gauss_legendre": None if other_same is None else {"wall_s": round(args.gl_wall, 3),
+                                                           "multiply": args.gl_backend,
                                                            "digits_identical_to_chudnovsky": other_same},
         "sha256": hashlib.sha256(s.encode()).hexdigest(),
         "last_digits": s[-20:], "cpu_baseline": cpu,
@@ -787,6 +794,8 @@ def main():
     ap.add_argument("--pi-mode", choices=["plain", "batched", "both"], default="both",
                     help="Chudnovsky binary splitting: one GPU call per product, level-batched, or both")
     ap.add_argument("--leaf-terms", type=int, default=0, help="terms per host-split leaf (0 = 64)")
+    ap.add_argument("--gl-backend", choices=["plain", "served"], default="plain",
+                    help="Gauss-Legendre products: one pimul_mul call each, or through the served form")
     ap.add_argument("--positions", type=int, default=256)
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)

@@ -172,6 +172,12 @@ int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uin
                         uint64_t* bytes_in_use);
 int pimul_service_reset_stats(void);
 
+/* pimul_mul's contract (host buffers, trimmed result, squares when a == b)
+ * carried out through the served form: upload, submit, wait, download,
+ * free.  Same signature as pimul_mul, so it can be a pimul_mul_fn backend. */
+int pimul_mul_served(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64_t* out, size_t out_cap,
+                     size_t* out_len);
+
 /* Signature of a multiply backend: pimul_mul's own. */
 typedef int (*pimul_mul_fn)(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64_t* out,
                             size_t out_cap, size_t* out_len);

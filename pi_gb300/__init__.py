@@ -309,6 +309,12 @@ def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
     return buf.raw[:digits].decode(), info
 
 
+def served_backend():
+    """Address of pimul_mul_served (pimul_mul's contract through the served
+    form), usable as the `backend` of pi_chudnovsky / pi_gauss_legendre."""
+    return ctypes.cast(lib().pimul_mul_served, ctypes.c_void_p).value
+
+
 def pi_chudnovsky_batched(digits: int, leaf_terms: int = 0):
     """Digits of pi by Chudnovsky with the binary splitting run level by level
     through the batched GPU multiply (pimul_pi_chudnovsky_batched); same

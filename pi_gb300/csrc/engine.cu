@@ -1887,6 +1887,37 @@ int pimul_service_reset_stats(void) {
   return PIMUL_OK;
 }
 
+// pimul_mul's contract through the served form: upload, submit, wait,
+// download, free.  A drop-in multiply backend for host drivers that want
+// every product to pass through the service.
+int pimul_mul_served(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64_t* out, size_t out_cap,
+                     size_t* out_len) {
+  if (!out_len) return fail(PIMUL_EINVAL, "null out_len");
+  *out_len = 0;
+  if (la == 0 || lb == 0) return PIMUL_OK;
+  if (!a || !b || !out) return fail(PIMUL_EINVAL, "null pointer");
+  if (out_cap < la + lb) return fail(PIMUL_EINVAL, "out_cap < la + lb");
+  const bool sq = a == b && la == lb;
+  uint64_t ha = 0, hb = 0, hc = 0, ticket = 0;
+  bool has_a = false, has_b = false, has_c = false;
+  int rc = pimul_upload(a, la, &ha);
+  has_a = rc == PIMUL_OK;
+  if (!rc && !sq) {
+    rc = pimul_upload(b, lb, &hb);
+    has_b = rc == PIMUL_OK;
+  }
+  if (!rc) {
+    rc = pimul_submit(sq ? PIMUL_OP_SQR : PIMUL_OP_MUL, ha, sq ? ha : hb, &hc, &ticket);
+    has_c = rc == PIMUL_OK;
+  }
+  if (!rc) rc = pimul_wait(ticket, -1);
+  if (!rc) rc = pimul_download(hc, out, out_cap, out_len);
+  if (has_c) pimul_free(hc);
+  if (has_b) pimul_free(hb);
+  if (has_a) pimul_free(ha);
+  return rc;
+}
+
 int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t lb, uint64_t* d_out,
                      void* stream) {
   if (la && lb && (!d_a || !d_b || !d_out)) return fail(PIMUL_EINVAL, "null device pointer");

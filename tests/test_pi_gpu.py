@@ -68,3 +68,12 @@ def test_batched_binary_splitting_1e6_matches_mpmath_and_plain():
     assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
     plain, _ = pm.pi_chudnovsky(1_000_000)
     assert plain == s
+
+
+def test_gauss_legendre_through_served_form():
+    # every product at or above 512 limbs goes upload -> submit -> wait -> download
+    with open(os.path.join(HERE, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    g, info = pm.pi_gauss_legendre(100_000, backend=pm.served_backend(), ntt_threshold=512)
+    assert g == ref
+    assert info["ntt_products"] > 0
