@@ -269,32 +269,27 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
   const uint64_t ct = blockIdx.x & ((1u << (S - T)) - 1);
   const uint64_t b0 = ((uint64_t)blockIdx.x >> (S - T)) << BC;
   const uint64_t j0 = ct << T;
-  load_tw512(tw, RT);
   auto gaddr = [&](uint32_t lin) {
     uint32_t j = lin & TM, i = (lin >> T) & ((1u << R) - 1), blk = lin >> (T + R);
     return ((b0 + blk) << mlog) + ((uint64_t)i << S) + j0 + j;
   };
-#pragma unroll 1
-  for (int g = 0; g < PER_THREAD; g += 8) {
-    uint64_t v8[8], t8[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) v8[q] = data[gaddr((g + q) * PASS_THREADS + tid)];
-    if (!FWD) {
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        uint32_t lin = (g + q) * PASS_THREADS + tid;
-        uint32_t i = (lin >> T) & ((1u << R) - 1);
-        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & TM)), true);
-      }
-#pragma unroll
-      for (int q = 0; q < 8; q++) v8[q] = gl::mul(v8[q], t8[q]);
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) sm[spad((g + q) * PASS_THREADS + tid)] = v8[q];
+  for (int q = 0; q < PER_THREAD; q++) {
+    const uint32_t lin = q * PASS_THREADS + tid;
+    cp_async8(sm + spad(lin), data + gaddr(lin));
   }
+  load_tw512(tw, RT);
+  cp_async_wait_all();
   __syncthreads();
-  if (FWD) tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
-  else tile_inv_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
+  if (FWD) {
+    tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
+  } else {
+    // inverse pass twiddles w_M^-(f*j), applied by the first inverse round
+    auto ptw = [&](uint32_t row, uint32_t j) {
+      return root_pow(RT, mlog, (uint64_t)row_freq_t<R>(row & ((1u << R) - 1)) * (j0 + j), true);
+    };
+    tile_inv_t<R, T, BC, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
+  }
 #pragma unroll 1
   for (int g = 0; g < PER_THREAD; g += 8) {
     uint64_t t8[8];
@@ -326,8 +321,13 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const 
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
   uint64_t* base = J.A + ((uint64_t)blockIdx.x << TILE_LOG);
+#pragma unroll
+  for (int q = 0; q < PER_THREAD; q++) {
+    const uint32_t lin = q * PASS_THREADS + tid;
+    cp_async8(sm + spad(lin), base + lin);
+  }
   load_tw512(tw, RT);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = base[lin];
+  cp_async_wait_all();
   __syncthreads();
   tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
   for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) base[lin] = sm[spad(lin)];
@@ -349,8 +349,13 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
   const uint64_t off = (uint64_t)blockIdx.x << TILE_LOG;
+#pragma unroll
+  for (int q = 0; q < PER_THREAD; q++) {
+    const uint32_t lin = q * PASS_THREADS + tid;
+    cp_async8(sm + spad(lin), c + off + lin);
+  }
   load_tw512(tw, RT);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) sm[spad(lin)] = c[off + lin];
+  cp_async_wait_all();
   __syncthreads();
   tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
   for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
@@ -446,27 +451,20 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
   const int tid = threadIdx.x;
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
-  load_tw512(tw, RT);
-#pragma unroll 1
-  for (int g = 0; g < PER_THREAD; g += 8) {
-    uint64_t v8[8], t8[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      uint32_t lin = (g + q) * PASS_THREADS + tid;
-      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-      v8[q] = data[((uint64_t)i << S) + j0 + j];
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      uint32_t lin = (g + q) * PASS_THREADS + tid;
-      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-      t8[q] = root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), true);
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) sm[spad((g + q) * PASS_THREADS + tid)] = gl::mul(v8[q], t8[q]);
+  for (int q = 0; q < PER_THREAD; q++) {
+    const uint32_t lin = q * PASS_THREADS + tid;
+    const uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
+    cp_async8(sm + spad(lin), data + ((uint64_t)i << S) + j0 + j);
   }
+  load_tw512(tw, RT);
+  cp_async_wait_all();
   __syncthreads();
-  tile_inv_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
+  // inverse pass twiddles w_N^-(f*j), applied by the first inverse round
+  auto ptw = [&](uint32_t row, uint32_t j) {
+    return root_pow(RT, L, (uint64_t)row_freq_t<R>(row) * (j0 + j), true);
+  };
+  tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
   for (uint32_t q = tid; q < (1u << (TILE_LOG - 3)); q += PASS_THREADS) {
     uint32_t i = q >> (T - 3), k = q & ((1u << (T - 3)) - 1);
     uint64_t w = ((((uint64_t)i << S) + j0) >> 3) + k;

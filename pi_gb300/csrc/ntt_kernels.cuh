@@ -19,6 +19,7 @@
 // butterflies' internal twiddles are constant shifts.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include "gl.cuh"
 
 namespace pimul {
@@ -61,6 +62,14 @@ __device__ __forceinline__ uint64_t round_tw(const Roots& R, int mlog, uint32_t 
 
 // Shared-memory index with one pad word per 16 to spread 8-byte banks.
 __device__ __forceinline__ uint32_t spad(uint32_t lin) { return lin + (lin >> 4); }
+
+// Asynchronous 8-byte global -> shared copy (no register round trip), and
+// the wait for all of this thread's outstanding copies.
+__device__ __forceinline__ void cp_async8(uint64_t* smem_dst, const uint64_t* gsrc) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // DIF radix-2 butterfly with a constant shift twiddle 2^S (S = 0: none).
 template <int S>
@@ -222,10 +231,17 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
   }
 }
 
-template <int R, int T, int BC, int B, int MLOG, int NT>
-__device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+// Pass twiddle applied by the first inverse round: none.
+struct NoPassTw {};
+
+// One inverse round; the first one executed (SLOG = 0, no round twiddles)
+// multiplies its inputs by the pass twiddles ptw(row, col) of the tile when
+// a functor is given, feeding the lazy products straight into the DFT.
+template <int R, int T, int BC, int B, int MLOG, int NT, class F>
+__device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512, int tid, const F& ptw) {
   constexpr int SLOG = MLOG - B;
   constexpr int ITEMS = 1 << (BC + R + T - B);
+  constexpr bool PTW = !std::is_same<F, NoPassTw>::value;
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
@@ -238,13 +254,18 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
     gl::Lz x[1 << B];
 #pragma unroll
     for (int k = 0; k < (1 << B); k++) v[k] = sm[spad(((row0 + (k << SLOG)) << T) | j)];
-    x[0] = gl::lz(v[0]);
+    if constexpr (SLOG == 0 && PTW) {
 #pragma unroll
-    for (int k = 1; k < (1 << B); k++) {
-      if constexpr (SLOG > 0) {
-        x[k] = gl::lz_mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
-      } else {
-        x[k] = gl::lz(v[k]);
+      for (int k = 0; k < (1 << B); k++) x[k] = gl::lz_mul(v[k], ptw(row0 + k, j));
+    } else {
+      x[0] = gl::lz(v[0]);
+#pragma unroll
+      for (int k = 1; k < (1 << B); k++) {
+        if constexpr (SLOG > 0) {
+          x[k] = gl::lz_mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
+        } else {
+          x[k] = gl::lz(v[k]);
+        }
       }
     }
     dft_inv_lz<B>(x, v);
@@ -262,10 +283,10 @@ __device__ __forceinline__ void tile_fwd_t(uint64_t* sm, const uint64_t* tw512, 
   }
 }
 
-template <int R, int T, int BC, int NT, int Q = rp_count(R) - 1>
-__device__ __forceinline__ void tile_inv_t(uint64_t* sm, const uint64_t* tw512, int tid) {
+template <int R, int T, int BC, int NT, int Q = rp_count(R) - 1, class F = NoPassTw>
+__device__ __forceinline__ void tile_inv_t(uint64_t* sm, const uint64_t* tw512, int tid, const F& ptw = F()) {
   if constexpr (Q >= 0) {
-    round_inv_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid);
+    round_inv_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid, ptw);
     __syncthreads();
     tile_inv_t<R, T, BC, NT, Q - 1>(sm, tw512, tid);
   }
