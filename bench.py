@@ -40,9 +40,12 @@ METRIC = "NTT-mul GB/s (2^30 x 2^30-bit product)"
 BITS_A = 1 << 30
 BITS_B = 1 << 30
 
-# DRAM traffic per launch of the dominant kernel from ncu (bytes read +
-# written, profiles/ summaries); None until captured for the current build.
-NCU_TRAFFIC_PER_LAUNCH = None
+# DRAM traffic of the dominant kernel class (forward passes) per transform
+# word: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
+# k_col_mid<9,fwd> (x2) and k_fwd_last<8> at N = 2^26 (mean 1023.2 MB per
+# launch = 15.25 bytes per word; profiles/ntt_pass_kernels_2e29_full.md).
+# Traffic grows in proportion to N, so a launch moves 15.25 N bytes.
+NCU_TRAFFIC_BYTES_PER_WORD = 15.25
 
 
 def b_mul(n, la, lb, square=False):
@@ -332,7 +335,7 @@ def run_gpu(args):
                     "api": "pimul_mul (host buffers, pinned)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": NCU_TRAFFIC_PER_LAUNCH,
+                         "traffic": round(NCU_TRAFFIC_BYTES_PER_WORD * N) if dom == "pass_fwd" else None,
                          "bytes_per_launch": per_launch, "avg_launch_ms": round(avg_ms, 4),
                          "step_achieved": round(step_achieved, 1),
                          "step_frac": round(step_achieved / peak, 4)},
