@@ -235,21 +235,22 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
   }
   __syncthreads();
   tile_fwd_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
-#pragma unroll 1
+  // element e of this thread: lin = e * 256 + tid, row (e << TL) + (tid >> T),
+  // column tid & (2^T - 1); address and twiddle exponent split into a
+  // per-thread part and a compile-time part
+  constexpr int TL = 8 - T;
+  const uint32_t tlo = tid >> T, jj = tid & ((1u << T) - 1);
+  const uint64_t gbase = ((uint64_t)tlo << S) + j0 + jj;
+  const uint32_t Jc = (uint32_t)(j0 + jj);
+  const uint32_t eJ = row_freq_t<R>(tlo) * Jc;
+#pragma unroll 2
   for (int g = 0; g < PER_THREAD; g += 8) {
     uint64_t t8[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      uint32_t lin = (g + q) * PASS_THREADS + tid;
-      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-      t8[q] = root_pow(RT, L, (uint64_t)row_freq_t<R>(i) * (j0 + j), false);
-    }
+    for (int q = 0; q < 8; q++) t8[q] = root_pow32(RT, L, eJ + row_freq_t<R>((g + q) << TL) * Jc, false);
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      uint32_t lin = (g + q) * PASS_THREADS + tid;
-      uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-      data[((uint64_t)i << S) + j0 + j] = gl::mul(sm[spad(lin)], t8[q]);
-    }
+    for (int q = 0; q < 8; q++)
+      data[gbase + ((uint64_t)((g + q) << TL) << S)] = gl::mul(sm[spad((g + q) * PASS_THREADS + tid)], t8[q]);
   }
 }
 
@@ -258,7 +259,9 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
 template <int R, bool FWD>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT) {
   constexpr int T = TILE_LOG - 9, BC = 9 - R;
-  constexpr uint32_t TM = (1u << T) - 1;
+  constexpr int TL = 8 - T;  // row bits covered by tid >> T
+  static_assert(R >= TL, "thread index must stay inside one block's rows");
+  constexpr uint32_t TM = (1u << T) - 1, RM = (1u << R) - 1;
   const Job J = job_of(jobs, one);
   if (FWD && which == 1 && is_square(J)) return;
   uint64_t* __restrict__ data = job_array(J, which);
@@ -269,44 +272,41 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
   const uint64_t ct = blockIdx.x & ((1u << (S - T)) - 1);
   const uint64_t b0 = ((uint64_t)blockIdx.x >> (S - T)) << BC;
   const uint64_t j0 = ct << T;
-  auto gaddr = [&](uint32_t lin) {
-    uint32_t j = lin & TM, i = (lin >> T) & ((1u << R) - 1), blk = lin >> (T + R);
-    return ((b0 + blk) << mlog) + ((uint64_t)i << S) + j0 + j;
+  // element q of this thread (lin = q * 256 + tid): block q >> (R - TL), row
+  // ((q << TL) & RM) + (tid >> T), column tid & TM
+  const uint32_t tlo = tid >> T, jj = tid & TM;
+  const uint64_t gbase = (b0 << mlog) + ((uint64_t)tlo << S) + j0 + jj;
+  auto gaddr = [&](int q) {
+    return gbase + ((uint64_t)(q >> (R - TL)) << mlog) + ((uint64_t)((q << TL) & RM) << S);
   };
 #pragma unroll
-  for (int q = 0; q < PER_THREAD; q++) {
-    const uint32_t lin = q * PASS_THREADS + tid;
-    cp_async8(sm + spad(lin), data + gaddr(lin));
-  }
+  for (int q = 0; q < PER_THREAD; q++) cp_async8(sm + spad(q * PASS_THREADS + tid), data + gaddr(q));
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();
+  const uint32_t Jc = (uint32_t)(j0 + jj);
   if (FWD) {
     tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
+    // outgoing pass twiddles w_M^(f*j)
+    const uint32_t eJ = row_freq_t<R>(tlo) * Jc;
+#pragma unroll 1
+    for (int g = 0; g < PER_THREAD; g += 8) {
+      uint64_t t8[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        t8[q] = root_pow32(RT, mlog, eJ + row_freq_t<R>(((g + q) << TL) & RM) * Jc, false);
+#pragma unroll
+      for (int q = 0; q < 8; q++) data[gaddr(g + q)] = gl::mul(sm[spad((g + q) * PASS_THREADS + tid)], t8[q]);
+    }
   } else {
-    // inverse pass twiddles w_M^-(f*j), applied by the first inverse round
-    auto ptw = [&](uint32_t row, uint32_t j) {
-      return root_pow(RT, mlog, (uint64_t)row_freq_t<R>(row & ((1u << R) - 1)) * (j0 + j), true);
+    // incoming pass twiddles w_M^-(f*j), applied by the first inverse round
+    auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+      const uint32_t f = row_freq_t<R>(row0 & RM) + row_freq_t<R>((uint32_t)k);
+      return root_pow32(RT, mlog, f * (uint32_t)(j0 + j), true);
     };
     tile_inv_t<R, T, BC, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
-  }
-#pragma unroll 1
-  for (int g = 0; g < PER_THREAD; g += 8) {
-    uint64_t t8[8];
-    if (FWD) {
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        uint32_t lin = (g + q) * PASS_THREADS + tid;
-        uint32_t i = (lin >> T) & ((1u << R) - 1);
-        t8[q] = root_pow(RT, mlog, (uint64_t)row_freq_t<R>(i) * (j0 + (lin & TM)), false);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      uint32_t lin = (g + q) * PASS_THREADS + tid;
-      uint64_t v = sm[spad(lin)];
-      data[gaddr(lin)] = FWD ? gl::mul(v, t8[q]) : v;
-    }
+    for (int q = 0; q < PER_THREAD; q++) data[gaddr(q)] = sm[spad(q * PASS_THREADS + tid)];
   }
 }
 
@@ -451,18 +451,18 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
   const int tid = threadIdx.x;
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
+  constexpr int TL = 8 - T;
+  const uint64_t gbase = ((uint64_t)(tid >> T) << S) + j0 + (tid & ((1u << T) - 1));
 #pragma unroll
-  for (int q = 0; q < PER_THREAD; q++) {
-    const uint32_t lin = q * PASS_THREADS + tid;
-    const uint32_t i = lin >> T, j = lin & ((1u << T) - 1);
-    cp_async8(sm + spad(lin), data + ((uint64_t)i << S) + j0 + j);
-  }
+  for (int q = 0; q < PER_THREAD; q++)
+    cp_async8(sm + spad(q * PASS_THREADS + tid), data + gbase + ((uint64_t)(q << TL) << S));
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();
   // inverse pass twiddles w_N^-(f*j), applied by the first inverse round
-  auto ptw = [&](uint32_t row, uint32_t j) {
-    return root_pow(RT, L, (uint64_t)row_freq_t<R>(row) * (j0 + j), true);
+  auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+    const uint32_t f = row_freq_t<R>(row0) + row_freq_t<R>((uint32_t)k);
+    return root_pow32(RT, L, f * (uint32_t)(j0 + j), true);
   };
   tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
   for (uint32_t q = tid; q < (1u << (TILE_LOG - 3)); q += PASS_THREADS) {

@@ -53,6 +53,16 @@ __device__ __forceinline__ uint64_t root_pow(const Roots& R, int mlog, uint64_t 
   return rho_pow(R, (uint32_t)(x << (32 - mlog)));
 }
 
+// root_pow for an exponent already reduced mod 2^32 (x is taken mod 2^mlog),
+// with 32-bit index arithmetic.
+__device__ __forceinline__ uint64_t root_pow32(const Roots& R, int mlog, uint32_t x, bool inverse) {
+  const uint32_t mask = mlog >= 32 ? 0xFFFFFFFFu : (1u << mlog) - 1;
+  x &= mask;
+  if (inverse) x = (0u - x) & mask;
+  if (mlog <= LVL_MAX) return __ldg(R.lvl + (1u << mlog) + x);
+  return rho_pow(R, x << (32 - mlog));
+}
+
 // w_(2^mlog)^x for x < 2^mlog <= 4096 from the 4096-entry table (forward or inverse).
 __device__ __forceinline__ uint64_t round_tw(const Roots& R, int mlog, uint32_t x, bool inverse) {
   uint32_t t = x << (12 - mlog);
@@ -61,7 +71,15 @@ __device__ __forceinline__ uint64_t round_tw(const Roots& R, int mlog, uint32_t 
 }
 
 // Shared-memory index with one pad word per 16 to spread 8-byte banks.
-__device__ __forceinline__ uint32_t spad(uint32_t lin) { return lin + (lin >> 4); }
+__host__ __device__ __forceinline__ constexpr uint32_t spad(uint32_t lin) { return lin + (lin >> 4); }
+
+// spad(base | (m << s)) = spad(base) + spad_step(m, s) whenever base has zero
+// bits where m << s lands (the bits below 4 either come from base alone or
+// the shifted m stays inside one 16-word run): per-element shared-memory
+// offsets of a butterfly group are compile-time constants.
+__host__ __device__ __forceinline__ constexpr uint32_t spad_step(uint32_t m, int s) {
+  return (m << s) + ((m << s) >> 4);
+}
 
 // Asynchronous 8-byte global -> shared copy (no register round trip), and
 // the wait for all of this thread's outstanding copies.
@@ -218,16 +236,18 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
     const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
+    const uint32_t sb = spad((row0 << T) | j);  // bits [SLOG+T, MLOG+T) are zero
     uint64_t v[1 << B];
 #pragma unroll
-    for (int m = 0; m < (1 << B); m++) v[m] = sm[spad(((row0 + (m << SLOG)) << T) | j)];
+    for (int m = 0; m < (1 << B); m++) v[m] = sm[sb + spad_step(m, SLOG + T)];
     dft_fwd<B>(v);
     if constexpr (SLOG > 0) {
+      const uint32_t jps = jp << (9 - MLOG);
 #pragma unroll
-      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[(k * jp) << (9 - MLOG)]);
+      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[k * jps]);
     }
 #pragma unroll
-    for (int k = 0; k < (1 << B); k++) sm[spad(((row0 + (k << SLOG)) << T) | j)] = v[k];
+    for (int k = 0; k < (1 << B); k++) sm[sb + spad_step(k, SLOG + T)] = v[k];
   }
 }
 
@@ -235,8 +255,9 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
 struct NoPassTw {};
 
 // One inverse round; the first one executed (SLOG = 0, no round twiddles)
-// multiplies its inputs by the pass twiddles ptw(row, col) of the tile when
-// a functor is given, feeding the lazy products straight into the DFT.
+// multiplies its inputs by the pass twiddles of the tile when a functor is
+// given (ptw(row0, k, col) for tile row row0 + k, row0 a multiple of 2^B),
+// feeding the lazy products straight into the DFT.
 template <int R, int T, int BC, int B, int MLOG, int NT, class F>
 __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512, int tid, const F& ptw) {
   constexpr int SLOG = MLOG - B;
@@ -250,19 +271,22 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
     const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
+    const uint32_t sb = spad((row0 << T) | j);  // bits [SLOG+T, MLOG+T) are zero
     uint64_t v[1 << B];
     gl::Lz x[1 << B];
 #pragma unroll
-    for (int k = 0; k < (1 << B); k++) v[k] = sm[spad(((row0 + (k << SLOG)) << T) | j)];
+    for (int k = 0; k < (1 << B); k++) v[k] = sm[sb + spad_step(k, SLOG + T)];
     if constexpr (SLOG == 0 && PTW) {
+      // rows row0 + k, row0 a multiple of 2^B
 #pragma unroll
-      for (int k = 0; k < (1 << B); k++) x[k] = gl::lz_mul(v[k], ptw(row0 + k, j));
+      for (int k = 0; k < (1 << B); k++) x[k] = gl::lz_mul(v[k], ptw(row0, k, j));
     } else {
       x[0] = gl::lz(v[0]);
+      const uint32_t jps = jp << (9 - MLOG);
 #pragma unroll
       for (int k = 1; k < (1 << B); k++) {
         if constexpr (SLOG > 0) {
-          x[k] = gl::lz_mul(v[k], tw512[(512 - ((k * jp) << (9 - MLOG))) & 511]);
+          x[k] = gl::lz_mul(v[k], tw512[(512 - k * jps) & 511]);
         } else {
           x[k] = gl::lz(v[k]);
         }
@@ -270,7 +294,7 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
     }
     dft_inv_lz<B>(x, v);
 #pragma unroll
-    for (int m = 0; m < (1 << B); m++) sm[spad(((row0 + (m << SLOG)) << T) | j)] = v[m];
+    for (int m = 0; m < (1 << B); m++) sm[sb + spad_step(m, SLOG + T)] = v[m];
   }
 }
 
@@ -294,8 +318,11 @@ __device__ __forceinline__ void tile_inv_t(uint64_t* sm, const uint64_t* tw512, 
 
 // Frequency index held at tile row `row` after the rounds of an R-bit DFT
 // (mixed-radix digit reversal of the row index).
+// (A bit permutation: row_freq_t(a | b) = row_freq_t(a) | row_freq_t(b) for
+// disjoint bit sets, which lets callers split a row into a per-thread part
+// and a compile-time part.)
 template <int R>
-__device__ __forceinline__ uint32_t row_freq_t(uint32_t row) {
+__host__ __device__ __forceinline__ constexpr uint32_t row_freq_t(uint32_t row) {
   uint32_t f = 0;
   int rem = R, sh = 0;
 #pragma unroll
