@@ -100,15 +100,17 @@ __device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
 // Forward DFT of 2^B values in registers: v[k] <- sum_m v[m] w^(m k), with
 // w = 2^(192 / 2^B) (the 8th root of unity is 2^24).  Natural-order output.
 // Radix 4 and 8 run on lazy values (see gl.cuh) and fold once at the end.
+// Forward DFT on lazy inputs (|k| <= 1, e.g. products from lz_mul).
 template <int B>
-__device__ __forceinline__ void dft_fwd(uint64_t* v) {
+__device__ __forceinline__ void dft_fwd_lz(const gl::Lz* x, uint64_t* v) {
   using namespace gl;
   if constexpr (B == 1) {
-    bfly_dif<0>(v[0], v[1]);
+    v[0] = fold(lz_add(x[0], x[1]));
+    v[1] = fold(lz_sub(x[0], x[1]));
   } else if constexpr (B == 2) {
-    Lz a0 = lz_add(lz(v[0]), lz(v[2])), c = lz_sub(lz(v[0]), lz(v[2]));
-    Lz a1 = lz_add(lz(v[1]), lz(v[3]));
-    Lz d = lz(lz_shl<48>(lz_sub(lz(v[1]), lz(v[3]))));
+    Lz a0 = lz_add(x[0], x[2]), c = lz_sub(x[0], x[2]);
+    Lz a1 = lz_add(x[1], x[3]);
+    Lz d = lz(lz_shl<48>(lz_sub(x[1], x[3])));
     v[0] = fold(lz_add(a0, a1));
     v[1] = fold(lz_add(c, d));
     v[2] = fold(lz_sub(a0, a1));
@@ -116,10 +118,10 @@ __device__ __forceinline__ void dft_fwd(uint64_t* v) {
   } else {
     static_assert(B == 3, "radix 2, 4 or 8");
     // stage 1: x_k +- x_(k+4), differences times w^k = 2^(24k)
-    Lz a0 = lz_add(lz(v[0]), lz(v[4])), d0 = lz_sub(lz(v[0]), lz(v[4]));
-    Lz a1 = lz_add(lz(v[1]), lz(v[5])), d1 = lz_sub(lz(v[1]), lz(v[5]));
-    Lz a2 = lz_add(lz(v[2]), lz(v[6])), d2 = lz_sub(lz(v[2]), lz(v[6]));
-    Lz a3 = lz_add(lz(v[3]), lz(v[7])), d3 = lz_sub(lz(v[3]), lz(v[7]));
+    Lz a0 = lz_add(x[0], x[4]), d0 = lz_sub(x[0], x[4]);
+    Lz a1 = lz_add(x[1], x[5]), d1 = lz_sub(x[1], x[5]);
+    Lz a2 = lz_add(x[2], x[6]), d2 = lz_sub(x[2], x[6]);
+    Lz a3 = lz_add(x[3], x[7]), d3 = lz_sub(x[3], x[7]);
     Lz b1 = lz(lz_shl<24>(d1)), b2 = lz(lz_shl<48>(d2)), b3 = lz(lz_shl<72>(d3));
     // stage 2: radix-4 halves, the odd difference times w^2 = 2^48
     Lz c0 = lz_add(a0, a2), c2 = lz_sub(a0, a2);
@@ -135,6 +137,18 @@ __device__ __forceinline__ void dft_fwd(uint64_t* v) {
     v[5] = fold(lz_sub(e0, e1));
     v[3] = fold(lz_add(e2, e3));
     v[7] = fold(lz_sub(e2, e3));
+  }
+}
+
+template <int B>
+__device__ __forceinline__ void dft_fwd(uint64_t* v) {
+  if constexpr (B == 1) {
+    bfly_dif<0>(v[0], v[1]);
+  } else {
+    gl::Lz x[1 << B];
+#pragma unroll
+    for (int k = 0; k < (1 << B); k++) x[k] = gl::lz(v[k]);
+    dft_fwd_lz<B>(x, v);
   }
 }
 
@@ -224,7 +238,12 @@ __host__ __device__ constexpr int rp_mlog(int r, int q) {
 // Tile of 2^BC blocks x 2^R rows x 2^T columns in shared memory; element
 // (row, col) of the flattened (BC+R)-bit row index at spad(row << T | col).
 // One forward round of radix 2^B over sub-problems of 2^MLOG rows.
-template <int R, int T, int BC, int B, int MLOG, int NT>
+// One forward round of radix 2^B over sub-problems of 2^MLOG rows.  The
+// twiddles of the previous round (radix 2^PB over 2^PMLOG rows, PB = 0: none)
+// are applied here, to the inputs, as lazy products that feed the DFT
+// directly: element row r had position jp' = r mod 2^MLOG and output index
+// k' = (r >> MLOG) mod 2^PB there, twiddle w_(2^PMLOG)^(k' jp').
+template <int R, int T, int BC, int B, int MLOG, int NT, int PB, int PMLOG>
 __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
   constexpr int SLOG = MLOG - B;
   constexpr int ITEMS = 1 << (BC + R + T - B);
@@ -238,14 +257,20 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
     const uint32_t row0 = ((rest >> SLOG) << MLOG) + jp;
     const uint32_t sb = spad((row0 << T) | j);  // bits [SLOG+T, MLOG+T) are zero
     uint64_t v[1 << B];
+    gl::Lz x[1 << B];
 #pragma unroll
     for (int m = 0; m < (1 << B); m++) v[m] = sm[sb + spad_step(m, SLOG + T)];
-    dft_fwd<B>(v);
-    if constexpr (SLOG > 0) {
-      const uint32_t jps = jp << (9 - MLOG);
+    if constexpr (PB > 0) {
+      static_assert(PMLOG - PB == MLOG, "rounds must nest");
+      const uint32_t kp = (rest >> SLOG) & ((1u << PB) - 1);
+      const uint32_t base = (kp * jp) << (9 - PMLOG), step = (kp << SLOG) << (9 - PMLOG);
 #pragma unroll
-      for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], tw512[k * jps]);
+      for (int m = 0; m < (1 << B); m++) x[m] = gl::lz_mul(v[m], tw512[base + m * step]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < (1 << B); m++) x[m] = gl::lz(v[m]);
     }
+    dft_fwd_lz<B>(x, v);
 #pragma unroll
     for (int k = 0; k < (1 << B); k++) sm[sb + spad_step(k, SLOG + T)] = v[k];
   }
@@ -301,7 +326,8 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
 template <int R, int T, int BC, int NT, int Q = 0>
 __device__ __forceinline__ void tile_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
   if constexpr (Q < rp_count(R)) {
-    round_fwd_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid);
+    round_fwd_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT, (Q > 0 ? rp_bits(R, Q - 1) : 0),
+                (Q > 0 ? rp_mlog(R, Q - 1) : 0)>(sm, tw512, tid);
     __syncthreads();
     tile_fwd_t<R, T, BC, NT, Q + 1>(sm, tw512, tid);
   }
