@@ -25,8 +25,12 @@
 #include <atomic>
 #include <chrono>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -40,7 +44,109 @@
 namespace pihost {
 
 typedef unsigned __int128 u128;
-using Limbs = std::vector<uint64_t>;
+
+// Limb arrays: large blocks (>= 1 MiB) come from a cache of freed blocks,
+// so the multi-GB temporaries of the Newton iterations reuse memory that is
+// already mapped instead of taking a page fault per 4 KiB each time, and
+// resize() without a value does not zero-fill (every such use writes all
+// words before reading them).
+struct BlockCache {
+  std::mutex mu;
+  std::multimap<size_t, void*> blocks;  // size class in bytes -> block
+  size_t cached = 0;
+};
+static BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache;  // never destroyed: usable during static destruction
+  return *c;
+}
+static const size_t BIG_BYTES = (size_t)1 << 20;
+static const size_t CACHE_MAX = (size_t)24 << 30;
+static size_t size_class(size_t bytes) {  // round up to an eighth of the next power of two
+  size_t p = 1;
+  while (p < bytes) p <<= 1;
+  size_t step = std::max<size_t>(p >> 3, 64);
+  return (bytes + step - 1) / step * step;
+}
+static void* big_alloc(size_t bytes) {
+  const size_t c = size_class(bytes);
+  BlockCache& bc = block_cache();
+  {
+    std::lock_guard<std::mutex> lk(bc.mu);
+    auto it = bc.blocks.find(c);
+    if (it != bc.blocks.end()) {
+      void* p = it->second;
+      bc.blocks.erase(it);
+      bc.cached -= c;
+      return p;
+    }
+  }
+  void* p = std::malloc(c);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+static void big_free(void* p, size_t bytes) {
+  const size_t c = size_class(bytes);
+  BlockCache& bc = block_cache();
+  {
+    std::lock_guard<std::mutex> lk(bc.mu);
+    if (bc.cached + c <= CACHE_MAX) {
+      bc.blocks.emplace(c, p);
+      bc.cached += c;
+      return;
+    }
+  }
+  std::free(p);
+}
+template <class T>
+struct LimbAlloc {
+  using value_type = T;
+  LimbAlloc() noexcept {}
+  template <class U>
+  LimbAlloc(const LimbAlloc<U>&) noexcept {}
+  T* allocate(size_t n) {
+    const size_t b = n * sizeof(T);
+    if (b >= BIG_BYTES) return static_cast<T*>(big_alloc(b));
+    T* p = static_cast<T*>(std::malloc(b ? b : 1));
+    if (!p) throw std::bad_alloc();
+    return p;
+  }
+  void deallocate(T* p, size_t n) {
+    const size_t b = n * sizeof(T);
+    if (b >= BIG_BYTES) big_free(p, b);
+    else std::free(p);
+  }
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+  template <class U>
+  bool operator==(const LimbAlloc<U>&) const noexcept { return true; }
+  template <class U>
+  bool operator!=(const LimbAlloc<U>&) const noexcept { return false; }
+};
+using Limbs = std::vector<uint64_t, LimbAlloc<uint64_t>>;
+
+// Host loops over large limb arrays run on all cores.
+static const size_t PAR_LIMBS = (size_t)1 << 18;
+static void parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn);
+static void par_range(size_t n, const std::function<void(size_t, size_t)>& fn) {
+  if (n < PAR_LIMBS) {
+    fn(0, n);
+    return;
+  }
+  const size_t chunk = (size_t)1 << 16;
+  const size_t nchunks = (n + chunk - 1) / chunk;
+  parallel_for(nchunks, [&](size_t lo, size_t hi) { fn(lo * chunk, std::min(n, hi * chunk)); });
+}
+static Limbs copy_limbs(const uint64_t* src, size_t n) {
+  Limbs out(n);
+  par_range(n, [&](size_t lo, size_t hi) { memcpy(out.data() + lo, src + lo, (hi - lo) * 8); });
+  return out;
+}
 
 // ------------------------------------------------------------------ config
 static size_t g_karatsuba_threshold = 32;   // config.rs:101
@@ -77,25 +183,83 @@ static Limbs add_mag(const Limbs& a, const Limbs& b) {  // integer.rs:351-365
   const Limbs& L = a.size() >= b.size() ? a : b;
   const Limbs& S = a.size() >= b.size() ? b : a;
   Limbs out(L.size() + 1);
-  u128 c = 0;
-  for (size_t i = 0; i < L.size(); i++) {
-    c += (u128)L[i] + (i < S.size() ? S[i] : 0);
-    out[i] = (uint64_t)c;
-    c >>= 64;
+  if (L.size() < PAR_LIMBS) {
+    u128 c = 0;
+    for (size_t i = 0; i < L.size(); i++) {
+      c += (u128)L[i] + (i < S.size() ? S[i] : 0);
+      out[i] = (uint64_t)c;
+      c >>= 64;
+    }
+    out[L.size()] = (uint64_t)c;
+  } else {
+    // chunks add with carry-in 0 and record their carry out; the carries
+    // are then rippled into the following chunks (rarely past one limb)
+    const size_t chunk = (size_t)1 << 16, nch = (L.size() + chunk - 1) / chunk;
+    std::vector<uint8_t> cout(nch);
+    parallel_for(nch, [&](size_t clo, size_t chi) {
+      for (size_t c = clo; c < chi; c++) {
+        u128 cy = 0;
+        for (size_t i = c * chunk; i < std::min(L.size(), (c + 1) * chunk); i++) {
+          cy += (u128)L[i] + (i < S.size() ? S[i] : 0);
+          out[i] = (uint64_t)cy;
+          cy >>= 64;
+        }
+        cout[c] = (uint8_t)cy;
+      }
+    });
+    uint64_t carry = 0;
+    for (size_t c = 0; c < nch; c++) {
+      size_t i = c * chunk, end = std::min(L.size(), (c + 1) * chunk);
+      uint64_t cin = carry;
+      while (cin && i < end) {
+        out[i] += 1;
+        cin = out[i] == 0;
+        i++;
+      }
+      carry = cout[c] + cin;
+    }
+    out[L.size()] = carry;
   }
-  out[L.size()] = (uint64_t)c;
   trim(out);
   return out;
 }
 
 static Limbs sub_mag(const Limbs& a, const Limbs& b) {  // a >= b, integer.rs:368-389
   Limbs out(a.size());
-  uint64_t borrow = 0;
-  for (size_t i = 0; i < a.size(); i++) {
-    uint64_t bi = i < b.size() ? b[i] : 0;
-    uint64_t d = a[i] - bi - borrow;
-    borrow = (a[i] < bi) || (a[i] - bi < borrow);
-    out[i] = d;
+  if (a.size() < PAR_LIMBS) {
+    uint64_t borrow = 0;
+    for (size_t i = 0; i < a.size(); i++) {
+      uint64_t bi = i < b.size() ? b[i] : 0;
+      uint64_t d = a[i] - bi - borrow;
+      borrow = (a[i] < bi) || (a[i] - bi < borrow);
+      out[i] = d;
+    }
+  } else {
+    const size_t chunk = (size_t)1 << 16, nch = (a.size() + chunk - 1) / chunk;
+    std::vector<uint8_t> bout(nch);
+    parallel_for(nch, [&](size_t clo, size_t chi) {
+      for (size_t c = clo; c < chi; c++) {
+        uint64_t borrow = 0;
+        for (size_t i = c * chunk; i < std::min(a.size(), (c + 1) * chunk); i++) {
+          uint64_t bi = i < b.size() ? b[i] : 0;
+          uint64_t d = a[i] - bi - borrow;
+          borrow = (a[i] < bi) || (a[i] - bi < borrow);
+          out[i] = d;
+        }
+        bout[c] = (uint8_t)borrow;
+      }
+    });
+    uint64_t borrow = 0;
+    for (size_t c = 0; c < nch; c++) {
+      size_t i = c * chunk, end = std::min(a.size(), (c + 1) * chunk);
+      uint64_t bin = borrow;
+      while (bin && i < end) {
+        bin = out[i] == 0;
+        out[i] -= 1;
+        i++;
+      }
+      borrow = bout[c] + bin;
+    }
   }
   trim(out);
   return out;
@@ -103,12 +267,17 @@ static Limbs sub_mag(const Limbs& a, const Limbs& b) {  // a >= b, integer.rs:36
 
 static Limbs shl_mag(const Limbs& a, uint64_t s) {  // integer.rs:1097-1125
   if (a.empty()) return {};
-  size_t w = s / 64, r = s % 64;
-  Limbs out(a.size() + w + 1, 0);
-  for (size_t i = 0; i < a.size(); i++) {
-    out[i + w] |= a[i] << r;
-    if (r) out[i + w + 1] |= a[i] >> (64 - r);
-  }
+  const size_t w = s / 64, r = s % 64, n = a.size() + w + 1;
+  Limbs out(n);
+  par_range(n, [&](size_t lo, size_t hi) {
+    for (size_t k = lo; k < hi; k++) {
+      // out[k] = a[k - w] << r | a[k - w - 1] >> (64 - r)
+      uint64_t v = 0;
+      if (k >= w && k - w < a.size()) v = a[k - w] << r;
+      if (r && k >= w + 1 && k - w - 1 < a.size()) v |= a[k - w - 1] >> (64 - r);
+      out[k] = v;
+    }
+  });
   trim(out);
   return out;
 }
@@ -117,11 +286,13 @@ static Limbs shr_mag(const Limbs& a, uint64_t s) {  // integer.rs:1127-1155
   size_t w = s / 64, r = s % 64;
   if (w >= a.size()) return {};
   Limbs out(a.size() - w);
-  for (size_t i = 0; i < out.size(); i++) {
-    uint64_t lo = a[i + w] >> r;
-    uint64_t hi = (r && i + w + 1 < a.size()) ? a[i + w + 1] << (64 - r) : 0;
-    out[i] = lo | hi;
-  }
+  par_range(out.size(), [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; i++) {
+      uint64_t v = a[i + w] >> r;
+      uint64_t h = (r && i + w + 1 < a.size()) ? a[i + w + 1] << (64 - r) : 0;
+      out[i] = v | h;
+    }
+  });
   trim(out);
   return out;
 }
@@ -371,8 +542,12 @@ static void round_to_prec(Flt& f) {  // float.rs:524-569 (round half up)
   uint64_t drop = b - f.prec;
   uint64_t rb = bit_at(f.mant, drop - 1);
   Limbs nl = shr_mag(f.mant, drop);
-  if (rb) nl = add_mag(nl, Limbs{1});
-  f.mant = nl;
+  if (rb) {  // + 1, in place
+    size_t i = 0;
+    while (i < nl.size() && ++nl[i] == 0) i++;
+    if (i == nl.size()) nl.push_back(1);
+  }
+  f.mant = std::move(nl);
   f.exp += (int64_t)drop;
   uint64_t nb = bits_of(f.mant);
   if (nb > f.prec) {
@@ -393,7 +568,7 @@ static Flt flt_from_u64(uint64_t v, uint64_t prec) {
 static Flt flt_from_int(const Int& v) {  // float.rs From<Integer>
   Flt f;
   f.sign = v.neg;
-  f.mant = v.m;
+  f.mant = copy_limbs(v.m.data(), v.m.size());
   f.prec = std::max<uint64_t>(bits_of(v.m), 64);
   return f;
 }
@@ -485,19 +660,39 @@ static Flt add_at_prec(const Flt& a, const Flt& b, uint64_t prec) {  // float.rs
     round_to_prec(r);
     return r;
   }
-  Limbs am = a.mant, bm = b.mant;
+  // align to the smaller exponent, then a signed add of the magnitudes
+  // (integer.rs:391-421) without copying the unshifted operand
   int64_t ae = a.exp, be = b.exp;
+  Limbs sa, sb;
+  const Limbs* pa = &a.mant;
+  const Limbs* pb = &b.mant;
   if (ae > be) {
-    am = shl_mag(am, (uint64_t)(ae - be));
-    ae = be;
+    sa = shl_mag(a.mant, (uint64_t)(ae - be));
+    pa = &sa;
   } else if (be > ae) {
-    bm = shl_mag(bm, (uint64_t)(be - ae));
+    sb = shl_mag(b.mant, (uint64_t)(be - ae));
+    pb = &sb;
   }
-  Int s = add(Int(am, a.sign), Int(bm, b.sign));
+  ae = std::min(ae, be);
+  Limbs m;
+  bool neg = false;
+  if (a.sign == b.sign) {
+    m = add_mag(*pa, *pb);
+    neg = a.sign;
+  } else {
+    int c = cmp_mag(*pa, *pb);
+    if (c > 0) {
+      m = sub_mag(*pa, *pb);
+      neg = a.sign;
+    } else if (c < 0) {
+      m = sub_mag(*pb, *pa);
+      neg = b.sign;
+    }
+  }
   Flt out;
   out.prec = prec;
-  out.sign = s.neg;
-  out.mant = s.m;
+  out.sign = m.empty() ? false : neg;
+  out.mant = std::move(m);
   out.exp = ae;
   round_to_prec(out);
   return out;
@@ -729,9 +924,168 @@ struct PQT {
   Int p, q, t;
 };
 
+// ------------------------------------------------------- small-range splitting
+// The same (P, Q, T) as the recursion below for a range of at most
+// LEAF_MAX terms, without heap traffic: terms from u128 arithmetic, then
+// neighbouring pairs merged level by level in two flat per-thread buffers
+// (schoolbook products; the merge is associative, so the bracketing does
+// not change the result).
+static const uint64_t LEAF_MAX = 128;
+
+struct RawNode {
+  uint32_t po, qo, to;  // offsets of |P|, |Q|, |T| in the level buffer
+  uint32_t pn, qn, tn;  // lengths in limbs (trimmed)
+  bool ps, ts;          // signs of P and T (Q > 0)
+};
+
+static uint32_t raw_trim(const uint64_t* x, uint32_t n) {
+  while (n && x[n - 1] == 0) n--;
+  return n;
+}
+
+static uint32_t raw_mul(const uint64_t* x, uint32_t nx, const uint64_t* y, uint32_t ny, uint64_t* z) {
+  if (!nx || !ny) return 0;
+  memset(z, 0, (nx + ny) * 8);
+  for (uint32_t i = 0; i < nx; i++) {
+    u128 carry = 0;
+    const uint64_t xi = x[i];
+    for (uint32_t j = 0; j < ny; j++) {
+      u128 cur = (u128)z[i + j] + (u128)xi * y[j] + carry;
+      z[i + j] = (uint64_t)cur;
+      carry = cur >> 64;
+    }
+    z[i + ny] = (uint64_t)carry;
+  }
+  return raw_trim(z, nx + ny);
+}
+
+static int raw_cmp(const uint64_t* x, uint32_t nx, const uint64_t* y, uint32_t ny) {
+  if (nx != ny) return nx < ny ? -1 : 1;
+  for (uint32_t i = nx; i-- > 0;)
+    if (x[i] != y[i]) return x[i] < y[i] ? -1 : 1;
+  return 0;
+}
+
+// z = (sx ? -|x| : |x|) + (sy ? -|y| : |y|); returns |z|'s length, sign in sz.
+static uint32_t raw_add_signed(const uint64_t* x, uint32_t nx, bool sx, const uint64_t* y, uint32_t ny, bool sy,
+                               uint64_t* z, bool& sz) {
+  if (sx == sy) {
+    if (nx < ny) {
+      std::swap(x, y);
+      std::swap(nx, ny);
+    }
+    u128 c = 0;
+    for (uint32_t i = 0; i < nx; i++) {
+      c += (u128)x[i] + (i < ny ? y[i] : 0);
+      z[i] = (uint64_t)c;
+      c >>= 64;
+    }
+    z[nx] = (uint64_t)c;
+    sz = sx;
+    return raw_trim(z, nx + 1);
+  }
+  int c = raw_cmp(x, nx, y, ny);
+  if (c == 0) {
+    sz = false;
+    return 0;
+  }
+  if (c < 0) {
+    std::swap(x, y);
+    std::swap(nx, ny);
+    std::swap(sx, sy);
+  }
+  uint64_t borrow = 0;
+  for (uint32_t i = 0; i < nx; i++) {
+    uint64_t yi = i < ny ? y[i] : 0;
+    uint64_t d = x[i] - yi - borrow;
+    borrow = (x[i] < yi || (x[i] == yi && borrow)) ? 1 : 0;
+    z[i] = d;
+  }
+  sz = sx;
+  return raw_trim(z, nx);
+}
+
+static PQT split_leaf(uint64_t a, uint64_t b) {
+  const uint32_t m = (uint32_t)(b - a);
+  thread_local std::vector<uint64_t> buf0, buf1, tq, pt;
+  const size_t cap = 64 * (size_t)m + 256;  // a level holds about 12 limbs per term
+  if (buf0.size() < cap) {
+    buf0.resize(cap);
+    buf1.resize(cap);
+    tq.resize(cap);
+    pt.resize(cap);
+  }
+  std::vector<RawNode> nodes(m), next;
+  uint64_t* cur = buf0.data();
+  uint64_t* nxt = buf1.data();
+  uint32_t off = 0;
+  for (uint32_t i = 0; i < m; i++) {
+    const uint64_t k = a + i;
+    // p = -(6k-5)(2k-1)(6k-1), q = (C^3/24) k^3, t = p (A + B k)   (chudnovsky.rs:377-390)
+    u128 pm = (u128)(6 * k - 5) * (2 * k - 1);
+    uint64_t p3[3], f[1] = {6 * k - 1};
+    uint64_t pl[2] = {(uint64_t)pm, (uint64_t)(pm >> 64)};
+    uint32_t pn = raw_mul(pl, raw_trim(pl, 2), f, 1, p3);
+    u128 k2 = (u128)k * k;
+    uint64_t k2l[2] = {(uint64_t)k2, (uint64_t)(k2 >> 64)}, kk[1] = {k}, k3[3], c3[1] = {C3_OVER_24}, q4[4];
+    uint32_t k3n = raw_mul(k2l, raw_trim(k2l, 2), kk, 1, k3);
+    uint32_t qn = raw_mul(k3, k3n, c3, 1, q4);
+    u128 ab = (u128)CH_A + (u128)CH_B * k;
+    uint64_t abl[2] = {(uint64_t)ab, (uint64_t)(ab >> 64)}, t5[5];
+    uint32_t tn = raw_mul(p3, pn, abl, raw_trim(abl, 2), t5);
+    RawNode& n = nodes[i];
+    n.po = off, n.pn = pn, memcpy(cur + off, p3, pn * 8), off += pn;
+    n.qo = off, n.qn = qn, memcpy(cur + off, q4, qn * 8), off += qn;
+    n.to = off, n.tn = tn, memcpy(cur + off, t5, tn * 8), off += tn;
+    n.ps = true;
+    n.ts = true;
+  }
+  while (nodes.size() > 1) {
+    const size_t np = nodes.size() / 2;
+    next.resize(np + (nodes.size() & 1));
+    uint32_t o = 0;
+    for (size_t i = 0; i < np; i++) {
+      const RawNode& L = nodes[2 * i];
+      const RawNode& R = nodes[2 * i + 1];
+      RawNode z;
+      z.po = o;
+      z.pn = raw_mul(cur + L.po, L.pn, cur + R.po, R.pn, nxt + o);
+      z.ps = L.ps != R.ps;
+      o += z.pn;
+      z.qo = o;
+      z.qn = raw_mul(cur + L.qo, L.qn, cur + R.qo, R.qn, nxt + o);
+      o += z.qn;
+      uint32_t a1 = raw_mul(cur + L.to, L.tn, cur + R.qo, R.qn, tq.data());
+      uint32_t a2 = raw_mul(cur + L.po, L.pn, cur + R.to, R.tn, pt.data());
+      z.to = o;
+      z.tn = raw_add_signed(tq.data(), a1, L.ts, pt.data(), a2, L.ps != R.ts, nxt + o, z.ts);
+      o += z.tn;
+      next[i] = z;
+    }
+    if (nodes.size() & 1) {
+      const RawNode& L = nodes.back();
+      RawNode z = L;
+      z.po = o, memcpy(nxt + o, cur + L.po, L.pn * 8), o += L.pn;
+      z.qo = o, memcpy(nxt + o, cur + L.qo, L.qn * 8), o += L.qn;
+      z.to = o, memcpy(nxt + o, cur + L.to, L.tn * 8), o += L.tn;
+      next[np] = z;
+    }
+    nodes.swap(next);
+    std::swap(cur, nxt);
+  }
+  const RawNode& r = nodes[0];
+  PQT out;
+  out.p = Int(Limbs(cur + r.po, cur + r.po + r.pn), r.ps);
+  out.q = Int(Limbs(cur + r.qo, cur + r.qo + r.qn), false);
+  out.t = Int(Limbs(cur + r.to, cur + r.to + r.tn), r.ts);
+  return out;
+}
+
 // chudnovsky.rs:377-413 (rayon::join on subtrees of >= 64 terms becomes a
-// host thread for the top levels)
+// host thread for the top levels); ranges of at most LEAF_MAX terms take
+// the flat path above.
 static PQT split(uint64_t a, uint64_t b, int depth) {
+  if (b - a <= LEAF_MAX && a >= 1) return split_leaf(a, b);
   if (b - a == 1) {
     Int k(a);
     Int f1 = sub(mulu(k, 6), Int(5)), f2 = sub(mulu(k, 6), Int(1)), f3 = sub(mulu(k, 2), Int(1));
@@ -889,6 +1243,9 @@ struct LevelStaging {
 };
 
 static std::atomic<uint64_t> g_batch_levels{0};
+// Wall-time split of the batched drivers (ms): host staging, GPU round trip
+// (copies + batch), host unpacking, host-side products, node combine.
+static double g_bt[5];
 
 // Products a[i] * b[i] of magnitudes.  Those whose smaller operand has at
 // least gpu_min limbs go to the GPU in one pimul_mul_batch call: operands
@@ -922,6 +1279,7 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
       out_w += A[gi[g]]->size() + B[gi[g]]->size();
     }
     ooff[gi.size()] = out_w;
+    double t0 = now_ms();
     int rc = S.host(std::max(in_w, out_w));
     if (!rc) rc = S.dev(in_w + out_w);
     if (rc) return rc;
@@ -940,11 +1298,13 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
       g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
     }
     g_ntt_calls.fetch_add(gi.size(), std::memory_order_relaxed);
+    double t1 = now_ms();
     if (cudaMemcpyAsync(d_in, S.h, in_w * 8, cudaMemcpyHostToDevice, S.st) != cudaSuccess) return PIMUL_ECUDA;
     rc = pimul_mul_batch(jobs.data(), jobs.size(), S.st);
     if (rc) return rc;
     if (cudaMemcpyAsync(S.h, d_out, out_w * 8, cudaMemcpyDeviceToHost, S.st) != cudaSuccess) return PIMUL_ECUDA;
     if (cudaStreamSynchronize(S.st) != cudaSuccess) return PIMUL_ECUDA;
+    double t2 = now_ms();
     parallel_for(gi.size(), [&](size_t lo, size_t hi) {
       for (size_t g = lo; g < hi; g++) {
         Limbs r(S.h + ooff[g], S.h + ooff[g + 1]);
@@ -952,10 +1312,16 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
         out[gi[g]] = std::move(r);
       }
     });
+    double t3 = now_ms();
+    g_bt[0] += t1 - t0;
+    g_bt[1] += t2 - t1;
+    g_bt[2] += t3 - t2;
   }
+  double t4 = now_ms();
   parallel_for(ci.size(), [&](size_t lo, size_t hi) {
     for (size_t c = lo; c < hi; c++) out[ci[c]] = mul_mag(*A[ci[c]], *B[ci[c]]);
   });
+  g_bt[3] += now_ms() - t4;
   return g_error.load();
 }
 
@@ -979,6 +1345,7 @@ static int merge_level(std::vector<PQT>& nodes, LevelStaging& S) {
   std::vector<Limbs> prod;
   int rc = batch_mul(A, B, prod, S, 1);
   if (rc) return rc;
+  double t0 = now_ms();
   std::vector<PQT> next(np + (nodes.size() & 1));
   parallel_for(np, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; i++) {
@@ -994,22 +1361,37 @@ static int merge_level(std::vector<PQT>& nodes, LevelStaging& S) {
   });
   if (nodes.size() & 1) next[np] = std::move(nodes.back());
   nodes.swap(next);
+  g_bt[4] += now_ms() - t0;
   g_batch_levels.fetch_add(1, std::memory_order_relaxed);
   return PIMUL_OK;
+}
+
+static double g_leaf_ms = 0;
+
+static void report_split(const char* what) {
+  if (!getenv("PIMUL_PI_TIMING")) return;
+  fprintf(stderr, "[pimul] %s: leaves %.1f ms, staging %.1f, gpu round trip %.1f, unpack %.1f, host products %.1f, "
+          "combine %.1f\n", what, g_leaf_ms, g_bt[0], g_bt[1], g_bt[2], g_bt[3], g_bt[4]);
+  for (double& x : g_bt) x = 0;
+  g_leaf_ms = 0;
 }
 
 static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
   const uint64_t nleaf = (b - a + leaf - 1) / leaf;
   std::vector<PQT> nodes(nleaf);
+  for (double& x : g_bt) x = 0;
+  double t0 = now_ms();
   parallel_for(nleaf, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; i++) nodes[i] = split(a + i * leaf, std::min(b, a + (i + 1) * leaf), 4);
   });
+  g_leaf_ms = now_ms() - t0;
   LevelStaging S;
   int rc = S.init();
   while (!rc && nodes.size() > 1) rc = merge_level(nodes, S);
   if (rc) return rc;
   q = std::move(nodes[0].q);
   t = std::move(nodes[0].t);
+  report_split("binary splitting");
   return PIMUL_OK;
 }
 
@@ -1078,6 +1460,7 @@ static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S) 
     });
     nodes.swap(next);
   }
+  report_split("decimal levels");
   const size_t per = (size_t)19 << kmin;
   std::string all(per * nodes.size(), '0');
   parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
@@ -1096,9 +1479,8 @@ static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S) 
 
 using namespace pihost;
 
-static int finish_digits(Flt pi, uint64_t digits, char* out, double* t_phase) {
+static int finish_digits(Flt pi, const Flt& scale, uint64_t digits, char* out, double* t_phase) {
   double t0 = now_ms();
-  Flt scale = pow_int(flt_from_u64(10, pi.prec), Int(digits - 1));
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
   std::string s = to_decimal_top(ip);
@@ -1121,10 +1503,15 @@ extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, p
   g_error.store(0);
   const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
   double t0 = now_ms();
+  // the decimal scale 10^(D-1) at the working precision runs beside the
+  // iterations (it depends on nothing else)
+  Flt scale;
+  std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
   Flt pi = gauss_legendre(prec);
   double t1 = now_ms();
+  scale_th.join();
   double tdc = 0;
-  int rc = finish_digits(pi, digits, out, &tdc);
+  int rc = finish_digits(pi, scale, digits, out, &tdc);
   if (phase_ms) {
     phase_ms[0] = t1 - t0;
     phase_ms[1] = 0;
@@ -1152,12 +1539,22 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
   const uint64_t n_terms = (uint64_t)std::ceil((double)digits / DIGITS_PER_TERM) + SAFETY_TERMS;
   double t0 = now_ms();
-  // sqrt(10005) * 426880 runs beside the binary splitting (chudnovsky.rs:118-126)
-  Flt sq;
+  // sqrt(10005) * 426880 runs beside the binary splitting (chudnovsky.rs:118-126),
+  // and so does the decimal scale 10^(D-1) at the working precision, which
+  // depends on nothing else (util.rs:25-83 computes it after pi).
+  Flt sq, scale;
+  double t_sqrt = 0, t_scale = 0;
   std::thread sqrt_th([&] {
+    double ts = now_ms();
     Flt p = flt_from_u64(10005, prec);
     sqrt_mut(p);
     sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
+    t_sqrt = now_ms() - ts;
+  });
+  std::thread scale_th([&] {
+    double ts = now_ms();
+    scale = pow_int(flt_from_u64(10, prec), Int(digits - 1));
+    t_scale = now_ms() - ts;
   });
   Int q, t;
   int brc = PIMUL_OK;
@@ -1167,19 +1564,22 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     split_root(1, n_terms + 1, q, t);
   if (brc) {
     sqrt_th.join();
+    scale_th.join();
     return brc;
   }
   double t1 = now_ms();
   // final assembly (chudnovsky.rs:146-204)
   Int denom = add(mul(Int(CH_A), q), t);
   Flt denf = flt_from_int(denom);
-  sqrt_th.join();
   Flt recip = reciprocal_at_prec(denf, prec + 16);
+  double t_recip = now_ms() - t1;
+  sqrt_th.join();
   Flt num = mul_at_prec(sq, flt_from_int(q), sq.prec);
   Flt pi = mul_at_prec(num, recip, prec);
   double t2 = now_ms();
   // decimal conversion (util.rs:25-83)
-  Flt scale = pow_int(flt_from_u64(10, pi.prec), Int(digits - 1));
+  scale_th.join();
+  double t_join = now_ms() - t2;
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
   std::string s;
@@ -1192,6 +1592,9 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     s = to_decimal_top(ip);
   }
   double t3 = now_ms();
+  if (getenv("PIMUL_PI_TIMING"))
+    fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms (waited %.1f), reciprocal %.1f ms\n", t_sqrt,
+            t_scale, t_join, t_recip);
   if (g_error.load()) return g_error.load();
   if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
   memcpy(out, s.data(), digits);

@@ -44,3 +44,13 @@ def test_batched_conversion_matches_python():
     cases += [10**6000 * 7 + 3, (10**5000 - 1) * 10**3000, 2**40000 - 1]
     for v in cases:
         assert pm.to_decimal(O.int_to_limbs(v), batched=True) == str(v)
+
+
+@pytest.mark.gpu
+def test_conversion_of_large_values_with_long_carries():
+    # above the host's parallel-loop size (2^18 limbs): all-ones limbs make
+    # every chunked add/subtract ripple its carries across chunk boundaries
+    for v in (2 ** (64 * 300_000) - 1, 10 ** 6_000_000 + 1):
+        want = str(v)
+        assert pm.to_decimal(O.int_to_limbs(v), batched=True) == want
+        assert pm.to_decimal(O.int_to_limbs(v), batched=False) == want
