@@ -850,17 +850,34 @@ static Int pow_u(uint64_t base, uint64_t e) {  // integer.rs:68-82
 // ------------------------------------------------------------------ decimal
 static const uint64_t DEC_CHUNK = 10000000000000000000ull;  // 10^19 (integer.rs:887-888)
 
+// (u1:u0) / d for the invariant d = 10^19 (bit 63 set) and u1 < d, with the
+// precomputed reciprocal v = floor((2^128 - 1) / d) - 2^64 (Moller and
+// Granlund, "Improved division by invariant integers", 2011, Algorithm 4).
+static const uint64_t DEC_CHUNK_INV = (uint64_t)((~(u128)0) / DEC_CHUNK - ((u128)1 << 64));
+static inline uint64_t div_dec_chunk(uint64_t u1, uint64_t u0, uint64_t& r) {
+  u128 q = (u128)DEC_CHUNK_INV * u1;
+  q += ((u128)(u1 + 1) << 64) | u0;
+  uint64_t q1 = (uint64_t)(q >> 64), q0 = (uint64_t)q;
+  uint64_t rr = u0 - q1 * DEC_CHUNK;
+  if (rr > q0) {
+    q1--;
+    rr += DEC_CHUNK;
+  }
+  if (rr >= DEC_CHUNK) {
+    q1++;
+    rr -= DEC_CHUNK;
+  }
+  r = rr;
+  return q1;
+}
+
 static std::string decimal_naive(Limbs mag) {  // integer.rs:968-983
   std::vector<uint64_t> chunks;
   while (!mag.empty()) {
-    u128 rem = 0;
-    for (size_t i = mag.size(); i-- > 0;) {
-      u128 cur = (rem << 64) | mag[i];
-      mag[i] = (uint64_t)(cur / DEC_CHUNK);
-      rem = cur % DEC_CHUNK;
-    }
+    uint64_t rem = 0;
+    for (size_t i = mag.size(); i-- > 0;) mag[i] = div_dec_chunk(rem, mag[i], rem);
     trim(mag);
-    chunks.push_back((uint64_t)rem);
+    chunks.push_back(rem);
   }
   std::string out = std::to_string(chunks.back());
   char buf[32];
@@ -1419,12 +1436,22 @@ static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S) 
   P[0] = Int(DEC_CHUNK);
   for (int k = 1; k < K; k++) P[k] = mul(P[k - 1], P[k - 1]);
   std::vector<Int> nodes{X};
+  // V_k ~ 2^(s_k) / P_k with s_k = 2 bits(P_k) + 64: Newton once at the top,
+  // then V_(k-1) = (P_(k-1) V_k) >> (s_k - s_(k-1)), since P_k = P_(k-1)^2
+  // (off by at most a few units; the quotient correction below absorbs it)
+  Int V;
+  uint64_t sh_prev = 0;
   for (int k = K - 1; k >= kmin; k--) {
     const uint64_t b = bits_of(P[k].m);
     const uint64_t sh = 2 * b + 64;
-    Flt r = reciprocal_at_prec(flt_from_int(P[k]), b + 128);
-    r.exp += (int64_t)sh;
-    const Int V = to_integer_down(r);
+    if (k == K - 1) {
+      Flt r = reciprocal_at_prec(flt_from_int(P[k]), b + 128);
+      r.exp += (int64_t)sh;
+      V = to_integer_down(r);
+    } else {
+      V = Int(shr_mag(mul_mag(P[k].m, V.m), sh_prev - sh), false);
+    }
+    sh_prev = sh;
     const size_t n = nodes.size();
     std::vector<const Limbs*> A(n), B(n, &V.m);
     for (size_t i = 0; i < n; i++) A[i] = &nodes[i].m;
