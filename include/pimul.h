@@ -113,6 +113,29 @@ typedef struct pimul_job {
 int pimul_mul_batch(const pimul_job* jobs, size_t n, void* stream);
 
 /*
+ * Batched add/subtract of device limb arrays: out[0..nout) = x + y
+ * (sub == 0) or x - y (sub != 0, x >= y), operands zero-extended to nout
+ * (nout >= max(nx, ny); for an addition max(nx, ny) + 1 holds every carry).
+ * Synchronous; PIMUL_EINVAL if a carry or borrow leaves the top limb.
+ * Replaces: crates/bignum/src/integer.rs:351-421 (add_mag / sub_mag under
+ * Integer addition) for the T sums of a binary-splitting level.
+ */
+typedef struct pimul_addsub_job {
+  const uint64_t* x;
+  size_t nx;
+  const uint64_t* y;
+  size_t ny;
+  uint64_t* out;
+  size_t nout;
+  int sub;
+} pimul_addsub_job;
+int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream);
+
+/* Trimmed lengths (highest nonzero limb + 1) of n device limb arrays of
+ * lengths lens[i]; out_lens on the host.  Synchronous. */
+int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n, size_t* out_lens, void* stream);
+
+/*
  * Batch plans: a fixed batch shape (la[i], lb[i]) laid out once, with all its
  * launches captured into a CUDA graph.  plan_run takes jobs of exactly that
  * shape (new pointers each time) and replays the graph; runs of one plan are

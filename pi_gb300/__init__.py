@@ -65,6 +65,8 @@ def load(build_if_stale: bool = True):
     L.pimul_plan.argtypes = [_sz, _sz, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]
     L.pimul_sync.argtypes = []
     L.pimul_mul_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_addsub_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_top_limbs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]
     L.pimul_batch_plan_create.argtypes = [ctypes.POINTER(_sz), ctypes.POINTER(_sz), _sz, ctypes.POINTER(ctypes.c_void_p)]
     L.pimul_batch_plan_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p]
     L.pimul_batch_plan_destroy.argtypes = [ctypes.c_void_p]
@@ -147,6 +149,38 @@ def mul_device(d_a, d_b, d_out, stream=None):
         stream = torch.cuda.current_stream(d_out.device).cuda_stream
     _check(lib().pimul_mul_device(d_a.data_ptr(), la, d_b.data_ptr(), lb, d_out.data_ptr(),
                                   ctypes.c_void_p(stream)))
+
+
+class AddSubJob(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_void_p), ("nx", _sz), ("y", ctypes.c_void_p), ("ny", _sz),
+                ("out", ctypes.c_void_p), ("nout", _sz), ("sub", ctypes.c_int)]
+
+
+def addsub_batch(jobs, stream=None):
+    """Batched add/subtract of torch CUDA uint64/int64 tensors:
+    jobs = [(x, y, out, sub)], out = x + y or x - y (x >= y) over out.numel()
+    limbs (pimul_addsub_batch; synchronous)."""
+    arr = (AddSubJob * len(jobs))()
+    for i, (x, y, out, sub) in enumerate(jobs):
+        arr[i] = AddSubJob(x.data_ptr() if x.numel() else None, x.numel(), y.data_ptr() if y.numel() else None,
+                           y.numel(), out.data_ptr(), out.numel(), int(bool(sub)))
+    if stream is None and jobs:
+        import torch
+        stream = torch.cuda.current_stream(jobs[0][2].device).cuda_stream
+    _check(lib().pimul_addsub_batch(arr, len(jobs), ctypes.c_void_p(stream) if stream else None))
+
+
+def top_limbs(arrays, stream=None):
+    """Trimmed lengths of torch CUDA limb tensors (pimul_top_limbs)."""
+    n = len(arrays)
+    ptrs = (ctypes.c_uint64 * n)(*[a.data_ptr() for a in arrays])
+    lens = (_sz * n)(*[a.numel() for a in arrays])
+    out = (_sz * n)()
+    if stream is None and arrays:
+        import torch
+        stream = torch.cuda.current_stream(arrays[0].device).cuda_stream
+    _check(lib().pimul_top_limbs(ptrs, lens, n, out, ctypes.c_void_p(stream) if stream else None))
+    return list(out)
 
 
 class PimulJob(ctypes.Structure):

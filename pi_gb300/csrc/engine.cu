@@ -875,6 +875,7 @@ static Sizes sizes_for(uint64_t la, uint64_t lb) {
 // Scratch bytes of one large product (A, B unless square, H, aux), each
 // piece rounded to 256 bytes.
 static uint64_t round256(uint64_t x) { return (x + 255) & ~255ull; }
+__host__ __device__ __forceinline__ uint64_t round_up_u64(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
 static uint64_t scratch_bytes(uint64_t la, uint64_t lb, bool square) {
   Sizes z = sizes_for(la, lb);
   return round256(z.N * 8) * (square ? 1 : 2) + round256(z.nwin * 8) + round256(z.aux_bytes);
@@ -1882,6 +1883,285 @@ int pimul_service_reset_stats(void) {
   g_svc.latencies.clear();
   g_svc.completed = 0;
   g_svc.batches = 0;
+  return PIMUL_OK;
+}
+
+// ------------------------------------------------- batched add / subtract
+// out = x + y or x - y (x >= y) for many limb arrays at once, the additions
+// and subtractions of a binary-splitting level done where its products
+// live.  Same carry-lookahead structure as the product's carry pass: windows
+// of 4 limbs add with carry-in 0 and report (generate, propagate); a scan
+// over chunk summaries gives every window its carry; windows that receive
+// one ripple it (+1 / -1) through their limbs.  A carry or borrow out of the
+// top limb is reported (it means x < y for a subtraction).
+constexpr int AS_THREADS = 256;
+constexpr int AS_W = 4;
+
+struct AsJob {
+  const uint64_t* x;
+  const uint64_t* y;
+  uint64_t* out;
+  uint64_t nx, ny, nout;
+  uint8_t* aux;  // per-warp masks, per-chunk (g, p) and carry-in bytes
+  uint32_t sub;
+};
+
+__host__ __device__ __forceinline__ uint64_t as_nwin(uint64_t nout) { return (nout + AS_W - 1) / AS_W; }
+__host__ __device__ __forceinline__ uint64_t as_nchunk(uint64_t nout) {
+  return (as_nwin(nout) + AS_THREADS - 1) / AS_THREADS;
+}
+__host__ __device__ __forceinline__ uint64_t as_aux_bytes(uint64_t nout) {
+  uint64_t nc = as_nchunk(nout);
+  return round_up_u64(nc * (AS_THREADS / 32) * 8 + 2 * nc + 16, 256);
+}
+
+__global__ void __launch_bounds__(AS_THREADS) k_as_local(const AsJob* jobs) {
+  const AsJob J = jobs[blockIdx.y];
+  const uint64_t nwin = as_nwin(J.nout), nchunk = as_nchunk(J.nout);
+  if (blockIdx.x >= nchunk) return;
+  uint32_t* masks = reinterpret_cast<uint32_t*>(J.aux);
+  uint8_t* chunk_gp = J.aux + nchunk * (AS_THREADS / 32) * 8;
+  __shared__ uint32_t sA[AS_THREADS / 32], sB[AS_THREADS / 32];
+  const uint64_t w = (uint64_t)blockIdx.x * AS_THREADS + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  bool g = false, p = false;
+  if (w < nwin) {
+    uint64_t c = 0;
+    bool all = true;
+#pragma unroll
+    for (int t = 0; t < AS_W; t++) {
+      const uint64_t i = AS_W * w + t;
+      if (i >= J.nout) break;
+      const uint64_t xi = i < J.nx ? J.x[i] : 0, yi = i < J.ny ? J.y[i] : 0;
+      uint64_t z;
+      if (J.sub) {
+        const uint64_t d = xi - yi;
+        const uint64_t b1 = xi < yi, b2 = d < c;
+        z = d - c;
+        c = b1 | b2;
+        all = all && z == 0;
+      } else {
+        const uint64_t s0 = xi + yi;
+        const uint64_t c1 = s0 < xi;
+        z = s0 + c;
+        c = c1 | (z < s0);
+        all = all && z == ~0ull;
+      }
+      J.out[i] = z;
+    }
+    g = c != 0;
+    p = all;
+  }
+  const uint32_t A = __ballot_sync(0xFFFFFFFFu, g || p);
+  const uint32_t Bm = __ballot_sync(0xFFFFFFFFu, g);
+  if (lane == 0) {
+    const uint64_t wi = (uint64_t)blockIdx.x * (AS_THREADS / 32) + warp;
+    masks[2 * wi] = A;
+    masks[2 * wi + 1] = Bm;
+    sA[warp] = A;
+    sB[warp] = Bm;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t cg = 0, cp = 1;  // chunk carry out for carry in 0 / 1
+    for (int k = 0; k < AS_THREADS / 32; k++) {
+      uint64_t sg = (uint64_t)sA[k] + sB[k] + cg;
+      uint64_t sp = (uint64_t)sA[k] + sB[k] + cp;
+      cg = (uint32_t)(sg >> 32);
+      cp = (uint32_t)(sp >> 32);
+    }
+    chunk_gp[blockIdx.x] = (uint8_t)(cg | (cp << 1));
+  }
+}
+
+// One CTA per job: carry into every chunk (segments of chunks per thread,
+// chained by thread 0).
+__global__ void __launch_bounds__(1024) k_as_scan(const AsJob* jobs) {
+  const AsJob J = jobs[blockIdx.x];
+  const uint64_t nchunk = as_nchunk(J.nout);
+  const uint8_t* chunk_gp = J.aux + nchunk * (AS_THREADS / 32) * 8;
+  uint8_t* chunk_cin = J.aux + nchunk * (AS_THREADS / 32) * 8 + nchunk;
+  __shared__ uint8_t seg_g[1024], seg_p[1024], seg_cin[1024];
+  const uint64_t per = (nchunk + 1023) / 1024;
+  const uint64_t lo = threadIdx.x * per, hi = lo + per < nchunk ? lo + per : nchunk;
+  uint8_t cg = 0, cp = 1;
+  for (uint64_t k = lo; k < hi; k++) {
+    uint8_t gp = chunk_gp[k];
+    uint8_t o0 = gp & 1, o1 = (gp >> 1) & 1;
+    cg = cg ? o1 : o0;
+    cp = cp ? o1 : o0;
+  }
+  seg_g[threadIdx.x] = cg;
+  seg_p[threadIdx.x] = cp;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint8_t cin = 0;
+    for (int k = 0; k < 1024; k++) {
+      seg_cin[k] = cin;
+      cin = cin ? seg_p[k] : seg_g[k];
+    }
+  }
+  __syncthreads();
+  uint8_t cin = seg_cin[threadIdx.x];
+  for (uint64_t k = lo; k < hi; k++) {
+    chunk_cin[k] = cin;
+    uint8_t gp = chunk_gp[k];
+    cin = cin ? ((gp >> 1) & 1) : (gp & 1);
+  }
+}
+
+// Windows that receive a carry ripple it; the top window's carry out
+// (generated, or propagated from its carry in) sets *overflow.
+__global__ void __launch_bounds__(AS_THREADS) k_as_apply(const AsJob* jobs, int* overflow) {
+  const AsJob J = jobs[blockIdx.y];
+  const uint64_t nwin = as_nwin(J.nout), nchunk = as_nchunk(J.nout);
+  if (blockIdx.x >= nchunk) return;
+  const uint32_t* masks = reinterpret_cast<const uint32_t*>(J.aux);
+  const uint8_t* chunk_cin = J.aux + nchunk * (AS_THREADS / 32) * 8 + nchunk;
+  const uint64_t w = (uint64_t)blockIdx.x * AS_THREADS + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t cin = chunk_cin[blockIdx.x];
+  const uint64_t wbase = (uint64_t)blockIdx.x * (AS_THREADS / 32);
+  for (int k = 0; k < warp; k++) {
+    uint64_t s = (uint64_t)masks[2 * (wbase + k)] + masks[2 * (wbase + k) + 1] + cin;
+    cin = (uint32_t)(s >> 32);
+  }
+  const uint32_t A = masks[2 * (wbase + warp)], Bm = masks[2 * (wbase + warp) + 1];
+  const uint32_t carries = (A + Bm + cin) ^ A ^ Bm;
+  if (w + 1 == nwin) {
+    const uint32_t g = (Bm >> lane) & 1, pg = (A >> lane) & 1, c = (carries >> lane) & 1;
+    if (g || (pg && c)) atomicExch(overflow, 1);
+  }
+  if (w < nwin && ((carries >> lane) & 1)) {
+    for (int t = 0; t < AS_W; t++) {
+      const uint64_t i = AS_W * w + t;
+      if (i >= J.nout) break;
+      if (J.sub) {
+        if (J.out[i]-- != 0) break;
+      } else {
+        if (++J.out[i] != 0) break;
+      }
+    }
+  }
+}
+
+// Highest nonzero limb + 1 of each array (0 for zero): *len must be zero
+// on entry; CTAs scan 2^12-limb chunks and keep the maximum.
+__global__ void __launch_bounds__(256) k_top_limb(const uint64_t* const* arrs, const uint64_t* n, uint64_t* len) {
+  const uint32_t j = blockIdx.y;
+  const uint64_t lo = (uint64_t)blockIdx.x << 12;
+  if (lo >= n[j]) return;
+  const uint64_t hi = lo + 4096 < n[j] ? lo + 4096 : n[j];
+  const uint64_t* a = arrs[j];
+  uint64_t best = 0;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += 256)
+    if (a[i]) best = i + 1;
+  for (int o = 16; o > 0; o >>= 1) {
+    uint64_t other = __shfl_down_sync(0xFFFFFFFFu, best, o);
+    best = other > best ? other : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best) atomicMax((unsigned long long*)&len[j], (unsigned long long)best);
+}
+
+// Batched add/subtract on `st` (asynchronous); *d_overflow (device int,
+// zeroed by the caller) is set when a carry or borrow leaves a top limb.
+static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st, int* d_overflow) {
+  if (n == 0) return PIMUL_OK;
+  uint64_t aux_total = 0, max_chunk = 0;
+  for (size_t i = 0; i < n; i++) {
+    aux_total += as_aux_bytes(jobs[i].nout);
+    max_chunk = std::max<uint64_t>(max_chunk, as_nchunk(jobs[i].nout));
+  }
+  const uint64_t desc = round_up_u64(n * sizeof(AsJob), 256);
+  uint8_t* dev = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dev, desc + aux_total, g_dev.pool, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("add/subtract scratch: ") + cudaGetErrorString(e));
+  }
+  std::vector<AsJob> h(n);
+  uint64_t off = desc;
+  for (size_t i = 0; i < n; i++) {
+    h[i] = AsJob{jobs[i].x, jobs[i].y, jobs[i].out, jobs[i].nx, jobs[i].ny, jobs[i].nout, dev + off,
+                 (uint32_t)(jobs[i].sub != 0)};
+    off += as_aux_bytes(jobs[i].nout);
+  }
+  e = cudaMemcpyAsync(dev, h.data(), n * sizeof(AsJob), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const AsJob* dj = reinterpret_cast<const AsJob*>(dev);
+    for (size_t j0 = 0; j0 < n; j0 += 65535) {
+      const unsigned nj = (unsigned)std::min<size_t>(65535, n - j0);
+      k_as_local<<<dim3((unsigned)max_chunk, nj), AS_THREADS, 0, st>>>(dj + j0);
+      k_as_scan<<<nj, 1024, 0, st>>>(dj + j0);
+      k_as_apply<<<dim3((unsigned)max_chunk, nj), AS_THREADS, 0, st>>>(dj + j0, d_overflow);
+    }
+    e = cudaGetLastError();
+  }
+  // the host image is pageable: the copy has been staged before return
+  cudaFreeAsync(dev, st);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("add/subtract launch: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
+  if (n && !jobs) return fail(PIMUL_EINVAL, "null job list");
+  for (size_t i = 0; i < n; i++) {
+    const pimul_addsub_job& j = jobs[i];
+    if (j.nout && !j.out) return fail(PIMUL_EINVAL, "null output");
+    if ((j.nx && !j.x) || (j.ny && !j.y)) return fail(PIMUL_EINVAL, "null operand");
+    if (j.nout < std::max(j.nx, j.ny)) return fail(PIMUL_EINVAL, "output shorter than an operand");
+  }
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  int* d_flag = nullptr;
+  CU(cudaMallocAsync((void**)&d_flag, sizeof(int), g_dev.pool, st));
+  CU(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
+  rc = addsub_launch(jobs, n, st, d_flag);
+  int h_flag = 0;
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(PIMUL_ECUDA, std::string("add/subtract: ") + cudaGetErrorString(e));
+  }
+  cudaFreeAsync(d_flag, st);
+  if (!rc && h_flag) rc = fail(PIMUL_EINVAL, "carry or borrow out of the top limb (x < y in a subtraction?)");
+  return rc;
+}
+
+int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n, size_t* out_lens, void* stream) {
+  if (n == 0) return PIMUL_OK;
+  if (!arrays || !lens || !out_lens) return fail(PIMUL_EINVAL, "null argument");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  uint64_t max_chunk = 0;
+  for (size_t i = 0; i < n; i++) max_chunk = std::max<uint64_t>(max_chunk, (lens[i] + 4095) / 4096);
+  if (max_chunk == 0) {
+    for (size_t i = 0; i < n; i++) out_lens[i] = 0;
+    return PIMUL_OK;
+  }
+  const uint64_t bytes = round_up_u64(n * 8, 256);
+  uint8_t* dev = nullptr;
+  CU(cudaMallocAsync((void**)&dev, 3 * bytes, g_dev.pool, st));
+  std::vector<uint64_t> hn(lens, lens + n);
+  CU(cudaMemcpyAsync(dev, arrays, n * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(dev + bytes, hn.data(), n * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(dev + 2 * bytes, 0, n * 8, st));
+  for (size_t j0 = 0; j0 < n; j0 += 65535) {
+    const unsigned nj = (unsigned)std::min<size_t>(65535, n - j0);
+    k_top_limb<<<dim3((unsigned)max_chunk, nj), 256, 0, st>>>(
+        reinterpret_cast<const uint64_t* const*>(dev) + j0, reinterpret_cast<const uint64_t*>(dev + bytes) + j0,
+        reinterpret_cast<uint64_t*>(dev + 2 * bytes) + j0);
+  }
+  CU(cudaGetLastError());
+  std::vector<uint64_t> res(n);
+  CU(cudaMemcpyAsync(res.data(), dev + 2 * bytes, n * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  cudaFreeAsync(dev, st);
+  for (size_t i = 0; i < n; i++) out_lens[i] = (size_t)res[i];
   return PIMUL_OK;
 }
 

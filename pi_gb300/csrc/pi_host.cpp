@@ -1387,10 +1387,177 @@ static double g_leaf_ms = 0;
 
 static void report_split(const char* what) {
   if (!getenv("PIMUL_PI_TIMING")) return;
-  fprintf(stderr, "[pimul] %s: leaves %.1f ms, staging %.1f, gpu round trip %.1f, unpack %.1f, host products %.1f, "
-          "combine %.1f\n", what, g_leaf_ms, g_bt[0], g_bt[1], g_bt[2], g_bt[3], g_bt[4]);
+  fprintf(stderr, "[pimul] %s: leaves %.1f ms, staging %.1f, gpu %.1f, unpack %.1f, host products %.1f, "
+          "bookkeeping %.1f\n", what, g_leaf_ms, g_bt[0], g_bt[1], g_bt[2], g_bt[3], g_bt[4]);
   for (double& x : g_bt) x = 0;
   g_leaf_ms = 0;
+}
+
+// ---------------------------------------------- device-resident splitting
+// The levels above the leaves without host round trips: the leaves' P, Q, T
+// are uploaded once, and every level's products (pimul_mul_batch), T sums
+// (pimul_addsub_batch) and trimmed lengths (pimul_top_limbs) run on the
+// device; only the root's Q and T come back.  Signs are static: every
+// p_k < 0, so P of m terms has sign (-1)^m, and T < 0 for every range
+// because its first term outweighs the rest (|p_k / q_k| < 10^-14), so
+// |T| = |T_L| Q_R + (-1)^(m_L) |P_L| |T_R| is a sum or a difference of
+// magnitudes (a borrow out of the top would be reported, never silent).
+struct DNode {
+  uint64_t* p;
+  uint64_t* q;
+  uint64_t* t;
+  size_t pn, qn, tn;
+  uint64_t terms;
+};
+
+static int split_root_device(const std::vector<PQT>& leaves, const std::vector<uint64_t>& terms, Int& q, Int& t) {
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  int rc = PIMUL_OK;
+  uint64_t* arena = nullptr;
+  std::vector<DNode> nodes(leaves.size());
+  LevelStaging S;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = PIMUL_ECUDA;
+    return e == cudaSuccess;
+  };
+  {
+    double t0 = now_ms();
+    std::vector<size_t> off(leaves.size() + 1, 0);
+    for (size_t i = 0; i < leaves.size(); i++)
+      off[i + 1] = off[i] + leaves[i].p.m.size() + leaves[i].q.m.size() + leaves[i].t.m.size();
+    rc = S.host(off.back());
+    if (!rc && cu(cudaMallocAsync((void**)&arena, std::max<size_t>(off.back(), 1) * 8, st))) {
+      parallel_for(leaves.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; i++) {
+          uint64_t* h = S.h + off[i];
+          const Limbs* parts[3] = {&leaves[i].p.m, &leaves[i].q.m, &leaves[i].t.m};
+          size_t o = 0;
+          for (const Limbs* x : parts) {
+            memcpy(h + o, x->data(), x->size() * 8);
+            o += x->size();
+          }
+          DNode& n = nodes[i];
+          n.pn = leaves[i].p.m.size();
+          n.qn = leaves[i].q.m.size();
+          n.tn = leaves[i].t.m.size();
+          n.p = arena + off[i];
+          n.q = n.p + n.pn;
+          n.t = n.q + n.qn;
+          n.terms = terms[i];
+        }
+      });
+      cu(cudaMemcpyAsync(arena, S.h, off.back() * 8, cudaMemcpyHostToDevice, st));
+    }
+    g_bt[0] += now_ms() - t0;
+  }
+  while (!rc && nodes.size() > 1) {
+    double t0 = now_ms();
+    const size_t np = nodes.size() / 2;
+    const bool need_p = nodes.size() > 2, odd = nodes.size() & 1;
+    // new level: Q, P, T per pair (and the odd node); temporaries T_L Q_R, P_L T_R
+    size_t lvl_w = 0, tmp_w = 0;
+    for (size_t i = 0; i < np; i++) {
+      const DNode& L = nodes[2 * i];
+      const DNode& R = nodes[2 * i + 1];
+      lvl_w += L.qn + R.qn + (need_p ? L.pn + R.pn : 0) + std::max(L.tn + R.qn, L.pn + R.tn) + 1;
+      tmp_w += L.tn + R.qn + L.pn + R.tn;
+    }
+    if (odd) lvl_w += nodes.back().pn + nodes.back().qn + nodes.back().tn;
+    uint64_t* nxt = nullptr;
+    uint64_t* tmp = nullptr;
+    if (!cu(cudaMallocAsync((void**)&nxt, lvl_w * 8, st)) || !cu(cudaMallocAsync((void**)&tmp, tmp_w * 8, st))) break;
+    std::vector<DNode> next(np + odd);
+    std::vector<pimul_job> mj;
+    std::vector<pimul_addsub_job> aj(np);
+    mj.reserve(np * 4);
+    size_t lo = 0, to = 0;
+    for (size_t i = 0; i < np; i++) {
+      const DNode& L = nodes[2 * i];
+      const DNode& R = nodes[2 * i + 1];
+      DNode& z = next[i];
+      z.terms = L.terms + R.terms;
+      z.q = nxt + lo, z.qn = L.qn + R.qn, lo += z.qn;
+      mj.push_back(pimul_job{L.q, L.qn, R.q, R.qn, z.q});
+      if (need_p) {
+        z.p = nxt + lo, z.pn = L.pn + R.pn, lo += z.pn;
+        mj.push_back(pimul_job{L.p, L.pn, R.p, R.pn, z.p});
+      } else {
+        z.p = nullptr, z.pn = 0;
+      }
+      uint64_t* tq = tmp + to;
+      to += L.tn + R.qn;
+      uint64_t* pt = tmp + to;
+      to += L.pn + R.tn;
+      mj.push_back(pimul_job{L.t, L.tn, R.q, R.qn, tq});
+      mj.push_back(pimul_job{L.p, L.pn, R.t, R.tn, pt});
+      z.tn = std::max(L.tn + R.qn, L.pn + R.tn) + 1;
+      z.t = nxt + lo, lo += z.tn;
+      aj[i] = pimul_addsub_job{tq, L.tn + R.qn, pt, L.pn + R.tn, z.t, z.tn, (int)(L.terms & 1)};
+    }
+    for (const pimul_job& j : mj) {
+      uint64_t L2 = 0;
+      while ((1ull << L2) < 4 * (j.la + j.lb) - 1) L2++;
+      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+    }
+    if (odd) {
+      const DNode& o = nodes.back();
+      DNode& z = next[np];
+      z = o;
+      z.p = nxt + lo, lo += o.pn;
+      z.q = nxt + lo, lo += o.qn;
+      z.t = nxt + lo, lo += o.tn;
+      cu(cudaMemcpyAsync(z.p, o.p, o.pn * 8, cudaMemcpyDeviceToDevice, st));
+      cu(cudaMemcpyAsync(z.q, o.q, o.qn * 8, cudaMemcpyDeviceToDevice, st));
+      cu(cudaMemcpyAsync(z.t, o.t, o.tn * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    g_ntt_calls.fetch_add(mj.size(), std::memory_order_relaxed);
+    double t1 = now_ms();
+    if (!rc) rc = pimul_mul_batch(mj.data(), mj.size(), st);
+    if (!rc) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
+    cudaFreeAsync(tmp, st);
+    cudaFreeAsync(arena, st);
+    arena = nxt;
+    // trimmed lengths of the new level
+    std::vector<const uint64_t*> arrs;
+    std::vector<size_t> lens;
+    arrs.reserve(next.size() * 3);
+    for (const DNode& z : next) {
+      if (z.pn) arrs.push_back(z.p), lens.push_back(z.pn);
+      arrs.push_back(z.q), lens.push_back(z.qn);
+      arrs.push_back(z.t), lens.push_back(z.tn);
+    }
+    std::vector<size_t> got(arrs.size());
+    if (!rc) rc = pimul_top_limbs(arrs.data(), lens.data(), arrs.size(), got.data(), st);
+    double t2 = now_ms();
+    if (!rc) {
+      size_t k = 0;
+      for (DNode& z : next) {
+        if (z.pn) z.pn = got[k++];
+        z.qn = got[k++];
+        z.tn = got[k++];
+      }
+    }
+    nodes.swap(next);
+    g_batch_levels.fetch_add(1, std::memory_order_relaxed);
+    g_bt[1] += t2 - t1;
+    g_bt[4] += (t1 - t0);
+  }
+  if (!rc) {
+    double t0 = now_ms();
+    const DNode& r = nodes[0];
+    Limbs qm(r.qn), tm(r.tn);
+    cu(cudaMemcpyAsync(qm.data(), r.q, r.qn * 8, cudaMemcpyDeviceToHost, st));
+    cu(cudaMemcpyAsync(tm.data(), r.t, r.tn * 8, cudaMemcpyDeviceToHost, st));
+    cu(cudaStreamSynchronize(st));
+    q = Int(std::move(qm), false);
+    t = Int(std::move(tm), true);
+    g_bt[2] += now_ms() - t0;
+  }
+  if (arena) cudaFreeAsync(arena, st);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return rc;
 }
 
 static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
@@ -1402,6 +1569,18 @@ static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int
     for (size_t i = lo; i < hi; i++) nodes[i] = split(a + i * leaf, std::min(b, a + (i + 1) * leaf), 4);
   });
   g_leaf_ms = now_ms() - t0;
+  // device-resident levels when the leaves carry the static signs
+  bool static_signs = nleaf > 1;
+  std::vector<uint64_t> terms(nleaf);
+  for (uint64_t i = 0; i < nleaf && static_signs; i++) {
+    terms[i] = std::min(b, a + (i + 1) * leaf) - (a + i * leaf);
+    static_signs = nodes[i].t.neg && nodes[i].p.neg == (bool)(terms[i] & 1);
+  }
+  if (static_signs) {
+    int rc = split_root_device(nodes, terms, q, t);
+    report_split("binary splitting (device-resident levels)");
+    return rc;
+  }
   LevelStaging S;
   int rc = S.init();
   while (!rc && nodes.size() > 1) rc = merge_level(nodes, S);
