@@ -778,6 +778,31 @@ static void sqrt_mut(Flt& self) {
   self = x;
 }
 
+// sqrt(n) for a small integer n at prec bits by the multiplication-only
+// Newton iteration for 1/sqrt(n), y <- y + y (1 - n y^2) / 2, at doubling
+// precision, then sqrt(n) = n y.  Used by the batched form only (the plain
+// form keeps the division-based iteration of float.rs:85-174, restated in
+// sqrt_mut); the two results agree to within an ulp of the working
+// precision, which sits 256 bits below the last digit.
+static Flt sqrt_int_fast(uint64_t n, uint64_t prec) {
+  const uint64_t target = prec + 64;
+  Flt y = flt_from_f64(1.0 / std::sqrt((double)n), 64);
+  const Flt nf = flt_from_u64(n, 64);
+  const Flt one = flt_from_u64(1, 64);
+  uint64_t cur = 48;  // bits right in the f64 start
+  while (cur < target) {
+    cur = std::min(2 * cur, target);
+    const uint64_t w = cur + 32;
+    Flt y2 = mul_at_prec(y, y, w);
+    Flt e = sub_at_prec(one, mul_at_prec(y2, nf, w), w);  // |e| ~ 2^-(cur/2)
+    e = truncated_to_prec(e, cur / 2 + 64);
+    Flt c = mul_at_prec(y, e, w);
+    c.exp -= 1;
+    y = add_at_prec(y, c, w);
+  }
+  return mul_at_prec(y, nf, prec);
+}
+
 static Flt pow_int(const Flt& base0, const Int& ex) {  // float.rs:246-270
   uint64_t prec = base0.prec;
   Flt result = flt_from_u64(1, prec);
@@ -1601,36 +1626,60 @@ static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int
 // (19 * 2^kmin digits each, zero-padded).  An integer has one decimal
 // string, so the output equals the reference's conversion
 // (crates/bignum/src/integer.rs:892-983).
-static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S) {
+// The divisors and reciprocals of the levels depend only on the number of
+// chunks, so a caller that knows the digit count can build them early.
+struct DecPlan {
+  int K = 0, kmin = 0;
+  std::vector<Int> P;       // P_k = (10^19)^(2^k)
+  std::vector<Int> V;       // V_k ~ 2^(s_k) / P_k, k >= kmin
+  std::vector<uint64_t> sh; // s_k = 2 bits(P_k) + 64
+};
+
+// Plan for integers of at most ndig decimal digits.  V_k: Newton once at the
+// top, then V_(k-1) = (P_(k-1) V_k) >> (s_k - s_(k-1)) since P_k = P_(k-1)^2
+// (off by at most a few units; the quotient correction absorbs it).
+static DecPlan make_dec_plan(uint64_t ndig) {
+  DecPlan D;
+  const uint64_t nch = (ndig + 18) / 19;
+  while ((1ull << D.K) < nch) D.K++;
+  D.kmin = std::min(D.K, 5);
+  D.P.resize(D.K);
+  D.V.resize(D.K);
+  D.sh.resize(D.K);
+  if (D.K == 0) return D;
+  D.P[0] = Int(DEC_CHUNK);
+  for (int k = 1; k < D.K; k++) D.P[k] = mul(D.P[k - 1], D.P[k - 1]);
+  for (int k = D.K - 1; k >= D.kmin; k--) {
+    const uint64_t b = bits_of(D.P[k].m);
+    D.sh[k] = 2 * b + 64;
+    if (k == D.K - 1) {
+      Flt r = reciprocal_at_prec(flt_from_int(D.P[k]), b + 128);
+      r.exp += (int64_t)D.sh[k];
+      D.V[k] = to_integer_down(r);
+    } else {
+      D.V[k] = Int(shr_mag(mul_mag(D.P[k].m, D.V[k + 1].m), D.sh[k + 1] - D.sh[k]), false);
+    }
+  }
+  return D;
+}
+
+static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, const DecPlan* plan = nullptr) {
   if (X.m.size() <= 256) {
     outs = to_decimal_top(X);
     return g_error.load();
   }
+  DecPlan own;
   const uint64_t ndig = dec_estimate(bits_of(X.m)) + 1;
-  const uint64_t nch = (ndig + 18) / 19;
-  int K = 0;
-  while ((1ull << K) < nch) K++;
-  const int kmin = std::min(K, 5);
-  std::vector<Int> P(K);
-  P[0] = Int(DEC_CHUNK);
-  for (int k = 1; k < K; k++) P[k] = mul(P[k - 1], P[k - 1]);
+  if (!plan || (1ull << plan->K) * 19 < ndig) {
+    own = make_dec_plan(ndig);
+    plan = &own;
+  }
+  const int K = plan->K, kmin = plan->kmin;
+  const std::vector<Int>& P = plan->P;
   std::vector<Int> nodes{X};
-  // V_k ~ 2^(s_k) / P_k with s_k = 2 bits(P_k) + 64: Newton once at the top,
-  // then V_(k-1) = (P_(k-1) V_k) >> (s_k - s_(k-1)), since P_k = P_(k-1)^2
-  // (off by at most a few units; the quotient correction below absorbs it)
-  Int V;
-  uint64_t sh_prev = 0;
   for (int k = K - 1; k >= kmin; k--) {
-    const uint64_t b = bits_of(P[k].m);
-    const uint64_t sh = 2 * b + 64;
-    if (k == K - 1) {
-      Flt r = reciprocal_at_prec(flt_from_int(P[k]), b + 128);
-      r.exp += (int64_t)sh;
-      V = to_integer_down(r);
-    } else {
-      V = Int(shr_mag(mul_mag(P[k].m, V.m), sh_prev - sh), false);
-    }
-    sh_prev = sh;
+    const Int& V = plan->V[k];
+    const uint64_t sh = plan->sh[k];
     const size_t n = nodes.size();
     std::vector<const Limbs*> A(n), B(n, &V.m);
     for (size_t i = 0; i < n; i++) A[i] = &nodes[i].m;
@@ -1752,8 +1801,13 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   double t_sqrt = 0, t_scale = 0;
   std::thread sqrt_th([&] {
     double ts = now_ms();
-    Flt p = flt_from_u64(10005, prec);
-    sqrt_mut(p);
+    Flt p;
+    if (leaf_terms) {
+      p = sqrt_int_fast(10005, prec);
+    } else {
+      p = flt_from_u64(10005, prec);
+      sqrt_mut(p);
+    }
     sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
     t_sqrt = now_ms() - ts;
   });
@@ -1761,6 +1815,11 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     double ts = now_ms();
     scale = pow_int(flt_from_u64(10, prec), Int(digits - 1));
     t_scale = now_ms() - ts;
+  });
+  // batched form: the decimal conversion's divisors and reciprocals too
+  DecPlan dplan;
+  std::thread plan_th([&] {
+    if (leaf_terms) dplan = make_dec_plan(digits + 1);
   });
   Int q, t;
   int brc = PIMUL_OK;
@@ -1771,6 +1830,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   if (brc) {
     sqrt_th.join();
     scale_th.join();
+    plan_th.join();
     return brc;
   }
   double t1 = now_ms();
@@ -1789,10 +1849,11 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
   std::string s;
+  plan_th.join();
   if (leaf_terms) {
     LevelStaging S;
     int crc = S.init();
-    if (!crc) crc = to_decimal_batched(ip, s, S);
+    if (!crc) crc = to_decimal_batched(ip, s, S, &dplan);
     if (crc) return crc;
   } else {
     s = to_decimal_top(ip);
