@@ -1012,6 +1012,9 @@ struct BatchLayout {
   int small_L = 0;                  // largest L among the small jobs
 };
 
+// Scratch bound of one group of same-length products in a batch.
+static const uint64_t BATCH_ARENA_CAP = 4ull << 30;
+
 static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
   std::vector<int> Ls(n);
   for (size_t i = 0; i < n; i++) {
@@ -1031,28 +1034,40 @@ static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
       byL[Ls[i]].push_back((uint32_t)i);
     }
   }
-  std::stable_sort(B.small.begin(), B.small.end(), [&](uint32_t x, uint32_t y) {
-    return jobs[x].la + jobs[x].lb > jobs[y].la + jobs[y].lb;
-  });
-  uint64_t off = 0;
+  // longest transforms first (a bucket pass by length, O(n))
+  {
+    std::vector<std::vector<uint32_t>> sb(SMALL_LOG_MAX + 1);
+    for (uint32_t i : B.small) sb[Ls[i]].push_back(i);
+    B.small.clear();
+    for (int L = SMALL_LOG_MAX; L >= 0; L--) B.small.insert(B.small.end(), sb[L].begin(), sb[L].end());
+  }
+  // Large products of one length run as groups of at most 65535 (grid.y)
+  // whose scratch fits BATCH_ARENA_CAP; groups run one after another on the
+  // stream, so they all reuse the same arena.
+  uint64_t arena = 0;
   for (int L = 32; L > SMALL_LOG_MAX; L--) {
     if (byL[L].empty()) continue;
-    // grid.y is limited to 65535 rows: split big buckets
-    for (size_t s = 0; s < byL[L].size(); s += 65535) {
+    size_t s = 0;
+    while (s < byL[L].size()) {
       BatchLayout::Bucket bk;
       bk.L = L;
       bk.max_chunk = 0;
-      for (size_t k = s; k < byL[L].size() && k < s + 65535; k++) {
+      uint64_t off = 0;
+      for (size_t k = s; k < byL[L].size() && bk.idx.size() < 65535; k++) {
         uint32_t i = byL[L][k];
+        const uint64_t need = scratch_bytes(jobs[i].la, jobs[i].lb, false);
+        if (!bk.idx.empty() && off + need > BATCH_ARENA_CAP) break;
         bk.idx.push_back(i);
         bk.max_chunk = std::max<uint64_t>(bk.max_chunk, n_chunks(n_windows(jobs[i].la, jobs[i].lb)));
         B.arena_off[i] = off;
-        off += scratch_bytes(jobs[i].la, jobs[i].lb, false);
+        off += need;
       }
+      s += bk.idx.size();
+      arena = std::max(arena, off);
       B.large.push_back(std::move(bk));
     }
   }
-  B.arena_bytes = off;
+  B.arena_bytes = arena;
   return PIMUL_OK;
 }
 
