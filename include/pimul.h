@@ -224,15 +224,19 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
                         double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33);
 
 /*
- * Batched form of pimul_pi_chudnovsky: the binary splitting runs level by
- * level, each level's independent products (T_L Q_R, P_L T_R, P_L P_R,
- * Q_L Q_R for every neighbouring pair) in one pimul_mul_batch call, from
- * leaves of leaf_terms terms (0 = 64) split on host threads.  The final
- * assembly and decimal conversion are pimul_pi_chudnovsky's (GPU multiply
- * at the reference's NTT threshold).  Optional outputs: phase_ms[3] as
- * above; gpu_products = products sent to the GPU (batched and plain);
- * levels = batched levels; ntt_hist33[L] = products with transform 2^L.
- * The digits are identical to pimul_pi_chudnovsky's.
+ * Batched, device-resident form of pimul_pi_chudnovsky.  The binary
+ * splitting runs level by level: leaves of leaf_terms terms (0 = 32) are
+ * split on host threads and uploaded once; every level above keeps P, Q and
+ * T in HBM, with all of the level's products (T_L Q_R, P_L T_R, Q_L Q_R,
+ * P_L P_R for every neighbouring pair) in one pimul_mul_batch call, the T
+ * sums in one pimul_addsub_batch call and the trimmed lengths from
+ * pimul_top_limbs; only the root's Q and T return to the host.  The decimal
+ * conversion is level-batched (pimul_to_decimal); its divisors and
+ * reciprocals, sqrt(10005) (by a multiplication-only Newton iteration) and
+ * the decimal scale are computed beside the splitting.  Optional outputs:
+ * phase_ms[3] as above; gpu_products = products sent to the GPU (batched and
+ * plain); levels = batched splitting levels; ntt_hist33[L] = products with
+ * transform 2^L.  The digits are identical to pimul_pi_chudnovsky's.
  *
  * Replaces: crates/pi-core/src/algorithm/chudnovsky.rs:75 Chudnovsky::compute,
  * whose binary splitting (chudnovsky.rs:377-413) issues each level's

@@ -1913,7 +1913,7 @@ extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size
 extern "C" int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms,
                                            double* phase_ms, uint64_t* gpu_products, uint64_t* levels,
                                            uint64_t* ntt_hist33) {
-  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : 64, phase_ms, gpu_products,
+  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : 32, phase_ms, gpu_products,
                       ntt_hist33);
   if (levels) *levels = g_batch_levels.load();
   return rc;
