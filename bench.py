@@ -599,7 +599,7 @@ def run_pi(args):
     gl_backend = pm.served_backend() if args.gl_backend == "served" else None
 
     def gl_run(d, **kw):
-        return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend))
+        return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend), fast_sqrt=args.gl_sqrt == "newton")
 
     if args.algorithm == "both":
         gl_run(min(D, 100_000))
@@ -670,6 +670,8 @@ def run_pi(args):
         "batched_binary_splitting": batched,
         "gauss_legendre": None if other_same is None else {"wall_s": round(args.gl_wall, 3),
                                                            "multiply": args.gl_backend,
+                                                           "sqrt": ("multiplication-only Newton" if args.gl_sqrt == "newton"
+                                                                    else "reference (division-based)"),
                                                            "digits_identical_to_chudnovsky": other_same},
         "sha256": hashlib.sha256(s.encode()).hexdigest(),
         "last_digits": s[-20:], "cpu_baseline": cpu,
@@ -799,6 +801,9 @@ def main():
     ap.add_argument("--leaf-terms", type=int, default=0, help="terms per host-split leaf (0 = 32)")
     ap.add_argument("--gl-backend", choices=["plain", "served"], default="plain",
                     help="Gauss-Legendre products: one pimul_mul call each, or through the served form")
+    ap.add_argument("--gl-sqrt", choices=["reference", "newton"], default="reference",
+                    help="Gauss-Legendre square roots: the reference's division-based iteration or the "
+                         "multiplication-only one (same digits)")
     ap.add_argument("--positions", type=int, default=256)
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)

@@ -269,6 +269,14 @@ int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size_t cap, siz
 int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
                             double* phase_ms, uint64_t* ntt_products);
 
+/* pimul_pi_gauss_legendre with options: PIMUL_PI_FAST_SQRT takes the square
+ * roots by a multiplication-only Newton iteration for 1/sqrt(x) instead of
+ * the reference's division-based one (float.rs:85-174); the digits are the
+ * same. */
+#define PIMUL_PI_FAST_SQRT 1u
+int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
+                               uint32_t flags, double* phase_ms, uint64_t* ntt_products);
+
 /* Transform plan for a product: N and the number of HBM passes per transform.
  * Mirrors the sizing of crates/bignum/src/ntt.rs:810-813. */
 int pimul_plan(size_t la, size_t lb, uint64_t* n_transform, int* passes);

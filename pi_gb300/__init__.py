@@ -89,6 +89,9 @@ def load(build_if_stale: bool = True):
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                               ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_to_decimal.argtypes = [_u64p, _sz, ctypes.c_char_p, _sz, ctypes.POINTER(_sz), ctypes.c_int]
+    L.pimul_pi_gauss_legendre_ex.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
+                                             ctypes.c_uint32, ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_pi_gauss_legendre.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
@@ -380,14 +383,15 @@ def to_decimal(limbs, batched: bool = True) -> str:
     return buf.raw[: n.value].decode()
 
 
-def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0):
+def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sqrt: bool = False):
     """Digits of pi by the Gauss-Legendre AGM
-    (crates/pi-core/src/algorithm/gauss_legendre.rs:61)."""
+    (crates/pi-core/src/algorithm/gauss_legendre.rs:61); fast_sqrt takes the
+    square roots by a multiplication-only Newton iteration (same digits)."""
     buf = ctypes.create_string_buffer(digits + 1)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
-    _check(lib().pimul_pi_gauss_legendre(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
-                                         ntt_threshold, ph, ctypes.byref(n)))
+    _check(lib().pimul_pi_gauss_legendre_ex(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
+                                            ntt_threshold, 1 if fast_sqrt else 0, ph, ctypes.byref(n)))
     return buf.raw[:digits].decode(), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
                                        "ntt_products": n.value}
 

@@ -803,6 +803,37 @@ static Flt sqrt_int_fast(uint64_t n, uint64_t prec) {
   return mul_at_prec(y, nf, prec);
 }
 
+// In-place square root of a positive Float by the same multiplication-only
+// iteration as sqrt_int_fast (a Newton iteration for 1/sqrt(x) from an f64
+// start, then sqrt(x) = x y), for drivers that opt out of the reference's
+// division-based sqrt_mut; results agree to within an ulp.
+static void sqrt_fast(Flt& self) {
+  if (self.zero()) return;
+  const uint64_t prec = self.prec, target = prec + 64;
+  double m;
+  int64_t e;
+  to_f64_with_exp(self.mant, m, e);
+  const int64_t tot = e + self.exp;  // value = m 2^tot, m in [1, 2)
+  const int64_t half = tot >= 0 ? tot / 2 : -((-tot + 1) / 2);
+  const double mc = (tot - 2 * half) ? 2.0 * m : m;
+  Flt y = flt_from_f64(1.0 / std::sqrt(mc), 64);
+  y.exp -= half;
+  const Flt one = flt_from_u64(1, 64);
+  uint64_t cur = 48;
+  while (cur < target) {
+    cur = std::min(2 * cur, target);
+    const uint64_t w = cur + 32;
+    Flt xt = truncated_to_prec(self, w);
+    Flt y2 = mul_at_prec(y, y, w);
+    Flt er = sub_at_prec(one, mul_at_prec(xt, y2, w), w);  // |er| ~ 2^-(cur/2)
+    er = truncated_to_prec(er, cur / 2 + 64);
+    Flt c = mul_at_prec(y, er, w);
+    c.exp -= 1;
+    y = add_at_prec(y, c, w);
+  }
+  self = mul_at_prec(self, y, prec);
+}
+
 static Flt pow_int(const Flt& base0, const Int& ex) {  // float.rs:246-270
   uint64_t prec = base0.prec;
   Flt result = flt_from_u64(1, prec);
@@ -1185,18 +1216,22 @@ static Flt flt_f64_prec(double v, uint64_t prec) {
 // Gauss-Legendre AGM (crates/pi-core/src/algorithm/gauss_legendre.rs:61-151):
 // iterations = ceil(log2 prec) + 2; per iteration a' = (a+b)/2,
 // b' = sqrt(a b), t -= p (a - a')^2, p <<= 1; pi = (a+b)^2 / t / 4.
-static Flt gauss_legendre(uint64_t prec) {
+static Flt gauss_legendre(uint64_t prec, bool fast_sqrt) {
+  auto root = [&](Flt& x) {
+    if (fast_sqrt) sqrt_fast(x);
+    else sqrt_mut(x);
+  };
   const uint32_t iters = (uint32_t)std::ceil(std::log2((double)prec)) + 2;
   Flt a = flt_from_u64(1, prec);
   Flt b = flt_f64_prec(0.5, prec);
-  sqrt_mut(b);
+  root(b);
   Flt t = flt_f64_prec(0.25, prec);
   Int p(1);
   for (uint32_t it = 0; it < iters; it++) {
     Flt an = add_at_prec(a, b, prec);
     an = div_at_prec(an, flt_from_u64(2, 64), prec);
     Flt bn = mul_at_prec(a, b, prec);
-    sqrt_mut(bn);
+    root(bn);
     Flt diff = sub_at_prec(a, an, prec);
     Flt dsq = mul_at_prec(diff, diff, prec);
     dsq = mul_at_prec(dsq, flt_from_int(p), prec);
@@ -1747,8 +1782,9 @@ static int finish_digits(Flt pi, const Flt& scale, uint64_t digits, char* out, d
 }
 
 // Digits of pi by Gauss-Legendre (see pimul.h).
-extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
-                                       uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products) {
+extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                          uint64_t ntt_threshold, uint32_t flags, double* phase_ms,
+                                          uint64_t* ntt_products) {
   if (digits == 0) return PIMUL_OK;
   if (!out || cap < digits) return PIMUL_EINVAL;
   g_backend = reinterpret_cast<mul_fn>(backend);
@@ -1762,7 +1798,7 @@ extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, p
   // iterations (it depends on nothing else)
   Flt scale;
   std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
-  Flt pi = gauss_legendre(prec);
+  Flt pi = gauss_legendre(prec, (flags & PIMUL_PI_FAST_SQRT) != 0);
   double t1 = now_ms();
   scale_th.join();
   double tdc = 0;
@@ -1774,6 +1810,11 @@ extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, p
   }
   if (ntt_products) *ntt_products = g_ntt_calls.load();
   return rc;
+}
+
+extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                       uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products) {
+  return pimul_pi_gauss_legendre_ex(digits, out, cap, backend, ntt_threshold, 0, phase_ms, ntt_products);
 }
 
 // Digits of pi by Chudnovsky (crates/pi-core/src/algorithm/chudnovsky.rs:75-235):

@@ -77,3 +77,10 @@ def test_gauss_legendre_through_served_form():
     g, info = pm.pi_gauss_legendre(100_000, backend=pm.served_backend(), ntt_threshold=512)
     assert g == ref
     assert info["ntt_products"] > 0
+
+
+def test_gauss_legendre_fast_sqrt_1e6_matches_mpmath():
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, _ = pm.pi_gauss_legendre(1_000_000, backend=pm.served_backend(), fast_sqrt=True)
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]

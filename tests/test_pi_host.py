@@ -34,3 +34,9 @@ def test_digits_vs_mpmath(digits, thr):
 def test_gauss_legendre_vs_mpmath(digits, thr):
     s, info = pm.pi_gauss_legendre(digits, backend=O.mul_abi_pointer(), ntt_threshold=thr)
     assert s == ref_digits()[:digits]
+
+
+@pytest.mark.parametrize("digits,thr", [(1, 0), (100, 0), (5000, 64), (30000, 256)])
+def test_gauss_legendre_fast_sqrt_vs_mpmath(digits, thr):
+    s, _ = pm.pi_gauss_legendre(digits, backend=O.mul_abi_pointer(), ntt_threshold=thr, fast_sqrt=True)
+    assert s == ref_digits()[:digits]
