@@ -35,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BASELINE_METRIC = "1e9-digit pi wall-s; NTT-mul GB/s, batched ops/s & p99 vs plain GPU, bit-exact"
+PROJECT_METRIC = "1e9-digit pi wall-s; NTT-mul GB/s, batched ops/s & p99 vs plain GPU, bit-exact"
 METRIC = "NTT-mul GB/s (2^30 x 2^30-bit product)"
 BITS_A = 1 << 30
 BITS_B = 1 << 30
@@ -309,7 +309,7 @@ def run_gpu(args):
     if rank == 0:
         line = {
             "metric": METRIC,
-            "baseline_metric": BASELINE_METRIC,
+            "project_metric": PROJECT_METRIC,
             "value": round(value, 2),
             "unit": "GB/s",
             "n_gpus": ws,
@@ -437,7 +437,7 @@ def run_batch(args):
         bytes_model += b_mul(N, int(x), int(y))
     line = {
         "metric": "batched products/s (4096 uneven products)",
-        "baseline_metric": BASELINE_METRIC,
+        "project_metric": PROJECT_METRIC,
         "value": round(nprod / (ms_plan * 1e-3), 1),
         "unit": "products/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -567,7 +567,7 @@ def run_served(args):
     lp = np.array(lat_plain) * 1e3
     line = {
         "metric": "served request stream: p50/p99 latency and ops/s vs plain per-call",
-        "baseline_metric": BASELINE_METRIC,
+        "project_metric": PROJECT_METRIC,
         "value": round(n / span_served, 1), "unit": "requests/s",
         "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * span_served, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -654,7 +654,7 @@ def run_pi(args):
             golden = hashlib.sha256(s.encode()).hexdigest() == g["sha256"]
     line = {
         "metric": f"pi wall-s ({'Gauss-Legendre' if args.algorithm == 'gl' else 'Chudnovsky'}, {D} digits)",
-        "baseline_metric": BASELINE_METRIC,
+        "project_metric": PROJECT_METRIC,
         "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
         "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "deterministic (no random input)",
@@ -693,7 +693,7 @@ def run_bbp(args):
     dt = time.perf_counter() - t0
     terms = 4.0 * float((pos.astype(np.float64) + 1).sum())
     line = {
-        "metric": "BBP hex-digit spot checks (positions/s)", "baseline_metric": BASELINE_METRIC,
+        "metric": "BBP hex-digit spot checks (positions/s)", "project_metric": PROJECT_METRIC,
         "value": round(args.positions / dt, 3), "unit": "positions/s", "n_gpus": 1, "steps": 1, "warmup": 1,
         "ms_per_step": round(1e3 * dt, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u64+f64", "data": f"seeded positions uniform in [0, {int(args.max_pos)})",
@@ -763,7 +763,7 @@ def run_reference(args):
     line = {
         "impl": "reference",
         "metric": METRIC,
-        "baseline_metric": BASELINE_METRIC,
+        "project_metric": PROJECT_METRIC,
         "value": round(value, 3),
         "unit": "GB/s",
         "n_gpus": ws,
