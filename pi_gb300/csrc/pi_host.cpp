@@ -26,6 +26,7 @@
 #include <chrono>
 #include <functional>
 #include <map>
+#include <condition_variable>
 #include <mutex>
 #include <cmath>
 #include <cstdint>
@@ -1470,51 +1471,70 @@ struct DNode {
   uint64_t terms;
 };
 
-static int split_root_device(const std::vector<PQT>& leaves, const std::vector<uint64_t>& terms, Int& q, Int& t) {
-  cudaStream_t st = nullptr;
-  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
-  int rc = PIMUL_OK;
+// Nodes on the device and the arenas that hold them.
+struct DLevel {
+  std::vector<DNode> nodes;
+  std::vector<uint64_t*> arenas;
+};
+
+static void dev_free(DLevel& L, cudaStream_t st) {
+  for (uint64_t* a : L.arenas) cudaFreeAsync(a, st);
+  L.arenas.clear();
+  L.nodes.clear();
+}
+
+// One upload of the leaves (|P|, Q, |T| back to back) into a fresh arena.
+static int dev_upload_leaves(const std::vector<PQT>& leaves, const std::vector<uint64_t>& terms, cudaStream_t st,
+                             LevelStaging& S, DLevel& out) {
+  double t0 = now_ms();
+  std::vector<size_t> off(leaves.size() + 1, 0);
+  for (size_t i = 0; i < leaves.size(); i++)
+    off[i + 1] = off[i] + leaves[i].p.m.size() + leaves[i].q.m.size() + leaves[i].t.m.size();
+  int rc = S.host(off.back());
+  if (rc) return rc;
   uint64_t* arena = nullptr;
-  std::vector<DNode> nodes(leaves.size());
-  LevelStaging S;
+  if (cudaMallocAsync((void**)&arena, std::max<size_t>(off.back(), 1) * 8, st) != cudaSuccess) return PIMUL_ENOMEM;
+  out.arenas.push_back(arena);
+  out.nodes.resize(leaves.size());
+  parallel_for(leaves.size(), [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; i++) {
+      uint64_t* h = S.h + off[i];
+      const Limbs* parts[3] = {&leaves[i].p.m, &leaves[i].q.m, &leaves[i].t.m};
+      size_t o = 0;
+      for (const Limbs* x : parts) {
+        memcpy(h + o, x->data(), x->size() * 8);
+        o += x->size();
+      }
+      DNode& n = out.nodes[i];
+      n.pn = leaves[i].p.m.size();
+      n.qn = leaves[i].q.m.size();
+      n.tn = leaves[i].t.m.size();
+      n.p = arena + off[i];
+      n.q = n.p + n.pn;
+      n.t = n.q + n.qn;
+      n.terms = terms[i];
+    }
+  });
+  if (cudaMemcpyAsync(arena, S.h, off.back() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) return PIMUL_ECUDA;
+  // the staging buffer is reused by the next upload: wait for this copy
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PIMUL_ECUDA;
+  g_bt[0] += now_ms() - t0;
+  return PIMUL_OK;
+}
+
+// Levels until one node is left; keep_p keeps P of the last node (needed
+// when it is merged again later).
+static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
+  int rc = PIMUL_OK;
   auto cu = [&](cudaError_t e) {
     if (e != cudaSuccess && !rc) rc = PIMUL_ECUDA;
     return e == cudaSuccess;
   };
-  {
-    double t0 = now_ms();
-    std::vector<size_t> off(leaves.size() + 1, 0);
-    for (size_t i = 0; i < leaves.size(); i++)
-      off[i + 1] = off[i] + leaves[i].p.m.size() + leaves[i].q.m.size() + leaves[i].t.m.size();
-    rc = S.host(off.back());
-    if (!rc && cu(cudaMallocAsync((void**)&arena, std::max<size_t>(off.back(), 1) * 8, st))) {
-      parallel_for(leaves.size(), [&](size_t lo, size_t hi) {
-        for (size_t i = lo; i < hi; i++) {
-          uint64_t* h = S.h + off[i];
-          const Limbs* parts[3] = {&leaves[i].p.m, &leaves[i].q.m, &leaves[i].t.m};
-          size_t o = 0;
-          for (const Limbs* x : parts) {
-            memcpy(h + o, x->data(), x->size() * 8);
-            o += x->size();
-          }
-          DNode& n = nodes[i];
-          n.pn = leaves[i].p.m.size();
-          n.qn = leaves[i].q.m.size();
-          n.tn = leaves[i].t.m.size();
-          n.p = arena + off[i];
-          n.q = n.p + n.pn;
-          n.t = n.q + n.qn;
-          n.terms = terms[i];
-        }
-      });
-      cu(cudaMemcpyAsync(arena, S.h, off.back() * 8, cudaMemcpyHostToDevice, st));
-    }
-    g_bt[0] += now_ms() - t0;
-  }
+  std::vector<DNode>& nodes = Lv.nodes;
   while (!rc && nodes.size() > 1) {
     double t0 = now_ms();
     const size_t np = nodes.size() / 2;
-    const bool need_p = nodes.size() > 2, odd = nodes.size() & 1;
+    const bool need_p = nodes.size() > 2 || keep_p, odd = nodes.size() & 1;
     // new level: Q, P, T per pair (and the odd node); temporaries T_L Q_R, P_L T_R
     size_t lvl_w = 0, tmp_w = 0;
     for (size_t i = 0; i < np; i++) {
@@ -1526,7 +1546,11 @@ static int split_root_device(const std::vector<PQT>& leaves, const std::vector<u
     if (odd) lvl_w += nodes.back().pn + nodes.back().qn + nodes.back().tn;
     uint64_t* nxt = nullptr;
     uint64_t* tmp = nullptr;
-    if (!cu(cudaMallocAsync((void**)&nxt, lvl_w * 8, st)) || !cu(cudaMallocAsync((void**)&tmp, tmp_w * 8, st))) break;
+    if (!cu(cudaMallocAsync((void**)&nxt, lvl_w * 8, st))) break;
+    if (!cu(cudaMallocAsync((void**)&tmp, tmp_w * 8, st))) {
+      cudaFreeAsync(nxt, st);
+      break;
+    }
     std::vector<DNode> next(np + odd);
     std::vector<pimul_job> mj;
     std::vector<pimul_addsub_job> aj(np);
@@ -1576,8 +1600,8 @@ static int split_root_device(const std::vector<PQT>& leaves, const std::vector<u
     if (!rc) rc = pimul_mul_batch(mj.data(), mj.size(), st);
     if (!rc) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
     cudaFreeAsync(tmp, st);
-    cudaFreeAsync(arena, st);
-    arena = nxt;
+    for (uint64_t* a : Lv.arenas) cudaFreeAsync(a, st);
+    Lv.arenas.assign(1, nxt);
     // trimmed lengths of the new level
     std::vector<const uint64_t*> arrs;
     std::vector<size_t> lens;
@@ -1603,18 +1627,93 @@ static int split_root_device(const std::vector<PQT>& leaves, const std::vector<u
     g_bt[1] += t2 - t1;
     g_bt[4] += (t1 - t0);
   }
+  return rc;
+}
+
+// Device-resident splitting over leaves [0, n): the leaves are computed by
+// host threads segment by segment while a GPU thread reduces the previous
+// segment to its root; the segment roots are then merged on the device and
+// only the final Q and |T| come back.  Returns PIMUL_EINVAL (nothing
+// computed on the device) if a leaf breaks the static signs.
+static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
+  const uint64_t nleaf = (b - a + leaf - 1) / leaf;
+  const size_t nseg = nleaf >= 64 ? 4 : 1;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  std::vector<std::vector<PQT>> seg_leaves(nseg);
+  std::vector<std::vector<uint64_t>> seg_terms(nseg);
+  std::vector<DLevel> roots(nseg);
+  std::mutex mu;
+  std::condition_variable cv;
+  size_t ready = 0;
+  bool abort_all = false;
+  int rc_gpu = PIMUL_OK;
+  std::thread gpu([&] {
+    LevelStaging S;
+    for (size_t sgi = 0; sgi < nseg; sgi++) {
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return ready > sgi || abort_all; });
+        if (abort_all) return;
+      }
+      int rc = dev_upload_leaves(seg_leaves[sgi], seg_terms[sgi], st, S, roots[sgi]);
+      if (!rc) rc = dev_reduce(roots[sgi], st, true);
+      if (rc) {
+        rc_gpu = rc;
+        return;
+      }
+      std::vector<PQT>().swap(seg_leaves[sgi]);
+    }
+  });
+  double tl = 0;
+  for (size_t sgi = 0; sgi < nseg; sgi++) {
+    const uint64_t l0 = nleaf * sgi / nseg, l1 = nleaf * (sgi + 1) / nseg;
+    std::vector<PQT> lv(l1 - l0);
+    std::vector<uint64_t> tv(l1 - l0);
+    double t0 = now_ms();
+    parallel_for(l1 - l0, [&](size_t lo, size_t hi) {
+      for (size_t i = lo; i < hi; i++) {
+        const uint64_t ka = a + (l0 + i) * leaf, kb = std::min(b, ka + leaf);
+        lv[i] = split(ka, kb, 4);
+        tv[i] = kb - ka;
+      }
+    });
+    tl += now_ms() - t0;
+    bool ok = true;
+    for (size_t i = 0; i < lv.size() && ok; i++) ok = lv[i].t.neg && lv[i].p.neg == (bool)(tv[i] & 1);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ok) {
+      abort_all = true;
+      cv.notify_all();
+      break;
+    }
+    seg_leaves[sgi] = std::move(lv);
+    seg_terms[sgi] = std::move(tv);
+    ready = sgi + 1;
+    cv.notify_all();
+  }
+  gpu.join();
+  g_leaf_ms += tl;
+  int rc = abort_all ? PIMUL_EINVAL : rc_gpu;
+  DLevel top;
+  for (DLevel& r : roots) {
+    for (const DNode& n : r.nodes) top.nodes.push_back(n);
+    top.arenas.insert(top.arenas.end(), r.arenas.begin(), r.arenas.end());
+  }
+  if (!rc) rc = dev_reduce(top, st, false);
   if (!rc) {
     double t0 = now_ms();
-    const DNode& r = nodes[0];
+    const DNode& r = top.nodes[0];
     Limbs qm(r.qn), tm(r.tn);
-    cu(cudaMemcpyAsync(qm.data(), r.q, r.qn * 8, cudaMemcpyDeviceToHost, st));
-    cu(cudaMemcpyAsync(tm.data(), r.t, r.tn * 8, cudaMemcpyDeviceToHost, st));
-    cu(cudaStreamSynchronize(st));
+    if (cudaMemcpyAsync(qm.data(), r.q, r.qn * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(tm.data(), r.t, r.tn * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = PIMUL_ECUDA;
     q = Int(std::move(qm), false);
     t = Int(std::move(tm), true);
     g_bt[2] += now_ms() - t0;
   }
-  if (arena) cudaFreeAsync(arena, st);
+  dev_free(top, st);
   cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
   return rc;
@@ -1622,25 +1721,21 @@ static int split_root_device(const std::vector<PQT>& leaves, const std::vector<u
 
 static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
   const uint64_t nleaf = (b - a + leaf - 1) / leaf;
-  std::vector<PQT> nodes(nleaf);
   for (double& x : g_bt) x = 0;
+  g_leaf_ms = 0;
+  // device-resident levels (every range obeys the static signs; a leaf that
+  // did not would send the splitting down the host-staged path below)
+  if (nleaf > 1) {
+    int rc = split_root_device(a, b, leaf, q, t);
+    report_split("binary splitting (device-resident levels)");
+    if (rc != PIMUL_EINVAL) return rc;
+  }
+  std::vector<PQT> nodes(nleaf);
   double t0 = now_ms();
   parallel_for(nleaf, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; i++) nodes[i] = split(a + i * leaf, std::min(b, a + (i + 1) * leaf), 4);
   });
   g_leaf_ms = now_ms() - t0;
-  // device-resident levels when the leaves carry the static signs
-  bool static_signs = nleaf > 1;
-  std::vector<uint64_t> terms(nleaf);
-  for (uint64_t i = 0; i < nleaf && static_signs; i++) {
-    terms[i] = std::min(b, a + (i + 1) * leaf) - (a + i * leaf);
-    static_signs = nodes[i].t.neg && nodes[i].p.neg == (bool)(terms[i] & 1);
-  }
-  if (static_signs) {
-    int rc = split_root_device(nodes, terms, q, t);
-    report_split("binary splitting (device-resident levels)");
-    return rc;
-  }
   LevelStaging S;
   int rc = S.init();
   while (!rc && nodes.size() > 1) rc = merge_level(nodes, S);
