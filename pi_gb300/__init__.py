@@ -343,7 +343,7 @@ def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
                                      ntt_threshold, ph, ctypes.byref(n), hist))
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
-    return buf.raw[:digits].decode(), info
+    return ctypes.string_at(buf, digits).decode("ascii"), info
 
 
 def served_backend():
@@ -366,7 +366,7 @@ def pi_chudnovsky_batched(digits: int, leaf_terms: int = 0):
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "batched_levels": lv.value,
             "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
-    return buf.raw[:digits].decode(), info
+    return ctypes.string_at(buf, digits).decode("ascii"), info
 
 
 def to_decimal(limbs, batched: bool = True) -> str:
@@ -392,7 +392,7 @@ def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sq
     n = ctypes.c_uint64(0)
     _check(lib().pimul_pi_gauss_legendre_ex(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
                                             ntt_threshold, 1 if fast_sqrt else 0, ph, ctypes.byref(n)))
-    return buf.raw[:digits].decode(), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
+    return ctypes.string_at(buf, digits).decode("ascii"), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
                                        "ntt_products": n.value}
 
 

@@ -1793,11 +1793,9 @@ static DecPlan make_dec_plan(uint64_t ndig) {
   return D;
 }
 
-static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, const DecPlan* plan = nullptr) {
-  if (X.m.size() <= 256) {
-    outs = to_decimal_top(X);
-    return g_error.load();
-  }
+// The levels of the batched conversion: X split down to nodes below
+// P_kmin, most significant first, each worth 19 * 2^kmin digits.
+static int dec_levels(const Int& X, LevelStaging& S, const DecPlan* plan, std::vector<Int>& out_nodes, int& kmin_out) {
   DecPlan own;
   const uint64_t ndig = dec_estimate(bits_of(X.m)) + 1;
   if (!plan || (1ull << plan->K) * 19 < ndig) {
@@ -1846,6 +1844,20 @@ static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, 
     nodes.swap(next);
   }
   report_split("decimal levels");
+  out_nodes.swap(nodes);
+  kmin_out = kmin;
+  return g_error.load();
+}
+
+static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, const DecPlan* plan = nullptr) {
+  if (X.m.size() <= 256) {
+    outs = to_decimal_top(X);
+    return g_error.load();
+  }
+  std::vector<Int> nodes;
+  int kmin = 0;
+  int rc = dec_levels(X, S, plan, nodes, kmin);
+  if (rc) return rc;
   const size_t per = (size_t)19 << kmin;
   std::string all(per * nodes.size(), '0');
   parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
@@ -1857,6 +1869,51 @@ static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, 
   });
   size_t nz = all.find_first_not_of('0');
   outs = nz == std::string::npos ? std::string("0") : all.substr(nz);
+  return g_error.load();
+}
+
+// Exactly `want` decimal digits of X < 10^want (zero-padded on the left),
+// written straight into out.
+static int to_decimal_batched_into(const Int& X, char* out, size_t want, LevelStaging& S, const DecPlan* plan) {
+  if (X.m.size() <= 256) {
+    std::string s = to_decimal_top(X);
+    if (s.size() > want) return PIMUL_EINVAL;
+    memset(out, '0', want - s.size());
+    memcpy(out + want - s.size(), s.data(), s.size());
+    return g_error.load();
+  }
+  std::vector<Int> nodes;
+  int kmin = 0;
+  int rc = dec_levels(X, S, plan, nodes, kmin);
+  if (rc) return rc;
+  const size_t per = (size_t)19 << kmin, total = per * nodes.size();
+  if (total < want) {
+    memset(out, '0', want - total);
+    out += want - total;
+    want = total;
+  }
+  const size_t skip = total - want;  // leading characters that must be zeros
+  std::atomic<int> bad{0};
+  parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
+    std::string buf(per, '0');
+    for (size_t i = lo; i < hi; i++) {
+      const size_t b0 = i * per;
+      if (b0 + per <= skip) {
+        if (!nodes[i].zero()) bad.store(1);
+        continue;
+      }
+      std::fill(buf.begin(), buf.end(), '0');
+      if (!nodes[i].zero()) {
+        std::string d = decimal_naive(nodes[i].m);
+        memcpy(&buf[per - d.size()], d.data(), d.size());
+      }
+      const size_t from = b0 < skip ? skip - b0 : 0;
+      for (size_t c = 0; c < from; c++)
+        if (buf[c] != '0') bad.store(1);
+      memcpy(out + b0 + from - skip, buf.data() + from, per - from);
+    }
+  });
+  if (bad.load()) return PIMUL_EINVAL;
   return g_error.load();
 }
 
@@ -1986,11 +2043,13 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   Int ip = to_integer_down(pi);
   std::string s;
   plan_th.join();
+  bool written = false;
   if (leaf_terms) {
     LevelStaging S;
     int crc = S.init();
-    if (!crc) crc = to_decimal_batched(ip, s, S, &dplan);
+    if (!crc) crc = to_decimal_batched_into(ip, out, digits, S, &dplan);
     if (crc) return crc;
+    written = true;
   } else {
     s = to_decimal_top(ip);
   }
@@ -1999,8 +2058,10 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms (waited %.1f), reciprocal %.1f ms\n", t_sqrt,
             t_scale, t_join, t_recip);
   if (g_error.load()) return g_error.load();
-  if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
-  memcpy(out, s.data(), digits);
+  if (!written) {
+    if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
+    memcpy(out, s.data(), digits);
+  }
   if (phase_ms) {
     phase_ms[0] = t1 - t0;
     phase_ms[1] = t2 - t1;
