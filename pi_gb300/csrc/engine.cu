@@ -908,6 +908,7 @@ struct Launcher {
   cudaStream_t st;
   bool stats;  // count and (optionally) time launches
   const Roots& R;
+  cudaEvent_t b_ready = nullptr;  // operand b's upload (plain host-buffer call): waited on before its first pass
 };
 
 // All launches of the large-product pipeline for `nj` products sharing the
@@ -921,6 +922,7 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
   const uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L (2^192 = 1)
   const int rl = pl.r[pl.np - 1];
   for (int which = 0; which < 2; which++) {
+    if (which == 1 && X.b_ready) cudaStreamWaitEvent(X.st, X.b_ready, 0);
     {
       KTimer kt(K_PACK, X.st, X.stats);
       PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L, X.R)));
@@ -963,13 +965,14 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
 
 // Device multiply: d_out[0 .. la+lb) = a * b, scratch from the memory pool.
 static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
-                      cudaStream_t st) {
+                      cudaStream_t st, cudaEvent_t b_ready = nullptr) {
   if (la == 0 || lb == 0) return PIMUL_OK;
   const Sizes z = sizes_for(la, lb);
   if (z.L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
   const Roots& R = g_dev.roots;
   const bool square = d_a == d_b && la == lb;
   if (z.L <= SMALL_LOG_MAX) {
+    if (b_ready) cudaStreamWaitEvent(st, b_ready, 0);
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
     {
       KTimer kt(K_SMALL, st, true);
@@ -986,7 +989,7 @@ static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uin
   }
   Job J{d_a, d_b, d_out, nullptr, nullptr, nullptr, nullptr, la, lb};
   carve_scratch(J, base, square);
-  Launcher X{st, true, R};
+  Launcher X{st, true, R, b_ready};
   run_large(X, nullptr, J, 1, z.L, z.nchunk);
   cudaError_t le = cudaGetLastError();
   cudaFreeAsync(base, st);
@@ -2244,9 +2247,28 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
     cudaGetLastError();
     return fail(PIMUL_ENOMEM, std::string("operand allocation: ") + cudaGetErrorString(e));
   }
+  // a is uploaded first; b follows on a helper stream while a's forward
+  // transform runs, and b's first pass waits for it
   cudaMemcpyAsync(da, a, la * 8, cudaMemcpyHostToDevice, st);
-  if (!square) cudaMemcpyAsync(db, b, lb * 8, cudaMemcpyHostToDevice, st);
-  rc = mul_device(da, la, square ? da : db, lb, dout, st);
+  thread_local cudaStream_t t_copy = nullptr;
+  thread_local cudaEvent_t t_ev[2] = {nullptr, nullptr};
+  thread_local int t_copy_dev = -1;
+  cudaEvent_t b_ready = nullptr;
+  if (!square) {
+    if (!t_copy || t_copy_dev != g_dev.device) {
+      CU(cudaStreamCreateWithFlags(&t_copy, cudaStreamNonBlocking));
+      CU(cudaEventCreateWithFlags(&t_ev[0], cudaEventDisableTiming));
+      CU(cudaEventCreateWithFlags(&t_ev[1], cudaEventDisableTiming));
+      t_copy_dev = g_dev.device;
+    }
+    CU(cudaEventRecord(t_ev[0], st));  // after db's allocation and a's upload
+    CU(cudaStreamWaitEvent(t_copy, t_ev[0], 0));
+    cudaMemcpyAsync(db, b, lb * 8, cudaMemcpyHostToDevice, t_copy);
+    CU(cudaEventRecord(t_ev[1], t_copy));
+    b_ready = t_ev[1];
+  }
+  rc = mul_device(da, la, square ? da : db, lb, dout, st, b_ready);
+  if (rc && b_ready) cudaStreamWaitEvent(st, b_ready, 0);  // db is freed below
   if (rc == PIMUL_OK) cudaMemcpyAsync(out, dout, (la + lb) * 8, cudaMemcpyDeviceToHost, st);
   cudaFreeAsync(da, st);
   if (db) cudaFreeAsync(db, st);
