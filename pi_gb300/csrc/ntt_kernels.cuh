@@ -11,7 +11,7 @@
 // pointwise product does not care, and the inverse passes (the exact mirror)
 // restore natural order.  This is the reference's four-step decomposition
 // (crates/bignum/src/ntt.rs:905-1105) without the transposes: strided tiles
-// are read as coalesced 128-byte row segments.
+// are read as coalesced 64-byte (or wider) row segments.
 //
 // Inside a pass the R_p-point DFT runs in shared memory as rounds of radix
 // 8 (or 4 / 2) held in registers.  2 is a 192nd root of unity mod p, and the
