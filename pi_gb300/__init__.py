@@ -96,6 +96,7 @@ def load(build_if_stale: bool = True):
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
     L.pimul_bbp_last_error.restype = ctypes.c_char_p
+    L.pimul_bbp_modops.argtypes = [_u64p, _u64p, _u64p, _sz, _u64p, _u64p]
     _lib = L
     return L
 
@@ -394,6 +395,18 @@ def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sq
                                             ntt_threshold, 1 if fast_sqrt else 0, ph, ctypes.byref(n)))
     return ctypes.string_at(buf, digits).decode("ascii"), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
                                        "ntt_products": n.value}
+
+
+def bbp_modops(e, d, p):
+    """16^e mod d and floor(p 2^64 / d) on the device (pimul_bbp_modops)."""
+    e, d, p = (np.ascontiguousarray(np.asarray(x, dtype=np.uint64)) for x in (e, d, p))
+    pw = np.zeros(e.size, dtype=np.uint64)
+    fr = np.zeros(e.size, dtype=np.uint64)
+    rc = lib().pimul_bbp_modops(e.ctypes.data_as(_u64p), d.ctypes.data_as(_u64p), p.ctypes.data_as(_u64p), e.size,
+                                pw.ctypes.data_as(_u64p), fr.ctypes.data_as(_u64p))
+    if rc:
+        raise PimulError(rc, lib().pimul_bbp_last_error().decode())
+    return pw, fr
 
 
 def bbp_hex_digits(positions, stop=None) -> np.ndarray:

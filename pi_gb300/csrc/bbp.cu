@@ -33,12 +33,18 @@ static int fail(int code, const std::string& m) {
   return code;
 }
 
-// -m^-1 mod 2^64 for odd m (Newton: each step doubles the correct bits).
+// -m^-1 mod 2^64 for odd m: Newton steps x <- x (2 - m x), each doubling the
+// correct low bits (5 from the start value), three in 32-bit arithmetic and
+// one in 64-bit.
 __device__ __forceinline__ uint64_t neg_inv64(uint64_t m) {
-  uint64_t x = (3 * m) ^ 2;  // 5 correct bits
-#pragma unroll
-  for (int i = 0; i < 4; i++) x *= 2 - m * x;
-  return 0 - x;
+  const uint32_t m0 = (uint32_t)m;
+  uint32_t x = (3 * m0) ^ 2;
+  x *= 2 - m0 * x;
+  x *= 2 - m0 * x;
+  x *= 2 - m0 * x;
+  uint64_t y = x;
+  y *= 2 - m * y;
+  return 0 - y;
 }
 
 // Montgomery product a*b*2^-64 mod m, a, b < m < 2^34, m odd.
@@ -51,51 +57,82 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t m,
   return r >= m ? r - m : r;
 }
 
+// r mod m in [0, m) for a signed r with |r| < 2^62 and 1 <= m < 2^34, from
+// a float reciprocal rm ~ 1/m (relative error below 2^-22): every estimate
+// floor(r rm) leaves |r| at most 2^-21 of its size plus m, so three passes
+// and a short final correction (bounded) reach [0, m).
+__device__ __forceinline__ uint64_t mod_est(int64_t r, uint64_t m, float rm, int64_t* qacc = nullptr) {
+  int64_t q = 0;
+#pragma unroll
+  for (int it = 0; it < 3; it++) {
+    if (r >= 0 && (uint64_t)r < m) break;
+    const int64_t c = __float2ll_rd(__fmul_rn((float)r, rm));
+    r -= c * (int64_t)m;
+    q += c;
+  }
+  for (int it = 0; it < 8 && r < 0; it++) r += (int64_t)m, q--;
+  for (int it = 0; it < 8 && (uint64_t)r >= m; it++) r -= (int64_t)m, q++;
+  if (qacc) *qacc += q;
+  return (uint64_t)r;
+}
+
+// 2^64 mod m for odd 3 <= m < 2^34: q0 ~ 2^64 / m from the float
+// reciprocal, then 2^64 - q0 m = (0 - q0 m) mod 2^64 is within 2^43 of the
+// remainder and mod_est finishes.
+__device__ __forceinline__ uint64_t pow2_64_mod(uint64_t m, float rm) {
+  const uint64_t q0 = __float2ull_rz(__fmul_rn(rm, 18446744073709551616.0f));
+  return mod_est((int64_t)(0 - q0 * m), m, rm);
+}
+
 // 16^e mod d for 1 <= d < 2^34 (d == 1 -> 0, like bbp.rs:123-125).
 __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
   if (d == 1) return 0;
   int t = __ffsll((long long)d) - 1;  // d = 2^t * m, m odd
   uint64_t m = d >> t;
-  uint64_t rm = 0;  // 16^e mod m
+  uint64_t rm_ = 0;   // 16^e mod m
+  uint64_t minv = 0;  // -m^-1 mod 2^64 (m > 1)
   if (m > 1) {
-    uint64_t minv = neg_inv64(m);
-    uint64_t r1 = (0 - m) % m;  // 2^64 mod m: Montgomery one
-    uint64_t base = (r1 << 4) % m;  // 16 * 2^64 mod m (r1 < m < 2^34)
+    const float rm = __frcp_rn((float)m);
+    minv = neg_inv64(m);
+    const uint64_t r1 = pow2_64_mod(m, rm);           // Montgomery one
+    const uint64_t base = mod_est((int64_t)(r1 << 4), m, rm);  // 16 in Montgomery form
     uint64_t x = r1;
     if (e) {
       int top = 63 - __clzll((long long)e);
       x = base;
       for (int b = top - 1; b >= 0; b--) {
         x = mont_mul(x, x, m, minv);
-        if ((e >> b) & 1) x = mont_mul(x, base, m, minv);
+        // times 16: Montgomery form is linear, so a shift and a reduction
+        if ((e >> b) & 1) x = mod_est((int64_t)(x << 4), m, rm);
       }
     }
-    rm = mont_mul(x, 1, m, minv);  // out of Montgomery form
+    rm_ = mont_mul(x, 1, m, minv);  // out of Montgomery form
   }
-  // 16^e mod 2^t: 0 if 4e >= t, else 16^e (t <= 2 here; e = 0 gives 1)
+  // 16^e mod 2^t: 0 if 4e >= t, else 16^e (e = 0 gives 1)
   uint64_t r2 = (4 * e >= (uint64_t)t) ? 0 : (1ull << (4 * e));
-  if (t == 0) return rm;
-  // CRT: x = rm (mod m), x = r2 (mod 2^t), x < d
-  uint64_t mask = (1ull << t) - 1;
-  // m * s = r2 - rm (mod 2^t); m odd so m^-1 mod 2^t exists (t <= 2: m^-1 = m)
-  uint64_t s = ((r2 - rm) * m) & mask;
-  return rm + m * s;
+  if (t == 0) return rm_;
+  // CRT: x = rm (mod m), x = r2 (mod 2^t), x < d: x = rm + m s with
+  // s = (r2 - rm) m^-1 (mod 2^t), m^-1 from the Montgomery constant
+  const uint64_t mask = (1ull << t) - 1;
+  const uint64_t inv = m > 1 ? (0 - minv) : 1;
+  const uint64_t s2 = ((r2 - rm_) * inv) & mask;
+  return rm_ + m * s2;
 }
 
-// floor(p * 2^64 / d) for p < d < 2^34 (the quotient fits in 64 bits):
-// long division in three 32-bit-safe steps.
+// floor(p * 2^64 / d) for p < d < 2^34 (the quotient fits in 64 bits): long
+// division in steps of 30, 30 and 4 bits (r << 30 < 2^64), each quotient
+// digit from the float reciprocal and mod_est's correction.
 __device__ __forceinline__ uint64_t frac64(uint64_t p, uint64_t d) {
-  uint64_t q = 0, r = p;
-  // 64 = 30 + 30 + 4 bits; r < d < 2^34 so r << 30 < 2^64
-  uint64_t x = r << 30;
-  uint64_t q1 = x / d;
-  r = x - q1 * d;
-  x = r << 30;
-  uint64_t q2 = x / d;
-  r = x - q2 * d;
-  x = r << 4;
-  uint64_t q3 = x / d;
-  q = (q1 << 34) | (q2 << 4) | q3;
+  const float rd = __frcp_rn((float)d);
+  uint64_t r = p, q = 0;
+  const int steps[3] = {30, 30, 4};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const uint64_t x = r << steps[k];
+    int64_t qd = (int64_t)__float2ull_rz(__fmul_rn((float)x, rd));
+    r = mod_est((int64_t)(x - (uint64_t)qd * d), d, rd, &qd);
+    q = (q << steps[k]) | (uint64_t)qd;
+  }
   return q;
 }
 
@@ -162,6 +199,15 @@ __global__ void k_bbp_combine(const uint64_t* __restrict__ pos, uint32_t npos, c
   digits[i] = (uint32_t)(c >> 32);
 }
 
+// Building blocks for given (e, d, p): 16^e mod d and floor(p 2^64 / d).
+__global__ void k_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_t* p, uint32_t n, uint64_t* pw,
+                             uint64_t* fr) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  pw[i] = pow16_mod(e[i], d[i]);
+  fr[i] = frac64(p[i], d[i]);
+}
+
 }  // namespace pimul_bbp
 
 using namespace pimul_bbp;
@@ -173,6 +219,29 @@ using namespace pimul_bbp;
   } while (0)
 
 extern "C" const char* pimul_bbp_last_error(void) { return t_err.c_str(); }
+
+// 16^e[i] mod d[i] and floor(p[i] 2^64 / d[i]) on the device (d < 2^34,
+// p < d): the modular building blocks of the extractor, for checking.
+extern "C" int pimul_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_t* p, size_t n, uint64_t* pow16,
+                                uint64_t* frac) {
+  if (n == 0) return PIMUL_OK;
+  if (!e || !d || !p || !pow16 || !frac) return fail(PIMUL_EINVAL, "null pointer");
+  for (size_t i = 0; i < n; i++)
+    if (d[i] == 0 || d[i] >= (1ull << 34) || p[i] >= d[i]) return fail(PIMUL_EINVAL, "need 1 <= d < 2^34, p < d");
+  int rc = PIMUL_OK;
+  uint64_t* buf = nullptr;
+  BCU(cudaMalloc((void**)&buf, 5 * n * 8));
+  BCU(cudaMemcpy(buf, e, n * 8, cudaMemcpyHostToDevice));
+  BCU(cudaMemcpy(buf + n, d, n * 8, cudaMemcpyHostToDevice));
+  BCU(cudaMemcpy(buf + 2 * n, p, n * 8, cudaMemcpyHostToDevice));
+  k_bbp_modops<<<(unsigned)((n + 255) / 256), 256>>>(buf, buf + n, buf + 2 * n, (uint32_t)n, buf + 3 * n, buf + 4 * n);
+  BCU(cudaGetLastError());
+  BCU(cudaMemcpy(pow16, buf + 3 * n, n * 8, cudaMemcpyDeviceToHost));
+  BCU(cudaMemcpy(frac, buf + 4 * n, n * 8, cudaMemcpyDeviceToHost));
+done:
+  if (buf) cudaFree(buf);
+  return rc;
+}
 
 // Batched hex digits: digits[i] = 8 hex digits of pi at positions[i].
 extern "C" int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uint32_t* digits,

@@ -64,3 +64,22 @@ def test_stop_flag_from_another_thread():
 def test_rejects_positions_above_limit():
     with pytest.raises(pm.PimulError):
         pm.bbp_hex_digits([1 << 32])
+
+
+def test_modular_building_blocks_at_large_moduli():
+    # 16^e mod d and floor(p 2^64 / d) against Python's integers, over the
+    # whole modulus range the extractor uses (d = 8k + j < 2^34, even and odd)
+    rng = np.random.default_rng(21)
+    d = np.concatenate([rng.integers(1, 1 << 34, 4000, dtype=np.uint64),
+                        np.array([1, 2, 3, 4, 6, 7, 9, 12, (1 << 34) - 1, (1 << 34) - 2, (1 << 33) + 1, 2**32 - 5],
+                                 dtype=np.uint64),
+                        8 * rng.integers(0, 1 << 31, 2000, dtype=np.uint64) + np.uint64(4)])
+    e = rng.integers(0, 1 << 31, d.size, dtype=np.uint64)
+    e[:20] = np.arange(20)
+    p = np.array([int(rng.integers(0, int(x))) if x > 1 else 0 for x in d], dtype=np.uint64)
+    p[-5:] = d[-5:] - np.uint64(1)
+    pw, fr = pm.bbp_modops(e, d, p)
+    for i in range(d.size):
+        dd, ee, pp = int(d[i]), int(e[i]), int(p[i])
+        assert int(pw[i]) == pow(16, ee, dd), (ee, dd)
+        assert int(fr[i]) == (pp << 64) // dd, (pp, dd)
