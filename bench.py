@@ -599,7 +599,8 @@ def run_pi(args):
     gl_backend = pm.served_backend() if args.gl_backend == "served" else None
 
     def gl_run(d, **kw):
-        return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend), fast_sqrt=args.gl_sqrt == "newton")
+        return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend), fast_sqrt=args.gl_sqrt == "newton",
+                                    device_decimal=args.gl_decimal == "device")
 
     if args.algorithm == "both":
         gl_run(min(D, 100_000))
@@ -672,6 +673,9 @@ def run_pi(args):
                                                            "multiply": args.gl_backend,
                                                            "sqrt": ("multiplication-only Newton" if args.gl_sqrt == "newton"
                                                                     else "reference (division-based)"),
+                                                           "decimal": ("device-resident level-batched"
+                                                                       if args.gl_decimal == "device"
+                                                                       else "reference recursion"),
                                                            "digits_identical_to_chudnovsky": other_same},
         "sha256": hashlib.sha256(s.encode()).hexdigest(),
         "last_digits": s[-20:], "cpu_baseline": cpu,
@@ -804,6 +808,9 @@ def main():
     ap.add_argument("--gl-sqrt", choices=["reference", "newton"], default="reference",
                     help="Gauss-Legendre square roots: the reference's division-based iteration or the "
                          "multiplication-only one (same digits)")
+    ap.add_argument("--gl-decimal", choices=["reference", "device"], default="reference",
+                    help="Gauss-Legendre decimal conversion: the reference's recursion (products one call "
+                         "each) or level-batched with the nodes on the GPU (same digits)")
     ap.add_argument("--positions", type=int, default=256)
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)

@@ -117,6 +117,8 @@ int pimul_mul_batch(const pimul_job* jobs, size_t n, void* stream);
  * (sub == 0) or x - y (sub != 0, x >= y), operands zero-extended to nout
  * (nout >= max(nx, ny); for an addition max(nx, ny) + 1 holds every carry).
  * Synchronous; PIMUL_EINVAL if a carry or borrow leaves the top limb.
+ * sub == PIMUL_SUB_MOD: x - y modulo 2^(64 nout), no borrow check (the low
+ * limbs of a difference known to fit in nout limbs).  out may equal x.
  * Replaces: crates/bignum/src/integer.rs:351-421 (add_mag / sub_mag under
  * Integer addition) for the T sums of a binary-splitting level.
  */
@@ -129,6 +131,7 @@ typedef struct pimul_addsub_job {
   size_t nout;
   int sub;
 } pimul_addsub_job;
+#define PIMUL_SUB_MOD 2
 int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream);
 
 /* Trimmed lengths (highest nonzero limb + 1) of n device limb arrays of
@@ -231,7 +234,7 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
  * P_L P_R for every neighbouring pair) in one pimul_mul_batch call, the T
  * sums in one pimul_addsub_batch call and the trimmed lengths from
  * pimul_top_limbs; only the root's Q and T return to the host.  The decimal
- * conversion is level-batched (pimul_to_decimal); its divisors and
+ * conversion is level-batched with its nodes in HBM (pimul_to_decimal); its divisors and
  * reciprocals, sqrt(10005) (by a multiplication-only Newton iteration) and
  * the decimal scale are computed beside the splitting.  Optional outputs:
  * phase_ms[3] as above; gpu_products = products sent to the GPU (batched and
@@ -271,9 +274,12 @@ int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn
 
 /* pimul_pi_gauss_legendre with options: PIMUL_PI_FAST_SQRT takes the square
  * roots by a multiplication-only Newton iteration for 1/sqrt(x) instead of
- * the reference's division-based one (float.rs:85-174); the digits are the
- * same. */
+ * the reference's division-based one (float.rs:85-174);
+ * PIMUL_PI_DEVICE_DECIMAL converts to decimal with the nodes on the device
+ * (the level-batched conversion of pimul_to_decimal) instead of the
+ * reference's recursion (util.rs:25-83).  The digits are the same. */
 #define PIMUL_PI_FAST_SQRT 1u
+#define PIMUL_PI_DEVICE_DECIMAL 2u
 int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
                                uint32_t flags, double* phase_ms, uint64_t* ntt_products);
 

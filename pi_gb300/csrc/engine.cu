@@ -25,6 +25,7 @@
 #include "gl.cuh"
 #include "ntt_kernels.cuh"
 #include "../../include/pimul.h"
+#include "hostcopy.h"
 
 namespace pimul {
 
@@ -811,6 +812,198 @@ static int get_stream(cudaStream_t* s) {
   CU(cudaSetDevice(g_dev.device));
   *s = t_stream;
   return PIMUL_OK;
+}
+
+// ------------------------------------------------------------- host copies
+// cudaMemcpy from or to PAGEABLE host memory (the limb arrays of a host
+// driver) runs through the driver's bounce buffer at a few GB/s.  From 1 MiB
+// up such copies are staged instead: host threads copy 32 MiB chunks into
+// one of two pinned buffers while the copy engine drains (or fills) the
+// other.  Pinned or registered host memory is copied directly.
+constexpr size_t STAGE_MIN = (size_t)1 << 20;
+constexpr size_t STAGE_CHUNK = (size_t)32 << 20;
+
+// memcpy on all host cores: a fixed set of workers, one copy at a time.
+class CopyPool {
+ public:
+  void copy(void* dst, const void* src, size_t bytes) {
+    std::call_once(once_, [this] { start(); });
+    if (bytes < ((size_t)4 << 20) || workers_ == 0) {
+      memcpy(dst, src, bytes);
+      return;
+    }
+    std::lock_guard<std::mutex> run(run_mu_);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      dst_ = static_cast<char*>(dst);
+      src_ = static_cast<const char*>(src);
+      bytes_ = bytes;
+      pending_ = workers_;
+      gen_++;
+    }
+    cv_.notify_all();
+    part(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [this] { return pending_ == 0; });
+  }
+
+ private:
+  void start() {
+    unsigned hw = std::thread::hardware_concurrency();
+    workers_ = (int)std::min(hw ? hw : 1u, 16u) - 1;
+    for (int i = 0; i < workers_; i++) std::thread([this, i] { run(i + 1); }).detach();
+  }
+  void part(int id) {
+    const size_t n = (size_t)workers_ + 1;
+    const size_t per = ((bytes_ + n - 1) / n + 63) & ~(size_t)63;
+    const size_t lo = std::min(bytes_, per * id), hi = std::min(bytes_, lo + per);
+    if (hi > lo) memcpy(dst_ + lo, src_ + lo, hi - lo);
+  }
+  void run(int id) {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+      }
+      part(id);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  std::once_flag once_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_;
+  int workers_ = 0, pending_ = 0;
+  uint64_t gen_ = 0;
+  char* dst_ = nullptr;
+  const char* src_ = nullptr;
+  size_t bytes_ = 0;
+};
+static CopyPool& copy_pool() {
+  static CopyPool* p = new CopyPool;  // workers are detached: never destroyed
+  return *p;
+}
+
+struct StageBuf {
+  void* h[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};  // last copy-engine use of h[j]
+  int device = -1;
+};
+static std::mutex g_stage_mu;
+static std::vector<StageBuf*> g_stage_free, g_stage_all;
+
+static StageBuf* stage_acquire() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  {
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    for (size_t i = 0; i < g_stage_free.size(); i++)
+      if (g_stage_free[i]->device == dev) {
+        StageBuf* b = g_stage_free[i];
+        g_stage_free.erase(g_stage_free.begin() + i);
+        return b;
+      }
+  }
+  StageBuf* b = new StageBuf;
+  b->device = dev;
+  for (int j = 0; j < 2; j++) {
+    if (cudaHostAlloc(&b->h[j], STAGE_CHUNK, cudaHostAllocPortable) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev[j], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      for (int k = 0; k < 2; k++) {
+        if (b->h[k]) cudaFreeHost(b->h[k]);
+        if (b->ev[k]) cudaEventDestroy(b->ev[k]);
+      }
+      delete b;
+      return nullptr;
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_stage_mu);
+  g_stage_all.push_back(b);
+  return b;
+}
+static void stage_release(StageBuf* b) {
+  std::lock_guard<std::mutex> lk(g_stage_mu);
+  g_stage_free.push_back(b);
+}
+
+static bool is_pageable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return a.type == cudaMemoryTypeUnregistered;
+}
+
+int host_to_device(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (!bytes) return PIMUL_OK;
+  StageBuf* b = bytes >= STAGE_MIN && is_pageable(src) ? stage_acquire() : nullptr;
+  if (!b) {
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return PIMUL_OK;
+  }
+  cudaError_t e = cudaSuccess;
+  int j = 0;
+  for (size_t off = 0; off < bytes && e == cudaSuccess; off += STAGE_CHUNK, j ^= 1) {
+    const size_t n = std::min(STAGE_CHUNK, bytes - off);
+    e = cudaEventSynchronize(b->ev[j]);  // the copy engine is done with h[j]
+    if (e != cudaSuccess) break;
+    copy_pool().copy(b->h[j], static_cast<const char*>(src) + off, n);
+    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, b->h[j], n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[j], st);
+  }
+  stage_release(b);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("staged upload: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+int device_to_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (!bytes) return PIMUL_OK;
+  StageBuf* b = bytes >= STAGE_MIN && is_pageable(dst) ? stage_acquire() : nullptr;
+  if (!b) {
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return PIMUL_OK;
+  }
+  const size_t nch = (bytes + STAGE_CHUNK - 1) / STAGE_CHUNK;
+  auto issue = [&](size_t i) {
+    const size_t off = i * STAGE_CHUNK, n = std::min(STAGE_CHUNK, bytes - off);
+    const int j = (int)(i & 1);
+    cudaError_t e = cudaEventSynchronize(b->ev[j]);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->h[j], static_cast<const char*>(src) + off, n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[j], st);
+    return e;
+  };
+  cudaError_t e = issue(0);
+  for (size_t i = 0; i < nch && e == cudaSuccess; i++) {
+    // chunk i + 1 lands in the other buffer while chunk i is copied out
+    if (i + 1 < nch) e = issue(i + 1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev[i & 1]);
+    if (e != cudaSuccess) break;
+    const size_t off = i * STAGE_CHUNK, n = std::min(STAGE_CHUNK, bytes - off);
+    copy_pool().copy(static_cast<char*>(dst) + off, b->h[i & 1], n);
+  }
+  stage_release(b);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("staged download: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+void release_host_staging() {
+  std::lock_guard<std::mutex> lk(g_stage_mu);
+  for (StageBuf* b : g_stage_all) {
+    for (int j = 0; j < 2; j++) {
+      cudaEventSynchronize(b->ev[j]);
+      cudaEventDestroy(b->ev[j]);
+      cudaFreeHost(b->h[j]);
+    }
+    delete b;
+  }
+  g_stage_all.clear();
+  g_stage_free.clear();
 }
 
 // Split L bits into HBM passes of at most 9 bits (each radix 2^6 .. 2^9).
@@ -1607,6 +1800,7 @@ int pimul_shutdown(void) {
   if (!g_dev.ready) return PIMUL_OK;
   cudaSetDevice(g_dev.device);
   cudaDeviceSynchronize();
+  release_host_staging();
   cudaFree(g_dev.d_roots);
   if (g_dev.pool) cudaMemPoolTrimTo(g_dev.pool, 0);
   g_dev = DeviceState{};
@@ -1732,7 +1926,7 @@ int pimul_upload(const uint64_t* host, size_t n, uint64_t* handle) {
   if (rc) return rc;
   uint64_t* d = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&d, bytes, g_dev.pool, st);
-  if (e == cudaSuccess && n) e = cudaMemcpyAsync(d, host, n * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n && host_to_device(d, host, n * 8, st)) e = cudaErrorUnknown;
   cudaEvent_t ev = nullptr;
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventRecord(ev, st);
@@ -1847,8 +2041,8 @@ int pimul_download(uint64_t handle, uint64_t* host, size_t cap, size_t* len) {
   int rc = get_stream(&st);
   if (rc) return rc;
   if (ready) CU(cudaStreamWaitEvent(st, ready, 0));
-  if (n) CU(cudaMemcpyAsync(host, d, n * 8, cudaMemcpyDeviceToHost, st));
-  CU(cudaStreamSynchronize(st));
+  rc = device_to_host(host, d, n * 8, st);
+  if (rc) return rc;
   size_t m = n;
   while (m && host[m - 1] == 0) m--;
   *len = m;
@@ -1922,6 +2116,7 @@ struct AsJob {
   uint64_t nx, ny, nout;
   uint8_t* aux;  // per-warp masks, per-chunk (g, p) and carry-in bytes
   uint32_t sub;
+  uint32_t check;  // report a carry or borrow out of the top limb
 };
 
 __host__ __device__ __forceinline__ uint64_t as_nwin(uint64_t nout) { return (nout + AS_W - 1) / AS_W; }
@@ -2046,7 +2241,7 @@ __global__ void __launch_bounds__(AS_THREADS) k_as_apply(const AsJob* jobs, int*
   }
   const uint32_t A = masks[2 * (wbase + warp)], Bm = masks[2 * (wbase + warp) + 1];
   const uint32_t carries = (A + Bm + cin) ^ A ^ Bm;
-  if (w + 1 == nwin) {
+  if (J.check && w + 1 == nwin) {
     const uint32_t g = (Bm >> lane) & 1, pg = (A >> lane) & 1, c = (carries >> lane) & 1;
     if (g || (pg && c)) atomicExch(overflow, 1);
   }
@@ -2101,7 +2296,7 @@ static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st
   uint64_t off = desc;
   for (size_t i = 0; i < n; i++) {
     h[i] = AsJob{jobs[i].x, jobs[i].y, jobs[i].out, jobs[i].nx, jobs[i].ny, jobs[i].nout, dev + off,
-                 (uint32_t)(jobs[i].sub != 0)};
+                 (uint32_t)(jobs[i].sub != 0), (uint32_t)(jobs[i].sub != PIMUL_SUB_MOD)};
     off += as_aux_bytes(jobs[i].nout);
   }
   e = cudaMemcpyAsync(dev, h.data(), n * sizeof(AsJob), cudaMemcpyHostToDevice, st);
@@ -2249,7 +2444,7 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
   }
   // a is uploaded first; b follows on a helper stream while a's forward
   // transform runs, and b's first pass waits for it
-  cudaMemcpyAsync(da, a, la * 8, cudaMemcpyHostToDevice, st);
+  rc = host_to_device(da, a, la * 8, st);
   thread_local cudaStream_t t_copy = nullptr;
   thread_local cudaEvent_t t_ev[2] = {nullptr, nullptr};
   thread_local int t_copy_dev = -1;
@@ -2263,13 +2458,13 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
     }
     CU(cudaEventRecord(t_ev[0], st));  // after db's allocation and a's upload
     CU(cudaStreamWaitEvent(t_copy, t_ev[0], 0));
-    cudaMemcpyAsync(db, b, lb * 8, cudaMemcpyHostToDevice, t_copy);
+    if (!rc) rc = host_to_device(db, b, lb * 8, t_copy);
     CU(cudaEventRecord(t_ev[1], t_copy));
     b_ready = t_ev[1];
   }
-  rc = mul_device(da, la, square ? da : db, lb, dout, st, b_ready);
+  if (!rc) rc = mul_device(da, la, square ? da : db, lb, dout, st, b_ready);
   if (rc && b_ready) cudaStreamWaitEvent(st, b_ready, 0);  // db is freed below
-  if (rc == PIMUL_OK) cudaMemcpyAsync(out, dout, (la + lb) * 8, cudaMemcpyDeviceToHost, st);
+  if (rc == PIMUL_OK) rc = device_to_host(out, dout, (la + lb) * 8, st);
   cudaFreeAsync(da, st);
   if (db) cudaFreeAsync(db, st);
   cudaFreeAsync(dout, st);

@@ -1,0 +1,22 @@
+// Internal: copies between the device and host memory that may be pageable
+// (defined in engine.cu, used by the engine's host entry points and by
+// dec.cu).  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace pimul {
+
+// dst (device) <- src (host), ordered on st.  On return src may be reused;
+// the last chunk may still be in flight on st.
+int host_to_device(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
+// dst (host) <- src (device), ordered after the work already on st.
+// Synchronous: dst holds the data on return.
+int device_to_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
+// Frees the pinned staging buffers (device idle).
+void release_host_staging();
+
+}  // namespace pimul

@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pimul.h"
+#include "dec.h"
 
 namespace pihost {
 
@@ -1750,12 +1751,11 @@ static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int
 // Level-synchronous divide and conquer on C = 10^19: with P_k = C^(2^k),
 // every node of level k (a value below P_k^2) splits into (q, r) = divmod by
 // P_k, high half first.  All nodes of a level share P_k and one reciprocal
-// V_k ~ 2^s / P_k (s = 2 bits(P_k) + 64), so floor(N V_k / 2^s) is within
-// one of the quotient; both products of the level (N V_k, then q P_k) go
-// through batch_mul.  Nodes below P_kmin are printed on host threads
-// (19 * 2^kmin digits each, zero-padded).  An integer has one decimal
-// string, so the output equals the reference's conversion
-// (crates/bignum/src/integer.rs:892-983).
+// V_k <= 2^s / P_k (s = 2 bits(P_k) + 64), so floor(N V_k / 2^s) is the
+// quotient or one less.  The levels run on the device with the nodes in HBM
+// (dec.cu): the value goes up once and only the digits come back.  An
+// integer has one decimal string, so the output equals the reference's
+// conversion (crates/bignum/src/integer.rs:892-983).
 // The divisors and reciprocals of the levels depend only on the number of
 // chunks, so a caller that knows the digit count can build them early.
 struct DecPlan {
@@ -1766,8 +1766,11 @@ struct DecPlan {
 };
 
 // Plan for integers of at most ndig decimal digits.  V_k: Newton once at the
-// top, then V_(k-1) = (P_(k-1) V_k) >> (s_k - s_(k-1)) since P_k = P_(k-1)^2
-// (off by at most a few units; the quotient correction absorbs it).
+// top, corrected to exactly floor(2^s / P), then V_(k-1) = (P_(k-1) V_k) >>
+// (s_k - s_(k-1)), which stays at or below floor(2^(s_(k-1)) / P_(k-1))
+// since P_k = P_(k-1)^2 and is within two units of it.  So every quotient
+// estimate floor(x V_k / 2^(s_k)) is at most x div P_k and, for x < P_k^2,
+// short of it by less than 2^-63 before the floor.
 static DecPlan make_dec_plan(uint64_t ndig) {
   DecPlan D;
   const uint64_t nch = (ndig + 18) / 19;
@@ -1786,6 +1789,19 @@ static DecPlan make_dec_plan(uint64_t ndig) {
       Flt r = reciprocal_at_prec(flt_from_int(D.P[k]), b + 128);
       r.exp += (int64_t)D.sh[k];
       D.V[k] = to_integer_down(r);
+      // P V <= 2^s < P (V + 1)
+      const Limbs two_s = shl_mag(Limbs(1, 1), D.sh[k]);
+      Limbs pv = mul_mag(D.P[k].m, D.V[k].m);
+      while (cmp_mag(pv, two_s) > 0) {
+        D.V[k] = sub(D.V[k], Int(1));
+        pv = sub_mag(pv, D.P[k].m);
+      }
+      for (;;) {
+        Limbs up = add_mag(pv, D.P[k].m);
+        if (cmp_mag(up, two_s) > 0) break;
+        D.V[k] = add(D.V[k], Int(1));
+        pv = std::move(up);
+      }
     } else {
       D.V[k] = Int(shr_mag(mul_mag(D.P[k].m, D.V[k + 1].m), D.sh[k + 1] - D.sh[k]), false);
     }
@@ -1793,88 +1809,9 @@ static DecPlan make_dec_plan(uint64_t ndig) {
   return D;
 }
 
-// The levels of the batched conversion: X split down to nodes below
-// P_kmin, most significant first, each worth 19 * 2^kmin digits.
-static int dec_levels(const Int& X, LevelStaging& S, const DecPlan* plan, std::vector<Int>& out_nodes, int& kmin_out) {
-  DecPlan own;
-  const uint64_t ndig = dec_estimate(bits_of(X.m)) + 1;
-  if (!plan || (1ull << plan->K) * 19 < ndig) {
-    own = make_dec_plan(ndig);
-    plan = &own;
-  }
-  const int K = plan->K, kmin = plan->kmin;
-  const std::vector<Int>& P = plan->P;
-  std::vector<Int> nodes{X};
-  for (int k = K - 1; k >= kmin; k--) {
-    const Int& V = plan->V[k];
-    const uint64_t sh = plan->sh[k];
-    const size_t n = nodes.size();
-    std::vector<const Limbs*> A(n), B(n, &V.m);
-    for (size_t i = 0; i < n; i++) A[i] = &nodes[i].m;
-    std::vector<Limbs> nv;
-    int rc = batch_mul(A, B, nv, S, 32);
-    if (rc) return rc;
-    std::vector<Int> q(n);
-    parallel_for(n, [&](size_t lo, size_t hi) {
-      for (size_t i = lo; i < hi; i++) q[i] = Int(shr_mag(nv[i], sh), false);
-    });
-    nv.clear();
-    std::vector<const Limbs*> Aq(n), Bp(n, &P[k].m);
-    for (size_t i = 0; i < n; i++) Aq[i] = &q[i].m;
-    std::vector<Limbs> qp;
-    rc = batch_mul(Aq, Bp, qp, S, 32);
-    if (rc) return rc;
-    std::vector<Int> next(2 * n);
-    parallel_for(n, [&](size_t lo, size_t hi) {
-      for (size_t i = lo; i < hi; i++) {
-        Int qi = std::move(q[i]);
-        Int ri = sub(nodes[i], Int(std::move(qp[i]), false));
-        while (ri.neg) {
-          qi = sub(qi, Int(1));
-          ri = add(ri, P[k]);
-        }
-        while (cmp_mag(ri.m, P[k].m) >= 0) {
-          qi = add(qi, Int(1));
-          ri = sub(ri, P[k]);
-        }
-        next[2 * i] = std::move(qi);
-        next[2 * i + 1] = std::move(ri);
-      }
-    });
-    nodes.swap(next);
-  }
-  report_split("decimal levels");
-  out_nodes.swap(nodes);
-  kmin_out = kmin;
-  return g_error.load();
-}
-
-static int to_decimal_batched(const Int& X, std::string& outs, LevelStaging& S, const DecPlan* plan = nullptr) {
-  if (X.m.size() <= 256) {
-    outs = to_decimal_top(X);
-    return g_error.load();
-  }
-  std::vector<Int> nodes;
-  int kmin = 0;
-  int rc = dec_levels(X, S, plan, nodes, kmin);
-  if (rc) return rc;
-  const size_t per = (size_t)19 << kmin;
-  std::string all(per * nodes.size(), '0');
-  parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
-    for (size_t i = lo; i < hi; i++) {
-      if (nodes[i].zero()) continue;
-      std::string d = decimal_naive(nodes[i].m);
-      memcpy(&all[i * per + per - d.size()], d.data(), d.size());
-    }
-  });
-  size_t nz = all.find_first_not_of('0');
-  outs = nz == std::string::npos ? std::string("0") : all.substr(nz);
-  return g_error.load();
-}
-
 // Exactly `want` decimal digits of X < 10^want (zero-padded on the left),
 // written straight into out.
-static int to_decimal_batched_into(const Int& X, char* out, size_t want, LevelStaging& S, const DecPlan* plan) {
+static int to_decimal_batched_into(const Int& X, char* out, size_t want, const DecPlan* plan) {
   if (X.m.size() <= 256) {
     std::string s = to_decimal_top(X);
     if (s.size() > want) return PIMUL_EINVAL;
@@ -1882,49 +1819,55 @@ static int to_decimal_batched_into(const Int& X, char* out, size_t want, LevelSt
     memcpy(out + want - s.size(), s.data(), s.size());
     return g_error.load();
   }
-  std::vector<Int> nodes;
-  int kmin = 0;
-  int rc = dec_levels(X, S, plan, nodes, kmin);
-  if (rc) return rc;
-  const size_t per = (size_t)19 << kmin, total = per * nodes.size();
-  if (total < want) {
+  DecPlan own;
+  const uint64_t ndig = std::max<uint64_t>(dec_estimate(bits_of(X.m)) + 1, want);
+  if (!plan || (1ull << plan->K) * 19 < ndig) {
+    own = make_dec_plan(ndig);
+    plan = &own;
+  }
+  if (g_error.load()) return g_error.load();
+  if (plan->kmin != pidec::LEAF_K) return PIMUL_EINVAL;
+  const size_t total = (size_t)19 << plan->K;
+  if (want > total) {
     memset(out, '0', want - total);
     out += want - total;
     want = total;
   }
-  const size_t skip = total - want;  // leading characters that must be zeros
-  std::atomic<int> bad{0};
-  parallel_for(nodes.size(), [&](size_t lo, size_t hi) {
-    std::string buf(per, '0');
-    for (size_t i = lo; i < hi; i++) {
-      const size_t b0 = i * per;
-      if (b0 + per <= skip) {
-        if (!nodes[i].zero()) bad.store(1);
-        continue;
-      }
-      std::fill(buf.begin(), buf.end(), '0');
-      if (!nodes[i].zero()) {
-        std::string d = decimal_naive(nodes[i].m);
-        memcpy(&buf[per - d.size()], d.data(), d.size());
-      }
-      const size_t from = b0 < skip ? skip - b0 : 0;
-      for (size_t c = 0; c < from; c++)
-        if (buf[c] != '0') bad.store(1);
-      memcpy(out + b0 + from - skip, buf.data() + from, per - from);
-    }
-  });
-  if (bad.load()) return PIMUL_EINVAL;
-  return g_error.load();
+  std::vector<pidec::Level> lv(plan->K);
+  for (int k = plan->kmin; k < plan->K; k++)
+    lv[k] = pidec::Level{plan->P[k].m.data(), plan->P[k].m.size(), plan->V[k].m.data(), plan->V[k].m.size(),
+                         plan->sh[k]};
+  double ms[3] = {0, 0, 0};
+  int rc = pidec::to_decimal_device(X.m.data(), X.m.size(), plan->K, lv.data(), out, want, ms);
+  if (getenv("PIMUL_PI_TIMING"))
+    fprintf(stderr, "[pimul] decimal conversion on the device: upload %.1f ms, levels %.1f, leaves + download %.1f\n",
+            ms[0], ms[1], ms[2]);
+  return rc;
+}
+
+static int to_decimal_batched(const Int& X, std::string& outs) {
+  std::string all(dec_estimate(bits_of(X.m)) + 1, '0');
+  int rc = to_decimal_batched_into(X, &all[0], all.size(), nullptr);
+  if (rc) return rc;
+  size_t nz = all.find_first_not_of('0');
+  outs = nz == std::string::npos ? std::string("0") : all.substr(nz);
+  return PIMUL_OK;
 }
 
 }  // namespace pihost
 
 using namespace pihost;
 
-static int finish_digits(Flt pi, const Flt& scale, uint64_t digits, char* out, double* t_phase) {
+static int finish_digits(Flt pi, const Flt& scale, uint64_t digits, char* out, double* t_phase,
+                         const DecPlan* device_plan = nullptr) {
   double t0 = now_ms();
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
+  if (device_plan) {
+    int rc = to_decimal_batched_into(ip, out, digits, device_plan);
+    if (t_phase) *t_phase = now_ms() - t0;
+    return rc ? rc : g_error.load();
+  }
   std::string s = to_decimal_top(ip);
   if (t_phase) *t_phase = now_ms() - t0;
   if (g_error.load()) return g_error.load();
@@ -1950,11 +1893,18 @@ extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap
   // iterations (it depends on nothing else)
   Flt scale;
   std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
+  // the device conversion's divisors and reciprocals too
+  const bool device_dec = (flags & PIMUL_PI_DEVICE_DECIMAL) != 0;
+  DecPlan dplan;
+  std::thread plan_th([&] {
+    if (device_dec) dplan = make_dec_plan(digits + 1);
+  });
   Flt pi = gauss_legendre(prec, (flags & PIMUL_PI_FAST_SQRT) != 0);
   double t1 = now_ms();
   scale_th.join();
+  plan_th.join();
   double tdc = 0;
-  int rc = finish_digits(pi, scale, digits, out, &tdc);
+  int rc = finish_digits(pi, scale, digits, out, &tdc, device_dec ? &dplan : nullptr);
   if (phase_ms) {
     phase_ms[0] = t1 - t0;
     phase_ms[1] = 0;
@@ -2045,9 +1995,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   plan_th.join();
   bool written = false;
   if (leaf_terms) {
-    LevelStaging S;
-    int crc = S.init();
-    if (!crc) crc = to_decimal_batched_into(ip, out, digits, S, &dplan);
+    int crc = to_decimal_batched_into(ip, out, digits, &dplan);
     if (crc) return crc;
     written = true;
   } else {
@@ -2091,9 +2039,7 @@ extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size
   if (x.zero()) {
     s = "0";
   } else if (batched) {
-    LevelStaging S;
-    int rc = S.init();
-    if (!rc) rc = to_decimal_batched(x, s, S);
+    int rc = to_decimal_batched(x, s);
     if (rc) return rc;
   } else {
     s = to_decimal_top(x);

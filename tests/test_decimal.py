@@ -1,6 +1,7 @@
 """Decimal conversion of big integers (crates/bignum/src/integer.rs:892-983):
 the reference's recursive divide and conquer on the host (CPU-only sizes
-here) and the level-batched form on the GPU, both against Python's str()."""
+here) and the level-batched form with its nodes on the GPU, both against
+Python's str()."""
 import sys
 
 import numpy as np
@@ -42,6 +43,24 @@ def test_batched_conversion_matches_python():
         cases.append(O.limbs_to_int(rng.integers(0, 2**64, nlimbs, dtype=np.uint64)))
     # long runs of zero and nine chunks stress the quotient corrections
     cases += [10**6000 * 7 + 3, (10**5000 - 1) * 10**3000, 2**40000 - 1]
+    # the level divisors 10^(19 2^k) themselves and their neighbours
+    for k in (6, 8, 10):
+        p = 10 ** (19 * 2**k)
+        cases += [p - 1, p, p + 1, p * p - 1, 3 * p + p // 7]
+    for v in cases:
+        assert pm.to_decimal(O.int_to_limbs(v), batched=True) == str(v)
+
+
+@pytest.mark.gpu
+def test_batched_conversion_corrects_low_quotients(monkeypatch):
+    # test hook: every quotient estimate lowered by one on the device, so
+    # that every remainder goes through the r >= P correction
+    monkeypatch.setenv("PIMUL_DEC_TEST_LOWER_Q", "1")
+    rng = np.random.default_rng(7)
+    p = 10 ** (19 * 2**8)
+    cases = [10**6000 * 7 + 3, (10**5000 - 1) * 10**3000, 2**40000 - 1, p - 1, p, p * p - 1]
+    for nlimbs in (257, 2049, 20000):
+        cases.append(O.limbs_to_int(rng.integers(0, 2**64, nlimbs, dtype=np.uint64)))
     for v in cases:
         assert pm.to_decimal(O.int_to_limbs(v), batched=True) == str(v)
 

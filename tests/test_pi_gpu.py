@@ -86,6 +86,13 @@ def test_gauss_legendre_fast_sqrt_1e6_matches_mpmath():
     assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
 
 
+def test_gauss_legendre_device_decimal_1e6_matches_mpmath():
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, _ = pm.pi_gauss_legendre(1_000_000, backend=pm.served_backend(), fast_sqrt=True, device_decimal=True)
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+
+
 @pytest.mark.parametrize("digits,leaf", [(1, 0), (17, 0), (500, 3), (1000, 0), (5000, 1), (20000, 5)])
 def test_batched_small_and_odd_shapes(digits, leaf):
     # one leaf, a single-term leaf size, odd leaf counts at every level
