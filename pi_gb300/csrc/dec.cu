@@ -71,21 +71,32 @@ __device__ __forceinline__ uint64_t div_chunk(uint64_t u1, uint64_t u0, uint64_t
   return q1;
 }
 
-// dst slot j = bits [sh + 64 j, sh + 64 j + 64) of src slot (zero past src_len).
-__global__ void k_shr_slots(const uint64_t* __restrict__ src, uint64_t src_stride, uint64_t src_len, uint64_t sh,
+// dst slot j = bits [sh + 64 j, sh + 64 j + 64) of src slot, bits outside
+// [0, 64 src_len) reading as zero (sh < 0 shifts left).
+__global__ void k_shr_slots(const uint64_t* __restrict__ src, uint64_t src_stride, uint64_t src_len, int64_t sh,
                             uint64_t* __restrict__ dst, uint64_t dst_stride, uint64_t dst_len, uint64_t n) {
-  const uint64_t ws = sh >> 6;
+  const int64_t ws = sh >> 6;  // floor
   const unsigned bs = (unsigned)(sh & 63);
   for (uint64_t node = blockIdx.y; node < n; node += gridDim.y) {
     const uint64_t* s = src + node * src_stride;
     uint64_t* d = dst + node * dst_stride;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < dst_len;
          j += (uint64_t)gridDim.x * blockDim.x) {
-      const uint64_t i = ws + j;
-      const uint64_t lo = i < src_len ? s[i] : 0;
-      const uint64_t hi = i + 1 < src_len ? s[i + 1] : 0;
+      const int64_t i = ws + (int64_t)j;
+      const uint64_t lo = i >= 0 && (uint64_t)i < src_len ? s[i] : 0;
+      const uint64_t hi = i + 1 >= 0 && (uint64_t)(i + 1) < src_len ? s[i + 1] : 0;
       d[j] = bs ? (lo >> bs) | (hi << (64 - bs)) : lo;
     }
+  }
+}
+
+// lo[i] = low word of x[i] a, hi[i + 1] = high word (lo[n] = hi[0] = 0):
+// x a = lo + hi with one addition.
+__global__ void k_mul_small_split(const uint64_t* __restrict__ x, uint64_t n, uint64_t a, uint64_t* __restrict__ lo,
+                                  uint64_t* __restrict__ hi) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x) {
+    lo[i] = i < n ? x[i] * a : 0;
+    hi[i] = i > 0 ? __umul64hi(x[i - 1], a) : 0;
   }
 }
 
@@ -234,7 +245,8 @@ struct Arena {
 
 }  // namespace
 
-int to_decimal_device(const uint64_t* x, size_t nx, int K, const Level* lv, char* out, size_t want, double* ms) {
+int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, const Level* lv, char* out, size_t want,
+                      double* ms) {
   if (!x || !nx || !lv || !out || K <= LEAF_K || K > 40) return PIMUL_EINVAL;
   if (lv[LEAF_K].lp + 1 != (size_t)LEAF_W) return PIMUL_EINVAL;
   const size_t total = (size_t)19 << K;
@@ -265,7 +277,8 @@ int to_decimal_device(const uint64_t* x, size_t nx, int K, const Level* lv, char
     rc = pimul::host_to_device(dpv + poff[k], lv[k].P, lv[k].lp * 8, st);
     if (!rc) rc = pimul::host_to_device(dpv + voff[k], lv[k].V, lv[k].lv * 8, st);
   }
-  if (!rc) rc = pimul::host_to_device(cur, x, nx * 8, st);
+  if (!rc && x_on_device) cu(cudaMemcpyAsync(cur, x, nx * 8, cudaMemcpyDeviceToDevice, st));
+  if (!rc && !x_on_device) rc = pimul::host_to_device(cur, x, nx * 8, st);
   const uint64_t one_h = 1;
   cu(cudaMemcpyAsync(one, &one_h, 8, cudaMemcpyHostToDevice, st));
   cu(cudaStreamSynchronize(st));  // one_h is on this stack frame
@@ -289,7 +302,8 @@ int to_decimal_device(const uint64_t* x, size_t nx, int K, const Level* lv, char
     jobs.resize(n);
     for (size_t i = 0; i < n; i++) jobs[i] = pimul_job{cur + i * w_in + t, hi_w, dV, L.lv, prod + i * prod_w};
     if ((rc = pimul_mul_batch(jobs.data(), n, st))) break;
-    k_shr_slots<<<slot_grid(w, n), 256, 0, st>>>(prod, prod_w, prod_w, L.sh - 64 * t, nxt, 2 * w, w, n);
+    k_shr_slots<<<slot_grid(w, n), 256, 0, st>>>(prod, prod_w, prod_w, (int64_t)(L.sh - 64 * t), nxt, 2 * w, w,
+                                                 n);
     if (lower_q) k_lower_q<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nxt, 2 * w, w, n);
     if (!cu(cudaGetLastError())) break;
     A.put(prod);
@@ -366,6 +380,200 @@ int to_decimal_device(const uint64_t* x, size_t nx, int K, const Level* lv, char
     ms[0] = t1 - t0;
     ms[1] = t2 - t1;
     ms[2] = now_ms() - t2;
+  }
+  return PIMUL_OK;
+}
+
+
+// ---------------------------------------------------------- final assembly
+// pi 10^(D-1) = W Q / (A Q - |T|) with W = 426880 sqrt(10005) 10^(D-1)
+// (chudnovsky.rs:146-204 followed by util.rs:25-83's scaling), from the
+// binary splitting's root Q and |T| where they lie in HBM:
+//   den = top limbs of A Q - |T|, normalized to nl = ceil((prec + 192) / 64)
+//         limbs with the top bit set (den ~ dn 2^ed);
+//   R   ~ 2^(128 nl) / dn by Newton's iteration with precision doubling,
+//         each step from h = 64m to c = 64m' bits (m' = min(2m - 1, nl)):
+//           E = 2^(h+c) - D_c Y_h    (D_c = the top m' limbs of dn; E >= 0)
+//           Y_c = Y_h 2^(c-h) + floor(Y_h E / 2^(2h)) - 4
+//         Y stays at or below rho 2^h (rho = 2^(64 nl) / dn): E needs only
+//         the low m' + 1 limbs of -D_c Y_h, and the -4 covers the
+//         truncation of D_c (at most 4 units of Y_c);
+//   ip  = floor(W Q_top R 2^e), Q_top = the top nl limbs of Q.
+namespace {
+
+// floor(2^(64 s) / d) for a small host divisor d (restoring division).
+std::vector<uint64_t> host_recip_pow2(const std::vector<uint64_t>& d, size_t s) {
+  const size_t nd = d.size();
+  std::vector<uint64_t> q(s + 1, 0), r(nd + 1, 0);
+  for (size_t bit = 64 * s + 1; bit-- > 0;) {
+    // r = 2 r + (bit == 64 s)
+    uint64_t carry = bit == 64 * s ? 1 : 0;
+    for (size_t i = 0; i <= nd; i++) {
+      const uint64_t nc = r[i] >> 63;
+      r[i] = (r[i] << 1) | carry;
+      carry = nc;
+    }
+    // r >= d ?
+    int c = r[nd] ? 1 : 0;
+    for (size_t i = nd; c == 0 && i-- > 0;) c = r[i] > d[i] ? 1 : (r[i] < d[i] ? -1 : 0);
+    if (c >= 0) {
+      uint64_t borrow = 0;
+      for (size_t i = 0; i <= nd; i++) {
+        const uint64_t di = i < nd ? d[i] : 0;
+        const uint64_t t = r[i] - di;
+        const uint64_t b1 = r[i] < di, b2 = t < borrow;
+        r[i] = t - borrow;
+        borrow = b1 | b2;
+      }
+      q[bit >> 6] |= 1ull << (bit & 63);
+    }
+  }
+  while (!q.empty() && q.back() == 0) q.pop_back();
+  return q;
+}
+
+}  // namespace
+
+int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, size_t tn, uint64_t A,
+                          const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
+                          double* ms) {
+  if (!dQ || !qn || (tn && !dT) || !wm || !wl || !d_ip || !ipn || !A) return PIMUL_EINVAL;
+  *d_ip = nullptr;
+  *ipn = 0;
+  const double t0 = now_ms();
+  Arena Ar;
+  if (cudaStreamCreateWithFlags(&Ar.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  const cudaStream_t st = Ar.st;
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
+    return rc == PIMUL_OK;
+  };
+  const size_t nl = (prec + 192 + 63) / 64;
+  // den window: limbs [s0, qn + 1) of A Q - |T| (carries from below s0 are
+  // dropped: a relative error below 2^-(64 nl))
+  const size_t dn = qn + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
+  if (tn > dn) return PIMUL_EINVAL;
+  uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr, *dnorm = nullptr, *consts = nullptr;
+  if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn)) || (rc = Ar.get(&dnorm, nl)) ||
+      (rc = Ar.get(&consts, 1)))
+    return rc;
+  k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(dQ + s0, qn - s0, A,
+                                                                                             lo, hi);
+  if (!cu(cudaGetLastError())) return rc;
+  pimul_addsub_job j1{lo, wn, hi, wn, den, wn, 0};
+  if ((rc = pimul_addsub_batch(&j1, 1, st))) return rc;
+  if (tn > s0) {
+    pimul_addsub_job j2{den, wn, dT + s0, tn - s0, den, wn, 1};
+    if ((rc = pimul_addsub_batch(&j2, 1, st))) return rc;
+  }
+  Ar.put(lo);
+  Ar.put(hi);
+  // bit length of the window, then dn = its top 64 nl bits
+  uint64_t top[3] = {0, 0, 0};
+  const size_t nt = std::min<size_t>(3, wn);
+  cu(cudaMemcpyAsync(top, den + (wn - nt), nt * 8, cudaMemcpyDeviceToHost, st));
+  cu(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  int64_t B = 0;
+  for (size_t i = nt; i-- > 0 && !B;)
+    if (top[i]) B = 64 * (int64_t)(wn - nt + i) + 64 - __builtin_clzll(top[i]);
+  if (B <= 64 * (int64_t)(wn - nt)) return PIMUL_EINVAL;  // den vanishes at the top: not a Chudnovsky root
+  const int64_t shn = B - 64 * (int64_t)nl;
+  k_shr_slots<<<slot_grid(nl, 1), 256, 0, st>>>(den, 0, wn, shn, dnorm, 0, nl, 1);
+  if (!cu(cudaGetLastError())) return rc;
+  const int64_t ed = 64 * (int64_t)s0 + shn;  // den ~ dn 2^ed
+  Ar.put(den);
+  // Newton: Y_(64 m0) from the top limbs of dn on the host
+  const size_t m0 = std::min<size_t>(8, nl - 2), k0 = m0 + 2;
+  std::vector<uint64_t> dtop(k0);
+  cu(cudaMemcpyAsync(dtop.data(), dnorm + (nl - k0), k0 * 8, cudaMemcpyDeviceToHost, st));
+  cu(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  // ceil of the truncated divisor keeps Y below rho 2^h
+  for (size_t i = 0; i < k0 && ++dtop[i] == 0; i++) {
+  }
+  if (dtop.back() == 0) dtop.push_back(1);
+  std::vector<uint64_t> y0 = host_recip_pow2(dtop, k0 + m0);
+  y0.resize(m0 + 1, 0);
+  uint64_t* Y = nullptr;
+  if ((rc = Ar.get(&Y, m0 + 1))) return rc;
+  cu(cudaMemcpyAsync(Y, y0.data(), (m0 + 1) * 8, cudaMemcpyHostToDevice, st));
+  const uint64_t four = 4;
+  cu(cudaMemcpyAsync(consts, &four, 8, cudaMemcpyHostToDevice, st));
+  cu(cudaStreamSynchronize(st));  // y0 and four are host locals
+  size_t m = m0;
+  while (!rc && m < nl) {
+    const size_t mp = std::min(2 * m - 1, nl);
+    const uint64_t* Dc = dnorm + (nl - mp);
+    uint64_t *Pr = nullptr, *E = nullptr, *YE = nullptr, *Yn = nullptr;
+    if ((rc = Ar.get(&Pr, mp + m + 1)) || (rc = Ar.get(&E, mp + 1))) break;
+    if ((rc = pimul_mul_device(Dc, mp, Y, m + 1, Pr, st))) break;
+    pimul_addsub_job je{nullptr, 0, Pr, mp + 1, E, mp + 1, PIMUL_SUB_MOD};  // E = 2^(h+c) - Pr
+    if ((rc = pimul_addsub_batch(&je, 1, st))) break;
+    Ar.put(Pr);
+    if ((rc = Ar.get(&YE, m + mp + 2)) || (rc = Ar.get(&Yn, mp + 1))) break;
+    if ((rc = pimul_mul_device(Y, m + 1, E, mp + 1, YE, st))) break;
+    if (mp > m) cu(cudaMemsetAsync(Yn, 0, (mp - m) * 8, st));
+    cu(cudaMemcpyAsync(Yn + (mp - m), Y, (m + 1) * 8, cudaMemcpyDeviceToDevice, st));
+    if (rc) break;
+    pimul_addsub_job ja{Yn, mp + 1, YE + 2 * m, mp - m + 2, Yn, mp + 1, 0};
+    if ((rc = pimul_addsub_batch(&ja, 1, st))) break;
+    pimul_addsub_job js{Yn, mp + 1, consts, 1, Yn, mp + 1, 1};
+    if ((rc = pimul_addsub_batch(&js, 1, st))) break;
+    Ar.put(E);
+    Ar.put(YE);
+    Ar.put(Y);
+    Y = Yn;
+    m = mp;
+  }
+  if (rc) return rc;
+  const double t1 = now_ms();
+  // ip = floor(W Q_top R 2^e2)
+  const size_t lq = std::min(qn, nl);
+  uint64_t *X1 = nullptr, *X2 = nullptr, *dW = nullptr;
+  if ((rc = Ar.get(&X1, lq + nl + 1))) return rc;
+  if ((rc = pimul_mul_device(dQ + (qn - lq), lq, Y, nl + 1, X1, st))) return rc;
+  Ar.put(Y);
+  if ((rc = Ar.get(&dW, wl)) || (rc = Ar.get(&X2, wl + nl + 1))) return rc;
+  if ((rc = pimul::host_to_device(dW, wm, wl * 8, st))) return rc;
+  if ((rc = pimul_mul_device(dW, wl, X1 + lq, nl + 1, X2, st))) return rc;
+  // W Q / den ~ X2 2^(64 lq) * 2^(we + 64 (qn - lq) - 128 nl - ed)
+  const int64_t e2 = we + 64 * (int64_t)qn - 128 * (int64_t)nl - ed;
+  const int64_t ip_bits = 64 * (int64_t)(wl + nl + 1) + e2;
+  if (e2 > 0 || ip_bits <= 0) return PIMUL_EINVAL;
+  const size_t n_ip = (size_t)((ip_bits + 63) / 64);
+  uint64_t* ip = nullptr;
+  if (cudaMalloc((void**)&ip, n_ip * 8) != cudaSuccess) {
+    cudaGetLastError();
+    return PIMUL_ENOMEM;
+  }
+  k_shr_slots<<<slot_grid(n_ip, 1), 256, 0, st>>>(X2, 0, wl + nl + 1, -e2, ip, 0, n_ip, 1);
+  cu(cudaGetLastError());
+  cu(cudaStreamSynchronize(st));
+  if (rc) {
+    cudaFree(ip);
+    return rc;
+  }
+  size_t len = n_ip;
+  // trimmed length (the top limbs of the estimate may be zero)
+  std::vector<uint64_t> tail(std::min<size_t>(n_ip, 4));
+  while (len) {
+    const size_t k = std::min(len, tail.size());
+    if (cudaMemcpy(tail.data(), ip + (len - k), k * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaFree(ip);
+      return PIMUL_ECUDA;
+    }
+    size_t z = 0;
+    while (z < k && tail[k - 1 - z] == 0) z++;
+    len -= z;
+    if (z < k) break;
+  }
+  *d_ip = ip;
+  *ipn = len;
+  if (ms) {
+    ms[0] = t1 - t0;
+    ms[1] = now_ms() - t1;
   }
   return PIMUL_OK;
 }

@@ -22,8 +22,22 @@ constexpr int LEAF_K = 5;
 // Writes the last `want` of the 19 * 2^K decimal digits of x (zero-padded on
 // the left) to out, with x split level by level on the device (levels K-1
 // down to LEAF_K, level k at lv[k]) and the leaves printed by a kernel.
-// x < 10^(19 * 2^K) is required; PIMUL_EINVAL if x has more than `want`
-// digits.  ms (optional, 3 entries): upload, levels, leaves + download.
-int to_decimal_device(const uint64_t* x, size_t nx, int K, const Level* lv, char* out, size_t want, double* ms);
+// x (host memory, or device memory ready for use when x_on_device) must be
+// below 10^(19 * 2^K); PIMUL_EINVAL if x has more than `want` digits.
+// ms (optional, 3 entries): upload, levels, leaves + download.
+int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, const Level* lv, char* out, size_t want,
+                      double* ms);
+
+// Chudnovsky's final assembly with Q and |T| in HBM (chudnovsky.rs:146-204
+// up to the decimal scaling of util.rs:25-83): *d_ip (allocated here, freed
+// by the caller with cudaFree) receives floor(W Q / (A Q - |T|)) in *ipn
+// limbs, with W = wm 2^we (the constant 426880 sqrt(10005) times the
+// decimal scale, host limbs).  The quotient comes from the top prec + 192
+// bits of each operand and a Newton reciprocal run on the device, so its
+// relative error is below 2^-(prec + 100).  ms (optional, 2 entries):
+// reciprocal, products.
+int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, size_t tn, uint64_t A,
+                          const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
+                          double* ms);
 
 }  // namespace pidec

@@ -1634,9 +1634,10 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
 // Device-resident splitting over leaves [0, n): the leaves are computed by
 // host threads segment by segment while a GPU thread reduces the previous
 // segment to its root; the segment roots are then merged on the device and
-// only the final Q and |T| come back.  Returns PIMUL_EINVAL (nothing
+// only the final Q and |T| come back, or, with keep, stay on the device
+// (keep->nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
 // computed on the device) if a leaf breaks the static signs.
-static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
+static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep) {
   const uint64_t nleaf = (b - a + leaf - 1) / leaf;
   const size_t nseg = nleaf >= 64 ? 4 : 1;
   cudaStream_t st = nullptr;
@@ -1702,6 +1703,12 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     top.arenas.insert(top.arenas.end(), r.arenas.begin(), r.arenas.end());
   }
   if (!rc) rc = dev_reduce(top, st, false);
+  if (!rc && keep) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    *keep = std::move(top);
+    return PIMUL_OK;
+  }
   if (!rc) {
     double t0 = now_ms();
     const DNode& r = top.nodes[0];
@@ -1720,14 +1727,14 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   return rc;
 }
 
-static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t) {
+static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep = nullptr) {
   const uint64_t nleaf = (b - a + leaf - 1) / leaf;
   for (double& x : g_bt) x = 0;
   g_leaf_ms = 0;
   // device-resident levels (every range obeys the static signs; a leaf that
   // did not would send the splitting down the host-staged path below)
   if (nleaf > 1) {
-    int rc = split_root_device(a, b, leaf, q, t);
+    int rc = split_root_device(a, b, leaf, q, t, keep);
     report_split("binary splitting (device-resident levels)");
     if (rc != PIMUL_EINVAL) return rc;
   }
@@ -1809,18 +1816,13 @@ static DecPlan make_dec_plan(uint64_t ndig) {
   return D;
 }
 
-// Exactly `want` decimal digits of X < 10^want (zero-padded on the left),
-// written straight into out.
-static int to_decimal_batched_into(const Int& X, char* out, size_t want, const DecPlan* plan) {
-  if (X.m.size() <= 256) {
-    std::string s = to_decimal_top(X);
-    if (s.size() > want) return PIMUL_EINVAL;
-    memset(out, '0', want - s.size());
-    memcpy(out + want - s.size(), s.data(), s.size());
-    return g_error.load();
-  }
+// Exactly `want` decimal digits of x < 10^want (zero-padded on the left),
+// written straight into out; x: n limbs on the host, or in device memory
+// (on_dev), of bit length xbits.
+static int to_decimal_core(const uint64_t* x, size_t n, bool on_dev, uint64_t xbits, char* out, size_t want,
+                           const DecPlan* plan) {
   DecPlan own;
-  const uint64_t ndig = std::max<uint64_t>(dec_estimate(bits_of(X.m)) + 1, want);
+  const uint64_t ndig = std::max<uint64_t>(dec_estimate(xbits) + 1, want);
   if (!plan || (1ull << plan->K) * 19 < ndig) {
     own = make_dec_plan(ndig);
     plan = &own;
@@ -1838,11 +1840,37 @@ static int to_decimal_batched_into(const Int& X, char* out, size_t want, const D
     lv[k] = pidec::Level{plan->P[k].m.data(), plan->P[k].m.size(), plan->V[k].m.data(), plan->V[k].m.size(),
                          plan->sh[k]};
   double ms[3] = {0, 0, 0};
-  int rc = pidec::to_decimal_device(X.m.data(), X.m.size(), plan->K, lv.data(), out, want, ms);
+  int rc = pidec::to_decimal_device(x, n, on_dev, plan->K, lv.data(), out, want, ms);
   if (getenv("PIMUL_PI_TIMING"))
     fprintf(stderr, "[pimul] decimal conversion on the device: upload %.1f ms, levels %.1f, leaves + download %.1f\n",
             ms[0], ms[1], ms[2]);
   return rc;
+}
+
+// Exactly `want` decimal digits of X < 10^want (zero-padded on the left),
+// written straight into out.
+static int to_decimal_batched_into(const Int& X, char* out, size_t want, const DecPlan* plan) {
+  if (X.m.size() <= 256) {
+    std::string s = to_decimal_top(X);
+    if (s.size() > want) return PIMUL_EINVAL;
+    memset(out, '0', want - s.size());
+    memcpy(out + want - s.size(), s.data(), s.size());
+    return g_error.load();
+  }
+  return to_decimal_core(X.m.data(), X.m.size(), false, bits_of(X.m), out, want, plan);
+}
+
+// The same for a trimmed integer of n limbs in device memory.
+static int to_decimal_batched_into_dev(const uint64_t* dx, size_t n, char* out, size_t want, const DecPlan* plan) {
+  if (n <= 256) {
+    Limbs h(n);
+    if (n && cudaMemcpy(h.data(), dx, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return PIMUL_ECUDA;
+    return to_decimal_batched_into(Int(std::move(h), false), out, want, plan);
+  }
+  uint64_t top = 0;
+  if (cudaMemcpy(&top, dx + (n - 1), 8, cudaMemcpyDeviceToHost) != cudaSuccess) return PIMUL_ECUDA;
+  const uint64_t xbits = 64 * (uint64_t)(n - 1) + (top ? 64 - __builtin_clzll(top) : 0);
+  return to_decimal_core(dx, n, true, xbits, out, want, plan);
 }
 
 static int to_decimal_batched(const Int& X, std::string& outs) {
@@ -1959,35 +1987,81 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     scale = pow_int(flt_from_u64(10, prec), Int(digits - 1));
     t_scale = now_ms() - ts;
   });
-  // batched form: the decimal conversion's divisors and reciprocals too
+  // batched form: the decimal conversion's divisors and reciprocals too,
+  // and W = 426880 sqrt(10005) 10^(D-1) for the device final assembly (this
+  // thread alone joins the two above; the main thread joins it)
   DecPlan dplan;
   std::thread plan_th([&] {
     if (leaf_terms) dplan = make_dec_plan(digits + 1);
   });
+  Flt W;
+  std::thread w_th;
+  if (leaf_terms)
+    w_th = std::thread([&] {
+      sqrt_th.join();
+      scale_th.join();
+      W = mul_at_prec(sq, scale, prec + 64);
+    });
+  auto join_sqrt = [&] { leaf_terms ? w_th.join() : sqrt_th.join(); };
+  auto join_scale = [&] {
+    if (!leaf_terms) scale_th.join();
+  };
   Int q, t;
+  DLevel droot;  // the root's Q and |T| when they stay on the device
   int brc = PIMUL_OK;
   if (leaf_terms)
-    brc = split_root_batched(1, n_terms + 1, leaf_terms, q, t);
+    brc = split_root_batched(1, n_terms + 1, leaf_terms, q, t, &droot);
   else
     split_root(1, n_terms + 1, q, t);
   if (brc) {
-    sqrt_th.join();
-    scale_th.join();
+    for (uint64_t* ar : droot.arenas) cudaFree(ar);
+    join_sqrt();
+    join_scale();
     plan_th.join();
     return brc;
   }
   double t1 = now_ms();
+  if (!droot.nodes.empty()) {
+    // final assembly and decimal conversion without leaving the device
+    join_sqrt();
+    const DNode& r = droot.nodes[0];
+    uint64_t* d_ip = nullptr;
+    size_t ipn = 0;
+    double fms[2] = {0, 0};
+    int frc = pidec::final_assembly_device(r.q, r.qn, r.t, r.tn, CH_A, W.mant.data(), W.mant.size(), W.exp, prec,
+                                           &d_ip, &ipn, fms);
+    for (uint64_t* ar : droot.arenas) cudaFree(ar);
+    double t2 = now_ms();
+    plan_th.join();
+    if (!frc) frc = to_decimal_batched_into_dev(d_ip, ipn, out, digits, &dplan);
+    if (d_ip) cudaFree(d_ip);
+    double t3 = now_ms();
+    if (getenv("PIMUL_PI_TIMING"))
+      fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms, final assembly on the device: "
+              "reciprocal %.1f ms, products %.1f ms\n", t_sqrt, t_scale, fms[0], fms[1]);
+    if (frc) return frc;
+    if (g_error.load()) return g_error.load();
+    if (phase_ms) {
+      phase_ms[0] = t1 - t0;
+      phase_ms[1] = t2 - t1;
+      phase_ms[2] = t3 - t2;
+    }
+    if (ntt_products) *ntt_products = g_ntt_calls.load();
+    if (ntt_hist33)
+      for (int i = 0; i < 33; i++) ntt_hist33[i] = g_ntt_hist[i].load();
+    return PIMUL_OK;
+  }
   // final assembly (chudnovsky.rs:146-204)
   Int denom = add(mul(Int(CH_A), q), t);
   Flt denf = flt_from_int(denom);
   Flt recip = reciprocal_at_prec(denf, prec + 16);
   double t_recip = now_ms() - t1;
-  sqrt_th.join();
+  join_sqrt();
   Flt num = mul_at_prec(sq, flt_from_int(q), sq.prec);
   Flt pi = mul_at_prec(num, recip, prec);
   double t2 = now_ms();
   // decimal conversion (util.rs:25-83)
-  scale_th.join();
+  join_scale();
   double t_join = now_ms() - t2;
   pi = mul_at_prec(pi, scale, pi.prec);
   Int ip = to_integer_down(pi);
