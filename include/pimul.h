@@ -134,6 +134,34 @@ typedef struct pimul_addsub_job {
 #define PIMUL_SUB_MOD 2
 int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream);
 
+/*
+ * Sums of two products for many operand sets at once (device pointers):
+ * out[0..nout) = a1 b1 + a2 b2, nout >= max(la1 + lb1, la2 + lb2) + 1
+ * (limbs above the sum are zeroed; an empty pair, la or lb zero, adds
+ * nothing, so a job with one pair is a plain product and nout >= la + lb
+ * suffices).  Long sums are added in the transform domain: four forward
+ * transforms, one inverse and one carry pass instead of two of each and an
+ * addition.  In this call and in pimul_mul_batch, products of one transform
+ * length whose operand b is the same array (same pointer and length) share
+ * b's transform.  Asynchronous on `stream`.
+ * This engine's own addition: the T = T_L Q_R + P_L T_R step of a binary
+ * splitting level (crates/pi-core/src/algorithm/chudnovsky.rs:399-413) as
+ * one job.
+ */
+typedef struct pimul_sum_job {
+  const uint64_t* a1;
+  size_t la1;
+  const uint64_t* b1;
+  size_t lb1;
+  const uint64_t* a2;
+  size_t la2;
+  const uint64_t* b2;
+  size_t lb2;
+  uint64_t* out;
+  size_t nout;
+} pimul_sum_job;
+int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream);
+
 /* Trimmed lengths (highest nonzero limb + 1) of n device limb arrays of
  * lengths lens[i]; out_lens on the host.  Synchronous. */
 int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n, size_t* out_lens, void* stream);

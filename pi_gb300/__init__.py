@@ -23,7 +23,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device",
+    "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device", "sum_batch", "SumJob",
     "plan", "sync", "bbp_hex_digits", "mul_batch", "BatchPlan", "autotune",
     "tuning_apply", "PimulJob", "set_budget", "upload", "submit", "wait", "download", "free",
     "handle_size", "pi_chudnovsky", "pi_gauss_legendre", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
@@ -66,6 +66,7 @@ def load(build_if_stale: bool = True):
     L.pimul_sync.argtypes = []
     L.pimul_mul_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
     L.pimul_addsub_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_sum_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
     L.pimul_top_limbs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]
     L.pimul_batch_plan_create.argtypes = [ctypes.POINTER(_sz), ctypes.POINTER(_sz), _sz, ctypes.POINTER(ctypes.c_void_p)]
     L.pimul_batch_plan_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p]
@@ -172,6 +173,30 @@ def addsub_batch(jobs, stream=None):
         import torch
         stream = torch.cuda.current_stream(jobs[0][2].device).cuda_stream
     _check(lib().pimul_addsub_batch(arr, len(jobs), ctypes.c_void_p(stream) if stream else None))
+
+
+class SumJob(ctypes.Structure):
+    """struct pimul_sum_job of include/pimul.h (device pointers)."""
+    _fields_ = [("a1", ctypes.c_void_p), ("la1", _sz), ("b1", ctypes.c_void_p), ("lb1", _sz),
+                ("a2", ctypes.c_void_p), ("la2", _sz), ("b2", ctypes.c_void_p), ("lb2", _sz),
+                ("out", ctypes.c_void_p), ("nout", _sz)]
+
+
+def sum_batch(jobs, stream=None):
+    """out = a1 * b1 + a2 * b2 for torch CUDA uint64/int64 tensors:
+    jobs = [(a1, b1, a2, b2, out)] (a2, b2 may be None), over out.numel()
+    limbs (pimul_sum_batch; asynchronous on the current torch stream)."""
+    arr = (SumJob * max(len(jobs), 1))()
+
+    def ptr(t):
+        return (t.data_ptr() if t.numel() else None, t.numel()) if t is not None else (None, 0)
+
+    for i, (a1, b1, a2, b2, out) in enumerate(jobs):
+        arr[i] = SumJob(*ptr(a1), *ptr(b1), *ptr(a2), *ptr(b2), out.data_ptr(), out.numel())
+    if stream is None and jobs:
+        import torch
+        stream = torch.cuda.current_stream(jobs[0][4].device).cuda_stream
+    _check(lib().pimul_sum_batch(arr, len(jobs), ctypes.c_void_p(stream) if stream else None))
 
 
 def top_limbs(arrays, stream=None):

@@ -192,16 +192,35 @@ struct Job {
   uint64_t* H;  // high parts of the carry windows
   uint8_t* aux; // carry-scan flags
   uint64_t la, lb;
+  const uint64_t* X;  // spectrum added to the pointwise product (a sum of two products), or null
+  uint64_t nout;      // output limbs (0: la + lb)
+  uint32_t flags;     // JF_* roles inside a batch (0: a plain product)
 };
+
+// Roles of a product inside a batch.  A spectrum shared by several products
+// with the same operand b is computed once, by its owner (JF_B_FULL); the
+// others point B at it (JF_B_SHARED) and skip b's passes.  With a full
+// spectrum in B, k_mid only multiplies and writes the product to A.  An
+// addend (JF_ADDEND) produces no output: its pointwise product A * B stays
+// in A, where the job it is added to reads it as X.
+constexpr uint32_t JF_B_SHARED = 1;
+constexpr uint32_t JF_B_FULL = 2;
+constexpr uint32_t JF_ADDEND = 4;
 
 __device__ __forceinline__ Job job_of(const Job* jobs, const Job& one) {
   if (jobs) return jobs[blockIdx.y];
   return one;
 }
 __device__ __forceinline__ bool is_square(const Job& J) { return J.a == J.b && J.la == J.lb; }
+// b's own passes are skipped for a square and for a borrowed spectrum.
+__device__ __forceinline__ bool skips_b(const Job& J) { return is_square(J) || (J.flags & JF_B_SHARED); }
+__device__ __forceinline__ bool b_spectrum(const Job& J) { return (J.flags & (JF_B_SHARED | JF_B_FULL)) != 0; }
+__host__ __device__ __forceinline__ uint64_t job_nout(const Job& J) { return J.nout ? J.nout : J.la + J.lb; }
 // Array a pass works on: 0 = A, 1 = B, 2 = the product array.
 __device__ __forceinline__ uint64_t* job_array(const Job& J, int which) {
-  return which == 0 ? J.A : (which == 1 || !is_square(J)) ? J.B : J.A;
+  if (which == 0) return J.A;
+  if (which == 1) return J.B;
+  return is_square(J) || b_spectrum(J) ? J.A : J.B;
 }
 
 // Forward pass 0 with the limb -> 16-bit coefficient split fused in
@@ -213,7 +232,7 @@ template <int R>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT) {
   constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
-  if (which == 1 && is_square(J)) return;
+  if (which == 1 && skips_b(J)) return;
   const uint64_t* __restrict__ limbs = which ? J.b : J.a;
   const uint64_t nl = which ? J.lb : J.la;
   uint64_t* __restrict__ data = which ? J.B : J.A;
@@ -264,7 +283,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
   static_assert(R >= TL, "thread index must stay inside one block's rows");
   constexpr uint32_t TM = (1u << T) - 1, RM = (1u << R) - 1;
   const Job J = job_of(jobs, one);
-  if (FWD && which == 1 && is_square(J)) return;
+  if (FWD && which == 1 && skips_b(J)) return;
+  if (!FWD && (J.flags & JF_ADDEND)) return;
   uint64_t* __restrict__ data = job_array(J, which);
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
@@ -311,17 +331,20 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
   }
 }
 
-// Last forward pass of operand a (stride 1): 2^(13-R) contiguous blocks of
-// 2^R words.  Squares skip it: their last pass is fused into k_mid.
+// Last forward pass (stride 1): 2^(13-R) contiguous blocks of 2^R words, of
+// operand a (which = 0) or, for a full spectrum of b (JF_B_FULL), of b.
+// Squares skip it: their last pass is fused into k_mid.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const Job* jobs, Job one, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const Job* jobs, Job one, int which,
+                                                                          Roots RT) {
   constexpr int BC = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   if (is_square(J)) return;
+  if (which == 1 && !(J.flags & JF_B_FULL)) return;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
-  uint64_t* base = J.A + ((uint64_t)blockIdx.x << TILE_LOG);
+  uint64_t* base = (which ? J.B : J.A) + ((uint64_t)blockIdx.x << TILE_LOG);
 #pragma unroll
   for (int q = 0; q < PER_THREAD; q++) {
     const uint32_t lin = q * PASS_THREADS + tid;
@@ -335,17 +358,21 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const 
 }
 
 // Fused middle of the multiply on one contiguous tile: last forward pass of
-// b, pointwise product with the spectrum of a (times N^-1, the inverse's
-// 1/N, crates/bignum/src/ntt.rs:383-390 and 845-853), first inverse pass;
-// the result overwrites b's array.  A square transforms and squares a's
-// array in place.
+// b, pointwise product with the spectrum of a (plus X for a sum of two
+// products; times N^-1, the inverse's 1/N, crates/bignum/src/ntt.rs:383-390
+// and 845-853), first inverse pass; the result overwrites b's array.  A
+// square transforms and squares a's array in place; with b's full spectrum
+// in B (shared or owned) the last pass is skipped and the result goes to A.
 template <int R>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
   constexpr int BC = TILE_LOG - R;
   const Job J = job_of(jobs, one);
-  const bool sq = is_square(J);
-  uint64_t* __restrict__ c = sq ? J.A : J.B;
-  const uint64_t* __restrict__ a = J.A;
+  if (J.flags & JF_ADDEND) return;
+  const bool sq = is_square(J), spec = b_spectrum(J);
+  const uint64_t* cin = sq ? J.A : J.B;
+  uint64_t* cout = sq || spec ? J.A : J.B;
+  const uint64_t* a = J.A;
+  const uint64_t* __restrict__ X = J.X;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
@@ -353,20 +380,30 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
 #pragma unroll
   for (int q = 0; q < PER_THREAD; q++) {
     const uint32_t lin = q * PASS_THREADS + tid;
-    cp_async8(sm + spad(lin), c + off + lin);
+    cp_async8(sm + spad(lin), cin + off + lin);
   }
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();
-  tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
+  if (!spec) tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
   for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
     uint64_t x = sm[spad(lin)];
     uint64_t y = sq ? x : a[off + lin];
-    sm[spad(lin)] = gl::mul(gl::mul(x, y), ninv);
+    uint64_t p = gl::mul(x, y);
+    if (X) p = gl::add(p, X[off + lin]);
+    sm[spad(lin)] = gl::mul(p, ninv);
   }
   __syncthreads();
   tile_inv_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) c[off + lin] = sm[spad(lin)];
+  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) cout[off + lin] = sm[spad(lin)];
+}
+
+// Addends: A <- A * B (spectra, element by element), read later as X.
+__global__ void __launch_bounds__(256) k_pointwise_addend(const Job* jobs, Job one, uint64_t n) {
+  const Job J = job_of(jobs, one);
+  if (!(J.flags & JF_ADDEND)) return;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    J.A[i] = gl::mul(J.A[i], J.B[i]);
 }
 
 // ---- carry normalisation (crates/bignum/src/ntt.rs:676-791) --------------
@@ -423,9 +460,11 @@ __device__ __forceinline__ Win fold16(const uint64_t* c16, int stride) {
 
 constexpr int CARRY_THREADS = 256;  // windows per CTA
 
-__host__ __device__ __forceinline__ uint64_t n_windows(uint64_t la, uint64_t lb) {
-  return (4 * la + 4 * lb - 1 + WIN_COEFFS - 1) / WIN_COEFFS;
+// Windows of an output of nout limbs (4 nout - 1 coefficients).
+__host__ __device__ __forceinline__ uint64_t n_windows_out(uint64_t nout) {
+  return (4 * nout - 1 + WIN_COEFFS - 1) / WIN_COEFFS;
 }
+__host__ __device__ __forceinline__ uint64_t n_windows(uint64_t la, uint64_t lb) { return n_windows_out(la + lb); }
 __host__ __device__ __forceinline__ uint64_t n_chunks(uint64_t nwin) {
   return (nwin + CARRY_THREADS - 1) / CARRY_THREADS;
 }
@@ -443,10 +482,11 @@ template <int R>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
   constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
+  if (J.flags & JF_ADDEND) return;
   const uint64_t* __restrict__ data = job_array(J, 2);
   uint64_t* __restrict__ out = J.out;
   uint64_t* __restrict__ H = J.H;
-  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb);
+  const uint64_t nlimbs = job_nout(J), nwin = n_windows_out(nlimbs);
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
@@ -487,7 +527,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
 // masks, per CTA the chunk's carry out for carry in 0 and 1.
 __global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb), nchunk = n_chunks(nwin);
+  if (J.flags & JF_ADDEND) return;
+  const uint64_t nlimbs = job_nout(J), nwin = n_windows_out(nlimbs), nchunk = n_chunks(nwin);
   if (blockIdx.x >= nchunk) return;  // uniform per CTA
   uint64_t* __restrict__ out = J.out;
   const uint64_t* __restrict__ H = J.H;
@@ -538,7 +579,8 @@ __global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, 
 constexpr int SCAN_THREADS = 1024;
 __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  const uint64_t nchunk = n_chunks(n_windows(J.la, J.lb));
+  if (J.flags & JF_ADDEND) return;
+  const uint64_t nchunk = n_chunks(n_windows_out(job_nout(J)));
   const uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;
   uint8_t* chunk_cin = const_cast<uint8_t*>(chunk_gp) + nchunk;
   __shared__ uint8_t seg_g[SCAN_THREADS], seg_p[SCAN_THREADS], seg_cin[SCAN_THREADS];
@@ -573,7 +615,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Jo
 // Carry pass 3: add the incoming carry to every window that receives one.
 __global__ void __launch_bounds__(CARRY_THREADS) k_carry_apply(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  const uint64_t nlimbs = J.la + J.lb, nwin = n_windows(J.la, J.lb), nchunk = n_chunks(nwin);
+  if (J.flags & JF_ADDEND) return;
+  const uint64_t nlimbs = job_nout(J), nwin = n_windows_out(nlimbs), nchunk = n_chunks(nwin);
   if (blockIdx.x >= nchunk) return;
   uint64_t* __restrict__ out = J.out;
   const uint32_t* masks = reinterpret_cast<const uint32_t*>(J.aux);
@@ -1108,7 +1151,8 @@ struct Launcher {
 // transform length 2^L: the products come from the device array `jobs`
 // (blockIdx.y) or, for nj == 1 and jobs == nullptr, from `one`.
 // max_chunk: largest carry-chunk count among the products.
-static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32_t nj, int L, uint64_t max_chunk) {
+static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32_t nj, int L, uint64_t max_chunk,
+                      bool any_b_full = false, bool any_addend = false) {
   const Plan pl = make_plan(L);
   const dim3 grid((unsigned)(1ull << (L - TILE_LOG)), nj);
   const size_t smem = pass_smem_bytes(TILE_LOG);
@@ -1126,10 +1170,15 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
       KTimer kt(K_PASS_FWD, X.st, X.stats);
       PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L - consumed, X.R)));
     }
-    if (which == 0) {
+    if (which == 0 || any_b_full) {
       KTimer kt(K_PASS_FWD, X.st, X.stats);
-      PIMUL_DISPATCH_R(rl, (k_fwd_last<RR><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, X.R)));
+      PIMUL_DISPATCH_R(rl, (k_fwd_last<RR><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, X.R)));
     }
+  }
+  if (any_addend) {
+    KTimer kt(K_POINTWISE, X.st, X.stats);
+    const uint64_t n = 1ull << L;
+    k_pointwise_addend<<<dim3((unsigned)std::min<uint64_t>(n / 1024, 4096), nj), 256, 0, X.st>>>(jobs, one, n);
   }
   {
     KTimer kt(K_POINTWISE, X.st, X.stats);
@@ -1191,38 +1240,71 @@ static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uin
 }
 
 // ------------------------------------------------------------------ batches
-// A batch of independent products on device buffers.  Products are grouped
-// by transform length: lengths up to 2^12 run as one CTA per product in a
-// persistent kernel over a size-sorted list; longer ones run the pass
-// pipeline once per length with one grid row (blockIdx.y) per product.
+// A batch of independent products (and sums of two products) on device
+// buffers.  Products are grouped by transform length: lengths up to 2^12
+// run as one CTA per product in a persistent kernel over a size-sorted list;
+// longer ones run the pass pipeline once per length with one grid row
+// (blockIdx.y) per descriptor.  Within a group of one length, products whose
+// operand b is the same array share b's spectrum (computed once), and a sum
+// a1 b1 + a2 b2 runs as two descriptors whose spectra are added before one
+// inverse transform and one carry pass.
+
+// One unit of a batch: a b, or a b + a2 b2 (la2 > 0; large lengths only).
+struct Unit {
+  const uint64_t* a;
+  uint64_t la;
+  const uint64_t* b;
+  uint64_t lb;
+  const uint64_t* a2;
+  uint64_t la2;
+  const uint64_t* b2;
+  uint64_t lb2;
+  uint64_t* out;
+  uint64_t nout;
+};
+
 struct BatchLayout {
-  std::vector<uint32_t> small;  // job indices, size-sorted descending
+  std::vector<uint32_t> small;  // unit indices, size-sorted descending
+  struct Desc {
+    uint32_t unit;
+    bool second;             // the a2 b2 half of a sum (an addend)
+    uint32_t flags;          // JF_*
+    int64_t owner = -1;      // descriptor whose B this one borrows
+    int64_t addend = -1;     // descriptor whose A holds this one's X
+    uint64_t off_a = 0, off_b = 0, off_h = 0, off_aux = 0;
+  };
+  std::vector<Desc> desc;  // large descriptors in launch order
   struct Bucket {
     int L;
-    std::vector<uint32_t> idx;
+    size_t d0, nd;
     uint64_t max_chunk;
+    bool any_b_full, any_addend;
   };
   std::vector<Bucket> large;
   uint64_t arena_bytes = 0;
-  std::vector<uint64_t> arena_off;  // per job (large only)
-  int small_L = 0;                  // largest L among the small jobs
+  int small_L = 0;  // largest L among the small jobs
 };
 
-// Scratch bound of one group of same-length products in a batch.
+// Scratch bound of one group of same-length descriptors in a batch.
 static const uint64_t BATCH_ARENA_CAP = 4ull << 30;
 
-static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
+static int unit_log_n(const Unit& u) {
+  if (u.la == 0 || u.lb == 0) return -1;
+  return log2_ceil(4 * u.nout - 1);
+}
+
+// share: let products with the same operand b borrow one spectrum (a batch
+// plan lays out a shape without pointers and never shares).
+static int layout_batch(const Unit* units, size_t n, BatchLayout& B, bool share) {
   std::vector<int> Ls(n);
   for (size_t i = 0; i < n; i++) {
-    if (jobs[i].la == 0 || jobs[i].lb == 0) { Ls[i] = -1; continue; }
-    int L = log2_ceil(4 * (uint64_t)jobs[i].la + 4 * (uint64_t)jobs[i].lb - 1);
-    if (L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32 in batch");
-    Ls[i] = L;
+    Ls[i] = unit_log_n(units[i]);
+    if (Ls[i] > 32) return fail(PIMUL_EINVAL, "transform length above 2^32 in batch");
   }
-  B.arena_off.assign(n, 0);
   std::vector<std::vector<uint32_t>> byL(33);
   for (size_t i = 0; i < n; i++) {
     if (Ls[i] < 0) continue;
+    if (Ls[i] <= SMALL_LOG_MAX && units[i].la2) return fail(PIMUL_EINVAL, "a sum of products below 2^13 in the pass pipeline");
     if (Ls[i] <= SMALL_LOG_MAX) {
       B.small.push_back((uint32_t)i);
       if (Ls[i] > B.small_L) B.small_L = Ls[i];
@@ -1237,30 +1319,96 @@ static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
     B.small.clear();
     for (int L = SMALL_LOG_MAX; L >= 0; L--) B.small.insert(B.small.end(), sb[L].begin(), sb[L].end());
   }
-  // Large products of one length run as groups of at most 65535 (grid.y)
-  // whose scratch fits BATCH_ARENA_CAP; groups run one after another on the
-  // stream, so they all reuse the same arena.
+  // Groups of one length: at most 65535 descriptors (grid.y) whose scratch
+  // fits BATCH_ARENA_CAP; groups run one after another on the stream, so
+  // they all reuse the same arena.
   uint64_t arena = 0;
   for (int L = 32; L > SMALL_LOG_MAX; L--) {
     if (byL[L].empty()) continue;
+    const uint64_t N = 1ull << L;
     size_t s = 0;
     while (s < byL[L].size()) {
-      BatchLayout::Bucket bk;
-      bk.L = L;
-      bk.max_chunk = 0;
-      uint64_t off = 0;
-      for (size_t k = s; k < byL[L].size() && bk.idx.size() < 65535; k++) {
-        uint32_t i = byL[L][k];
-        const uint64_t need = scratch_bytes(jobs[i].la, jobs[i].lb, false);
-        if (!bk.idx.empty() && off + need > BATCH_ARENA_CAP) break;
-        bk.idx.push_back(i);
-        bk.max_chunk = std::max<uint64_t>(bk.max_chunk, n_chunks(n_windows(jobs[i].la, jobs[i].lb)));
-        B.arena_off[i] = off;
-        off += need;
+      BatchLayout::Bucket bk{L, B.desc.size(), 0, 0, false, false};
+      // the group's units: descriptor count and a scratch bound (no sharing)
+      uint64_t bound = 0;
+      size_t e = s;
+      for (; e < byL[L].size(); e++) {
+        const Unit& u = units[byL[L][e]];
+        const size_t nd = u.la2 ? 2 : 1;
+        const uint64_t need = round256(N * 8) * 2 * nd + round256(n_windows_out(u.nout) * 8) +
+                              round256(aux_bytes_for(n_windows_out(u.nout)));
+        if (e > s && (bk.nd + nd > 65535 || bound + need > BATCH_ARENA_CAP)) break;
+        bk.nd += nd;
+        bound += need;
       }
-      s += bk.idx.size();
+      // descriptors; the first of several with the same b owns its spectrum
+      std::unordered_map<const uint64_t*, std::vector<size_t>> by_b;
+      for (size_t k = s; k < e; k++) {
+        const uint32_t ui = byL[L][k];
+        const Unit& u = units[ui];
+        BatchLayout::Desc d1;
+        d1.unit = ui;
+        d1.second = false;
+        d1.flags = 0;
+        B.desc.push_back(d1);
+        const size_t i1 = B.desc.size() - 1;
+        const bool sq1 = u.a == u.b && u.la == u.lb;
+        if (share && !sq1) by_b[u.b].push_back(i1);
+        if (u.la2) {
+          BatchLayout::Desc d2;
+          d2.unit = ui;
+          d2.second = true;
+          d2.flags = JF_ADDEND;
+          B.desc.push_back(d2);
+          const size_t i2 = B.desc.size() - 1;
+          B.desc[i1].addend = (int64_t)i2;
+          if (share) by_b[u.b2].push_back(i2);
+          bk.any_addend = true;
+        }
+      }
+      for (auto& kv : by_b) {
+        std::vector<size_t>& v = kv.second;
+        // same array and same length
+        std::unordered_map<uint64_t, size_t> owner_of;
+        for (size_t di : v) {
+          const BatchLayout::Desc& d = B.desc[di];
+          const uint64_t lb = d.second ? units[d.unit].lb2 : units[d.unit].lb;
+          auto it = owner_of.find(lb);
+          if (it == owner_of.end()) {
+            owner_of.emplace(lb, di);
+          } else {
+            B.desc[di].flags |= JF_B_SHARED;
+            B.desc[di].owner = (int64_t)it->second;
+            B.desc[it->second].flags |= JF_B_FULL;
+          }
+        }
+      }
+      // an addend needs b's full spectrum; scratch offsets
+      uint64_t off = 0;
+      for (size_t di = bk.d0; di < bk.d0 + bk.nd; di++) {
+        BatchLayout::Desc& d = B.desc[di];
+        const Unit& u = units[d.unit];
+        if ((d.flags & JF_ADDEND) && !(d.flags & JF_B_SHARED)) d.flags |= JF_B_FULL;
+        if (d.flags & JF_B_FULL) bk.any_b_full = true;
+        const bool sq = !d.second && u.a == u.b && u.la == u.lb;
+        d.off_a = off;
+        off += round256(N * 8);
+        if (!sq && !(d.flags & JF_B_SHARED)) {
+          d.off_b = off;
+          off += round256(N * 8);
+        }
+        if (!d.second) {
+          const uint64_t nwin = n_windows_out(u.nout);
+          d.off_h = off;
+          off += round256(nwin * 8);
+          d.off_aux = off;
+          off += round256(aux_bytes_for(nwin));
+          bk.max_chunk = std::max<uint64_t>(bk.max_chunk, n_chunks(nwin));
+        }
+      }
       arena = std::max(arena, off);
-      B.large.push_back(std::move(bk));
+      B.large.push_back(bk);
+      s = e;
     }
   }
   B.arena_bytes = arena;
@@ -1269,17 +1417,35 @@ static int layout_batch(const pimul_job* jobs, size_t n, BatchLayout& B) {
 
 // Host images of the device descriptors, in launch order: small jobs first,
 // then each large bucket.
-static void fill_descriptors(const pimul_job* jobs, const BatchLayout& B, uint8_t* arena, SmallJob* sd, Job* ld) {
+static void fill_descriptors(const Unit* units, const BatchLayout& B, uint8_t* arena, SmallJob* sd, Job* ld) {
   size_t k = 0;
   for (uint32_t i : B.small)
-    sd[k++] = SmallJob{jobs[i].a, jobs[i].b, jobs[i].out, (uint32_t)jobs[i].la, (uint32_t)jobs[i].lb};
-  k = 0;
-  for (const auto& bk : B.large)
-    for (uint32_t i : bk.idx) {
-      Job J{jobs[i].a, jobs[i].b, jobs[i].out, nullptr, nullptr, nullptr, nullptr, jobs[i].la, jobs[i].lb};
-      carve_scratch(J, arena + B.arena_off[i], false);
-      ld[k++] = J;
+    sd[k++] = SmallJob{units[i].a, units[i].b, units[i].out, (uint32_t)units[i].la, (uint32_t)units[i].lb};
+  for (size_t di = 0; di < B.desc.size(); di++) {
+    const BatchLayout::Desc& d = B.desc[di];
+    const Unit& u = units[d.unit];
+    Job J{};
+    if (d.second) {
+      J.a = u.a2, J.la = u.la2, J.b = u.b2, J.lb = u.lb2;
+      J.out = nullptr;
+      J.nout = u.la2 + u.lb2;
+    } else {
+      J.a = u.a, J.la = u.la, J.b = u.b, J.lb = u.lb;
+      J.out = u.out;
+      J.nout = u.nout;
     }
+    J.flags = d.flags;
+    const bool sq = !d.second && u.a == u.b && u.la == u.lb;
+    J.A = reinterpret_cast<uint64_t*>(arena + d.off_a);
+    if (d.flags & JF_B_SHARED)
+      J.B = reinterpret_cast<uint64_t*>(arena + B.desc[d.owner].off_b);
+    else
+      J.B = sq ? nullptr : reinterpret_cast<uint64_t*>(arena + d.off_b);
+    J.H = d.second ? nullptr : reinterpret_cast<uint64_t*>(arena + d.off_h);
+    J.aux = d.second ? nullptr : arena + d.off_aux;
+    J.X = d.addend >= 0 ? reinterpret_cast<const uint64_t*>(arena + B.desc[d.addend].off_a) : nullptr;
+    ld[di] = J;
+  }
 }
 
 static void launch_batch(const Launcher& X, const BatchLayout& B, const SmallJob* d_small, const Job* d_large) {
@@ -1292,20 +1458,15 @@ static void launch_batch(const Launcher& X, const BatchLayout& B, const SmallJob
     k_small_mul<<<(unsigned)grid, SMALL_THREADS, small_smem_bytes(B.small_L), X.st>>>(
         d_small, SmallJob{}, (uint32_t)B.small.size(), X.R);
   }
-  size_t off = 0;
-  for (const auto& bk : B.large) {
-    run_large(X, d_large + off, Job{}, (uint32_t)bk.idx.size(), bk.L, bk.max_chunk);
-    off += bk.idx.size();
-  }
+  for (const auto& bk : B.large)
+    run_large(X, d_large + bk.d0, Job{}, (uint32_t)bk.nd, bk.L, bk.max_chunk, bk.any_b_full, bk.any_addend);
 }
 
-static int mul_batch(const pimul_job* jobs, size_t n, cudaStream_t st) {
+static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   BatchLayout B;
-  int rc = layout_batch(jobs, n, B);
+  int rc = layout_batch(units, n, B, share);
   if (rc) return rc;
-  const size_t ns = B.small.size();
-  size_t nl = 0;
-  for (const auto& bk : B.large) nl += bk.idx.size();
+  const size_t ns = B.small.size(), nl = B.desc.size();
   if (ns + nl == 0) return PIMUL_OK;
   const size_t desc_bytes = round256(ns * sizeof(SmallJob)) + nl * sizeof(Job);
   uint8_t* dev = nullptr;
@@ -1319,7 +1480,7 @@ static int mul_batch(const pimul_job* jobs, size_t n, cudaStream_t st) {
   std::vector<uint8_t> host(desc_bytes);
   SmallJob* hs = reinterpret_cast<SmallJob*>(host.data());
   Job* hl = reinterpret_cast<Job*>(host.data() + round256(ns * sizeof(SmallJob)));
-  fill_descriptors(jobs, B, arena, hs, hl);
+  fill_descriptors(units, B, arena, hs, hl);
   e = cudaMemcpyAsync(desc, host.data(), desc_bytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     Launcher X{st, true, g_dev.roots};
@@ -1330,6 +1491,16 @@ static int mul_batch(const pimul_job* jobs, size_t n, cudaStream_t st) {
   cudaFreeAsync(dev, st);
   if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("batch launch: ") + cudaGetErrorString(e));
   return PIMUL_OK;
+}
+
+static Unit unit_of(const pimul_job& j) {
+  return Unit{j.a, j.la, j.b, j.lb, nullptr, 0, nullptr, 0, j.out, j.la + j.lb};
+}
+
+static int mul_batch(const pimul_job* jobs, size_t n, cudaStream_t st) {
+  std::vector<Unit> u(n);
+  for (size_t i = 0; i < n; i++) u[i] = unit_of(jobs[i]);
+  return run_units(u.data(), n, st, true);
 }
 
 // A batch plan: the layout, arena and descriptors of a fixed batch shape,
@@ -1356,12 +1527,13 @@ static int plan_create(const size_t* la, const size_t* lb, size_t n, BatchPlan**
   P->la.assign(la, la + n);
   P->lb.assign(lb, lb + n);
   // shape-only jobs (distinct dummy pointers: no job is a square)
-  std::vector<pimul_job> shape(n);
-  for (size_t i = 0; i < n; i++) shape[i] = pimul_job{nullptr, la[i], (const uint64_t*)(uintptr_t)(8 + 16 * i), lb[i], nullptr};
-  rc = layout_batch(shape.data(), n, P->B);
+  std::vector<Unit> shape(n);
+  for (size_t i = 0; i < n; i++)
+    shape[i] = unit_of(pimul_job{nullptr, la[i], (const uint64_t*)(uintptr_t)(8 + 16 * i), lb[i], nullptr});
+  rc = layout_batch(shape.data(), n, P->B, false);
   if (rc) { delete P; return rc; }
   P->ns = P->B.small.size();
-  for (const auto& bk : P->B.large) P->nl += bk.idx.size();
+  P->nl = P->B.desc.size();
   P->desc_bytes = round256(P->ns * sizeof(SmallJob)) + P->nl * sizeof(Job);
   cudaError_t e = cudaMalloc((void**)&P->dev, round256(P->B.arena_bytes) + P->desc_bytes + 256);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&P->staging, P->desc_bytes + 256);
@@ -1404,7 +1576,9 @@ static int plan_run(BatchPlan* P, const pimul_job* jobs, size_t n, cudaStream_t 
   if (P->launched) CU(cudaEventSynchronize(P->done));
   SmallJob* hs = reinterpret_cast<SmallJob*>(P->staging);
   Job* hl = reinterpret_cast<Job*>(P->staging + round256(P->ns * sizeof(SmallJob)));
-  fill_descriptors(jobs, P->B, P->dev, hs, hl);
+  std::vector<Unit> u(n);
+  for (size_t i = 0; i < n; i++) u[i] = unit_of(jobs[i]);
+  fill_descriptors(u.data(), P->B, P->dev, hs, hl);
   CU(cudaGraphLaunch(P->exec, st));
   CU(cudaEventRecord(P->done, st));
   P->launched = true;
@@ -2340,6 +2514,75 @@ int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
   }
   cudaFreeAsync(d_flag, st);
   if (!rc && h_flag) rc = fail(PIMUL_EINVAL, "carry or borrow out of the top limb (x < y in a subtraction?)");
+  return rc;
+}
+
+int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream) {
+  if (n && !jobs) return fail(PIMUL_EINVAL, "null job list");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  // fused sums go to the pass pipeline; a sum of short products (or with a
+  // square) is two products into scratch and one batched addition
+  std::vector<Unit> units;
+  units.reserve(n);
+  std::vector<size_t> fb;  // jobs computed as two products + an addition
+  std::vector<std::pair<uint64_t*, uint64_t>> zero;  // output limbs above the result
+  uint64_t tmp_words = 0;
+  for (size_t i = 0; i < n; i++) {
+    const pimul_sum_job& j = jobs[i];
+    const bool p1 = j.la1 && j.lb1, p2 = j.la2 && j.lb2;
+    if ((p1 && (!j.a1 || !j.b1)) || (p2 && (!j.a2 || !j.b2))) return fail(PIMUL_EINVAL, "null operand");
+    const uint64_t n1 = p1 ? j.la1 + j.lb1 : 0, n2 = p2 ? j.la2 + j.lb2 : 0;
+    const uint64_t need = std::max(n1, n2) + (p1 && p2 ? 1 : 0);
+    if (j.nout < need) return fail(PIMUL_EINVAL, "nout below max(la1 + lb1, la2 + lb2) + 1");
+    if (j.nout && !j.out) return fail(PIMUL_EINVAL, "null output");
+    if (j.nout > need) zero.emplace_back(j.out + need, j.nout - need);
+    if (!p1 && !p2) continue;
+    if (p1 != p2) {
+      units.push_back(p1 ? Unit{j.a1, j.la1, j.b1, j.lb1, nullptr, 0, nullptr, 0, j.out, n1}
+                         : Unit{j.a2, j.la2, j.b2, j.lb2, nullptr, 0, nullptr, 0, j.out, n2});
+      continue;
+    }
+    const bool sq = (j.a1 == j.b1 && j.la1 == j.lb1) || (j.a2 == j.b2 && j.la2 == j.lb2);
+    const int L = log2_ceil(4 * need - 1);
+    if (L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32 in batch");
+    // fused only when both products already need that transform length (a
+    // shorter second product would run at twice its own length)
+    const bool same = log2_ceil(4 * n1 - 1) == L && log2_ceil(4 * n2 - 1) == L;
+    if (sq || L <= SMALL_LOG_MAX || !same) {
+      fb.push_back(i);
+      tmp_words += n1 + n2;
+      continue;
+    }
+    units.push_back(Unit{j.a1, j.la1, j.b1, j.lb1, j.a2, j.la2, j.b2, j.lb2, j.out, need});
+  }
+  uint8_t* tmp = nullptr;
+  std::vector<pimul_addsub_job> aj;
+  if (!fb.empty()) {
+    CU(cudaMallocAsync((void**)&tmp, tmp_words * 8 + 256, g_dev.pool, st));
+    uint64_t* t = reinterpret_cast<uint64_t*>(tmp + 256);  // first 256 bytes: the overflow flag
+    for (size_t i : fb) {
+      const pimul_sum_job& j = jobs[i];
+      const uint64_t n1 = j.la1 + j.lb1, n2 = j.la2 + j.lb2;
+      units.push_back(Unit{j.a1, j.la1, j.b1, j.lb1, nullptr, 0, nullptr, 0, t, n1});
+      units.push_back(Unit{j.a2, j.la2, j.b2, j.lb2, nullptr, 0, nullptr, 0, t + n1, n2});
+      aj.push_back(pimul_addsub_job{t, n1, t + n1, n2, j.out, std::max(n1, n2) + 1, 0});
+      t += n1 + n2;
+    }
+  }
+  for (const auto& z : zero) {
+    cudaError_t e = cudaMemsetAsync(z.first, 0, z.second * 8, st);
+    if (e != cudaSuccess && !rc) rc = fail(PIMUL_ECUDA, std::string("sum batch: ") + cudaGetErrorString(e));
+  }
+  if (!rc) rc = run_units(units.data(), units.size(), st, true);
+  if (!rc && !aj.empty()) {
+    cudaError_t e = cudaMemsetAsync(tmp, 0, sizeof(int), st);
+    if (e == cudaSuccess) rc = addsub_launch(aj.data(), aj.size(), st, reinterpret_cast<int*>(tmp));
+    else rc = fail(PIMUL_ECUDA, std::string("sum batch: ") + cudaGetErrorString(e));
+  }
+  if (tmp) cudaFreeAsync(tmp, st);
   return rc;
 }
 

@@ -1536,26 +1536,36 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
     double t0 = now_ms();
     const size_t np = nodes.size() / 2;
     const bool need_p = nodes.size() > 2 || keep_p, odd = nodes.size() & 1;
-    // new level: Q, P, T per pair (and the odd node); temporaries T_L Q_R, P_L T_R
+    // new level: Q, P, T per pair (and the odd node).  T = T_L Q_R + P_L T_R
+    // is one fused sum (its spectra added before one inverse transform);
+    // a difference goes through the temporaries T_L Q_R, P_L T_R and a
+    // batched subtraction.  Q_L Q_R and T_L Q_R share Q_R's spectrum.
     size_t lvl_w = 0, tmp_w = 0;
     for (size_t i = 0; i < np; i++) {
       const DNode& L = nodes[2 * i];
       const DNode& R = nodes[2 * i + 1];
       lvl_w += L.qn + R.qn + (need_p ? L.pn + R.pn : 0) + std::max(L.tn + R.qn, L.pn + R.tn) + 1;
-      tmp_w += L.tn + R.qn + L.pn + R.tn;
+      if (L.terms & 1) tmp_w += L.tn + R.qn + L.pn + R.tn;
     }
     if (odd) lvl_w += nodes.back().pn + nodes.back().qn + nodes.back().tn;
     uint64_t* nxt = nullptr;
     uint64_t* tmp = nullptr;
     if (!cu(cudaMallocAsync((void**)&nxt, lvl_w * 8, st))) break;
-    if (!cu(cudaMallocAsync((void**)&tmp, tmp_w * 8, st))) {
+    if (tmp_w && !cu(cudaMallocAsync((void**)&tmp, tmp_w * 8, st))) {
       cudaFreeAsync(nxt, st);
       break;
     }
     std::vector<DNode> next(np + odd);
-    std::vector<pimul_job> mj;
-    std::vector<pimul_addsub_job> aj(np);
-    mj.reserve(np * 4);
+    std::vector<pimul_sum_job> sj;
+    std::vector<pimul_addsub_job> aj;
+    sj.reserve(np * 3);
+    size_t nprod = 0;
+    auto count = [&](size_t la, size_t lb) {
+      uint64_t L2 = 0;
+      while ((1ull << L2) < 4 * (la + lb) - 1) L2++;
+      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+      nprod++;
+    };
     size_t lo = 0, to = 0;
     for (size_t i = 0; i < np; i++) {
       const DNode& L = nodes[2 * i];
@@ -1563,27 +1573,30 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
       DNode& z = next[i];
       z.terms = L.terms + R.terms;
       z.q = nxt + lo, z.qn = L.qn + R.qn, lo += z.qn;
-      mj.push_back(pimul_job{L.q, L.qn, R.q, R.qn, z.q});
+      sj.push_back(pimul_sum_job{L.q, L.qn, R.q, R.qn, nullptr, 0, nullptr, 0, z.q, z.qn});
+      count(L.qn, R.qn);
       if (need_p) {
         z.p = nxt + lo, z.pn = L.pn + R.pn, lo += z.pn;
-        mj.push_back(pimul_job{L.p, L.pn, R.p, R.pn, z.p});
+        sj.push_back(pimul_sum_job{L.p, L.pn, R.p, R.pn, nullptr, 0, nullptr, 0, z.p, z.pn});
+        count(L.pn, R.pn);
       } else {
         z.p = nullptr, z.pn = 0;
       }
-      uint64_t* tq = tmp + to;
-      to += L.tn + R.qn;
-      uint64_t* pt = tmp + to;
-      to += L.pn + R.tn;
-      mj.push_back(pimul_job{L.t, L.tn, R.q, R.qn, tq});
-      mj.push_back(pimul_job{L.p, L.pn, R.t, R.tn, pt});
       z.tn = std::max(L.tn + R.qn, L.pn + R.tn) + 1;
       z.t = nxt + lo, lo += z.tn;
-      aj[i] = pimul_addsub_job{tq, L.tn + R.qn, pt, L.pn + R.tn, z.t, z.tn, (int)(L.terms & 1)};
-    }
-    for (const pimul_job& j : mj) {
-      uint64_t L2 = 0;
-      while ((1ull << L2) < 4 * (j.la + j.lb) - 1) L2++;
-      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+      count(L.tn, R.qn);
+      count(L.pn, R.tn);
+      if (!(L.terms & 1)) {
+        sj.push_back(pimul_sum_job{L.t, L.tn, R.q, R.qn, L.p, L.pn, R.t, R.tn, z.t, z.tn});
+      } else {
+        uint64_t* tq = tmp + to;
+        to += L.tn + R.qn;
+        uint64_t* pt = tmp + to;
+        to += L.pn + R.tn;
+        sj.push_back(pimul_sum_job{L.t, L.tn, R.q, R.qn, nullptr, 0, nullptr, 0, tq, L.tn + R.qn});
+        sj.push_back(pimul_sum_job{L.p, L.pn, R.t, R.tn, nullptr, 0, nullptr, 0, pt, L.pn + R.tn});
+        aj.push_back(pimul_addsub_job{tq, L.tn + R.qn, pt, L.pn + R.tn, z.t, z.tn, 1});
+      }
     }
     if (odd) {
       const DNode& o = nodes.back();
@@ -1596,11 +1609,11 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
       cu(cudaMemcpyAsync(z.q, o.q, o.qn * 8, cudaMemcpyDeviceToDevice, st));
       cu(cudaMemcpyAsync(z.t, o.t, o.tn * 8, cudaMemcpyDeviceToDevice, st));
     }
-    g_ntt_calls.fetch_add(mj.size(), std::memory_order_relaxed);
+    g_ntt_calls.fetch_add(nprod, std::memory_order_relaxed);
     double t1 = now_ms();
-    if (!rc) rc = pimul_mul_batch(mj.data(), mj.size(), st);
-    if (!rc) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
-    cudaFreeAsync(tmp, st);
+    if (!rc) rc = pimul_sum_batch(sj.data(), sj.size(), st);
+    if (!rc && !aj.empty()) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
+    if (tmp) cudaFreeAsync(tmp, st);
     for (uint64_t* a : Lv.arenas) cudaFreeAsync(a, st);
     Lv.arenas.assign(1, nxt);
     // trimmed lengths of the new level
@@ -1623,6 +1636,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
         z.tn = got[k++];
       }
     }
+    if (getenv("PIMUL_PI_TIMING") && !next.empty())
+      fprintf(stderr, "[pimul]   level: %zu pairs, %zu products, top Q %zu limbs, %.1f ms\n", np, nprod,
+              next[0].qn, t2 - t1);
     nodes.swap(next);
     g_batch_levels.fetch_add(1, std::memory_order_relaxed);
     g_bt[1] += t2 - t1;
@@ -1639,7 +1655,13 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
 // computed on the device) if a leaf breaks the static signs.
 static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep) {
   const uint64_t nleaf = (b - a + leaf - 1) / leaf;
-  const size_t nseg = nleaf >= 64 ? 4 : 1;
+  // four equal segments (Q and T of a range do not depend on where it is
+  // split, so neither do the results)
+  std::vector<uint64_t> seg_lo{0};
+  if (nleaf >= 64)
+    for (uint64_t w : {1, 2, 3}) seg_lo.push_back(nleaf * w / 4);
+  seg_lo.push_back(nleaf);
+  const size_t nseg = seg_lo.size() - 1;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
   std::vector<std::vector<PQT>> seg_leaves(nseg);
@@ -1669,7 +1691,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   });
   double tl = 0;
   for (size_t sgi = 0; sgi < nseg; sgi++) {
-    const uint64_t l0 = nleaf * sgi / nseg, l1 = nleaf * (sgi + 1) / nseg;
+    const uint64_t l0 = seg_lo[sgi], l1 = seg_lo[sgi + 1];
     std::vector<PQT> lv(l1 - l0);
     std::vector<uint64_t> tv(l1 - l0);
     double t0 = now_ms();
