@@ -618,7 +618,7 @@ def run_pi(args):
         t0 = time.perf_counter()
         sb, binfo = pm.pi_chudnovsky_batched(D, args.leaf_terms)
         bwall = time.perf_counter() - t0
-        batched = {"wall_s": round(bwall, 3), "leaf_terms": args.leaf_terms or 32,
+        batched = {"wall_s": round(bwall, 3), "leaf_terms": args.leaf_terms or "auto (at most 32, per quarter of the terms)",
                    "phases_ms": {k: round(v, 1) for k, v in binfo.items() if k.endswith("_ms")},
                    "gpu_products": binfo["ntt_products"], "batched_levels": binfo["batched_levels"],
                    "sha256": hashlib.sha256(sb.encode()).hexdigest()}
@@ -802,7 +802,8 @@ def main():
     ap.add_argument("--algorithm", choices=["chudnovsky", "gl", "both"], default="chudnovsky")
     ap.add_argument("--pi-mode", choices=["plain", "batched", "both"], default="both",
                     help="Chudnovsky binary splitting: one GPU call per product, level-batched, or both")
-    ap.add_argument("--leaf-terms", type=int, default=0, help="terms per host-split leaf (0 = 32)")
+    ap.add_argument("--leaf-terms", type=int, default=0,
+                    help="terms per host-split leaf (0 = chosen per quarter of the terms, at most 32)")
     ap.add_argument("--gl-backend", choices=["plain", "served"], default="plain",
                     help="Gauss-Legendre products: one pimul_mul call each, or through the served form")
     ap.add_argument("--gl-sqrt", choices=["reference", "newton"], default="reference",

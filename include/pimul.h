@@ -103,8 +103,10 @@ typedef struct pimul_job {
  * Batched form: n independent products on device buffers in one call
  * (asynchronous on `stream`, NULL = the calling thread's stream).  Products
  * are grouped by transform length: up to 2^12 one CTA per product in a
- * persistent kernel, longer ones one launch per pass for the whole group.
- * Each out[i] is written exactly as pimul_mul_device would write it.
+ * persistent kernel, longer ones one launch per pass for the whole group;
+ * products of one length whose operand b is the same array (same pointer
+ * and length) compute b's transform once.  Each out[i] is written exactly
+ * as pimul_mul_device would write it.
  *
  * Replaces: the independent mul_mag calls of one binary-splitting level
  * (crates/pi-core/src/algorithm/chudnovsky.rs:399-413, run through
@@ -256,18 +258,22 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
 
 /*
  * Batched, device-resident form of pimul_pi_chudnovsky.  The binary
- * splitting runs level by level: leaves of leaf_terms terms (0 = 32) are
- * split on host threads and uploaded once; every level above keeps P, Q and
- * T in HBM, with all of the level's products (T_L Q_R, P_L T_R, Q_L Q_R,
- * P_L P_R for every neighbouring pair) in one pimul_mul_batch call, the T
- * sums in one pimul_addsub_batch call and the trimmed lengths from
- * pimul_top_limbs; only the root's Q and T return to the host.  The decimal
- * conversion is level-batched with its nodes in HBM (pimul_to_decimal); its divisors and
- * reciprocals, sqrt(10005) (by a multiplication-only Newton iteration) and
- * the decimal scale are computed beside the splitting.  Optional outputs:
- * phase_ms[3] as above; gpu_products = products sent to the GPU (batched and
- * plain); levels = batched splitting levels; ntt_hist33[L] = products with
- * transform 2^L.  The digits are identical to pimul_pi_chudnovsky's.
+ * splitting runs level by level: leaves of leaf_terms terms (0: chosen per
+ * quarter of the terms, at most 32, so that each level's products fill
+ * their transform lengths) are split on host threads and uploaded once;
+ * every level above keeps P, Q and T in HBM, with all of the level's
+ * products in one pimul_sum_batch call (Q_L Q_R, P_L P_R, and T_L Q_R +
+ * P_L T_R as one fused sum; Q_L Q_R and T_L Q_R share Q_R's transform) and
+ * the trimmed lengths from pimul_top_limbs.  The root's Q and T stay in HBM
+ * for the final assembly (a Newton reciprocal of A Q + T on the device) and
+ * the decimal conversion (level-batched with its nodes in HBM, as
+ * pimul_to_decimal); only the digits return to the host.  The conversion's
+ * divisors and reciprocals, sqrt(10005) (by a multiplication-only Newton
+ * iteration) and the decimal scale are computed beside the splitting.
+ * Optional outputs: phase_ms[3] as above; gpu_products = products sent to
+ * the GPU (batched and plain); levels = batched splitting levels;
+ * ntt_hist33[L] = products with transform 2^L.  The digits are identical to
+ * pimul_pi_chudnovsky's.
  *
  * Replaces: crates/pi-core/src/algorithm/chudnovsky.rs:75 Chudnovsky::compute,
  * whose binary splitting (chudnovsky.rs:377-413) issues each level's

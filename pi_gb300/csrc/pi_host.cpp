@@ -1647,6 +1647,20 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
   return rc;
 }
 
+// Leaf size chosen per term range (pimul_pi_chudnovsky_batched with
+// leaf_terms = 0).  A node of m terms near k has about m (3 log2 k +
+// log2(C^3 / 24)) bits of Q, and every level doubles m, so the products of
+// the first level (2 leaves, 2 m Q-bits in 16-bit coefficients) set the
+// fill of every transform above it: leaves of at most 4096 / (bits per term
+// + 1) terms keep those products within 512 coefficients (and all higher
+// ones within their power of two) instead of just over it.  Capped at 32,
+// where the host's leaf cost starts to grow.
+static const uint64_t LEAF_AUTO = ~0ull;
+static uint64_t auto_leaf(uint64_t k_hi) {
+  const double bits = 3.0 * std::log2((double)std::max<uint64_t>(k_hi, 2)) + std::log2(10939058860032000.0) + 1.0;
+  return std::max<uint64_t>(8, std::min<uint64_t>(32, (uint64_t)(4096.0 / bits)));
+}
+
 // Device-resident splitting over leaves [0, n): the leaves are computed by
 // host threads segment by segment while a GPU thread reduces the previous
 // segment to its root; the segment roots are then merged on the device and
@@ -1654,14 +1668,13 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
 // (keep->nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
 // computed on the device) if a leaf breaks the static signs.
 static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep) {
-  const uint64_t nleaf = (b - a + leaf - 1) / leaf;
-  // four equal segments (Q and T of a range do not depend on where it is
-  // split, so neither do the results)
-  std::vector<uint64_t> seg_lo{0};
-  if (nleaf >= 64)
-    for (uint64_t w : {1, 2, 3}) seg_lo.push_back(nleaf * w / 4);
-  seg_lo.push_back(nleaf);
-  const size_t nseg = seg_lo.size() - 1;
+  // four equal term ranges, each with its own leaf size (Q and T of a range
+  // do not depend on where it is split, so neither do the results)
+  const size_t nseg = (b - a) / 32 >= 64 ? 4 : 1;
+  std::vector<uint64_t> seg_k(nseg + 1), seg_leaf(nseg);
+  for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (b - a) * s / nseg;
+  seg_k[nseg] = b;
+  for (size_t s = 0; s < nseg; s++) seg_leaf[s] = leaf == LEAF_AUTO ? auto_leaf(seg_k[s + 1]) : leaf;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
   std::vector<std::vector<PQT>> seg_leaves(nseg);
@@ -1691,13 +1704,14 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   });
   double tl = 0;
   for (size_t sgi = 0; sgi < nseg; sgi++) {
-    const uint64_t l0 = seg_lo[sgi], l1 = seg_lo[sgi + 1];
-    std::vector<PQT> lv(l1 - l0);
-    std::vector<uint64_t> tv(l1 - l0);
+    const uint64_t k0 = seg_k[sgi], k1 = seg_k[sgi + 1], lf = seg_leaf[sgi];
+    const uint64_t nl = (k1 - k0 + lf - 1) / lf;
+    std::vector<PQT> lv(nl);
+    std::vector<uint64_t> tv(nl);
     double t0 = now_ms();
-    parallel_for(l1 - l0, [&](size_t lo, size_t hi) {
+    parallel_for(nl, [&](size_t lo, size_t hi) {
       for (size_t i = lo; i < hi; i++) {
-        const uint64_t ka = a + (l0 + i) * leaf, kb = std::min(b, ka + leaf);
+        const uint64_t ka = k0 + i * lf, kb = std::min(k1, ka + lf);
         lv[i] = split(ka, kb, 4);
         tv[i] = kb - ka;
       }
@@ -1750,7 +1764,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
 }
 
 static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep = nullptr) {
-  const uint64_t nleaf = (b - a + leaf - 1) / leaf;
+  const uint64_t nleaf = (b - a + (leaf == LEAF_AUTO ? 32 : leaf) - 1) / (leaf == LEAF_AUTO ? 32 : leaf);
   for (double& x : g_bt) x = 0;
   g_leaf_ms = 0;
   // device-resident levels (every range obeys the static signs; a leaf that
@@ -1760,6 +1774,7 @@ static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int
     report_split("binary splitting (device-resident levels)");
     if (rc != PIMUL_EINVAL) return rc;
   }
+  if (leaf == LEAF_AUTO) leaf = 32;
   std::vector<PQT> nodes(nleaf);
   double t0 = now_ms();
   parallel_for(nleaf, [&](size_t lo, size_t hi) {
@@ -2152,7 +2167,7 @@ extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size
 extern "C" int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms,
                                            double* phase_ms, uint64_t* gpu_products, uint64_t* levels,
                                            uint64_t* ntt_hist33) {
-  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : 32, phase_ms, gpu_products,
+  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : LEAF_AUTO, phase_ms, gpu_products,
                       ntt_hist33);
   if (levels) *levels = g_batch_levels.load();
   return rc;
