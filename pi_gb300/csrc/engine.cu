@@ -363,12 +363,14 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const 
 // and 845-853), first inverse pass; the result overwrites b's array.  A
 // square transforms and squares a's array in place; with b's full spectrum
 // in B (shared or owned) the last pass is skipped and the result goes to A.
-template <int R>
+// EXT = false: plain products only (no shared spectrum, no addend), the
+// form every single product and every batch without those roles uses.
+template <int R, bool EXT>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
   constexpr int BC = TILE_LOG - R;
   const Job J = job_of(jobs, one);
-  if (J.flags & JF_ADDEND) return;
-  const bool sq = is_square(J), spec = b_spectrum(J);
+  if (EXT && (J.flags & JF_ADDEND)) return;
+  const bool sq = is_square(J), spec = EXT && b_spectrum(J);
   const uint64_t* cin = sq ? J.A : J.B;
   uint64_t* cout = sq || spec ? J.A : J.B;
   const uint64_t* a = J.A;
@@ -390,7 +392,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
     uint64_t x = sm[spad(lin)];
     uint64_t y = sq ? x : a[off + lin];
     uint64_t p = gl::mul(x, y);
-    if (X) p = gl::add(p, X[off + lin]);
+    if (EXT && X) p = gl::add(p, X[off + lin]);
     sm[spad(lin)] = gl::mul(p, ninv);
   }
   __syncthreads();
@@ -807,7 +809,8 @@ static cudaError_t set_smem_attrs_r() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_col_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd_last<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return e;
 }
 
@@ -1182,7 +1185,11 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
   }
   {
     KTimer kt(K_POINTWISE, X.st, X.stats);
-    PIMUL_DISPATCH_R(rl, (k_mid<RR><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, ninv, X.R)));
+    if (any_b_full || any_addend) {
+      PIMUL_DISPATCH_R(rl, (k_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, ninv, X.R)));
+    } else {
+      PIMUL_DISPATCH_R(rl, (k_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, ninv, X.R)));
+    }
   }
   int consumed = L - rl;
   for (int p = pl.np - 2; p >= 1; p--) {
