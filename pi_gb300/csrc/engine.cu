@@ -655,38 +655,66 @@ struct SmallJob {
   uint32_t la, lb;
 };
 
-__device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* smA, uint64_t* smB) {
+// Threads per product: an eighth of the transform length (one radix-8
+// butterfly per thread and round), at least a warp; SMALL_THREADS / G
+// products of one length run side by side in a CTA.
+__host__ __device__ __forceinline__ int small_group_threads(int L) {
+  const int g = (1 << L) / 8;
+  return g < 32 ? 32 : (g > SMALL_THREADS ? SMALL_THREADS : g);
+}
+// Dynamic shared memory of a CTA running products of length 2^L.
+__host__ __device__ __forceinline__ size_t small_cta_smem(int L) {
+  return (size_t)(SMALL_THREADS / small_group_threads(L)) * small_smem_bytes(L);
+}
+
+// count (<= SMALL_THREADS / G(L)) consecutive jobs of length 2^L from first.
+struct SmallChunk {
+  uint32_t first, count;
+  int L;
+};
+
+// One product by the G threads of a group (gtid = thread in the group, gw0
+// = the CTA-wide index of the group's first warp).  Inactive groups run
+// every barrier and ballot with no work, so a CTA's groups stay in step.
+__device__ void small_multiply(const SmallJob& job, bool active, int L, const Roots& R, uint64_t* smA, uint64_t* smB,
+                               int gtid, int G, int gw0) {
   const int tid = threadIdx.x;
-  const uint32_t la = job.la, lb = job.lb;
-  const uint32_t n_out = 4 * la + 4 * lb - 1;
-  int L = 0;
-  while ((1u << L) < n_out) L++;
+  const uint32_t la = active ? job.la : 0, lb = active ? job.lb : 0;
   const uint32_t N = 1u << L;
-  const bool square = job.a == job.b && la == lb;
-  for (uint32_t i = tid; i < N; i += SMALL_THREADS) {
-    uint32_t l = i >> 2, sh = 16 * (i & 3);
-    smA[spad(i)] = l < la ? (job.a[l] >> sh) & 0xFFFF : 0;
-    if (!square) smB[spad(i)] = l < lb ? (job.b[l] >> sh) & 0xFFFF : 0;
+  const uint32_t n_out = active ? 4 * la + 4 * lb - 1 : 0;
+  const bool square = active && job.a == job.b && la == lb;
+  // one limb per thread and step -> its four 16-bit coefficients
+  for (uint32_t l = gtid; active && l < N / 4; l += G) {
+    const uint64_t xa = l < la ? job.a[l] : 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) smA[spad(4 * l + q)] = (xa >> (16 * q)) & 0xFFFF;
+    if (!square) {
+      const uint64_t xb = l < lb ? job.b[l] : 0;
+#pragma unroll
+      for (int q = 0; q < 4; q++) smB[spad(4 * l + q)] = (xb >> (16 * q)) & 0xFFFF;
+    }
   }
   __syncthreads();
   TileGeom g{L, 0, 0};
-  tile_dft_fwd(smA, g, R, tid, SMALL_THREADS);
-  if (!square) tile_dft_fwd(smB, g, R, tid, SMALL_THREADS);
-  // times N^-1 = 2^(-L) = 2^(192 - L)
-  const uint64_t ninv = gl::pow(2, 192 - L);
-  for (uint32_t i = tid; i < N; i += SMALL_THREADS) {
+  const int rt = active ? gtid : (1 << 30);  // an inactive group's rounds do no work
+  tile_dft_fwd(smA, g, R, rt, G);
+  tile_dft_fwd(smB, g, R, square ? (1 << 30) : rt, G);
+  // times N^-1 = 2^(-L): with 2^96 = -1 and 2^64 = 2^32 - 1 (mod p),
+  // 2^(-L) = -2^(96-L) = p - (2^(64-L) - 2^(32-L)) for 1 <= L <= 32
+  const uint64_t ninv = gl::P - ((1ull << (64 - L)) - (1ull << (32 - L)));
+  for (uint32_t i = gtid; active && i < N; i += G) {
     uint64_t x = smA[spad(i)];
     uint64_t y = square ? x : smB[spad(i)];
     smA[spad(i)] = gl::mul(gl::mul(x, y), ninv);
   }
   __syncthreads();
-  tile_dft_inv(smA, g, R, tid, SMALL_THREADS);
-  // carry: windows of 16 coefficients, one per thread (N/16 <= 256)
+  tile_dft_inv(smA, g, R, rt, G);
+  // carry: windows of 16 coefficients, one per thread (N/16 <= G)
   const uint32_t nwin = (n_out + 15) / 16, nl = la + lb;
   uint64_t* sH = smB;  // reuse: B no longer needed
   __shared__ uint32_t sA[SMALL_THREADS / 32], sBm[SMALL_THREADS / 32];
   Win v{{0, 0, 0, 0}, 0};
-  const uint32_t w = tid;
+  const uint32_t w = gtid;
   if (w < nwin) {
     uint64_t c[16];
 #pragma unroll
@@ -711,7 +739,7 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
   if ((tid & 31) == 0) { sA[tid >> 5] = A; sBm[tid >> 5] = Bm; }
   __syncthreads();
   uint32_t cin = 0;
-  for (int k = 0; k < (tid >> 5); k++) {
+  for (int k = gw0; k < (tid >> 5); k++) {
     uint64_t s = (uint64_t)sA[k] + sBm[k] + cin;
     cin = (uint32_t)(s >> 32);
   }
@@ -728,18 +756,29 @@ __device__ void small_multiply(const SmallJob& job, const Roots& R, uint64_t* sm
   }
 }
 
-// One CTA per product; with a device job list the CTAs stride over it
-// (a persistent kernel over a size-sorted bucket).
-__global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* jobs, SmallJob one, uint32_t njobs,
-                                                               Roots R) {
+// Chunks of same-length products; with device lists the CTAs stride over
+// the chunks (a persistent kernel over a size-sorted batch).  jobs ==
+// nullptr: the single product `one`.
+__global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* jobs, const SmallChunk* chunks,
+                                                               SmallJob one, uint32_t nchunks, Roots R) {
   extern __shared__ uint64_t sm[];
-  for (uint32_t k = blockIdx.x; k < njobs; k += gridDim.x) {
-    const SmallJob job = jobs ? jobs[k] : one;
-    const uint32_t n_out = 4 * job.la + 4 * job.lb - 1;
-    int L = 0;
-    while ((1u << L) < n_out) L++;
-    uint32_t N = 1u << L;
-    small_multiply(job, R, sm, sm + spad(N));
+  for (uint32_t k = blockIdx.x; k < nchunks; k += gridDim.x) {
+    SmallChunk ch;
+    if (chunks) {
+      ch = chunks[k];
+    } else {
+      const uint32_t n_out = 4 * one.la + 4 * one.lb - 1;
+      int L = 0;
+      while ((1u << L) < n_out) L++;
+      ch = SmallChunk{0, 1, L};
+    }
+    const int G = small_group_threads(ch.L);
+    const uint32_t grp = threadIdx.x / G;
+    const bool active = grp < ch.count;
+    const SmallJob job = active ? (jobs ? jobs[ch.first + grp] : one) : SmallJob{};
+    const uint32_t sp = spad(1u << ch.L);
+    uint64_t* base = sm + (size_t)grp * 2 * sp;
+    small_multiply(job, active, ch.L, R, base, base + sp, (int)(threadIdx.x % G), G, (int)(grp * G / 32));
     __syncthreads();
   }
 }
@@ -820,7 +859,7 @@ static cudaError_t set_smem_attrs() {
   if (e == cudaSuccess) e = set_smem_attrs_r<8>();
   if (e == cudaSuccess) e = set_smem_attrs_r<9>();
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem_bytes(SMALL_LOG_MAX));
+    e = cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_cta_smem(SMALL_LOG_MAX));
   return e;
 }
 
@@ -1225,7 +1264,7 @@ static int mul_device(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uin
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
     {
       KTimer kt(K_SMALL, st, true);
-      k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(nullptr, job, 1, R);
+      k_small_mul<<<1, SMALL_THREADS, small_cta_smem(z.L), st>>>(nullptr, nullptr, job, 1, R);
     }
     CU(cudaGetLastError());
     return PIMUL_OK;
@@ -1290,6 +1329,8 @@ struct BatchLayout {
   std::vector<Bucket> large;
   uint64_t arena_bytes = 0;
   int small_L = 0;  // largest L among the small jobs
+  std::vector<SmallChunk> chunks;  // the small jobs in same-length chunks
+  size_t small_smem = 0;           // dynamic shared memory of their CTAs
 };
 
 // Scratch bound of one group of same-length descriptors in a batch.
@@ -1324,7 +1365,13 @@ static int layout_batch(const Unit* units, size_t n, BatchLayout& B, bool share)
     std::vector<std::vector<uint32_t>> sb(SMALL_LOG_MAX + 1);
     for (uint32_t i : B.small) sb[Ls[i]].push_back(i);
     B.small.clear();
-    for (int L = SMALL_LOG_MAX; L >= 0; L--) B.small.insert(B.small.end(), sb[L].begin(), sb[L].end());
+    for (int L = SMALL_LOG_MAX; L >= 0; L--) {
+      const uint32_t per = SMALL_THREADS / small_group_threads(L);
+      for (size_t k = 0; k < sb[L].size(); k += per)
+        B.chunks.push_back(SmallChunk{(uint32_t)(B.small.size() + k), (uint32_t)std::min<size_t>(per, sb[L].size() - k), L});
+      if (!sb[L].empty()) B.small_smem = std::max(B.small_smem, small_cta_smem(L));
+      B.small.insert(B.small.end(), sb[L].begin(), sb[L].end());
+    }
   }
   // Groups of one length: at most 65535 descriptors (grid.y) whose scratch
   // fits BATCH_ARENA_CAP; groups run one after another on the stream, so
@@ -1424,10 +1471,17 @@ static int layout_batch(const Unit* units, size_t n, BatchLayout& B, bool share)
 
 // Host images of the device descriptors, in launch order: small jobs first,
 // then each large bucket.
+// Bytes of the small jobs' descriptors and chunks at the head of the image.
+static size_t small_desc_bytes(const BatchLayout& B) {
+  return round256(B.small.size() * sizeof(SmallJob)) + round256(B.chunks.size() * sizeof(SmallChunk));
+}
+
 static void fill_descriptors(const Unit* units, const BatchLayout& B, uint8_t* arena, SmallJob* sd, Job* ld) {
   size_t k = 0;
   for (uint32_t i : B.small)
     sd[k++] = SmallJob{units[i].a, units[i].b, units[i].out, (uint32_t)units[i].la, (uint32_t)units[i].lb};
+  SmallChunk* sc = reinterpret_cast<SmallChunk*>(reinterpret_cast<uint8_t*>(sd) + round256(B.small.size() * sizeof(SmallJob)));
+  for (size_t c = 0; c < B.chunks.size(); c++) sc[c] = B.chunks[c];
   for (size_t di = 0; di < B.desc.size(); di++) {
     const BatchLayout::Desc& d = B.desc[di];
     const Unit& u = units[d.unit];
@@ -1460,10 +1514,12 @@ static void launch_batch(const Launcher& X, const BatchLayout& B, const SmallJob
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_dev.device);
     uint64_t grid = (uint64_t)sms * (uint64_t)g_small_ctas_per_sm.load();
-    if (grid > B.small.size()) grid = B.small.size();
+    if (grid > B.chunks.size()) grid = B.chunks.size();
+    const SmallChunk* d_chunks = reinterpret_cast<const SmallChunk*>(reinterpret_cast<const uint8_t*>(d_small) +
+                                                                     round256(B.small.size() * sizeof(SmallJob)));
     KTimer kt(K_SMALL, X.st, X.stats);
-    k_small_mul<<<(unsigned)grid, SMALL_THREADS, small_smem_bytes(B.small_L), X.st>>>(
-        d_small, SmallJob{}, (uint32_t)B.small.size(), X.R);
+    k_small_mul<<<(unsigned)grid, SMALL_THREADS, B.small_smem, X.st>>>(d_small, d_chunks, SmallJob{},
+                                                                      (uint32_t)B.chunks.size(), X.R);
   }
   for (const auto& bk : B.large)
     run_large(X, d_large + bk.d0, Job{}, (uint32_t)bk.nd, bk.L, bk.max_chunk, bk.any_b_full, bk.any_addend);
@@ -1475,7 +1531,7 @@ static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   if (rc) return rc;
   const size_t ns = B.small.size(), nl = B.desc.size();
   if (ns + nl == 0) return PIMUL_OK;
-  const size_t desc_bytes = round256(ns * sizeof(SmallJob)) + nl * sizeof(Job);
+  const size_t desc_bytes = small_desc_bytes(B) + nl * sizeof(Job);
   uint8_t* dev = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&dev, round256(B.arena_bytes) + desc_bytes, g_dev.pool, st);
   if (e != cudaSuccess) {
@@ -1486,12 +1542,12 @@ static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   uint8_t* desc = dev + round256(B.arena_bytes);
   std::vector<uint8_t> host(desc_bytes);
   SmallJob* hs = reinterpret_cast<SmallJob*>(host.data());
-  Job* hl = reinterpret_cast<Job*>(host.data() + round256(ns * sizeof(SmallJob)));
+  Job* hl = reinterpret_cast<Job*>(host.data() + small_desc_bytes(B));
   fill_descriptors(units, B, arena, hs, hl);
   e = cudaMemcpyAsync(desc, host.data(), desc_bytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     Launcher X{st, true, g_dev.roots};
-    launch_batch(X, B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + round256(ns * sizeof(SmallJob))));
+    launch_batch(X, B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + small_desc_bytes(B)));
     e = cudaGetLastError();
   }
   // the host image must outlive the copy (pageable source: staged before return)
@@ -1541,7 +1597,7 @@ static int plan_create(const size_t* la, const size_t* lb, size_t n, BatchPlan**
   if (rc) { delete P; return rc; }
   P->ns = P->B.small.size();
   P->nl = P->B.desc.size();
-  P->desc_bytes = round256(P->ns * sizeof(SmallJob)) + P->nl * sizeof(Job);
+  P->desc_bytes = small_desc_bytes(P->B) + P->nl * sizeof(Job);
   cudaError_t e = cudaMalloc((void**)&P->dev, round256(P->B.arena_bytes) + P->desc_bytes + 256);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&P->staging, P->desc_bytes + 256);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming);
@@ -1553,8 +1609,7 @@ static int plan_create(const size_t* la, const size_t* lb, size_t n, BatchPlan**
     if (e == cudaSuccess) {
       cudaMemcpyAsync(desc, P->staging, P->desc_bytes, cudaMemcpyHostToDevice, cs);
       Launcher X{cs, false, g_dev.roots};
-      launch_batch(X, P->B, reinterpret_cast<SmallJob*>(desc),
-                   reinterpret_cast<Job*>(desc + round256(P->ns * sizeof(SmallJob))));
+      launch_batch(X, P->B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + small_desc_bytes(P->B)));
       e = cudaStreamEndCapture(cs, &P->graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&P->exec, P->graph, 0);
@@ -1582,7 +1637,7 @@ static int plan_run(BatchPlan* P, const pimul_job* jobs, size_t n, cudaStream_t 
   // the previous run's descriptor copy must have read the staging image
   if (P->launched) CU(cudaEventSynchronize(P->done));
   SmallJob* hs = reinterpret_cast<SmallJob*>(P->staging);
-  Job* hl = reinterpret_cast<Job*>(P->staging + round256(P->ns * sizeof(SmallJob)));
+  Job* hl = reinterpret_cast<Job*>(P->staging + small_desc_bytes(P->B));
   std::vector<Unit> u(n);
   for (size_t i = 0; i < n; i++) u[i] = unit_of(jobs[i]);
   fill_descriptors(u.data(), P->B, P->dev, hs, hl);
@@ -2809,7 +2864,7 @@ static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* 
   const Roots& R = nd->roots;
   if (z.L <= SMALL_LOG_MAX) {  // whole product in one CTA's shared memory: no scratch
     SmallJob job{d_a, d_b, d_out, (uint32_t)la, (uint32_t)lb};
-    k_small_mul<<<1, SMALL_THREADS, small_smem_bytes(z.L), st>>>(nullptr, job, 1, R);
+    k_small_mul<<<1, SMALL_THREADS, small_cta_smem(z.L), st>>>(nullptr, nullptr, job, 1, R);
     CU(cudaGetLastError());
     return PIMUL_OK;
   }
