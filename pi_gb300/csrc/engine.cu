@@ -18,6 +18,7 @@
 #include <thread>
 #include <unordered_map>
 #include <atomic>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -1540,11 +1541,12 @@ static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   }
   uint8_t* arena = dev;
   uint8_t* desc = dev + round256(B.arena_bytes);
-  std::vector<uint8_t> host(desc_bytes);
-  SmallJob* hs = reinterpret_cast<SmallJob*>(host.data());
-  Job* hl = reinterpret_cast<Job*>(host.data() + small_desc_bytes(B));
+  std::unique_ptr<uint8_t[]> host(new uint8_t[desc_bytes]);  // every used byte is written below
+  SmallJob* hs = reinterpret_cast<SmallJob*>(host.get());
+  Job* hl = reinterpret_cast<Job*>(host.get() + small_desc_bytes(B));
   fill_descriptors(units, B, arena, hs, hl);
-  e = cudaMemcpyAsync(desc, host.data(), desc_bytes, cudaMemcpyHostToDevice, st);
+  // descriptors of a large batch go up through the staged copy
+  if (host_to_device(desc, host.get(), desc_bytes, st)) e = cudaErrorUnknown;
   if (e == cudaSuccess) {
     Launcher X{st, true, g_dev.roots};
     launch_batch(X, B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + small_desc_bytes(B)));
@@ -2361,7 +2363,7 @@ __host__ __device__ __forceinline__ uint64_t as_nchunk(uint64_t nout) {
 }
 __host__ __device__ __forceinline__ uint64_t as_aux_bytes(uint64_t nout) {
   uint64_t nc = as_nchunk(nout);
-  return round_up_u64(nc * (AS_THREADS / 32) * 8 + 2 * nc + 16, 256);
+  return round_up_u64(nc * (AS_THREADS / 32) * 8 + 2 * nc + 16, 16);
 }
 
 __global__ void __launch_bounds__(AS_THREADS) k_as_local(const AsJob* jobs) {
@@ -2469,7 +2471,7 @@ __global__ void __launch_bounds__(AS_THREADS) k_as_apply(const AsJob* jobs, int*
   const uint8_t* chunk_cin = J.aux + nchunk * (AS_THREADS / 32) * 8 + nchunk;
   const uint64_t w = (uint64_t)blockIdx.x * AS_THREADS + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t cin = chunk_cin[blockIdx.x];
+  uint32_t cin = nchunk == 1 ? 0 : chunk_cin[blockIdx.x];  // one chunk: no scan ran
   const uint64_t wbase = (uint64_t)blockIdx.x * (AS_THREADS / 32);
   for (int k = 0; k < warp; k++) {
     uint64_t s = (uint64_t)masks[2 * (wbase + k)] + masks[2 * (wbase + k) + 1] + cin;
@@ -2535,13 +2537,13 @@ static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st
                  (uint32_t)(jobs[i].sub != 0), (uint32_t)(jobs[i].sub != PIMUL_SUB_MOD)};
     off += as_aux_bytes(jobs[i].nout);
   }
-  e = cudaMemcpyAsync(dev, h.data(), n * sizeof(AsJob), cudaMemcpyHostToDevice, st);
+  if (host_to_device(dev, h.data(), n * sizeof(AsJob), st)) e = cudaErrorUnknown;
   if (e == cudaSuccess) {
     const AsJob* dj = reinterpret_cast<const AsJob*>(dev);
     for (size_t j0 = 0; j0 < n; j0 += 65535) {
       const unsigned nj = (unsigned)std::min<size_t>(65535, n - j0);
       k_as_local<<<dim3((unsigned)max_chunk, nj), AS_THREADS, 0, st>>>(dj + j0);
-      k_as_scan<<<nj, 1024, 0, st>>>(dj + j0);
+      if (max_chunk > 1) k_as_scan<<<nj, 1024, 0, st>>>(dj + j0);
       k_as_apply<<<dim3((unsigned)max_chunk, nj), AS_THREADS, 0, st>>>(dj + j0, d_overflow);
     }
     e = cudaGetLastError();
@@ -2665,8 +2667,12 @@ int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n,
   uint8_t* dev = nullptr;
   CU(cudaMallocAsync((void**)&dev, 3 * bytes, g_dev.pool, st));
   std::vector<uint64_t> hn(lens, lens + n);
-  CU(cudaMemcpyAsync(dev, arrays, n * 8, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(dev + bytes, hn.data(), n * 8, cudaMemcpyHostToDevice, st));
+  if (!rc) rc = host_to_device(dev, arrays, n * 8, st);
+  if (!rc) rc = host_to_device(dev + bytes, hn.data(), n * 8, st);
+  if (rc) {
+    cudaFreeAsync(dev, st);
+    return rc;
+  }
   CU(cudaMemsetAsync(dev + 2 * bytes, 0, n * 8, st));
   for (size_t j0 = 0; j0 < n; j0 += 65535) {
     const unsigned nj = (unsigned)std::min<size_t>(65535, n - j0);
@@ -2676,9 +2682,9 @@ int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n,
   }
   CU(cudaGetLastError());
   std::vector<uint64_t> res(n);
-  CU(cudaMemcpyAsync(res.data(), dev + 2 * bytes, n * 8, cudaMemcpyDeviceToHost, st));
-  CU(cudaStreamSynchronize(st));
+  rc = device_to_host(res.data(), dev + 2 * bytes, n * 8, st);
   cudaFreeAsync(dev, st);
+  if (rc) return rc;
   for (size_t i = 0; i < n; i++) out_lens[i] = (size_t)res[i];
   return PIMUL_OK;
 }

@@ -1560,10 +1560,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
     std::vector<pimul_addsub_job> aj;
     sj.reserve(np * 3);
     size_t nprod = 0;
+    uint64_t hist[33] = {0};
     auto count = [&](size_t la, size_t lb) {
-      uint64_t L2 = 0;
-      while ((1ull << L2) < 4 * (la + lb) - 1) L2++;
-      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+      hist[64 - __builtin_clzll(4 * (la + lb) - 2)]++;  // ceil(log2(4 (la + lb) - 1))
       nprod++;
     };
     size_t lo = 0, to = 0;
@@ -1610,9 +1609,13 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
       cu(cudaMemcpyAsync(z.t, o.t, o.tn * 8, cudaMemcpyDeviceToDevice, st));
     }
     g_ntt_calls.fetch_add(nprod, std::memory_order_relaxed);
+    for (int L2 = 0; L2 < 33; L2++)
+      if (hist[L2]) g_ntt_hist[L2].fetch_add(hist[L2], std::memory_order_relaxed);
     double t1 = now_ms();
     if (!rc) rc = pimul_sum_batch(sj.data(), sj.size(), st);
+    const double t_sum = now_ms();
     if (!rc && !aj.empty()) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
+    const double t_as = now_ms();
     if (tmp) cudaFreeAsync(tmp, st);
     for (uint64_t* a : Lv.arenas) cudaFreeAsync(a, st);
     Lv.arenas.assign(1, nxt);
@@ -1626,6 +1629,7 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
       arrs.push_back(z.t), lens.push_back(z.tn);
     }
     std::vector<size_t> got(arrs.size());
+    const double t_arr = now_ms();
     if (!rc) rc = pimul_top_limbs(arrs.data(), lens.data(), arrs.size(), got.data(), st);
     double t2 = now_ms();
     if (!rc) {
@@ -1637,8 +1641,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
       }
     }
     if (getenv("PIMUL_PI_TIMING") && !next.empty())
-      fprintf(stderr, "[pimul]   level: %zu pairs, %zu products, top Q %zu limbs, %.1f ms\n", np, nprod,
-              next[0].qn, t2 - t1);
+      fprintf(stderr, "[pimul]   level: %zu pairs, %zu products, top Q %zu limbs, %.1f ms (build %.1f, sum call %.1f, "
+              "subtract %.1f, lengths %.1f + %.1f)\n", np, nprod, next[0].qn, t2 - t1, t1 - t0, t_sum - t1,
+              t_as - t_sum, t_arr - t_as, t2 - t_arr);
     nodes.swap(next);
     g_batch_levels.fetch_add(1, std::memory_order_relaxed);
     g_bt[1] += t2 - t1;
