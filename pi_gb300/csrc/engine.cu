@@ -785,11 +785,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* 
 }
 
 // ------------------------------------------------------------------ host side
-static int log2_ceil(uint64_t x) {
-  int L = 0;
-  while ((1ull << L) < x) L++;
-  return L;
-}
+static int log2_ceil(uint64_t x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
 
 // Host copies of the root tables: lo, hi, w12, level tables (in this order).
 constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (2u << LVL_MAX);

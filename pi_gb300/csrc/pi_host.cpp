@@ -1673,9 +1673,10 @@ static uint64_t auto_leaf(uint64_t k_hi) {
 // (keep->nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
 // computed on the device) if a leaf breaks the static signs.
 static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep) {
-  // four equal term ranges, each with its own leaf size (Q and T of a range
-  // do not depend on where it is split, so neither do the results)
-  const size_t nseg = (b - a) / 32 >= 64 ? 4 : 1;
+  // eight equal term ranges, each with its own leaf size: the GPU starts
+  // after an eighth of the leaves (Q and T of a range do not depend on
+  // where it is split, so neither do the results)
+  const size_t nseg = (b - a) / 32 >= 128 ? 8 : 1;
   std::vector<uint64_t> seg_k(nseg + 1), seg_leaf(nseg);
   for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (b - a) * s / nseg;
   seg_k[nseg] = b;
