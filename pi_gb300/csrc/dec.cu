@@ -434,9 +434,9 @@ std::vector<uint64_t> host_recip_pow2(const std::vector<uint64_t>& d, size_t s) 
 
 }  // namespace
 
-int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, size_t tn, uint64_t A,
-                          const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
-                          double* ms) {
+int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const uint64_t* dT, size_t tn,
+                          uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec,
+                          uint64_t** d_ip, size_t* ipn, double* ms) {
   if (!dQ || !qn || (tn && !dT) || !wm || !wl || !d_ip || !ipn || !A) return PIMUL_EINVAL;
   *d_ip = nullptr;
   *ipn = 0;
@@ -450,21 +450,23 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, siz
     return rc == PIMUL_OK;
   };
   const size_t nl = (prec + 192 + 63) / 64;
-  // den window: limbs [s0, qn + 1) of A Q - |T| (carries from below s0 are
-  // dropped: a relative error below 2^-(64 nl))
-  const size_t dn = qn + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
-  if (tn > dn) return PIMUL_EINVAL;
+  // den window: limbs [s0, qt + 1) of A Q - |T| (qt = Q's length with its
+  // offset; carries from below s0 are dropped: a relative error below
+  // 2^-(64 nl)); the stored parts of Q and |T| must reach down to s0
+  const size_t qt = qn + q_off, tt = tn + t_off;
+  const size_t dn = qt + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
+  if (tt > dn || s0 < q_off || (tt > s0 && s0 < t_off) || qn < std::min(qt, nl)) return PIMUL_EINVAL;
   uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr, *dnorm = nullptr, *consts = nullptr;
   if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn)) || (rc = Ar.get(&dnorm, nl)) ||
       (rc = Ar.get(&consts, 1)))
     return rc;
-  k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(dQ + s0, qn - s0, A,
-                                                                                             lo, hi);
+  k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(
+      dQ + (s0 - q_off), qt - s0, A, lo, hi);
   if (!cu(cudaGetLastError())) return rc;
   pimul_addsub_job j1{lo, wn, hi, wn, den, wn, 0};
   if ((rc = pimul_addsub_batch(&j1, 1, st))) return rc;
-  if (tn > s0) {
-    pimul_addsub_job j2{den, wn, dT + s0, tn - s0, den, wn, 1};
+  if (tt > s0) {
+    pimul_addsub_job j2{den, wn, dT + (s0 - t_off), tt - s0, den, wn, 1};
     if ((rc = pimul_addsub_batch(&j2, 1, st))) return rc;
   }
   Ar.put(lo);
@@ -530,7 +532,7 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, siz
   if (rc) return rc;
   const double t1 = now_ms();
   // ip = floor(W Q_top R 2^e2)
-  const size_t lq = std::min(qn, nl);
+  const size_t lq = std::min(qt, nl);
   uint64_t *X1 = nullptr, *X2 = nullptr, *dW = nullptr;
   if ((rc = Ar.get(&X1, lq + nl + 1))) return rc;
   if ((rc = pimul_mul_device(dQ + (qn - lq), lq, Y, nl + 1, X1, st))) return rc;
@@ -538,8 +540,8 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, siz
   if ((rc = Ar.get(&dW, wl)) || (rc = Ar.get(&X2, wl + nl + 1))) return rc;
   if ((rc = pimul::host_to_device(dW, wm, wl * 8, st))) return rc;
   if ((rc = pimul_mul_device(dW, wl, X1 + lq, nl + 1, X2, st))) return rc;
-  // W Q / den ~ X2 2^(64 lq) * 2^(we + 64 (qn - lq) - 128 nl - ed)
-  const int64_t e2 = we + 64 * (int64_t)qn - 128 * (int64_t)nl - ed;
+  // W Q / den ~ X2 2^(64 lq) * 2^(we + 64 (qt - lq) - 128 nl - ed)
+  const int64_t e2 = we + 64 * (int64_t)qt - 128 * (int64_t)nl - ed;
   const int64_t ip_bits = 64 * (int64_t)(wl + nl + 1) + e2;
   if (e2 > 0 || ip_bits <= 0) return PIMUL_EINVAL;
   const size_t n_ip = (size_t)((ip_bits + 63) / 64);

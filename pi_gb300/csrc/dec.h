@@ -32,12 +32,15 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
 // up to the decimal scaling of util.rs:25-83): *d_ip (allocated here, freed
 // by the caller with cudaFree) receives floor(W Q / (A Q - |T|)) in *ipn
 // limbs, with W = wm 2^we (the constant 426880 sqrt(10005) times the
-// decimal scale, host limbs).  The quotient comes from the top prec + 192
-// bits of each operand and a Newton reciprocal run on the device, so its
-// relative error is below 2^-(prec + 100).  ms (optional, 2 entries):
-// reciprocal, products.
-int final_assembly_device(const uint64_t* dQ, size_t qn, const uint64_t* dT, size_t tn, uint64_t A,
-                          const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
-                          double* ms);
+// decimal scale, host limbs) and Q = dQ[0..qn) 2^(64 q_off), |T| = dT[0..tn)
+// 2^(64 t_off).  The quotient comes from the top prec + 192 bits of each
+// operand and a Newton reciprocal run on the device, so its relative error
+// is below 2^-(prec + 100).  ms (optional, 2 entries): reciprocal, products.
+int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const uint64_t* dT, size_t tn,
+                          uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec,
+                          uint64_t** d_ip, size_t* ipn, double* ms);
+
+// Top limbs of Q (and of A Q + |T|) that final_assembly_device reads.
+inline uint64_t final_assembly_top_limbs(uint64_t prec) { return (prec + 192 + 63) / 64 + 3; }
 
 }  // namespace pidec

@@ -1525,14 +1525,14 @@ static int dev_upload_leaves(const std::vector<PQT>& leaves, const std::vector<u
 
 // Levels until one node is left; keep_p keeps P of the last node (needed
 // when it is merged again later).
-static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
+static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1) {
   int rc = PIMUL_OK;
   auto cu = [&](cudaError_t e) {
     if (e != cudaSuccess && !rc) rc = PIMUL_ECUDA;
     return e == cudaSuccess;
   };
   std::vector<DNode>& nodes = Lv.nodes;
-  while (!rc && nodes.size() > 1) {
+  while (!rc && nodes.size() > stop) {
     double t0 = now_ms();
     const size_t np = nodes.size() / 2;
     const bool need_p = nodes.size() > 2 || keep_p, odd = nodes.size() & 1;
@@ -1652,6 +1652,86 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p) {
   return rc;
 }
 
+// The root's Q and |T| left on the device for the final assembly; with
+// top_limbs set (the number of top limbs of Q and of A Q + T the consumer
+// reads) the root is Q_hi 2^(64 q_off), |T|_hi 2^(64 t_off), from operands
+// cut to their top limbs.
+struct DevRoot {
+  DLevel lvl;
+  uint64_t top_limbs = 0;
+  uint64_t q_off = 0, t_off = 0;
+};
+
+// Root merge from the operands' top m + 2 limbs (m = top_limbs + 2): the
+// cut parts move Q = Q_L Q_R and T = T_L Q_R +- P_L T_R by less than
+// 2^-(64 m) relative (every dropped limb is below the kept m + 2 of its
+// operand, and P_L T_R is the smaller term), and the products are about
+// half as long: the root's 2^30-point transforms of a 10^9-digit run
+// become 2^29-point ones.  T's two products drop the same total D of limbs
+// so that their sum stays aligned; Q_R is cut the same way in Q and T
+// (one shared spectrum).
+static int dev_root_truncated(DLevel& Lv, cudaStream_t st, uint64_t top_limbs, DevRoot* keep) {
+  const DNode& L = Lv.nodes[0];
+  const DNode& R = Lv.nodes[1];
+  const uint64_t m2 = top_limbs + 4;
+  auto cut = [&](uint64_t n) { return n > m2 ? n - m2 : 0; };
+  const uint64_t dxq = cut(L.qn), dyq = cut(R.qn), dx1 = cut(L.tn);
+  const uint64_t D = dx1 + dyq;
+  const uint64_t dy2 = std::min<uint64_t>(D, R.tn ? R.tn - 1 : 0), dx2 = D - dy2;
+  if (!L.pn || !R.tn || !L.tn || dx2 + 1 > L.pn) return PIMUL_OK;  // leave the root to dev_reduce
+  int rc = PIMUL_OK;
+  const uint64_t qn = (L.qn - dxq) + (R.qn - dyq);
+  const uint64_t n1 = (L.tn - dx1) + (R.qn - dyq), n2 = (L.pn - dx2) + (R.tn - dy2);
+  const uint64_t tn = std::max(n1, n2) + 1;
+  uint64_t* arena = nullptr;
+  uint64_t* tmp = nullptr;
+  const bool diff = (L.terms & 1) != 0;
+  if (cudaMallocAsync((void**)&arena, (qn + tn) * 8, st) != cudaSuccess) return PIMUL_ENOMEM;
+  if (diff && cudaMallocAsync((void**)&tmp, (n1 + n2) * 8, st) != cudaSuccess) {
+    cudaFreeAsync(arena, st);
+    return PIMUL_ENOMEM;
+  }
+  DNode z{};
+  z.terms = L.terms + R.terms;
+  z.q = arena, z.qn = qn;
+  z.t = arena + qn, z.tn = tn;
+  z.p = nullptr, z.pn = 0;
+  std::vector<pimul_sum_job> sj;
+  sj.push_back(pimul_sum_job{L.q + dxq, L.qn - dxq, R.q + dyq, R.qn - dyq, nullptr, 0, nullptr, 0, z.q, qn});
+  if (!diff) {
+    sj.push_back(pimul_sum_job{L.t + dx1, L.tn - dx1, R.q + dyq, R.qn - dyq, L.p + dx2, L.pn - dx2, R.t + dy2,
+                               R.tn - dy2, z.t, tn});
+  } else {
+    sj.push_back(pimul_sum_job{L.t + dx1, L.tn - dx1, R.q + dyq, R.qn - dyq, nullptr, 0, nullptr, 0, tmp, n1});
+    sj.push_back(pimul_sum_job{L.p + dx2, L.pn - dx2, R.t + dy2, R.tn - dy2, nullptr, 0, nullptr, 0, tmp + n1, n2});
+  }
+  g_ntt_calls.fetch_add(3, std::memory_order_relaxed);
+  rc = pimul_sum_batch(sj.data(), sj.size(), st);
+  if (!rc && diff) {
+    pimul_addsub_job aj{tmp, n1, tmp + n1, n2, z.t, tn, 1};
+    rc = pimul_addsub_batch(&aj, 1, st);
+  }
+  if (tmp) cudaFreeAsync(tmp, st);
+  if (rc) {
+    cudaFreeAsync(arena, st);
+    return rc;
+  }
+  const uint64_t* arrs[2] = {z.q, z.t};
+  size_t lens[2] = {z.qn, z.tn}, got[2] = {0, 0};
+  rc = pimul_top_limbs(arrs, lens, 2, got, st);
+  if (rc) {
+    cudaFreeAsync(arena, st);
+    return rc;
+  }
+  z.qn = got[0], z.tn = got[1];
+  for (uint64_t* ar : Lv.arenas) cudaFreeAsync(ar, st);
+  Lv.arenas.assign(1, arena);
+  Lv.nodes.assign(1, z);
+  keep->q_off = dxq + dyq;
+  keep->t_off = D;
+  return PIMUL_OK;
+}
+
 // Leaf size chosen per term range (pimul_pi_chudnovsky_batched with
 // leaf_terms = 0).  A node of m terms near k has about m (3 log2 k +
 // log2(C^3 / 24)) bits of Q, and every level doubles m, so the products of
@@ -1670,15 +1750,17 @@ static uint64_t auto_leaf(uint64_t k_hi) {
 // host threads segment by segment while a GPU thread reduces the previous
 // segment to its root; the segment roots are then merged on the device and
 // only the final Q and |T| come back, or, with keep, stay on the device
-// (keep->nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
+// (keep->lvl.nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
 // computed on the device) if a leaf breaks the static signs.
-static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep) {
+static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DevRoot* keep) {
   // eight equal term ranges, each with its own leaf size: the GPU starts
   // after an eighth of the leaves (Q and T of a range do not depend on
   // where it is split, so neither do the results)
   const size_t nseg = (b - a) / 32 >= 128 ? 8 : 1;
   std::vector<uint64_t> seg_k(nseg + 1), seg_leaf(nseg);
-  for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (b - a) * s / nseg;
+  // even term counts before every boundary, so that merged left nodes have
+  // an even number of terms and their T is a sum (fused on the device)
+  for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (((b - a) * s / nseg) & ~1ull);
   seg_k[nseg] = b;
   for (size_t s = 0; s < nseg; s++) seg_leaf[s] = leaf == LEAF_AUTO ? auto_leaf(seg_k[s + 1]) : leaf;
   cudaStream_t st = nullptr;
@@ -1744,11 +1826,15 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     for (const DNode& n : r.nodes) top.nodes.push_back(n);
     top.arenas.insert(top.arenas.end(), r.arenas.begin(), r.arenas.end());
   }
+  if (keep && keep->top_limbs && !rc) {
+    rc = dev_reduce(top, st, true, 2);
+    if (!rc && top.nodes.size() == 2) rc = dev_root_truncated(top, st, keep->top_limbs, keep);
+  }
   if (!rc) rc = dev_reduce(top, st, false);
   if (!rc && keep) {
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
-    *keep = std::move(top);
+    keep->lvl = std::move(top);
     return PIMUL_OK;
   }
   if (!rc) {
@@ -1769,7 +1855,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   return rc;
 }
 
-static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DLevel* keep = nullptr) {
+static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DevRoot* keep = nullptr) {
   const uint64_t nleaf = (b - a + (leaf == LEAF_AUTO ? 32 : leaf) - 1) / (leaf == LEAF_AUTO ? 32 : leaf);
   for (double& x : g_bt) x = 0;
   g_leaf_ms = 0;
@@ -2050,30 +2136,31 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     if (!leaf_terms) scale_th.join();
   };
   Int q, t;
-  DLevel droot;  // the root's Q and |T| when they stay on the device
+  DevRoot droot;  // the root's Q and |T| when they stay on the device
+  droot.top_limbs = pidec::final_assembly_top_limbs(prec);
   int brc = PIMUL_OK;
   if (leaf_terms)
     brc = split_root_batched(1, n_terms + 1, leaf_terms, q, t, &droot);
   else
     split_root(1, n_terms + 1, q, t);
   if (brc) {
-    for (uint64_t* ar : droot.arenas) cudaFree(ar);
+    for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
     join_sqrt();
     join_scale();
     plan_th.join();
     return brc;
   }
   double t1 = now_ms();
-  if (!droot.nodes.empty()) {
+  if (!droot.lvl.nodes.empty()) {
     // final assembly and decimal conversion without leaving the device
     join_sqrt();
-    const DNode& r = droot.nodes[0];
+    const DNode& r = droot.lvl.nodes[0];
     uint64_t* d_ip = nullptr;
     size_t ipn = 0;
     double fms[2] = {0, 0};
-    int frc = pidec::final_assembly_device(r.q, r.qn, r.t, r.tn, CH_A, W.mant.data(), W.mant.size(), W.exp, prec,
-                                           &d_ip, &ipn, fms);
-    for (uint64_t* ar : droot.arenas) cudaFree(ar);
+    int frc = pidec::final_assembly_device(r.q, r.qn, droot.q_off, r.t, r.tn, droot.t_off, CH_A, W.mant.data(),
+                                           W.mant.size(), W.exp, prec, &d_ip, &ipn, fms);
+    for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
     double t2 = now_ms();
     plan_th.join();
     if (!frc) frc = to_decimal_batched_into_dev(d_ip, ipn, out, digits, &dplan);
