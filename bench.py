@@ -338,7 +338,9 @@ def run_gpu(args):
                          "traffic": round(NCU_TRAFFIC_BYTES_PER_WORD * N) if dom == "pass_fwd" else None,
                          "bytes_per_launch": per_launch, "avg_launch_ms": round(avg_ms, 4),
                          "step_achieved": round(step_achieved, 1),
-                         "step_frac": round(step_achieved / peak, 4)},
+                         "step_frac": round(step_achieved / peak, 4),
+                         "binding_unit": "integer ALU pipe, not HBM (ncu: ALU 62-70 % busy, issue 59-67 %, "
+                                         "DRAM 13-35 % of peak; profiles/ntt_pass_kernels_2e29_full.md)"},
             "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ks.items()},
             "gpu_launches": launches,
             "clocks": clk.summary(),
