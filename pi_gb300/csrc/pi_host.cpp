@@ -42,6 +42,7 @@
 
 #include "../../include/pimul.h"
 #include "dec.h"
+#include "leaves.h"
 
 namespace pihost {
 
@@ -1484,45 +1485,6 @@ static void dev_free(DLevel& L, cudaStream_t st) {
   L.nodes.clear();
 }
 
-// One upload of the leaves (|P|, Q, |T| back to back) into a fresh arena.
-static int dev_upload_leaves(const std::vector<PQT>& leaves, const std::vector<uint64_t>& terms, cudaStream_t st,
-                             LevelStaging& S, DLevel& out) {
-  double t0 = now_ms();
-  std::vector<size_t> off(leaves.size() + 1, 0);
-  for (size_t i = 0; i < leaves.size(); i++)
-    off[i + 1] = off[i] + leaves[i].p.m.size() + leaves[i].q.m.size() + leaves[i].t.m.size();
-  int rc = S.host(off.back());
-  if (rc) return rc;
-  uint64_t* arena = nullptr;
-  if (cudaMallocAsync((void**)&arena, std::max<size_t>(off.back(), 1) * 8, st) != cudaSuccess) return PIMUL_ENOMEM;
-  out.arenas.push_back(arena);
-  out.nodes.resize(leaves.size());
-  parallel_for(leaves.size(), [&](size_t lo, size_t hi) {
-    for (size_t i = lo; i < hi; i++) {
-      uint64_t* h = S.h + off[i];
-      const Limbs* parts[3] = {&leaves[i].p.m, &leaves[i].q.m, &leaves[i].t.m};
-      size_t o = 0;
-      for (const Limbs* x : parts) {
-        memcpy(h + o, x->data(), x->size() * 8);
-        o += x->size();
-      }
-      DNode& n = out.nodes[i];
-      n.pn = leaves[i].p.m.size();
-      n.qn = leaves[i].q.m.size();
-      n.tn = leaves[i].t.m.size();
-      n.p = arena + off[i];
-      n.q = n.p + n.pn;
-      n.t = n.q + n.qn;
-      n.terms = terms[i];
-    }
-  });
-  if (cudaMemcpyAsync(arena, S.h, off.back() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) return PIMUL_ECUDA;
-  // the staging buffer is reused by the next upload: wait for this copy
-  if (cudaStreamSynchronize(st) != cudaSuccess) return PIMUL_ECUDA;
-  g_bt[0] += now_ms() - t0;
-  return PIMUL_OK;
-}
-
 // Levels until one node is left; keep_p keeps P of the last node (needed
 // when it is merged again later).
 static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1) {
@@ -1736,22 +1698,23 @@ static int dev_root_truncated(DLevel& Lv, cudaStream_t st, uint64_t top_limbs, D
 // leaf_terms = 0).  A node of m terms near k has about m (3 log2 k +
 // log2(C^3 / 24)) bits of Q, and every level doubles m, so the products of
 // the first level (2 leaves, 2 m Q-bits in 16-bit coefficients) set the
-// fill of every transform above it: leaves of at most 4096 / (bits per term
+// fill of every transform above it: runs of at most 4096 / (bits per term
 // + 1) terms keep those products within 512 coefficients (and all higher
-// ones within their power of two) instead of just over it.  Capped at 32,
-// where the host's leaf cost starts to grow.
+// ones within their power of two) instead of just over it.  The device
+// leaves take two such runs (at most 64 terms).
 static const uint64_t LEAF_AUTO = ~0ull;
 static uint64_t auto_leaf(uint64_t k_hi) {
   const double bits = 3.0 * std::log2((double)std::max<uint64_t>(k_hi, 2)) + std::log2(10939058860032000.0) + 1.0;
   return std::max<uint64_t>(8, std::min<uint64_t>(32, (uint64_t)(4096.0 / bits)));
 }
 
-// Device-resident splitting over leaves [0, n): the leaves are computed by
-// host threads segment by segment while a GPU thread reduces the previous
-// segment to its root; the segment roots are then merged on the device and
-// only the final Q and |T| come back, or, with keep, stay on the device
-// (keep->lvl.nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL (nothing
-// computed on the device) if a leaf breaks the static signs.
+// Device-resident splitting over terms [a, b): segment by segment, the
+// leaves are computed on the device (leaves.cu) into fixed slots and the
+// segment is reduced to its root; the segment roots are then merged on the
+// device and only the final Q and |T| come back, or, with keep, stay on the
+// device (keep->lvl.nodes[0], arenas owned by keep).  Returns PIMUL_EINVAL
+// (the caller then takes the host-staged path) if a leaf breaks the static
+// signs or outgrows its slot, or a leaf is longer than the kernel takes.
 static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DevRoot* keep) {
   // eight equal term ranges, each with its own leaf size: the GPU starts
   // after an eighth of the leaves (Q and T of a range do not depend on
@@ -1762,65 +1725,54 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   // an even number of terms and their T is a sum (fused on the device)
   for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (((b - a) * s / nseg) & ~1ull);
   seg_k[nseg] = b;
-  for (size_t s = 0; s < nseg; s++) seg_leaf[s] = leaf == LEAF_AUTO ? auto_leaf(seg_k[s + 1]) : leaf;
+  for (size_t s = 0; s < nseg; s++) seg_leaf[s] = leaf == LEAF_AUTO ? 2 * auto_leaf(seg_k[s + 1]) : leaf;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
-  std::vector<std::vector<PQT>> seg_leaves(nseg);
-  std::vector<std::vector<uint64_t>> seg_terms(nseg);
   std::vector<DLevel> roots(nseg);
-  std::mutex mu;
-  std::condition_variable cv;
-  size_t ready = 0;
-  bool abort_all = false;
-  int rc_gpu = PIMUL_OK;
-  std::thread gpu([&] {
-    LevelStaging S;
-    for (size_t sgi = 0; sgi < nseg; sgi++) {
-      {
-        std::unique_lock<std::mutex> lk(mu);
-        cv.wait(lk, [&] { return ready > sgi || abort_all; });
-        if (abort_all) return;
-      }
-      int rc = dev_upload_leaves(seg_leaves[sgi], seg_terms[sgi], st, S, roots[sgi]);
-      if (!rc) rc = dev_reduce(roots[sgi], st, true);
-      if (rc) {
-        rc_gpu = rc;
-        return;
-      }
-      std::vector<PQT>().swap(seg_leaves[sgi]);
-    }
-  });
+  int rc = PIMUL_OK;
   double tl = 0;
-  for (size_t sgi = 0; sgi < nseg; sgi++) {
+  for (size_t sgi = 0; sgi < nseg && !rc; sgi++) {
     const uint64_t k0 = seg_k[sgi], k1 = seg_k[sgi + 1], lf = seg_leaf[sgi];
-    const uint64_t nl = (k1 - k0 + lf - 1) / lf;
-    std::vector<PQT> lv(nl);
-    std::vector<uint64_t> tv(nl);
-    double t0 = now_ms();
-    parallel_for(nl, [&](size_t lo, size_t hi) {
-      for (size_t i = lo; i < hi; i++) {
-        const uint64_t ka = k0 + i * lf, kb = std::min(k1, ka + lf);
-        lv[i] = split(ka, kb, 4);
-        tv[i] = kb - ka;
-      }
-    });
-    tl += now_ms() - t0;
-    bool ok = true;
-    for (size_t i = 0; i < lv.size() && ok; i++) ok = lv[i].t.neg && lv[i].p.neg == (bool)(tv[i] & 1);
-    std::lock_guard<std::mutex> lk(mu);
-    if (!ok) {
-      abort_all = true;
-      cv.notify_all();
+    if (lf > pileaf::MAX_TERMS) {
+      rc = PIMUL_EINVAL;
       break;
     }
-    seg_leaves[sgi] = std::move(lv);
-    seg_terms[sgi] = std::move(tv);
-    ready = sgi + 1;
-    cv.notify_all();
+    const uint64_t nl = (k1 - k0 + lf - 1) / lf;
+    double t0 = now_ms();
+    // slots sized from the segment's last full leaf (the largest values),
+    // plus two limbs; a leaf that outgrows its slot is reported, not written
+    const uint64_t kl = k1 - k0 >= lf ? k0 + ((k1 - k0) / lf - 1) * lf : k0;
+    const PQT big = split_leaf(kl, std::min(k1, kl + lf));
+    const uint32_t sp = (uint32_t)big.p.m.size() + 2, sq = (uint32_t)big.q.m.size() + 2,
+                   stt = (uint32_t)big.t.m.size() + 2;
+    uint64_t* arena = nullptr;
+    if (cudaMallocAsync((void**)&arena, std::max<uint64_t>(nl * (sp + sq + stt), 1) * 8, st) != cudaSuccess) {
+      cudaGetLastError();
+      rc = PIMUL_ENOMEM;
+      break;
+    }
+    roots[sgi].arenas.push_back(arena);
+    std::vector<uint32_t> lens(3 * nl);
+    std::vector<uint8_t> signs(nl);
+    rc = pileaf::leaves_device(k0, k1, (uint32_t)lf, (uint32_t)nl, sp, sq, stt, arena, lens.data(), signs.data(), st);
+    tl += now_ms() - t0;
+    if (rc) break;
+    std::vector<DNode>& nodes = roots[sgi].nodes;
+    nodes.resize(nl);
+    for (uint64_t i = 0; i < nl && !rc; i++) {
+      const uint64_t terms = std::min(k1, k0 + (i + 1) * lf) - (k0 + i * lf);
+      // static signs: T < 0 and P of m terms has sign (-1)^m
+      if (!(signs[i] & 2) || (bool)(signs[i] & 1) != (bool)(terms & 1)) rc = PIMUL_EINVAL;
+      DNode& nd = nodes[i];
+      nd.p = arena + i * (sp + sq + stt);
+      nd.q = nd.p + sp;
+      nd.t = nd.q + sq;
+      nd.pn = lens[3 * i], nd.qn = lens[3 * i + 1], nd.tn = lens[3 * i + 2];
+      nd.terms = terms;
+    }
+    if (!rc) rc = dev_reduce(roots[sgi], st, true);
   }
-  gpu.join();
   g_leaf_ms += tl;
-  int rc = abort_all ? PIMUL_EINVAL : rc_gpu;
   DLevel top;
   for (DLevel& r : roots) {
     for (const DNode& n : r.nodes) top.nodes.push_back(n);
