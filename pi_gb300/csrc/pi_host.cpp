@@ -1726,8 +1726,14 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   for (size_t s = 0; s < nseg; s++) seg_k[s] = a + (((b - a) * s / nseg) & ~1ull);
   seg_k[nseg] = b;
   for (size_t s = 0; s < nseg; s++) seg_leaf[s] = leaf == LEAF_AUTO ? 2 * auto_leaf(seg_k[s + 1]) : leaf;
+  // the splitting's stream has the highest priority: the products of the
+  // threads running beside it (sqrt(10005), the decimal scale, the
+  // conversion's divisors) fill the gaps between its levels instead of
+  // slowing them down
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   cudaStream_t st = nullptr;
-  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_hi) != cudaSuccess) return PIMUL_ECUDA;
   std::vector<DLevel> roots(nseg);
   int rc = PIMUL_OK;
   double tl = 0;
