@@ -600,8 +600,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Jo
   seg_p[threadIdx.x] = cp;
   __syncthreads();
   if (threadIdx.x == 0) {
+    // only the first ceil(nchunk / per) segments hold chunks
+    const int used = (int)((nchunk + per - 1) / per);
     uint8_t cin = 0;
-    for (int k = 0; k < SCAN_THREADS; k++) {
+    for (int k = 0; k < used; k++) {
       seg_cin[k] = cin;
       cin = cin ? seg_p[k] : seg_g[k];
     }
@@ -2442,8 +2444,10 @@ __global__ void __launch_bounds__(1024) k_as_scan(const AsJob* jobs) {
   seg_p[threadIdx.x] = cp;
   __syncthreads();
   if (threadIdx.x == 0) {
+    // only the first ceil(nchunk / per) segments hold chunks
+    const int used = (int)((nchunk + per - 1) / per);
     uint8_t cin = 0;
-    for (int k = 0; k < 1024; k++) {
+    for (int k = 0; k < used; k++) {
       seg_cin[k] = cin;
       cin = cin ? seg_p[k] : seg_g[k];
     }
