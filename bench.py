@@ -602,7 +602,8 @@ def run_pi(args):
 
     def gl_run(d, **kw):
         return pm.pi_gauss_legendre(d, backend=kw.get("backend", gl_backend), fast_sqrt=args.gl_sqrt == "newton",
-                                    device_decimal=args.gl_decimal == "device")
+                                    device_decimal=args.gl_decimal == "device",
+                                    device_agm=args.gl_backend == "device")
 
     if args.algorithm == "both":
         gl_run(min(D, 100_000))
@@ -806,8 +807,9 @@ def main():
                     help="Chudnovsky binary splitting: one GPU call per product, level-batched, or both")
     ap.add_argument("--leaf-terms", type=int, default=0,
                     help="terms per host-split leaf (0 = chosen per quarter of the terms, at most 32)")
-    ap.add_argument("--gl-backend", choices=["plain", "served"], default="plain",
-                    help="Gauss-Legendre products: one pimul_mul call each, or through the served form")
+    ap.add_argument("--gl-backend", choices=["plain", "served", "device"], default="plain",
+                    help="Gauss-Legendre products: one pimul_mul call each, through the served form, or the whole "
+                         "iteration on the device in fixed point")
     ap.add_argument("--gl-sqrt", choices=["reference", "newton"], default="reference",
                     help="Gauss-Legendre square roots: the reference's division-based iteration or the "
                          "multiplication-only one (same digits)")

@@ -314,6 +314,11 @@ int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn
  * reference's recursion (util.rs:25-83).  The digits are the same. */
 #define PIMUL_PI_FAST_SQRT 1u
 #define PIMUL_PI_DEVICE_DECIMAL 2u
+/* PIMUL_PI_DEVICE_AGM: the whole iteration on the device in fixed point
+ * (a, b, t in HBM, square roots by a Newton iteration for 1/sqrt(x) carried
+ * from step to step), then the device quotient and decimal conversion; the
+ * backend is not used.  The digits are the same. */
+#define PIMUL_PI_DEVICE_AGM 4u
 int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
                                uint32_t flags, double* phase_ms, uint64_t* ntt_products);
 

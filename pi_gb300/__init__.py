@@ -410,15 +410,16 @@ def to_decimal(limbs, batched: bool = True) -> str:
 
 
 def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sqrt: bool = False,
-                      device_decimal: bool = False):
+                      device_decimal: bool = False, device_agm: bool = False):
     """Digits of pi by the Gauss-Legendre AGM
     (crates/pi-core/src/algorithm/gauss_legendre.rs:61); fast_sqrt takes the
     square roots by a multiplication-only Newton iteration, device_decimal
-    converts with the nodes on the GPU (same digits)."""
+    converts with the nodes on the GPU, device_agm runs the whole iteration
+    on the GPU in fixed point (same digits)."""
     buf = ctypes.create_string_buffer(digits + 1)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
-    flags = (1 if fast_sqrt else 0) | (2 if device_decimal else 0)
+    flags = (1 if fast_sqrt else 0) | (2 if device_decimal else 0) | (4 if device_agm else 0)
     _check(lib().pimul_pi_gauss_legendre_ex(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
                                             ntt_threshold, flags, ph, ctypes.byref(n)))
     return ctypes.string_at(buf, digits).decode("ascii"), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],

@@ -434,6 +434,10 @@ std::vector<uint64_t> host_recip_pow2(const std::vector<uint64_t>& d, size_t s) 
 
 }  // namespace
 
+static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
+                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip,
+                         size_t* ipn, double* ms, double t0);
+
 int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const uint64_t* dT, size_t tn,
                           uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec,
                           uint64_t** d_ip, size_t* ipn, double* ms) {
@@ -456,10 +460,8 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
   const size_t qt = qn + q_off, tt = tn + t_off;
   const size_t dn = qt + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
   if (tt > dn || s0 < q_off || (tt > s0 && s0 < t_off) || qn < std::min(qt, nl)) return PIMUL_EINVAL;
-  uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr, *dnorm = nullptr, *consts = nullptr;
-  if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn)) || (rc = Ar.get(&dnorm, nl)) ||
-      (rc = Ar.get(&consts, 1)))
-    return rc;
+  uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr;
+  if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn))) return rc;
   k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(
       dQ + (s0 - q_off), qt - s0, A, lo, hi);
   if (!cu(cudaGetLastError())) return rc;
@@ -471,6 +473,30 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
   }
   Ar.put(lo);
   Ar.put(hi);
+  // W Q / den with Q's top lq = min(qt, nl) limbs
+  const size_t lq = std::min(qt, nl);
+  return quotient_tail(Ar, den, wn, 64 * (int64_t)s0, dQ + (qn - lq), lq, 64 * (int64_t)(qt - lq), wm, wl, we, prec,
+                       d_ip, ipn, ms, t0);
+}
+
+// floor(W N / D): D = den[0..wn) 2^den_exp on the device, N = n_top[0..lq)
+// 2^n_exp (lq <= nl, its top limbs), W = wm 2^we on the host.  D's top
+// 64 nl bits are normalised, R ~ 2^(128 nl) / D comes from Newton's
+// iteration (precision doubling from 576 bits found on the host), and the
+// quotient is floor(W (N_top R >> 64 lq) 2^e).
+static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
+                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip,
+                         size_t* ipn, double* ms, double t0) {
+  const cudaStream_t st = Ar.st;
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
+    return rc == PIMUL_OK;
+  };
+  const size_t nl = (prec + 192 + 63) / 64;
+  if (!den || !wn || !n_top || !lq || lq > nl || !wm || !wl || !d_ip || !ipn) return PIMUL_EINVAL;
+  uint64_t *dnorm = nullptr, *consts = nullptr;
+  if ((rc = Ar.get(&dnorm, nl)) || (rc = Ar.get(&consts, 1))) return rc;
   // bit length of the window, then dn = its top 64 nl bits
   uint64_t top[3] = {0, 0, 0};
   const size_t nt = std::min<size_t>(3, wn);
@@ -480,12 +506,11 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
   int64_t B = 0;
   for (size_t i = nt; i-- > 0 && !B;)
     if (top[i]) B = 64 * (int64_t)(wn - nt + i) + 64 - __builtin_clzll(top[i]);
-  if (B <= 64 * (int64_t)(wn - nt)) return PIMUL_EINVAL;  // den vanishes at the top: not a Chudnovsky root
+  if (B <= 64 * (int64_t)(wn - nt)) return PIMUL_EINVAL;  // the divisor vanishes in its top limbs
   const int64_t shn = B - 64 * (int64_t)nl;
   k_shr_slots<<<slot_grid(nl, 1), 256, 0, st>>>(den, 0, wn, shn, dnorm, 0, nl, 1);
   if (!cu(cudaGetLastError())) return rc;
-  const int64_t ed = 64 * (int64_t)s0 + shn;  // den ~ dn 2^ed
-  Ar.put(den);
+  const int64_t ed = den_exp + shn;  // D ~ dn 2^ed
   // Newton: Y_(64 m0) from the top limbs of dn on the host
   const size_t m0 = std::min<size_t>(8, nl - 2), k0 = m0 + 2;
   std::vector<uint64_t> dtop(k0);
@@ -531,17 +556,16 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
   }
   if (rc) return rc;
   const double t1 = now_ms();
-  // ip = floor(W Q_top R 2^e2)
-  const size_t lq = std::min(qt, nl);
+  // ip = floor(W N_top R 2^e2)
   uint64_t *X1 = nullptr, *X2 = nullptr, *dW = nullptr;
   if ((rc = Ar.get(&X1, lq + nl + 1))) return rc;
-  if ((rc = pimul_mul_device(dQ + (qn - lq), lq, Y, nl + 1, X1, st))) return rc;
+  if ((rc = pimul_mul_device(n_top, lq, Y, nl + 1, X1, st))) return rc;
   Ar.put(Y);
   if ((rc = Ar.get(&dW, wl)) || (rc = Ar.get(&X2, wl + nl + 1))) return rc;
   if ((rc = pimul::host_to_device(dW, wm, wl * 8, st))) return rc;
   if ((rc = pimul_mul_device(dW, wl, X1 + lq, nl + 1, X2, st))) return rc;
-  // W Q / den ~ X2 2^(64 lq) * 2^(we + 64 (qt - lq) - 128 nl - ed)
-  const int64_t e2 = we + 64 * (int64_t)qt - 128 * (int64_t)nl - ed;
+  // W N / D ~ X2 2^(64 lq) * 2^(we + n_exp - 128 nl - ed)
+  const int64_t e2 = we + 64 * (int64_t)lq + n_exp - 128 * (int64_t)nl - ed;
   const int64_t ip_bits = 64 * (int64_t)(wl + nl + 1) + e2;
   if (e2 > 0 || ip_bits <= 0) return PIMUL_EINVAL;
   const size_t n_ip = (size_t)((ip_bits + 63) / 64);
@@ -578,6 +602,17 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
     ms[1] = now_ms() - t1;
   }
   return PIMUL_OK;
+}
+
+int quotient_device(const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq, int64_t n_exp,
+                    const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
+                    double* ms) {
+  if (!d_ip || !ipn) return PIMUL_EINVAL;
+  *d_ip = nullptr;
+  *ipn = 0;
+  Arena Ar;
+  if (cudaStreamCreateWithFlags(&Ar.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  return quotient_tail(Ar, den, wn, den_exp, n_top, lq, n_exp, wm, wl, we, prec, d_ip, ipn, ms, now_ms());
 }
 
 }  // namespace pidec

@@ -40,6 +40,15 @@ int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const u
                           uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec,
                           uint64_t** d_ip, size_t* ipn, double* ms);
 
+// floor(W N / D) with D = den[0..wn) 2^den_exp and N = n_top[0..lq) 2^n_exp
+// in device memory (ready for use; lq <= (prec + 192 + 63) / 64 top limbs
+// of N, D's top limb nonzero within its top three), W = wm 2^we on the
+// host: the final assembly's Newton reciprocal and products for any
+// quotient.  *d_ip is freed by the caller with cudaFree.
+int quotient_device(const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq, int64_t n_exp,
+                    const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
+                    double* ms);
+
 // Top limbs of Q (and of A Q + |T|) that final_assembly_device reads.
 inline uint64_t final_assembly_top_limbs(uint64_t prec) { return (prec + 192 + 63) / 64 + 3; }
 

@@ -43,6 +43,7 @@
 #include "../../include/pimul.h"
 #include "dec.h"
 #include "leaves.h"
+#include "agm.h"
 
 namespace pihost {
 
@@ -2004,6 +2005,40 @@ extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap
   g_error.store(0);
   const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
   double t0 = now_ms();
+  if (flags & PIMUL_PI_DEVICE_AGM) {
+    // the AGM, the quotient and the conversion on the device; the decimal
+    // scale and the conversion's divisors on threads beside the iteration
+    Flt scale;
+    std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
+    DecPlan dplan;
+    std::thread plan_th([&] { dplan = make_dec_plan(digits + 1); });
+    piagm::AgmOut A;
+    int rc = piagm::agm_device(prec, &A, nullptr);
+    const double t1 = now_ms();
+    scale_th.join();
+    plan_th.join();
+    uint64_t* d_ip = nullptr;
+    size_t ipn = 0;
+    if (!rc && g_error.load()) rc = g_error.load();
+    if (!rc) {
+      // pi 10^(D-1) = scale (a + b)^2 / (4 t)
+      const size_t nl = (prec + 192 + 63) / 64, lq = std::min(A.num_limbs, nl);
+      rc = pidec::quotient_device(A.den, A.den_limbs, A.den_exp, A.num + (A.num_limbs - lq), lq,
+                                  A.num_exp + 64 * (int64_t)(A.num_limbs - lq), scale.mant.data(), scale.mant.size(),
+                                  scale.exp - 2, prec, &d_ip, &ipn, nullptr);
+    }
+    if (A.num) cudaFree(A.num);
+    if (A.den) cudaFree(A.den);
+    if (!rc) rc = to_decimal_batched_into_dev(d_ip, ipn, out, digits, &dplan);
+    if (d_ip) cudaFree(d_ip);
+    if (phase_ms) {
+      phase_ms[0] = t1 - t0;
+      phase_ms[1] = 0;
+      phase_ms[2] = now_ms() - t1;
+    }
+    if (ntt_products) *ntt_products = g_ntt_calls.load();
+    return rc;
+  }
   // the decimal scale 10^(D-1) at the working precision runs beside the
   // iterations (it depends on nothing else)
   Flt scale;

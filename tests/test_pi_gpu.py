@@ -86,6 +86,18 @@ def test_gauss_legendre_fast_sqrt_1e6_matches_mpmath():
     assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
 
 
+def test_gauss_legendre_device_agm_matches_golden():
+    with open(os.path.join(HERE, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    for d in (100, 5000, 100_000):
+        s, _ = pm.pi_gauss_legendre(d, device_agm=True)
+        assert s == ref[:d], d
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, _ = pm.pi_gauss_legendre(1_000_000, device_agm=True)
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+
+
 def test_gauss_legendre_device_decimal_1e6_matches_mpmath():
     with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
         want = json.load(f)["1000000"]
