@@ -3,7 +3,7 @@
 // The level-synchronous divide and conquer of the batched pi pipeline: every
 // node x of level k (x < P_(k+1) = P_k^2, P_k = 10^(19 * 2^k)) splits into
 // x div P_k and x mod P_k, all nodes of a level at once, from the top level
-// down to leaves below 10^608, which a kernel prints.  An integer has one
+// down to leaves below 10^1216, which a kernel prints.  An integer has one
 // decimal string, so the output equals the reference's recursive conversion
 // (crates/bignum/src/integer.rs:892-983, 10^19 chunks at integer.rs:887-888).
 //
@@ -23,7 +23,7 @@
 //
 // Slots: the outputs of level k are 2n nodes of w = |P_k| + 1 limbs, q at
 // slot 2i and r at slot 2i + 1 (the digit order), zero-padded.  The leaves
-// (w = 33 limbs, 32 chunks of 19 digits) are printed one node per thread
+// (w = 65 limbs, 64 chunks of 19 digits) are printed one node per thread
 // into shared memory and stored as 16-byte vectors.
 #include <cuda_runtime.h>
 
@@ -43,9 +43,9 @@ namespace {
 
 constexpr uint64_t CHUNK = 10000000000000000000ull;  // 10^19, bit 63 set
 constexpr int LEAF_CH = 1 << LEAF_K;                 // chunks per leaf
-constexpr int LEAF_W = LEAF_CH + 1;                  // leaf slot: |10^608| = 32 limbs, plus one
-constexpr int LEAF_DIGITS = 19 * LEAF_CH;            // 608 (a multiple of 16)
-constexpr int LEAF_THREADS = 64;
+constexpr int LEAF_W = LEAF_CH + 1;                  // leaf slot: |10^1216| = 64 limbs, plus one
+constexpr int LEAF_DIGITS = 19 * LEAF_CH;            // 1216 (a multiple of 16)
+constexpr int LEAF_THREADS = 32;  // 38 KB of staged digits per CTA
 static_assert(LEAF_DIGITS % 16 == 0, "leaf rows are stored as 16-byte vectors");
 
 // floor((2^128 - 1) / 10^19) - 2^64 (Moller and Granlund, "Improved division
@@ -168,8 +168,8 @@ __device__ __forceinline__ void put19(char* p, uint64_t v) {
   }
 }
 
-// Leaves (slots of LEAF_W limbs, values below 10^608) to LEAF_DIGITS
-// characters each: 32 divisions by 10^19 per node in registers, the digits
+// Leaves (slots of LEAF_W limbs, values below 10^1216) to LEAF_DIGITS
+// characters each: 64 divisions by 10^19 per node in registers, the digits
 // staged in shared memory and stored as 16-byte vectors.
 __global__ void __launch_bounds__(LEAF_THREADS) k_dec_leaves(const uint64_t* __restrict__ nodes, uint64_t n,
                                                              char* __restrict__ out) {

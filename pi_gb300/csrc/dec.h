@@ -17,7 +17,7 @@ struct Level {
 };
 
 // Base-10^19 chunks per leaf (levels k >= LEAF_K run on the device).
-constexpr int LEAF_K = 5;
+constexpr int LEAF_K = 6;
 
 // Writes the last `want` of the 19 * 2^K decimal digits of x (zero-padded on
 // the left) to out, with x split level by level on the device (levels K-1

@@ -1870,7 +1870,7 @@ static DecPlan make_dec_plan(uint64_t ndig) {
   DecPlan D;
   const uint64_t nch = (ndig + 18) / 19;
   while ((1ull << D.K) < nch) D.K++;
-  D.kmin = std::min(D.K, 5);
+  D.kmin = std::min(D.K, pidec::LEAF_K);
   D.P.resize(D.K);
   D.V.resize(D.K);
   D.sh.resize(D.K);
