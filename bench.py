@@ -621,7 +621,7 @@ def run_pi(args):
         t0 = time.perf_counter()
         sb, binfo = pm.pi_chudnovsky_batched(D, args.leaf_terms)
         bwall = time.perf_counter() - t0
-        batched = {"wall_s": round(bwall, 3), "leaf_terms": args.leaf_terms or "auto (at most 32, per quarter of the terms)",
+        batched = {"wall_s": round(bwall, 3), "leaf_terms": args.leaf_terms or "auto (at most 64, per eighth of the terms)",
                    "phases_ms": {k: round(v, 1) for k, v in binfo.items() if k.endswith("_ms")},
                    "gpu_products": binfo["ntt_products"], "batched_levels": binfo["batched_levels"],
                    "sha256": hashlib.sha256(sb.encode()).hexdigest()}
@@ -806,7 +806,7 @@ def main():
     ap.add_argument("--pi-mode", choices=["plain", "batched", "both"], default="both",
                     help="Chudnovsky binary splitting: one GPU call per product, level-batched, or both")
     ap.add_argument("--leaf-terms", type=int, default=0,
-                    help="terms per host-split leaf (0 = chosen per quarter of the terms, at most 32)")
+                    help="terms per binary-splitting leaf (0 = chosen per eighth of the terms, at most 64)")
     ap.add_argument("--gl-backend", choices=["plain", "served", "device"], default="plain",
                     help="Gauss-Legendre products: one pimul_mul call each, through the served form, or the whole "
                          "iteration on the device in fixed point")

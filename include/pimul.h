@@ -259,8 +259,9 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
 /*
  * Batched, device-resident form of pimul_pi_chudnovsky.  The binary
  * splitting runs level by level: leaves of leaf_terms terms (0: chosen per
- * quarter of the terms, at most 32, so that each level's products fill
- * their transform lengths) are split on host threads and uploaded once;
+ * eighth of the terms, at most 64, so that each level's products fill
+ * their transform lengths; at most 64 in any case) are computed on the
+ * device;
  * every level above keeps P, Q and T in HBM, with all of the level's
  * products in one pimul_sum_batch call (Q_L Q_R, P_L P_R, and T_L Q_R +
  * P_L T_R as one fused sum; Q_L Q_R and T_L Q_R share Q_R's transform) and
