@@ -120,7 +120,8 @@ int pimul_mul_batch(const pimul_job* jobs, size_t n, void* stream);
  * (nout >= max(nx, ny); for an addition max(nx, ny) + 1 holds every carry).
  * Synchronous; PIMUL_EINVAL if a carry or borrow leaves the top limb.
  * sub == PIMUL_SUB_MOD: x - y modulo 2^(64 nout), no borrow check (the low
- * limbs of a difference known to fit in nout limbs).  out may equal x.
+ * limbs of a difference known to fit in nout limbs); a call whose jobs are
+ * all PIMUL_SUB_MOD is asynchronous on `stream`.  out may equal x.
  * Replaces: crates/bignum/src/integer.rs:351-421 (add_mag / sub_mag under
  * Integer addition) for the T sums of a binary-splitting level.
  */

@@ -86,7 +86,8 @@ struct Agm {
     k_shift<<<std::max(1u, blocks), 256, 0, st>>>(src, src_len, sh, dst, dst_len);
     cu(cudaGetLastError());
   }
-  // z = x + y or x - y (x >= y) over W limbs (in place allowed)
+  // z = x + y or x - y (x >= y; sub = PIMUL_SUB_MOD: modulo, asynchronous)
+  // over W limbs (in place allowed)
   void addsub(const uint64_t* x, const uint64_t* y, uint64_t* z, int sub) {
     if (rc) return;
     pimul_addsub_job j{x, W, y, W, z, W, sub};
@@ -133,29 +134,45 @@ struct Agm {
   }
 };
 
-// Refines y ~ 1/sqrt(x), given to about acc limbs.  Each step runs at the
-// precision its correction needs (twice the accuracy the step starts from,
-// measured as |x y^2 - 1|), the last ones at nf limbs, until |x y^2 - 1| <
-// 2^(-64 (nf - 1)); at most 64 steps.
-void inv_sqrt(Agm& G, const uint64_t* x, uint64_t* y, size_t acc, const uint64_t* one, uint64_t* u, uint64_t* v,
-              uint64_t* d, uint64_t* tmp) {
+// Refines y ~ 1/sqrt(x), given to about acc limbs, by y' = y (3 - x y^2) / 2,
+// which has no sign to decide, so the reduced-precision steps queue on the
+// stream without a host round trip.  Their precisions are planned down
+// from nf (each a little over half the next), so the first full-precision
+// step starts from more than half the limbs and leaves y correct to nf - 1;
+// full-precision steps measure |x y^2 - 1| first (at most 8 of them).
+void inv_sqrt(Agm& G, const uint64_t* x, uint64_t* y, size_t acc, const uint64_t* one, const uint64_t* three,
+              uint64_t* u, uint64_t* v, uint64_t* d, uint64_t* tmp) {
   const size_t nf = G.nf;
-  size_t m = std::min(nf, 2 * acc + 2);
-  for (int step = 0; step < 64 && !G.rc; step++) {
-    G.mul(y, y, u, m, tmp);
-    G.mul(x, u, v, m, tmp);
-    const bool above = G.limb(v, nf) >= 1;  // x y^2 >= 1
-    G.addsub(above ? v : one, above ? one : v, d, 1);
-    const size_t L = G.trimmed(d, G.W);
-    if (m == nf && L <= 1) return;  // converged
-    const size_t got = nf > L ? nf - L : 0;  // limbs of accuracy before this step
+  std::vector<size_t> plan{nf};
+  // x -> (x + 1) / 2 + 3 decreases strictly above 7: the loop ends
+  while (plan.back() > std::max<size_t>(2 * acc + 6, 8)) plan.push_back((plan.back() + 1) / 2 + 3);
+  std::reverse(plan.begin(), plan.end());
+  auto update = [&](size_t m) {
+    G.addsub(three, v, d, PIMUL_SUB_MOD);  // 3 - x y^2 > 0
     G.mul(y, d, u, m, tmp);
-    G.shift(u, G.W, 1, v, G.W);  // y |d| / 2
-    G.addsub(y, v, y, above ? 1 : 0);
-    // a full-precision step from half the limbs leaves an error below
-    // 2^(-64 (nf - 1)): no second pass to measure it
-    if (m == nf && 2 * got >= nf + 1) return;
-    m = std::min(nf, 2 * got + 2);
+    G.shift(u, G.W, 1, y, G.W);  // y (3 - x y^2) / 2
+  };
+  // from a start that is right to a few bits only (acc = 0), six cheap
+  // steps at two limbs bring it to the plan's first precision
+  for (int k = 0; acc == 0 && k < 6 && !G.rc; k++) {
+    G.mul(y, y, u, std::min<size_t>(2, nf), tmp);
+    G.mul(x, u, v, std::min<size_t>(2, nf), tmp);
+    update(std::min<size_t>(2, nf));
+  }
+  for (size_t k = 0; k + 1 < plan.size() && !G.rc; k++) {
+    G.mul(y, y, u, plan[k], tmp);
+    G.mul(x, u, v, plan[k], tmp);
+    update(plan[k]);
+  }
+  for (int full = 0; full < 8 && !G.rc; full++) {
+    G.mul(y, y, u, nf, tmp);
+    G.mul(x, u, v, nf, tmp);
+    G.absdiff(v, one, d);
+    const size_t L = G.trimmed(d, G.W);
+    const size_t got = nf > L ? nf - L : 0;  // limbs of accuracy before this step
+    if (got + 1 >= nf) return;                // converged already
+    update(nf);
+    if (2 * got >= nf + 1) return;  // the step squared an error below 2^(-32 (nf + 1))
   }
   if (!G.rc) G.rc = PIMUL_EINVAL;  // no convergence: not expected for x in (0, 4)
 }
@@ -181,20 +198,22 @@ int agm_device(uint64_t prec, AgmOut* out, double* ms) {
   uint64_t* v = G.alloc(W);
   uint64_t* d = G.alloc(W);
   uint64_t* one = G.alloc(W);
+  uint64_t* three = G.alloc(W);
   uint64_t* tmp = G.alloc(2 * W + 2);
   if (G.rc) return G.rc;
   // constants: 1, 1/2, 1/4, and y ~ 1/sqrt(1/2) = sqrt(2) from an f64
-  const uint64_t h_one = 1, h_half = 1ull << 63, h_quarter = 1ull << 62;
+  const uint64_t h_one = 1, h_three = 3, h_half = 1ull << 63, h_quarter = 1ull << 62;
   const double frac = std::sqrt(2.0) - 1.0;
   const uint64_t h_y[2] = {(uint64_t)std::ldexp(frac, 64), 1};
   G.cu(cudaMemcpyAsync(one + nf, &h_one, 8, cudaMemcpyHostToDevice, G.st));
+  G.cu(cudaMemcpyAsync(three + nf, &h_three, 8, cudaMemcpyHostToDevice, G.st));
   G.cu(cudaMemcpyAsync(a + nf, &h_one, 8, cudaMemcpyHostToDevice, G.st));
   G.cu(cudaMemcpyAsync(x + nf - 1, &h_half, 8, cudaMemcpyHostToDevice, G.st));
   G.cu(cudaMemcpyAsync(t + nf - 1, &h_quarter, 8, cudaMemcpyHostToDevice, G.st));
   G.cu(cudaMemcpyAsync(y + nf - 1, h_y, 16, cudaMemcpyHostToDevice, G.st));
   G.cu(cudaStreamSynchronize(G.st));  // host constants are locals
   // b = sqrt(1/2) = x y
-  inv_sqrt(G, x, y, 0, one, u, v, d, tmp);
+  inv_sqrt(G, x, y, 0, one, three, u, v, d, tmp);
   G.mul(x, y, b, nf, tmp);
   const uint32_t iters = (uint32_t)std::ceil(std::log2((double)prec)) + 2;
   const bool timing = getenv("PIMUL_PI_TIMING") != nullptr;
@@ -209,7 +228,7 @@ int agm_device(uint64_t prec, AgmOut* out, double* ms) {
     const size_t ld = G.trimmed(d, W);
     const size_t acc = ld + 1 < nf ? nf - ld - 1 : 0;
     G.mul(a, b, x, nf, tmp);
-    inv_sqrt(G, x, y, acc, one, u, v, d, tmp);
+    inv_sqrt(G, x, y, acc, one, three, u, v, d, tmp);
     // t -= 2^it (a - a')^2: |a - a'| has lsq limbs, its square only
     // matters in its limbs above the fraction's nf
     G.absdiff(a, an, d);

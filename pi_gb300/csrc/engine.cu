@@ -2569,7 +2569,13 @@ int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
   int* d_flag = nullptr;
   CU(cudaMallocAsync((void**)&d_flag, sizeof(int), g_dev.pool, st));
   CU(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
+  bool all_mod = true;
+  for (size_t i = 0; i < n && all_mod; i++) all_mod = jobs[i].sub == PIMUL_SUB_MOD;
   rc = addsub_launch(jobs, n, st, d_flag);
+  if (all_mod) {  // nothing to check: stay asynchronous
+    cudaFreeAsync(d_flag, st);
+    return rc;
+  }
   int h_flag = 0;
   if (!rc) {
     cudaError_t e = cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
