@@ -10,9 +10,9 @@
 // GPU design: the (position, series, k) space is flattened; every CTA owns
 // one (position, series) pair and its threads stride over k.  The wrapping
 // u64 sum is associative and commutative, so any split of k gives the same
-// bits.  16^e mod d uses 64-bit Montgomery multiplication for the odd part
-// of d (d = 8k+4 and 8k+6 are even: the power-of-two factor is restored by
-// CRT).  The f64 tail uses explicitly rounded IEEE operations (no FMA
+// bits.  16^e mod d uses Montgomery multiplication on the odd part of d
+// (32-bit arithmetic below 2^32, 64-bit above; d = 8k+4 and 8k+6 are even:
+// the power-of-two factor is restored by CRT).  The f64 tail uses explicitly rounded IEEE operations (no FMA
 // contraction), so it matches the reference's f64 arithmetic exactly.
 // A stop flag in mapped host memory is polled every 10^4 terms (like
 // bbp.rs:88-92); no thread ever waits on it.
@@ -84,6 +84,36 @@ __device__ __forceinline__ uint64_t pow2_64_mod(uint64_t m, float rm) {
   return mod_est((int64_t)(0 - q0 * m), m, rm);
 }
 
+// Montgomery product a*b*2^-32 mod m for a, b < m < 2^32, m odd: t + u m
+// can pass 2^64 when m is near 2^32, so its carry is kept.
+__device__ __forceinline__ uint32_t mont_mul32(uint32_t a, uint32_t b, uint32_t m, uint32_t minv) {
+  const uint64_t t = (uint64_t)a * b;
+  const uint32_t u = (uint32_t)t * minv;
+  const uint64_t s = t + (uint64_t)u * m;
+  const uint64_t r = (s >> 32) | ((uint64_t)(s < t) << 32);  // < 2m
+  return (uint32_t)(r >= m ? r - m : r);
+}
+
+// 16^e mod m for odd 3 <= m < 2^32 in 32-bit Montgomery arithmetic (the
+// moduli of positions below about 5.4e8): a square is one wide multiply and
+// two narrow ones, and the factor 16 is a Montgomery product with 16 R.
+__device__ __forceinline__ uint64_t pow16_mod_odd32(uint64_t e, uint32_t m, float rm) {
+  const uint32_t minv = (uint32_t)neg_inv64(m);
+  const uint64_t q0 = __float2ull_rz(__fmul_rn(rm, 4294967296.0f));
+  const uint32_t r1 = (uint32_t)mod_est((int64_t)((1ull << 32) - q0 * m), m, rm);  // R mod m
+  const uint32_t b16 = (uint32_t)mod_est((int64_t)((uint64_t)r1 << 4), m, rm);     // 16 R mod m
+  uint32_t x = r1;
+  if (e) {
+    const int top = 63 - __clzll((long long)e);
+    x = b16;
+    for (int b = top - 1; b >= 0; b--) {
+      x = mont_mul32(x, x, m, minv);
+      if ((e >> b) & 1) x = mont_mul32(x, b16, m, minv);
+    }
+  }
+  return mont_mul32(x, 1, m, minv);  // out of Montgomery form
+}
+
 // 16^e mod d for 1 <= d < 2^34 (d == 1 -> 0, like bbp.rs:123-125).
 __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
   if (d == 1) return 0;
@@ -91,7 +121,10 @@ __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
   uint64_t m = d >> t;
   uint64_t rm_ = 0;   // 16^e mod m
   uint64_t minv = 0;  // -m^-1 mod 2^64 (m > 1)
-  if (m > 1) {
+  if (m > 1 && m < (1ull << 32)) {
+    minv = neg_inv64(m);
+    rm_ = pow16_mod_odd32(e, (uint32_t)m, __frcp_rn((float)m));
+  } else if (m > 1) {
     const float rm = __frcp_rn((float)m);
     minv = neg_inv64(m);
     const uint64_t r1 = pow2_64_mod(m, rm);           // Montgomery one
