@@ -686,6 +686,60 @@ def run_pi(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- verify-hex
+def run_hex(args):
+    """verify-hex's decimal -> hex conversion (crates/pi-cli/src/verify_hex.rs:
+    553-629) of D digits of pi computed by the batched Chudnovsky run
+    (untimed): wall time of pimul_decimal_to_hex from host text to host
+    text, hex digits spot-checked against BBP at seeded positions.  The CPU
+    baseline is the oracle's exact-integer restatement on a bounded sample."""
+    import hashlib
+    import pi_gb300 as pm
+    pm.init(0)
+    D = args.digits
+    s, _ = pm.pi_chudnovsky_batched(D)
+    text = "3." + s[1:]
+    del s
+    pm.decimal_to_hex(text[: min(len(text), 100_002)])  # warm-up
+    t0 = time.perf_counter()
+    x, ph = pm.decimal_to_hex(text, phases=True)
+    wall = time.perf_counter() - t0
+    frac = x[2:]
+    h = len(frac)
+    rng = np.random.default_rng(2026)
+    hi = max(1, min(h - 40, 4_000_000))  # BBP cost grows with the position
+    pos = np.unique(np.concatenate([[0], rng.integers(0, hi, size=args.hex_checks)]).astype(np.uint64))
+    d = pm.bbp_hex_digits(pos)
+    bbp_ok = all(frac[int(p): int(p) + 8] == format(int(v), "08x") for p, v in zip(pos, d))
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        n = min(D, args.hex_cpu_digits)
+        t1 = time.perf_counter()
+        xc = oracle.decimal_to_hex(text[: n + 1])
+        ct = time.perf_counter() - t1
+        xg = pm.decimal_to_hex(text[: n + 1])
+        cpu = {"value": round(ct, 3), "unit": "s", "cores": 1, "kind": "port",
+               "sample": f"the first {n} digits through the oracle's restatement of verify_hex.rs:553-629 with "
+                         "Python's exact integers (CPython's subquadratic string parse and division; the "
+                         "reference's own parse is quadratic, integer.rs:127-148)",
+               "gpu_same_sample_s": None, "gpu_matches_cpu": xc == xg}
+        t2 = time.perf_counter()
+        pm.decimal_to_hex(text[: n + 1])
+        cpu["gpu_same_sample_s"] = round(time.perf_counter() - t2, 4)
+    line = {
+        "metric": f"decimal->hex conversion wall-s ({D} digits of pi)", "project_metric": PROJECT_METRIC,
+        "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "pi's digits from the batched Chudnovsky run (deterministic)",
+        "config": {"workload": f"verify-hex conversion of {D} decimal digits to {h} hex digits, host text in and out"},
+        "phases_ms": {k: round(v, 1) for k, v in zip(("parse", "power_of_ten", "quotient", "hex_digits"), ph)},
+        "hex_digits": h, "bbp_positions_checked": int(pos.size), "bbp_matches": bbp_ok,
+        "sha256": hashlib.sha256(x.encode()).hexdigest(), "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------- BBP
 def run_bbp(args):
     """Config 5's spot checks: batched BBP hex digits at seeded positions
@@ -820,10 +874,12 @@ def main():
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)
     ap.add_argument("--cpu-depth", type=float, default=2e6)
-    ap.add_argument("--workload", choices=["mul", "batch", "served", "pi", "bbp"], default="mul",
+    ap.add_argument("--workload", choices=["mul", "batch", "served", "pi", "bbp", "hex"], default="mul",
                     help="mul: the 2^30-bit product (headline); batch: 4096 uneven products; "
                          "served: Poisson request stream through the multiply service")
     ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--hex-checks", type=int, default=8, help="BBP spot checks of the hex conversion")
+    ap.add_argument("--hex-cpu-digits", type=int, default=1_000_000)
     ap.add_argument("--load", type=float, default=0.8)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--bits", type=int, default=30,
@@ -843,6 +899,8 @@ def main():
         run_pi(args)
     elif args.workload == "bbp":
         run_bbp(args)
+    elif args.workload == "hex":
+        run_hex(args)
     else:
         run_gpu(args)
 

@@ -298,6 +298,26 @@ int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t
 int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size_t cap, size_t* len, int batched);
 
 /*
+ * verify-hex's decimal -> hex conversion of pi: text[0..len) is "3." and E
+ * decimal digits (ASCII whitespace around it is ignored); out receives "3."
+ * and the h = floor(E log2(10) / 4) hex digits (lower case) of
+ * m = floor(N 16^h / 10^E) after its leading 3, N the E + 1 digits as an
+ * integer, without a terminator or newline.  *out_len = h + 2 is set before
+ * `out` and `cap` are checked (a NULL or short out returns PIMUL_EINVAL).
+ * PIMUL_EINVAL with the reference's messages for text not starting with
+ * "3.", non-digit characters or E > 2^32 - 1.  Parsing, 10^E, the quotient
+ * and the hex digits all run on the device (parse: 19-digit chunks, then
+ * x = hi 10^(19 2^k) + lo level by level through pimul_mul_batch; quotient:
+ * a Newton reciprocal and an exact remainder correction).  phase_ms
+ * (optional, 4 entries): parse, power of ten, quotient, hex digits.
+ *
+ * Replaces: crates/pi-cli/src/verify_hex.rs:553-629 convert_decimal_to_hex
+ * (its quadratic Integer::parse_radix, integer.rs:102-153, and the
+ * division of integer.rs:1004-1083) up to writing the file.
+ */
+int pimul_decimal_to_hex(const char* text, size_t len, char* out, size_t cap, size_t* out_len, double* phase_ms);
+
+/*
  * Digits of pi by the Gauss-Legendre AGM, same conventions as
  * pimul_pi_chudnovsky (phase_ms: iterations + final assembly, unused,
  * decimal conversion).

@@ -180,6 +180,44 @@ def bbp_batch(positions) -> np.ndarray:
     return out
 
 
+# ---------------------------------------------------------------- verify-hex
+_WS = " \t\n\r\x0b\x0c"
+
+
+def decimal_to_hex(text) -> str:
+    """Restatement of crates/pi-cli/src/verify_hex.rs:553-629
+    (convert_decimal_to_hex up to the file write) with Python's exact
+    integers: trim, require "3." and digits (:563-574), N = the digits
+    with the point removed (:575-581; parse_radix, integer.rs:102-153),
+    h = floor((D-1) * log2(10) / 4) in f64 (:584-585), m = N 16^h div
+    10^(D-1) (:592-593), and "3." + hex(m)[1:] after the leading-'3' check
+    (:597-613, to_string_radix(16) at integer.rs:169-177: lower case, no
+    leading zeros).  Raises ValueError with the reference's messages."""
+    import math
+    import sys
+
+    if hasattr(sys, "set_int_max_str_digits"):
+        sys.set_int_max_str_digits(0)
+    if isinstance(text, (bytes, bytearray)):
+        text = bytes(text).decode("ascii", errors="replace")
+    t = text.strip(_WS)
+    if not t.startswith("3."):
+        raise ValueError("doesn't start with \"3.\"")
+    frac = t[2:]
+    if not all("0" <= c <= "9" for c in frac):
+        raise ValueError("has non-digit characters after \"3.\"")
+    e = len(frac)
+    if e > 0xFFFFFFFF:
+        raise ValueError("fractional decimal digit count exceeds u32::MAX")
+    n = int("3" + frac)
+    h = int(float(e) * (math.log2(10.0) / 4.0))
+    m = (n << (4 * h)) // (10 ** e)
+    x = format(m, "x")
+    if not x.startswith("3"):
+        raise ValueError("internal: hex conversion didn't produce a leading '3'")
+    return "3." + x[1:]
+
+
 # ---------------------------------------------------------------- helpers
 def limbs_to_int(x) -> int:
     x = _as_u64(x)

@@ -27,6 +27,7 @@ __all__ = [
     "plan", "sync", "bbp_hex_digits", "mul_batch", "BatchPlan", "autotune",
     "tuning_apply", "PimulJob", "set_budget", "upload", "submit", "wait", "download", "free",
     "handle_size", "pi_chudnovsky", "pi_gauss_legendre", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
+    "decimal_to_hex", "convert_decimal_to_hex",
 ]
 
 LIB_PATH = _build.LIB
@@ -90,6 +91,8 @@ def load(build_if_stale: bool = True):
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                               ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_to_decimal.argtypes = [_u64p, _sz, ctypes.c_char_p, _sz, ctypes.POINTER(_sz), ctypes.c_int]
+    L.pimul_decimal_to_hex.argtypes = [ctypes.c_char_p, _sz, ctypes.c_char_p, _sz, ctypes.POINTER(_sz),
+                                       ctypes.POINTER(ctypes.c_double)]
     L.pimul_pi_gauss_legendre_ex.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
                                              ctypes.c_uint32, ctypes.POINTER(ctypes.c_double),
                                              ctypes.POINTER(ctypes.c_uint64)]
@@ -407,6 +410,39 @@ def to_decimal(limbs, batched: bool = True) -> str:
     _check(lib().pimul_to_decimal(a.ctypes.data_as(_u64p), a.size, buf, n.value + 1, ctypes.byref(n),
                                   int(batched)))
     return buf.raw[: n.value].decode()
+
+
+def decimal_to_hex(text, phases: bool = False):
+    """verify-hex's conversion of pi's decimal text "3.ddd..." to "3.hhh..."
+    (pimul_decimal_to_hex; crates/pi-cli/src/verify_hex.rs:553-629): the
+    floor(N 16^h / 10^E) hex digits, computed on the GPU.  With phases, also
+    returns the phase times in ms (parse, power of ten, quotient, hex)."""
+    raw = text.encode() if isinstance(text, str) else bytes(text)
+    n = _sz(0)
+    rc = lib().pimul_decimal_to_hex(raw, len(raw), None, 0, ctypes.byref(n), None)
+    if n.value == 0:  # the text was rejected before its length was known
+        _check(rc)
+    buf = ctypes.create_string_buffer(n.value)
+    ph = (ctypes.c_double * 4)()
+    _check(lib().pimul_decimal_to_hex(raw, len(raw), buf, n.value, ctypes.byref(n), ph))
+    out = buf.raw[: n.value].decode()
+    return (out, list(ph)) if phases else out
+
+
+def convert_decimal_to_hex(decimal_path, hex_path):
+    """The file form of verify_hex.rs:553-629: reads the decimal file, writes
+    "3." + hex digits + a newline to hex_path through a .tmp file and a
+    rename."""
+    with open(decimal_path, "rb") as f:
+        raw = f.read()
+    out = decimal_to_hex(raw)
+    hex_path = os.fspath(hex_path)
+    tmp = os.path.splitext(hex_path)[0] + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(out.encode() + b"\n")
+        f.flush()
+        os.fsync(f.fileno())
+    os.replace(tmp, hex_path)
 
 
 def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sqrt: bool = False,

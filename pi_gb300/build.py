@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimul.so")
 
-SOURCES = ["engine.cu", "bbp.cu", "dec.cu", "leaves.cu", "agm.cu", "pi_host.cpp"]
+SOURCES = ["engine.cu", "bbp.cu", "dec.cu", "leaves.cu", "agm.cu", "hexconv.cu", "pi_host.cpp"]
 HEADERS = ["gl.cuh", "ntt_kernels.cuh", "dec.h", "hostcopy.h", "leaves.h", "agm.h"]
 
 NVCC_FLAGS = [

@@ -1076,6 +1076,8 @@ int device_to_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
   return PIMUL_OK;
 }
 
+int set_error(int code, const char* msg) { return fail(code, msg); }
+
 void release_host_staging() {
   std::lock_guard<std::mutex> lk(g_stage_mu);
   for (StageBuf* b : g_stage_all) {

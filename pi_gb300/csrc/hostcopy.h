@@ -1,6 +1,6 @@
-// Internal: copies between the device and host memory that may be pageable
-// (defined in engine.cu, used by the engine's host entry points and by
-// dec.cu).  Not part of the C ABI.
+// Internal: copies between the device and host memory that may be pageable,
+// and the error message of the C ABI (defined in engine.cu, used by the
+// engine's host entry points, dec.cu and hexconv.cu).  Not part of the C ABI.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -18,5 +18,8 @@ int device_to_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
 
 // Frees the pinned staging buffers (device idle).
 void release_host_staging();
+
+// Sets the calling thread's pimul_last_error() message; returns code.
+int set_error(int code, const char* msg);
 
 }  // namespace pimul

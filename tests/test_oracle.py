@@ -240,3 +240,31 @@ def test_bbp_overlap_and_interrupt():
     assert O.bbp_hex_digits_at(10_000_000, stop=True) is None
     got = O.bbp_batch([0, 1, 7, 8, 100, 999])
     assert list(got) == [O.bbp_hex_digits_at(n) for n in (0, 1, 7, 8, 100, 999)]
+
+
+# ---------------------------------------------------------------- verify-hex conversion
+def test_decimal_to_hex_pinned_to_bbp(golden):
+    # crates/pi-cli/src/verify_hex.rs:553-629 on the first 100 decimal digits
+    # (util.rs:126-127) against the reference's hex prefix and BBP known
+    # values (bbp.rs:153-175); the last TAIL_SKIP = 32 digits are exempt
+    # (verify_hex.rs:540-547)
+    x = O.decimal_to_hex(golden["first_100_digits"])
+    assert x.startswith("3.")
+    frac = x[2:]
+    assert len(frac) == int(99 * (np.log2(10.0) / 4.0))
+    assert [int(c, 16) for c in frac[: len(golden["pi_hex_prefix"])]] == golden["pi_hex_prefix"]
+    for n, v in golden["bbp_known"].items():
+        assert frac[int(n): int(n) + 8] == format(v, "08x")
+    for n in range(0, len(frac) - 32 - 8):
+        assert frac[n: n + 8] == format(O.bbp_hex_digits_at(n), "08x")
+
+
+def test_decimal_to_hex_edges_and_errors():
+    # h = floor(E log2(10) / 4): "3." -> no digits, "3.1" -> none, "3.14" -> one
+    assert O.decimal_to_hex("3.") == "3."
+    assert O.decimal_to_hex(" 3.1\n") == "3."
+    assert O.decimal_to_hex("3.14") == "3.2"
+    assert O.decimal_to_hex("3.5000") == "3.800"
+    for bad, msg in (("2.14", "3."), ("314", "3."), ("3.1a4", "non-digit"), ("", "3.")):
+        with pytest.raises(ValueError, match=msg.replace(".", r"\.")):
+            O.decimal_to_hex(bad)
