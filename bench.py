@@ -340,7 +340,13 @@ def run_gpu(args):
                          "step_achieved": round(step_achieved, 1),
                          "step_frac": round(step_achieved / peak, 4),
                          "binding_unit": "integer ALU pipe, not HBM (ncu: ALU 62-70 % busy, issue 59-67 %, "
-                                         "DRAM 13-35 % of peak; profiles/ntt_pass_kernels_2e29_full.md)"},
+                                         "DRAM 13-35 % of peak; profiles/ntt_pass_kernels_2e29_full.md)",
+                         "io_effective_gbs": round(16 * (la + lb) / (ms_step * 1e-3) / 1e9, 1),
+                         "integer_model": {
+                             "butterflies": 3 * (N // 2) * L, "pointwise_mulmods": 2 * N,
+                             "butterflies_per_s": round(3 * (N // 2) * L / (ms_step * 1e-3), 1),
+                             "model": "3 (N/2) log2 N radix-2-equivalent butterflies + 2N pointwise/scale "
+                                      "products per multiply"}},
             "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ks.items()},
             "gpu_launches": launches,
             "clocks": clk.summary(),

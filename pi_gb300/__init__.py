@@ -422,11 +422,13 @@ def decimal_to_hex(text, phases: bool = False):
     rc = lib().pimul_decimal_to_hex(raw, len(raw), None, 0, ctypes.byref(n), None)
     if n.value == 0:  # the text was rejected before its length was known
         _check(rc)
-    buf = ctypes.create_string_buffer(n.value)
+    out = bytearray(n.value)  # written in place (no zero-filled ctypes buffer and copy)
     ph = (ctypes.c_double * 4)()
-    _check(lib().pimul_decimal_to_hex(raw, len(raw), buf, n.value, ctypes.byref(n), ph))
-    out = buf.raw[: n.value].decode()
-    return (out, list(ph)) if phases else out
+    dst = ctypes.cast((ctypes.c_char * len(out)).from_buffer(out), ctypes.c_char_p)
+    _check(lib().pimul_decimal_to_hex(raw, len(raw), dst, n.value, ctypes.byref(n), ph))
+    del dst
+    res = out.decode("ascii")
+    return (res, list(ph)) if phases else res
 
 
 def convert_decimal_to_hex(decimal_path, hex_path):

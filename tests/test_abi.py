@@ -47,3 +47,17 @@ def test_version_and_plan_without_gpu():
     assert n == 1 << 27
     with pytest.raises(pi_gb300.PimulError):
         pi_gb300.plan(1 << 30, 1 << 30)
+
+
+def test_decimal_to_hex_host_checks_without_gpu():
+    # verify_hex.rs:563-569 prefix check and the E = 0 case return before any
+    # device work; the output length h + 2 (h = floor(E log2(10) / 4)) is
+    # reported before the buffer is checked
+    with pytest.raises(pi_gb300.PimulError, match="doesn't start"):
+        pi_gb300.decimal_to_hex("2.718")
+    with pytest.raises(pi_gb300.PimulError, match="doesn't start"):
+        pi_gb300.decimal_to_hex("  ")
+    assert pi_gb300.decimal_to_hex(" 3.\n") == "3."
+    n = ctypes.c_size_t(0)
+    rc = pi_gb300.lib().pimul_decimal_to_hex(b"3." + b"1" * 1000, 1002, None, 0, ctypes.byref(n), None)
+    assert rc != 0 and n.value == 2 + int(1000 * (__import__("math").log2(10.0) / 4.0))
