@@ -703,20 +703,29 @@ def run_hex(args):
     import pi_gb300 as pm
     pm.init(0)
     D = args.digits
-    s, _ = pm.pi_chudnovsky_batched(D)
-    text = "3." + s[1:]
-    del s
+    if args.hex_input == "pi":
+        s, _ = pm.pi_chudnovsky_batched(D)
+        text = "3." + s[1:]
+        del s
+    else:  # seeded uniform digits: the conversion alone (profiling)
+        digs = np.random.default_rng(2027).integers(0, 10, size=D - 1, dtype=np.uint8) + ord("0")
+        text = "3." + digs.tobytes().decode()
+        del digs
     pm.decimal_to_hex(text[: min(len(text), 100_002)])  # warm-up
     t0 = time.perf_counter()
     x, ph = pm.decimal_to_hex(text, phases=True)
     wall = time.perf_counter() - t0
     frac = x[2:]
     h = len(frac)
+    if args.hex_input != "pi":
+        args.hex_checks = 0
     rng = np.random.default_rng(2026)
     hi = max(1, min(h - 40, 4_000_000))  # BBP cost grows with the position
     pos = np.unique(np.concatenate([[0], rng.integers(0, hi, size=args.hex_checks)]).astype(np.uint64))
-    d = pm.bbp_hex_digits(pos)
-    bbp_ok = all(frac[int(p): int(p) + 8] == format(int(v), "08x") for p, v in zip(pos, d))
+    bbp_ok = None
+    if args.hex_input == "pi":
+        d = pm.bbp_hex_digits(pos)
+        bbp_ok = all(frac[int(p): int(p) + 8] == format(int(v), "08x") for p, v in zip(pos, d))
     cpu = None
     if not args.no_cpu_baseline:
         import oracle
@@ -737,10 +746,11 @@ def run_hex(args):
         "metric": f"decimal->hex conversion wall-s ({D} digits of pi)", "project_metric": PROJECT_METRIC,
         "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
         "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u64", "data": "pi's digits from the batched Chudnovsky run (deterministic)",
+        "dtype": "u64", "data": ("pi's digits from the batched Chudnovsky run (deterministic)" if args.hex_input == "pi"
+                                 else "seeded uniform decimal digits after \"3.\""),
         "config": {"workload": f"verify-hex conversion of {D} decimal digits to {h} hex digits, host text in and out"},
         "phases_ms": {k: round(v, 1) for k, v in zip(("parse", "power_of_ten", "quotient", "hex_digits"), ph)},
-        "hex_digits": h, "bbp_positions_checked": int(pos.size), "bbp_matches": bbp_ok,
+        "hex_digits": h, "bbp_positions_checked": int(pos.size) if bbp_ok is not None else 0, "bbp_matches": bbp_ok,
         "sha256": hashlib.sha256(x.encode()).hexdigest(), "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -886,6 +896,8 @@ def main():
     ap.add_argument("--requests", type=int, default=1000)
     ap.add_argument("--hex-checks", type=int, default=8, help="BBP spot checks of the hex conversion")
     ap.add_argument("--hex-cpu-digits", type=int, default=1_000_000)
+    ap.add_argument("--hex-input", choices=["pi", "random"], default="pi",
+                    help="text to convert: pi's digits (BBP-checked) or seeded random digits")
     ap.add_argument("--load", type=float, default=0.8)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--bits", type=int, default=30,

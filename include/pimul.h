@@ -381,6 +381,12 @@ const char* pimul_bbp_last_error(void);
 int pimul_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_t* p, size_t n, uint64_t* pow16,
                      uint64_t* frac);
 
+/* The term the extractor sums, out[i] = floor((16^e[i] mod d[i]) 2^64 / d[i])
+ * (bbp.rs:117-140), computed as the device computes it (an exact 2-adic
+ * quotient, no division) for 1 <= d[i] < 2^34, e[i] < 2^40.  For checking;
+ * synchronous. */
+int pimul_bbp_terms(const uint64_t* e, const uint64_t* d, size_t n, uint64_t* out);
+
 /* Synchronise the calling thread's own stream. */
 int pimul_sync(void);
 

@@ -101,6 +101,7 @@ def load(build_if_stale: bool = True):
     L.pimul_bbp_hex_digits.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
     L.pimul_bbp_last_error.restype = ctypes.c_char_p
     L.pimul_bbp_modops.argtypes = [_u64p, _u64p, _u64p, _sz, _u64p, _u64p]
+    L.pimul_bbp_terms.argtypes = [_u64p, _u64p, _sz, _u64p]
     _lib = L
     return L
 
@@ -474,6 +475,17 @@ def bbp_modops(e, d, p):
     if rc:
         raise PimulError(rc, lib().pimul_bbp_last_error().decode())
     return pw, fr
+
+
+def bbp_terms(e, d):
+    """floor((16^e mod d) 2^64 / d) on the device, the term the extractor
+    sums (pimul_bbp_terms)."""
+    e, d = (np.ascontiguousarray(np.asarray(x, dtype=np.uint64)) for x in (e, d))
+    out = np.zeros(e.size, dtype=np.uint64)
+    rc = lib().pimul_bbp_terms(e.ctypes.data_as(_u64p), d.ctypes.data_as(_u64p), e.size, out.ctypes.data_as(_u64p))
+    if rc:
+        raise PimulError(rc, lib().pimul_bbp_last_error().decode())
+    return out
 
 
 def bbp_hex_digits(positions, stop=None) -> np.ndarray:

@@ -7,21 +7,28 @@
 // and tail_j is the f64 sum of 20 terms 1/(16^o (8(n+o)+j)) converted with
 // a truncating cast.
 //
-// GPU design: the (position, series, k) space is flattened; every CTA owns
-// one (position, series) pair and its threads stride over k.  The wrapping
-// u64 sum is associative and commutative, so any split of k gives the same
-// bits.  16^e mod d uses Montgomery multiplication on the odd part of d
-// (32-bit arithmetic below 2^32, 64-bit above; d = 8k+4 and 8k+6 are even:
-// the power-of-two factor is restored by CRT).  The f64 tail uses explicitly rounded IEEE operations (no FMA
-// contraction), so it matches the reference's f64 arithmetic exactly.
-// A stop flag in mapped host memory is polled every 10^4 terms (like
-// bbp.rs:88-92); no thread ever waits on it.
+// GPU design: the (position, series, k) space is cut into equal work items
+// of 2^16 terms, run by a persistent grid (one full wave of CTAs); each
+// warp adds its partial sum to its (position, series) slot with a 64-bit
+// atomic.  The wrapping u64 sum is associative and commutative, so any
+// split of k gives the same bits.  Each term floor((16^e mod d) 2^64 / d) is an exact 2-adic
+// quotient (bbp_term): 2^(4e + 64 - t) mod m by Montgomery squarings and
+// doublings on the odd part m of d = 2^t m (32-bit arithmetic below 2^32,
+// 64-bit above), then one product with m^-1 mod 2^64; no term divides or
+// converts a 64-bit integer to floating point (on this GPU those
+// conversions run on the FP64 pipe).  The f64 tail uses explicitly rounded
+// IEEE operations (no FMA contraction), so it matches the reference's f64
+// arithmetic exactly.
+// A stop flag in mapped host memory is read every 16 work items per warp
+// (like bbp.rs:88-92); no thread ever waits on it.
 #include <cuda_runtime.h>
 #include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <string>
 #include <thread>
+#include <vector>
+#include <algorithm>
 
 #include "../../include/pimul.h"
 
@@ -86,12 +93,44 @@ __device__ __forceinline__ uint64_t pow2_64_mod(uint64_t m, float rm) {
 
 // Montgomery product a*b*2^-32 mod m for a, b < m < 2^32, m odd: t + u m
 // can pass 2^64 when m is near 2^32, so its carry is kept.
+// In 32-bit words: t = a b = (th:tl), u = tl minv, and t + u m has low word
+// 0 with a carry into the high word exactly when tl != 0; the high word sum
+// th + hi(u m) + (tl != 0) is r = c 2^32 + h < 2m, and r >= m iff
+// c - borrow(h - m) >= 0, in which case the result is h - m mod 2^32.
 __device__ __forceinline__ uint32_t mont_mul32(uint32_t a, uint32_t b, uint32_t m, uint32_t minv) {
-  const uint64_t t = (uint64_t)a * b;
-  const uint32_t u = (uint32_t)t * minv;
-  const uint64_t s = t + (uint64_t)u * m;
-  const uint64_t r = (s >> 32) | ((uint64_t)(s < t) << 32);  // < 2m
-  return (uint32_t)(r >= m ? r - m : r);
+  uint32_t r;
+  asm("{\n\t.reg .u32 tl, th, u, uh, z, c, d;\n\t.reg .pred p;\n\t"
+      "mul.lo.u32 tl, %1, %2;\n\t"
+      "mul.hi.u32 th, %1, %2;\n\t"
+      "mul.lo.u32 u, tl, %4;\n\t"
+      "mul.hi.u32 uh, u, %3;\n\t"
+      "add.cc.u32 z, tl, 0xFFFFFFFF;\n\t"
+      "addc.cc.u32 th, th, uh;\n\t"
+      "addc.u32 c, 0, 0;\n\t"
+      "sub.cc.u32 d, th, %3;\n\t"
+      "subc.u32 c, c, 0;\n\t"
+      "setp.ge.s32 p, c, 0;\n\t"
+      "selp.u32 %0, d, th, p;\n\t"
+      "}"
+      : "=r"(r)
+      : "r"(a), "r"(b), "r"(m), "r"(minv));
+  return r;
+}
+
+// 2x mod m for x < m < 2^32 (the same carry and borrow test).
+__device__ __forceinline__ uint32_t dbl_mod32(uint32_t x, uint32_t m) {
+  uint32_t r;
+  asm("{\n\t.reg .u32 lo, c, d;\n\t.reg .pred p;\n\t"
+      "add.cc.u32 lo, %1, %1;\n\t"
+      "addc.u32 c, 0, 0;\n\t"
+      "sub.cc.u32 d, lo, %2;\n\t"
+      "subc.u32 c, c, 0;\n\t"
+      "setp.ge.s32 p, c, 0;\n\t"
+      "selp.u32 %0, d, lo, p;\n\t"
+      "}"
+      : "=r"(r)
+      : "r"(x), "r"(m));
+  return r;
 }
 
 // 16^e mod m for odd 3 <= m < 2^32 in 32-bit Montgomery arithmetic (the
@@ -152,6 +191,53 @@ __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
   return rm_ + m * s2;
 }
 
+// 2^E mod m for odd 3 <= m < 2^32 and E >= 1 in 32-bit Montgomery
+// arithmetic (R = 2^32): x runs through the Montgomery forms of 2^(prefix
+// of E), one square per bit and one doubling per set bit.  R mod m comes
+// from a 32-bit remainder; nothing converts 64-bit integers to floats.
+__device__ __forceinline__ uint32_t pow2_mod_odd32(uint64_t E, uint32_t m, uint32_t minv) {
+  uint32_t x = (0u - m) % m;  // R mod m: the Montgomery form of 1
+  const int top = 63 - __clzll((long long)E);
+  for (int b = top; b >= 0; b--) {
+    if (b != top) x = mont_mul32(x, x, m, minv);
+    if ((E >> b) & 1) x = dbl_mod32(x, m);
+  }
+  return mont_mul32(x, 1, m, minv);
+}
+
+// The same for odd 2^32 <= m < 2^34 in 64-bit Montgomery arithmetic.
+__device__ __forceinline__ uint64_t pow2_mod_odd64(uint64_t E, uint64_t m, uint64_t minv) {
+  uint64_t x = pow2_64_mod(m, __frcp_rn((float)m));  // R mod m (R = 2^64)
+  const int top = 63 - __clzll((long long)E);
+  for (int b = top; b >= 0; b--) {
+    if (b != top) x = mont_mul(x, x, m, minv);
+    if ((E >> b) & 1) {
+      x <<= 1;  // < 2^35
+      if (x >= m) x -= m;
+    }
+  }
+  return mont_mul(x, 1, m, minv);
+}
+
+// One term of bbp.rs:117-140, floor((16^e mod d) 2^64 / d) for
+// 1 <= d < 2^34, without a division.  With d = 2^t m (m odd) and
+// p = 16^e mod d < d, p 2^(64-t) = q m + r' with q < 2^64 and
+// r' = p 2^(64-t) mod m = 2^(4e + 64 - t) mod m, so q is the exact 2-adic
+// quotient (p 2^(64-t) - r') m^-1 mod 2^64, and p 2^(64-t) mod 2^64 needs
+// only p mod 2^t = 16^e mod 2^t.  d = 1 gives 0 (bbp.rs:123-125).
+__device__ __forceinline__ uint64_t bbp_term(uint64_t e, uint64_t d) {
+  if (d == 1) return 0;
+  const int t = __ffsll((long long)d) - 1;
+  const uint64_t m = d >> t;
+  const uint64_t lo = (t == 0 || 4 * e >= (uint64_t)t) ? 0 : (1ull << (4 * e + 64 - (uint64_t)t));
+  if (m == 1) return lo;
+  const uint64_t E = 4 * e + 64 - (uint64_t)t;
+  const uint64_t minv = neg_inv64(m);  // -m^-1 mod 2^64
+  const uint64_t r = m < (1ull << 32) ? (uint64_t)pow2_mod_odd32(E, (uint32_t)m, (uint32_t)minv)
+                                      : pow2_mod_odd64(E, m, minv);
+  return (lo - r) * (0 - minv);
+}
+
 // floor(p * 2^64 / d) for p < d < 2^34 (the quotient fits in 64 bits): long
 // division in steps of 30, 30 and 4 bits (r << 30 < 2^64), each quotient
 // digit from the float reciprocal and mod_est's correction.
@@ -170,37 +256,47 @@ __device__ __forceinline__ uint64_t frac64(uint64_t p, uint64_t d) {
 }
 
 constexpr int BBP_THREADS = 256;
-constexpr uint64_t POLL_EVERY = 10000;
+constexpr uint64_t CHUNK_TERMS = 1ull << 16;  // terms per work item (256 per thread)
+constexpr uint32_t POLL_CHUNKS = 16;          // stop flag read every 16 items per warp
 
-// One CTA per (position, series): partial wrapping sums of the modular part.
+// Persistent grid over equal work items: item c is chunk c - first[p] of
+// pair p = (position p / 4, series j_(p mod 4)), i.e. terms
+// k in [CHUNK_TERMS (c - first[p]), min(+CHUNK_TERMS, n + 1)), with
+// first[] the prefix sums of the pairs' chunk counts (first[npairs] =
+// total).  Positions uniform in [0, 8e8) make the pairs' term counts differ
+// by orders of magnitude; equal items keep every SM busy to the end.  Each
+// warp adds its wrapping partial sum to sums[p] with one 64-bit atomic
+// (wrapping addition is associative, so the bits do not depend on order).
 __global__ void __launch_bounds__(BBP_THREADS)
-k_bbp_series(const uint64_t* __restrict__ pos, uint32_t npos, uint64_t* __restrict__ sums,
-             const volatile int* stop, int* status) {
-  const uint32_t pair = blockIdx.x;
-  const uint32_t pi = pair >> 2;
+k_bbp_series(const uint64_t* __restrict__ pos, uint32_t npairs, const uint64_t* __restrict__ first,
+             unsigned long long* __restrict__ sums, const volatile int* stop, int* status) {
   const uint32_t js[4] = {1, 4, 5, 6};
-  const uint64_t j = js[pair & 3];
-  const uint64_t n = pos[pi];
-  uint64_t acc = 0;
-  uint64_t done = 0;
-  for (uint64_t k = threadIdx.x; k <= n; k += BBP_THREADS) {
-    if (stop && (done++ % POLL_EVERY) == 0 && *stop) {
-      *status = 1;
-      break;
+  const uint64_t total = first[npairs];
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t iter = 0;
+  for (uint64_t c = blockIdx.x; c < total; c += gridDim.x, iter++) {
+    if (stop && iter % POLL_CHUNKS == 0) {
+      int s = 0;
+      if (lane == 0) s = *stop;
+      if (__shfl_sync(0xFFFFFFFFu, s, 0)) {
+        if (lane == 0) *status = 1;
+        return;
+      }
     }
-    uint64_t d = 8 * k + j;
-    uint64_t p = pow16_mod(n - k, d);
-    acc += frac64(p, d);
-  }
-  // block reduction of the wrapping sums
-  __shared__ uint64_t red[BBP_THREADS / 32];
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint64_t s = 0;
-    for (int w = 0; w < BBP_THREADS / 32; w++) s += red[w];
-    sums[pair] = s;
+    // the pair of item c: the last p with first[p] <= c
+    uint32_t lo = 0, hi = npairs;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (first[mid] <= c) lo = mid;
+      else hi = mid;
+    }
+    const uint64_t n = pos[lo >> 2], j = js[lo & 3];
+    const uint64_t k0 = (c - first[lo]) * CHUNK_TERMS;
+    const uint64_t k1 = min(k0 + CHUNK_TERMS, n + 1);
+    uint64_t acc = 0;
+    for (uint64_t k = k0 + threadIdx.x; k < k1; k += BBP_THREADS) acc += bbp_term(n - k, 8 * k + j);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    if (lane == 0 && acc) atomicAdd(sums + lo, (unsigned long long)acc);
   }
 }
 
@@ -241,6 +337,11 @@ __global__ void k_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_
   fr[i] = frac64(p[i], d[i]);
 }
 
+__global__ void k_bbp_terms(const uint64_t* e, const uint64_t* d, uint32_t n, uint64_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = bbp_term(e[i], d[i]);
+}
+
 }  // namespace pimul_bbp
 
 using namespace pimul_bbp;
@@ -276,6 +377,27 @@ done:
   return rc;
 }
 
+// floor((16^e[i] mod d[i]) 2^64 / d[i]) on the device, the term the
+// series kernel sums (d < 2^34, e < 2^40), for checking.
+extern "C" int pimul_bbp_terms(const uint64_t* e, const uint64_t* d, size_t n, uint64_t* out) {
+  if (n == 0) return PIMUL_OK;
+  if (!e || !d || !out) return fail(PIMUL_EINVAL, "null pointer");
+  if (n > (1u << 30)) return fail(PIMUL_EINVAL, "too many terms for one call");
+  for (size_t i = 0; i < n; i++)
+    if (d[i] == 0 || d[i] >= (1ull << 34) || e[i] >= (1ull << 40)) return fail(PIMUL_EINVAL, "need 1 <= d < 2^34, e < 2^40");
+  int rc = PIMUL_OK;
+  uint64_t* buf = nullptr;
+  BCU(cudaMalloc((void**)&buf, 3 * n * 8));
+  BCU(cudaMemcpy(buf, e, n * 8, cudaMemcpyHostToDevice));
+  BCU(cudaMemcpy(buf + n, d, n * 8, cudaMemcpyHostToDevice));
+  k_bbp_terms<<<(unsigned)((n + 255) / 256), 256>>>(buf, buf + n, (uint32_t)n, buf + 2 * n);
+  BCU(cudaGetLastError());
+  BCU(cudaMemcpy(out, buf + 2 * n, n * 8, cudaMemcpyDeviceToHost));
+done:
+  if (buf) cudaFree(buf);
+  return rc;
+}
+
 // Batched hex digits: digits[i] = 8 hex digits of pi at positions[i].
 extern "C" int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uint32_t* digits,
                                     const volatile int* stop) {
@@ -288,6 +410,8 @@ extern "C" int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uin
   cudaStream_t st = nullptr;
   uint64_t* d_pos = nullptr;
   uint64_t* d_sums = nullptr;
+  uint64_t* d_first = nullptr;
+  std::vector<uint64_t> first;
   uint32_t* d_dig = nullptr;
   int* h_flag = nullptr;
   int* d_flag = nullptr;
@@ -303,10 +427,25 @@ extern "C" int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uin
   *h_status = 0;
   BCU(cudaHostGetDevicePointer((void**)&d_flag, h_flag, 0));
   BCU(cudaHostGetDevicePointer((void**)&d_status, h_status, 0));
-  BCU(cudaMemcpyAsync(d_pos, positions, count * 8, cudaMemcpyHostToDevice, st));
-  k_bbp_series<<<(unsigned)(4 * count), BBP_THREADS, 0, st>>>(d_pos, (uint32_t)count, d_sums,
-                                                              stop ? (const volatile int*)d_flag : nullptr,
-                                                              d_status);
+  {
+    // work items: chunks of CHUNK_TERMS terms per (position, series) pair
+    first.resize(4 * count + 1);
+    first[0] = 0;
+    for (size_t p = 0; p < 4 * count; p++)
+      first[p + 1] = first[p] + (positions[p / 4] + 1 + CHUNK_TERMS - 1) / CHUNK_TERMS;
+    int dev = 0, sms = 0, per_sm = 0;
+    BCU(cudaGetDevice(&dev));
+    BCU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BCU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bbp_series, BBP_THREADS, 0));
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(first.back(), (uint64_t)sms * std::max(per_sm, 1)));
+    BCU(cudaMallocAsync((void**)&d_first, first.size() * 8, st));
+    BCU(cudaMemcpyAsync(d_pos, positions, count * 8, cudaMemcpyHostToDevice, st));
+    BCU(cudaMemcpyAsync(d_first, first.data(), first.size() * 8, cudaMemcpyHostToDevice, st));
+    BCU(cudaMemsetAsync(d_sums, 0, count * 4 * 8, st));
+    k_bbp_series<<<(unsigned)grid, BBP_THREADS, 0, st>>>(d_pos, (uint32_t)(4 * count), d_first,
+                                                         (unsigned long long*)d_sums,
+                                                         stop ? (const volatile int*)d_flag : nullptr, d_status);
+  }
   k_bbp_combine<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(d_pos, (uint32_t)count, d_sums, d_dig);
   BCU(cudaGetLastError());
   // Wait, forwarding the caller's stop flag to the kernels (bounded sleep
@@ -328,6 +467,7 @@ done:
   if (st) cudaStreamSynchronize(st);
   if (d_pos) cudaFreeAsync(d_pos, st);
   if (d_sums) cudaFreeAsync(d_sums, st);
+  if (d_first) cudaFreeAsync(d_first, st);
   if (d_dig) cudaFreeAsync(d_dig, st);
   if (st) {
     cudaStreamSynchronize(st);

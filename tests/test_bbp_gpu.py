@@ -83,3 +83,25 @@ def test_modular_building_blocks_at_large_moduli():
         dd, ee, pp = int(d[i]), int(e[i]), int(p[i])
         assert int(pw[i]) == pow(16, ee, dd), (ee, dd)
         assert int(fr[i]) == (pp << 64) // dd, (pp, dd)
+
+
+def test_terms_exact_division_at_large_moduli():
+    # the summed term floor((16^e mod d) 2^64 / d) (bbp.rs:117-140) as the
+    # series kernel computes it, against Python's integers: both Montgomery
+    # widths (odd part below and above 2^32), t = 0, 1, 2 and larger powers
+    # of two, e = 0 and exponents near 2^31
+    rng = np.random.default_rng(33)
+    k = rng.integers(0, 1 << 31, 3000, dtype=np.uint64)
+    d = np.concatenate([8 * k[:750] + np.uint64(1), 8 * k[750:1500] + np.uint64(4),
+                        8 * k[1500:2250] + np.uint64(5), 8 * k[2250:] + np.uint64(6),
+                        rng.integers(1, 1 << 34, 2000, dtype=np.uint64),
+                        np.array([1, 2, 3, 4, 5, 6, 8, 12, 13, 14, 16, 1 << 20, 3 << 30, (1 << 32) - 1, (1 << 32) + 1,
+                                  (1 << 33) + 12, (1 << 34) - 1, (1 << 34) - 2, 2**32 - 5], dtype=np.uint64)])
+    e = rng.integers(0, 1 << 31, d.size, dtype=np.uint64)
+    e[:40] = np.arange(40)
+    e[-19:] = np.array([0, 1, 0, 1, 2, 0, 1, 0, 3, 7, 1, 5, 9, (1 << 31) - 1, 1 << 30, 12345, 0, 1, 77],
+                       dtype=np.uint64)
+    got = pm.bbp_terms(e, d)
+    for i in range(d.size):
+        dd, ee = int(d[i]), int(e[i])
+        assert int(got[i]) == (pow(16, ee, dd) << 64) // dd, (ee, dd)
