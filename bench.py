@@ -332,7 +332,10 @@ def run_gpu(args):
             "e2e": None if not e2e_steps else {
                     "value": round(e2e_value, 2), "unit": "GB/s", "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
                     "h2d_bytes_per_step": 8 * (la + lb), "d2h_bytes_per_step": 8 * (la + lb),
-                    "api": "pimul_mul (host buffers, pinned)"},
+                    "api": "pimul_mul (host buffers, pinned)",
+                    "host_link": "pinned copies measured on this box at 209 GB/s H2D and 192 GB/s D2H (copy engines "
+                                 "and SM copy kernels alike): a's upload and the product's download cannot overlap "
+                                 "the multiply; b's upload is hidden behind a's forward transform"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": round(NCU_TRAFFIC_BYTES_PER_WORD * N) if dom == "pass_fwd" else None,
