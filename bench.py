@@ -812,10 +812,23 @@ def cpu_baseline_sample(la, lb, n):
     t0 = time.perf_counter()
     oracle.mul_mag_ntt(a, b)
     dt = time.perf_counter() - t0
+    # one core: a bounded sample (a 2^26 x 2^26-bit product), same bytes model
+    sa, sb = make_operands(1 << 20, 1 << 20, seed=8)
+    sn = 1 << next_pow2_log(4 * (2 << 20) - 1)
+    oracle.set_threads(1)
+    try:
+        t1 = time.perf_counter()
+        oracle.mul_mag_ntt(sa, sb)
+        dt1 = time.perf_counter() - t1
+    finally:
+        oracle.set_threads(threads)
     return {"value": round(b_mul(n, la, lb) / dt / 1e9, 3), "unit": "GB/s", "cores": threads,
             "kind": "port", "seconds": round(dt, 2),
             "sample": f"one {la}x{lb}-limb product (the full workload) through the C restatement of "
-                      f"mul_mag_ntt (crates/bignum/src/ntt.rs:806-865), OpenMP on {threads} threads"}
+                      f"mul_mag_ntt (crates/bignum/src/ntt.rs:806-865), OpenMP on {threads} threads",
+            "one_core": {"value": round(b_mul(sn, 1 << 20, 1 << 20) / dt1 / 1e9, 3), "unit": "GB/s",
+                         "seconds": round(dt1, 2),
+                         "sample": "one 2^26 x 2^26-bit product (2^20 x 2^20 limbs) on 1 thread"}}
 
 
 def run_reference(args):
