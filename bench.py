@@ -465,9 +465,52 @@ def run_batch(args):
         "model_gbs": round(bytes_model / (ms_plan * 1e-3) / 1e9, 1),
         "bit_exact_vs_plain": exact,
         "autotune": tune,
+        "cpu_baseline": None if args.no_cpu_baseline else batch_cpu_baseline(ops_a, ops_b, d_out, out_off),
     }
     plan.close()
     print(json.dumps(line), flush=True)
+
+
+def batch_cpu_baseline(ops_a, ops_b, d_out, out_off):
+    """The oracle's mul_mag (the reference's dispatch: schoolbook, Karatsuba,
+    NTT at >= 8192 limbs) on the same products: all 4096 across a pool of
+    single-threaded workers (one product per task), and a seeded 1/8
+    subsample one after another on one thread (scaled to 4096)."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    oracle.build()
+    threads = oracle.max_threads()
+    n = len(ops_a)
+
+    def one(i):
+        oracle.set_threads(1)  # this worker's OpenMP setting
+        return oracle.mul_mag(ops_a[i], ops_b[i])
+
+    try:
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            res = list(ex.map(one, range(n)))
+        t_pool = time.perf_counter() - t0
+        sub = np.random.default_rng(9).choice(n, size=n // 8, replace=False)
+        oracle.set_threads(1)
+        t1 = time.perf_counter()
+        for i in sub:
+            oracle.mul_mag(ops_a[i], ops_b[i])
+        t_serial = (time.perf_counter() - t1) * n / len(sub)
+    finally:
+        oracle.set_threads(threads)
+    # the pool's products against the GPU's (device output, trimmed)
+    out = d_out.cpu().numpy().view(np.uint64)
+    same = all(np.array_equal(res[i], np.trim_zeros(out[int(out_off[i]): int(out_off[i]) + ops_a[i].size +
+                                                         ops_b[i].size], "b")) for i in range(n))
+    return {"value": round(n / t_pool, 1), "unit": "products/s", "cores": threads, "kind": "port",
+            "seconds": round(t_pool, 3),
+            "sample": f"the same {n} products through the C restatement of mul_mag (integer.rs:445-486 dispatch), "
+                      f"a pool of {threads} single-threaded workers",
+            "serial_one_core": {"value": round(n / t_serial, 1), "unit": "products/s",
+                                "seconds_scaled": round(t_serial, 3),
+                                "sample": f"{n // 8} seeded products of the batch on one thread, scaled to {n}"},
+            "gpu_matches_cpu": bool(same)}
 
 
 # ----------------------------------------------------------------- served form
