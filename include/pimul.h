@@ -375,9 +375,11 @@ int pimul_bbp_hex_digits(const uint64_t* positions, size_t count, uint32_t* digi
                          const volatile int* stop);
 const char* pimul_bbp_last_error(void);
 
-/* The extractor's modular building blocks on the device, for checking:
+/* The reference's two modular building blocks on the device, for checking:
  * pow16[i] = 16^e[i] mod d[i] and frac[i] = floor(p[i] 2^64 / d[i]) for
- * 1 <= d[i] < 2^34 and p[i] < d[i] (bbp.rs:117-140).  Synchronous. */
+ * 1 <= d[i] < 2^34 and p[i] < d[i] (bbp.rs:117-140).  The series kernel
+ * computes their composition as one division-free term (pimul_bbp_terms).
+ * Synchronous. */
 int pimul_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_t* p, size_t n, uint64_t* pow16,
                      uint64_t* frac);
 

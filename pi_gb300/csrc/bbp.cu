@@ -328,7 +328,9 @@ __global__ void k_bbp_combine(const uint64_t* __restrict__ pos, uint32_t npos, c
   digits[i] = (uint32_t)(c >> 32);
 }
 
-// Building blocks for given (e, d, p): 16^e mod d and floor(p 2^64 / d).
+// The reference's building blocks for given (e, d, p), 16^e mod d and
+// floor(p 2^64 / d), each on its own (the series kernel fuses them in
+// bbp_term); for checking.
 __global__ void k_bbp_modops(const uint64_t* e, const uint64_t* d, const uint64_t* p, uint32_t n, uint64_t* pw,
                              uint64_t* fr) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
