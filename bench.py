@@ -766,8 +766,11 @@ def run_hex(args):
     if args.hex_input != "pi":
         args.hex_checks = 0
     rng = np.random.default_rng(2026)
-    hi = max(1, min(h - 40, 4_000_000))  # BBP cost grows with the position
-    pos = np.unique(np.concatenate([[0], rng.integers(0, hi, size=args.hex_checks)]).astype(np.uint64))
+    # seeded positions over the whole text, the first and the last one before
+    # verify-hex's 32-digit tail (verify_hex.rs:540-547); at 2^31 and above
+    # the BBP kernel's moduli would pass 2^34
+    hi = max(1, min(h - 40, 1 << 31))
+    pos = np.unique(np.concatenate([[0, hi - 1], rng.integers(0, hi, size=args.hex_checks)]).astype(np.uint64))
     bbp_ok = None
     if args.hex_input == "pi":
         d = pm.bbp_hex_digits(pos)
