@@ -197,10 +197,24 @@ __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
 // from a 32-bit remainder; nothing converts 64-bit integers to floats.
 __device__ __forceinline__ uint32_t pow2_mod_odd32(uint64_t E, uint32_t m, uint32_t minv) {
   uint32_t x = (0u - m) % m;  // R mod m: the Montgomery form of 1
-  const int top = 63 - __clzll((long long)E);
-  for (int b = top; b >= 0; b--) {
-    if (b != top) x = mont_mul32(x, x, m, minv);
-    if ((E >> b) & 1) x = dbl_mod32(x, m);
+  // bits 32 and up (E < 2^40) first, then the low word's 32 bits unrolled
+  // with the current bit in the sign position; while x is the Montgomery
+  // one (leading zeros of a small E) squaring leaves it unchanged
+  const uint32_t eh = (uint32_t)(E >> 32);
+  if (eh) {
+    const int top = 31 - __clz((int)eh);
+    x = dbl_mod32(x, m);
+    for (int b = top - 1; b >= 0; b--) {
+      x = mont_mul32(x, x, m, minv);
+      if ((eh >> b) & 1) x = dbl_mod32(x, m);
+    }
+  }
+  uint32_t el = (uint32_t)E;
+#pragma unroll
+  for (int b = 0; b < 32; b++) {
+    x = mont_mul32(x, x, m, minv);
+    if ((int32_t)el < 0) x = dbl_mod32(x, m);
+    el <<= 1;
   }
   return mont_mul32(x, 1, m, minv);
 }
