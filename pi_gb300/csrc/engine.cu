@@ -262,6 +262,28 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
   constexpr int TL = 8 - T;
   const uint32_t tlo = tid >> T, jj = tid & ((1u << T) - 1);
   const uint64_t gbase = ((uint64_t)tlo << S) + j0 + jj;
+  if (L > LVL_MAX) {
+    // w^(f (j0 + jj)) = w^(f j0) w^(f jj): the first factor for the tile's
+    // 2^R frequencies replaces the round twiddles in tw (the rounds are
+    // done), the second (f jj < 4096) comes from the L1-resident near table
+    for (uint32_t f = tid; f < (1u << R); f += PASS_THREADS) tw[f] = root_pow32(RT, L, f * (uint32_t)j0, false);
+    __syncthreads();
+    const uint64_t* __restrict__ nt = near_table(RT, L, false);
+    const uint32_t f0 = row_freq_t<R>(tlo);
+#pragma unroll 2
+    for (int g = 0; g < PER_THREAD; g += 8) {
+      uint64_t t8[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint32_t f = f0 + row_freq_t<R>((g + q) << TL);
+        t8[q] = gl::mul(tw[f], __ldg(nt + f * jj));
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        data[gbase + ((uint64_t)((g + q) << TL) << S)] = gl::mul(sm[spad((g + q) * PASS_THREADS + tid)], t8[q]);
+    }
+    return;
+  }
   const uint32_t Jc = (uint32_t)(j0 + jj);
   const uint32_t eJ = row_freq_t<R>(tlo) * Jc;
 #pragma unroll 2
@@ -500,15 +522,37 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
 #pragma unroll
   for (int q = 0; q < PER_THREAD; q++)
     cp_async8(sm + spad(q * PASS_THREADS + tid), data + gbase + ((uint64_t)(q << TL) << S));
-  load_tw512(tw, RT);
-  cp_async_wait_all();
-  __syncthreads();
-  // inverse pass twiddles w_N^-(f*j), applied by the first inverse round
-  auto ptw = [&](uint32_t row0, int k, uint32_t j) {
-    const uint32_t f = row_freq_t<R>(row0) + row_freq_t<R>((uint32_t)k);
-    return root_pow32(RT, L, f * (uint32_t)(j0 + j), true);
-  };
-  tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
+  if (L > LVL_MAX) {
+    // inverse pass twiddles w^-(f (j0 + j)) = w^-(f j0) w^-(f j): the first
+    // factor for the tile's 2^R frequencies is staged in tw, which the
+    // first inverse round does not need for round twiddles (its sub-problems
+    // are the radix itself); the round twiddles are loaded after it
+    constexpr int QL = rp_count(R) - 1;
+    static_assert(rp_mlog(R, QL) == rp_bits(R, QL), "the first inverse round has no round twiddles");
+    for (uint32_t f = tid; f < (1u << R); f += PASS_THREADS) tw[f] = root_pow32(RT, L, f * (uint32_t)j0, true);
+    cp_async_wait_all();
+    __syncthreads();
+    const uint64_t* __restrict__ nt = near_table(RT, L, true);
+    auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+      const uint32_t f = row_freq_t<R>(row0) + row_freq_t<R>((uint32_t)k);
+      return gl::mul(tw[f], __ldg(nt + f * j));
+    };
+    round_inv_t<R, T, 0, rp_bits(R, QL), rp_mlog(R, QL), PASS_THREADS>(sm, tw, tid, ptw);
+    __syncthreads();
+    load_tw512(tw, RT);
+    __syncthreads();
+    tile_inv_t<R, T, 0, PASS_THREADS, QL - 1>(sm, tw, tid);
+  } else {
+    load_tw512(tw, RT);
+    cp_async_wait_all();
+    __syncthreads();
+    // inverse pass twiddles w_N^-(f*j), applied by the first inverse round
+    auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+      const uint32_t f = row_freq_t<R>(row0) + row_freq_t<R>((uint32_t)k);
+      return root_pow32(RT, L, f * (uint32_t)(j0 + j), true);
+    };
+    tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
+  }
   for (uint32_t q = tid; q < (1u << (TILE_LOG - 3)); q += PASS_THREADS) {
     uint32_t i = q >> (T - 3), k = q & ((1u << (T - 3)) - 1);
     uint64_t w = ((((uint64_t)i << S) + j0) >> 3) + k;
@@ -790,7 +834,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* 
 static int log2_ceil(uint64_t x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
 
 // Host copies of the root tables: lo, hi, w12, level tables (in this order).
-constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (2u << LVL_MAX);
+constexpr size_t ROOT_WORDS = 2 * 65536 + 4096 + (2u << LVL_MAX) + (size_t)NEAR_LEVELS * 2 * 4096;
 
 static void build_roots(uint64_t* t) {
   uint64_t rho = find_rho();
@@ -815,10 +859,19 @@ static void build_roots(uint64_t* t) {
   for (int k = LVL_MAX - 1; k >= 1; k--)
     for (uint32_t i = 0; i < (1u << k); i++) lvl[(1u << k) + i] = lvl[(2u << k) + 2 * i];
   lvl[0] = lvl[1] = 1;
+  // near tables: w_(2^L)^(+-x) = rho^(+-x 2^(32-L)) for x < 4096
+  uint64_t* nt = lvl + (2u << LVL_MAX);
+  for (int L = LVL_MAX + 1; L <= 32; L++)
+    for (int dir = 0; dir < 2; dir++)
+      for (uint32_t xx = 0; xx < 4096; xx++) {
+        const uint32_t e0 = (uint32_t)((uint64_t)xx << (32 - L));
+        const uint32_t e = dir ? 0u - e0 : e0;
+        nt[((size_t)(L - LVL_MAX - 1) * 2 + dir) * 4096 + xx] = hf::mul(lo[e & 0xFFFFu], hi[e >> 16]);
+      }
 }
 
 static Roots roots_at(const uint64_t* d) {
-  return Roots{d, d + 65536, d + 2 * 65536, d + 2 * 65536 + 4096};
+  return Roots{d, d + 65536, d + 2 * 65536, d + 2 * 65536 + 4096, d + 2 * 65536 + 4096 + (2u << LVL_MAX)};
 }
 
 struct DeviceState {

@@ -32,9 +32,19 @@ struct Roots {
   const uint64_t* hi;   // rho^(e * 2^16), e in [0, 2^16)
   const uint64_t* w12;  // w_4096^t = rho^(t * 2^20), t in [0, 4096)
   const uint64_t* lvl;  // per-level tables: w_(2^k)^x at lvl[2^k + x], 1 <= k <= LVL_MAX
+  const uint64_t* near; // w_(2^L)^(+-x) for x < 4096, LVL_MAX < L <= 32 (see near_table)
 };
 
 constexpr int LVL_MAX = 20;
+constexpr int NEAR_LEVELS = 32 - LVL_MAX;  // transform lengths 2^21 .. 2^32
+
+// The 4096 powers w_(2^L)^x (inverse: w_(2^L)^-x), x < 4096, of a length
+// 2^L > 2^LVL_MAX.  A first-pass twiddle w^(f (j0 + jj)) with f jj < 4096
+// is w^(f j0) (staged per CTA) times one entry of this 32 KB table, which
+// stays in L1, instead of two loads from the 512 KB rho tables.
+__device__ __forceinline__ const uint64_t* near_table(const Roots& R, int L, bool inverse) {
+  return R.near + ((size_t)(L - LVL_MAX - 1) * 2 + (inverse ? 1 : 0)) * 4096;
+}
 
 // rho^e for e in [0, 2^32).
 __device__ __forceinline__ uint64_t rho_pow(const Roots& R, uint32_t e) {
