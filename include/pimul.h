@@ -76,7 +76,7 @@ int pimul_mul_device(const uint64_t* d_a, size_t la, const uint64_t* d_b, size_t
  * when they multiply (a GPU whose memory belongs to another allocator, a
  * loop where cudaMalloc's implicit synchronisation is not allowed, a runtime
  * that allocates only at start-up).  It uses no memory pool: its scratch is
- * a fixed device array inside this library (17 MiB of scratch plus 17 MiB
+ * a fixed device array inside this library (17 MiB of scratch plus 18 MiB
  * of root tables, resident on every GPU that loads the library until exit), so products are limited to
  * la + lb <= 262144 limbs (transform length <= 2^20); larger ones return
  * PIMUL_EINVAL.  All calls share that array: calls that overlap on the GPU

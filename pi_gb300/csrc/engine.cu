@@ -2866,7 +2866,7 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //  * scratch holds two transform arrays of at most 2^20 words plus the carry
 //    windows and scan flags: la + lb <= 262144 limbs (transform length
 //    N <= 2^20); larger products are rejected with PIMUL_EINVAL.  The
-//    scratch (17 MiB) and this path's own root tables (17 MiB) stay
+//    scratch (17 MiB) and this path's own root tables (18 MiB) stay
 //    resident on every GPU that loads this library, until the process exits.
 //  * every call uses the same array, and the array keeps the previous call's
 //    contents; the kernels overwrite every scratch word before reading it,
