@@ -407,6 +407,12 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
     const uint32_t lin = q * PASS_THREADS + tid;
     cp_async8(sm + spad(lin), cin + off + lin);
   }
+  // a's (and the addend's) tile is read after b's rounds: start it towards
+  // L2 now (tiles are 32 KB at 32 KB offsets of 256-byte aligned arrays)
+  if (tid == 0) {
+    if (!sq) prefetch_l2_bulk(a + off, (8u << TILE_LOG));
+    if (EXT && X) prefetch_l2_bulk(X + off, (8u << TILE_LOG));
+  }
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();

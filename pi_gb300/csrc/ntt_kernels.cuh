@@ -99,6 +99,12 @@ __device__ __forceinline__ void cp_async8(uint64_t* smem_dst, const uint64_t* gs
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// Bulk prefetch of [src, src + bytes) into L2 (no completion to wait for);
+// src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // DIF radix-2 butterfly with a constant shift twiddle 2^S (S = 0: none).
 template <int S>
 __device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
