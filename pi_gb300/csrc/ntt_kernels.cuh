@@ -251,6 +251,31 @@ __host__ __device__ constexpr int rp_mlog(int r, int q) {
   return m;
 }
 
+// Item order of a round: with one pad word per 16, a half-warp of some
+// rounds puts two lanes on one 8-byte bank (rows 64 words apart land 4
+// banks apart).  Swapping item-number bits 3 and k, a bijection on the
+// round's items, spreads them; k per round from a model of the padded
+// layout (0: keep the order).
+template <int R, int T, int BC, int MLOG>
+__host__ __device__ constexpr int round_swap_bit() {
+  return (T == 3 && BC == 0 && R == 9 && MLOG == 3)   ? 4
+         : (T == 0 && R == 9 && MLOG == 6)             ? 4
+         : (T == 3 && (R == 8 || R == 7) && MLOG == 2) ? 5
+         : (T == 3 && R == 6 && MLOG == 3)             ? 4
+         : (T == 0 && R == 6 && MLOG == 6)             ? 4
+                                                       : 0;
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t swap_bit3(uint32_t w) {
+  if constexpr (K == 0) {
+    return w;
+  } else {
+    const uint32_t d = ((w >> 3) ^ (w >> K)) & 1u;
+    return w ^ (d << 3) ^ (d << K);
+  }
+}
+
 // Tile of 2^BC blocks x 2^R rows x 2^T columns in shared memory; element
 // (row, col) of the flattened (BC+R)-bit row index at spad(row << T | col).
 // One forward round of radix 2^B over sub-problems of 2^MLOG rows.
@@ -266,7 +291,7 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
-    const uint32_t w = it * NT + tid;
+    const uint32_t w = swap_bit3<round_swap_bit<R, T, BC, MLOG>()>(it * NT + tid);
     const uint32_t j = w & ((1u << T) - 1);
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
@@ -307,7 +332,7 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
-    const uint32_t w = it * NT + tid;
+    const uint32_t w = swap_bit3<round_swap_bit<R, T, BC, MLOG>()>(it * NT + tid);
     const uint32_t j = w & ((1u << T) - 1);
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
