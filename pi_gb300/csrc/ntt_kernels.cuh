@@ -252,28 +252,36 @@ __host__ __device__ constexpr int rp_mlog(int r, int q) {
 }
 
 // Item order of a round: with one pad word per 16, a half-warp of some
-// rounds puts two lanes on one 8-byte bank (rows 64 words apart land 4
-// banks apart).  Swapping item-number bits 3 and k, a bijection on the
-// round's items, spreads them; k per round from a model of the padded
-// layout (0: keep the order).
+// rounds puts two or four lanes on one 8-byte bank (rows 64 words apart
+// land 4 banks apart).  Up to two swaps of item-number bits, a bijection on
+// the round's items, spread them; the swaps per round come from a model of
+// the padded layout, packed as a1 | b1 << 4 | a2 << 8 | b2 << 12 (a == b:
+// no swap).
 template <int R, int T, int BC, int MLOG>
-__host__ __device__ constexpr int round_swap_bit() {
-  return (T == 3 && BC == 0 && R == 9 && MLOG == 3)   ? 4
-         : (T == 0 && R == 9 && MLOG == 6)             ? 4
-         : (T == 3 && (R == 8 || R == 7) && MLOG == 2) ? 5
-         : (T == 3 && R == 6 && MLOG == 3)             ? 4
-         : (T == 0 && R == 6 && MLOG == 6)             ? 4
+__host__ __device__ constexpr int round_swaps() {
+  return (T == 3 && BC == 0 && R == 9 && MLOG == 3)   ? (3 | 4 << 4)
+         : (T == 0 && R == 9 && MLOG == 6)             ? (3 | 4 << 4)
+         : (T == 3 && (R == 8 || R == 7) && MLOG == 2) ? (3 | 5 << 4)
+         : (T == 3 && R == 6 && MLOG == 3)             ? (3 | 4 << 4)
+         : (T == 0 && R == 6 && MLOG == 6)             ? (3 | 4 << 4)
+         : (T == 0 && R == 7 && MLOG == 4)             ? (0 | 4 << 4 | 1 << 8 | 5 << 12)
+         : (T == 0 && R == 8 && MLOG == 5)             ? (0 | 1 << 4 | 1 << 8 | 4 << 12)
                                                        : 0;
 }
 
-template <int K>
-__device__ __forceinline__ uint32_t swap_bit3(uint32_t w) {
-  if constexpr (K == 0) {
+template <int A, int B>
+__device__ __forceinline__ uint32_t swap_bits(uint32_t w) {
+  if constexpr (A == B) {
     return w;
   } else {
-    const uint32_t d = ((w >> 3) ^ (w >> K)) & 1u;
-    return w ^ (d << 3) ^ (d << K);
+    const uint32_t d = ((w >> A) ^ (w >> B)) & 1u;
+    return w ^ (d << A) ^ (d << B);
   }
+}
+
+template <int S>
+__device__ __forceinline__ uint32_t round_item(uint32_t w) {
+  return swap_bits<(S >> 8) & 15, (S >> 12) & 15>(swap_bits<S & 15, (S >> 4) & 15>(w));
 }
 
 // Tile of 2^BC blocks x 2^R rows x 2^T columns in shared memory; element
@@ -291,7 +299,7 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
-    const uint32_t w = swap_bit3<round_swap_bit<R, T, BC, MLOG>()>(it * NT + tid);
+    const uint32_t w = round_item<round_swaps<R, T, BC, MLOG>()>(it * NT + tid);
     const uint32_t j = w & ((1u << T) - 1);
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
@@ -332,7 +340,7 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
-    const uint32_t w = swap_bit3<round_swap_bit<R, T, BC, MLOG>()>(it * NT + tid);
+    const uint32_t w = round_item<round_swaps<R, T, BC, MLOG>()>(it * NT + tid);
     const uint32_t j = w & ((1u << T) - 1);
     const uint32_t rest = w >> T;
     const uint32_t jp = rest & ((1u << SLOG) - 1);
