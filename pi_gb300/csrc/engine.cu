@@ -2068,6 +2068,7 @@ static uint64_t svc_new_handle(uint64_t limbs, uint64_t* d, bool pending, uint64
   return id;
 }
 
+void noalloc_forget();  // defined with the no-alloc entry point below
 }  // namespace pimul
 
 // ====================================================================== C ABI
@@ -2082,6 +2083,7 @@ const char* pimul_last_error(void) { return t_err.c_str(); }
 int pimul_init(int device) { return ensure_init(device); }
 
 int pimul_shutdown(void) {
+  pimul::noalloc_forget();
   {
     std::unique_lock<std::mutex> sl(g_svc.mu);
     if (g_svc.running) {
@@ -2883,6 +2885,9 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //    current: it resolves the arrays' device addresses with
 //    cudaGetSymbolAddress and copies the root tables in with a synchronous
 //    cudaMemcpyToSymbol.  Make that first call before any stream capture.
+//    pimul_shutdown forgets the set-up, so a call after a cudaDeviceReset
+//    (made after pimul_shutdown) resolves the addresses and copies the
+//    tables again.
 namespace pimul {
 constexpr int NOALLOC_LOG_MAX = 20;
 constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;
@@ -2903,6 +2908,14 @@ struct NoAllocDev {
 static std::mutex g_na_mu;
 static NoAllocDev g_na[64];
 static uint64_t g_na_host_roots[ROOT_WORDS];  // staging, no heap use
+
+// Forget every device's set-up (pimul_shutdown): the next no-alloc call on a
+// device resolves the symbol addresses and copies the root tables again, as
+// it must after a cudaDeviceReset.
+void noalloc_forget() {
+  std::lock_guard<std::mutex> lk(g_na_mu);
+  for (NoAllocDev& d : g_na) d = NoAllocDev{};
+}
 
 static int noalloc_setup(NoAllocDev** out) {
   int dev = 0;
@@ -2958,7 +2971,9 @@ extern "C" int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const ui
                                         uint64_t* d_out, void* stream) {
   if (la == 0 || lb == 0) return PIMUL_OK;
   if (!d_a || !d_b || !d_out) return fail(PIMUL_EINVAL, "null device pointer");
-  if (la + lb > NOALLOC_N_MAX / 4)
+  // each operand is checked before the sum is formed, so that no size_t
+  // wrap-around can let an oversized pair through
+  if (la > NOALLOC_N_MAX / 4 || lb > NOALLOC_N_MAX / 4 - la)
     return fail(PIMUL_EINVAL, "product too large for the no-alloc scratch: la + lb must be <= 262144 limbs "
                               "(transform length <= 2^20)");
   return mul_device_noalloc(d_a, la, d_b, lb, d_out, (cudaStream_t)stream);

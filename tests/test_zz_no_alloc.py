@@ -35,9 +35,11 @@ def _dev(x):
     return torch.from_numpy(np.ascontiguousarray(x).view(np.int64)).cuda()
 
 
-# (la, lb) pairs: one-CTA path, multi-pass paths, the size limit, a square
+# (la, lb) pairs, each run as two calls in a row: a one-CTA product (N <= 2^12)
+# followed by a 2-pass one (3000 x 1500 limbs, N = 2^15); two multi-pass
+# products; a product at the size limit (N = 2^20) followed by a small one
 CASES = [
-    ((3, 5), (700, 300)),
+    ((3, 5), (3000, 1500)),
     ((20000, 9000), (1 << 17, 1 << 17)),
     ((100000, 162144), (4096, 4096)),
 ]
@@ -72,11 +74,13 @@ def test_noalloc_matches_pool_entry_point_twice(first, second):
         assert torch.equal(got, ref), (la, lb)
 
 
-def test_noalloc_square_and_repeat():
+@pytest.mark.parametrize("n", [50000, 1 << 17])
+def test_noalloc_square_and_repeat(n):
+    # 2^17 limbs squared is the largest square the fixed scratch holds (N = 2^20)
     import torch
     lib = pm.lib()
     noalloc = _fn(lib)
-    a = rand_limbs(50000, 77)
+    a = rand_limbs(n, 77 + n)
     da = _dev(a)
     ref = torch.zeros(2 * a.size, dtype=torch.int64, device="cuda")
     out1 = torch.zeros_like(ref)
@@ -99,3 +103,7 @@ def test_noalloc_rejects_products_above_the_limit():
     # the size check runs on the host before any device work
     assert noalloc(p, 1 << 17, p, (1 << 17) + 1, p, None) == 1
     assert b"262144" in lib.pimul_last_error()
+    # sizes whose sum wraps around in size_t are rejected too
+    assert noalloc(p, (1 << 64) - 1, p, 2, p, None) == 1
+    assert noalloc(p, 1 << 63, p, 1 << 63, p, None) == 1
+    assert noalloc(p, 2, p, (1 << 64) - 1, p, None) == 1
