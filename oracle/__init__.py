@@ -73,6 +73,8 @@ def lib():
         L.orc_mul_abi.argtypes = [_u64p, _sz, _u64p, _sz, _u64p, _sz, ctypes.POINTER(_sz)]
         L.orc_bbp_batch.restype = None
         L.orc_bbp_batch.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_bbp_hex_digits_deep.restype = ctypes.c_uint32
+        L.orc_bbp_hex_digits_deep.argtypes = [_u64]
         _lib = L
     return _lib
 
@@ -178,6 +180,13 @@ def bbp_batch(positions) -> np.ndarray:
     out = np.empty(pos.size, dtype=np.uint32)
     lib().orc_bbp_batch(_p(pos), pos.size, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
     return out
+
+
+def bbp_deep(n: int) -> int:
+    """Digits at one deep position, each series' terms split over all
+    OpenMP threads (same bits as bbp_hex_digits_at; the series sum is
+    wrapping addition, so the split does not matter)."""
+    return int(lib().orc_bbp_hex_digits_deep(int(n)))
 
 
 # ---------------------------------------------------------------- verify-hex

@@ -542,6 +542,8 @@ static uint64_t mod_pow_16(uint64_t e, uint64_t m) {
   return (uint64_t)r;
 }
 
+static void series_tail(uint64_t j, uint64_t n, uint64_t* res);
+
 /* bbp.rs:82-117; stop is polled every 10^4 terms like bbp.rs:88-92.
  * Returns 0 on success, 1 if stopped. */
 static int series_fixed(uint64_t j, uint64_t n, const volatile int* stop, uint64_t* res) {
@@ -553,6 +555,14 @@ static int series_fixed(uint64_t j, uint64_t n, const volatile int* stop, uint64
     u128 term = ((u128)p << 64) / d;
     sum += (uint64_t)term;
   }
+  uint64_t tail_fixed;
+  series_tail(j, n, &tail_fixed);
+  *res = sum + tail_fixed;
+  return 0;
+}
+
+/* bbp.rs:99-115: the f64 tail of the series past k = n, in fixed point. */
+static void series_tail(uint64_t j, uint64_t n, uint64_t* res) {
   double tail = 0.0;
   for (int off = 1; off <= 20; off++) {
     uint64_t k = n + (uint64_t)off;
@@ -563,9 +573,7 @@ static int series_fixed(uint64_t j, uint64_t n, const volatile int* stop, uint64
     if (term == 0.0) break;
     tail += term;
   }
-  uint64_t tail_fixed = (uint64_t)(tail * 18446744073709551616.0);
-  *res = sum + tail_fixed;
-  return 0;
+  *res = (uint64_t)(tail * 18446744073709551616.0);
 }
 
 /* bbp.rs:63-80: returns 0 and the packed digits, or 1 when stopped. */
@@ -578,6 +586,31 @@ int orc_bbp_hex_digits_at(uint64_t n, const volatile int* stop, uint32_t* digits
   uint64_t c = 4 * s1 - 2 * s4 - s5 - s6;
   *digits = (uint32_t)(c >> 32);
   return 0;
+}
+
+/* One deep position with each series' terms split across the OpenMP
+ * threads: the series sum is wrapping u64 addition (bbp.rs:93-97), which is
+ * associative and commutative, so any split gives the same bits as
+ * series_fixed.  Only the scheduling differs from bbp.rs:82-117. */
+static uint64_t series_fixed_par(uint64_t j, uint64_t n) {
+  uint64_t sum = 0;
+#pragma omp parallel for schedule(static, 65536) reduction(+ : sum)
+  for (int64_t k = 0; k <= (int64_t)n; k++) {
+    uint64_t d = 8 * (uint64_t)k + j;
+    uint64_t p = mod_pow_16(n - (uint64_t)k, d);
+    u128 term = ((u128)p << 64) / d;
+    sum += (uint64_t)term;
+  }
+  uint64_t tail_sum;
+  series_tail(j, n, &tail_sum);
+  return sum + tail_sum;
+}
+
+uint32_t orc_bbp_hex_digits_deep(uint64_t n) {
+  uint64_t s1 = series_fixed_par(1, n), s4 = series_fixed_par(4, n);
+  uint64_t s5 = series_fixed_par(5, n), s6 = series_fixed_par(6, n);
+  uint64_t c = 4 * s1 - 2 * s4 - s5 - s6;
+  return (uint32_t)(c >> 32);
 }
 
 /* Many positions across threads (the verify-hex check loop's shape). */

@@ -40,6 +40,17 @@ def test_deeper_positions_match_oracle():
     assert np.array_equal(pm.bbp_hex_digits(pos), O.bbp_batch(pos))
 
 
+@pytest.mark.parametrize("n", [12_345_678, 87_654_321, 550_000_007])
+def test_deep_positions_match_oracle(n):
+    # Positions of config 5's range [0, 8e8).  At 550,000,007 the odd moduli
+    # d = 8k + 1 and 8k + 5 pass 2^32 for k >= 2^29, so the kernel's 64-bit
+    # Montgomery branch computes about 2.6e7 of the terms; below 5.4e8 every
+    # odd part stays under 2^32.  The oracle splits each series over all
+    # host threads (tens of seconds at the deepest position).
+    got = int(pm.bbp_hex_digits(np.array([n], dtype=np.uint64))[0])
+    assert got == O.bbp_deep(n), n
+
+
 def test_stop_flag_cancels():
     # bbp.rs:199-204: a stop flag set before the call returns without digits
     flag = ctypes.c_int(1)

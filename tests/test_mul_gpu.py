@@ -52,6 +52,7 @@ def test_golden_digest_32768(golden):
 SIZES = [(1, 1), (1, 4), (4, 4), (8, 5), (32, 16), (60, 60), (200, 200), (255, 256), (256, 256),
          (511, 512), (512, 512), (513, 512), (1000, 3000), (3000, 1000), (1, 5000), (8192, 8192),
          (4096, 1), (10000, 12345), (1 << 15, 1 << 15), (1 << 16, 1 << 16), (1 << 17, 1 << 16),
+         (1 << 18, 1 << 18),
          (1 << 18, 5), (3, 1 << 18), (1 << 19, 1 << 19)]
 
 
@@ -155,57 +156,20 @@ def test_concurrent_callers():
 
 
 # --------------------------------------------------------------- full sizes
-def residues(limbs, primes):
-    """value mod q for each q (< 2^31) from 32-bit halves, vectorised."""
-    h = np.asarray(limbs, dtype=np.uint64).view(np.uint32).astype(np.int64)
-    out = []
-    K = 4096
-    pad = (-h.size) % K
-    hb = np.concatenate([h, np.zeros(pad, dtype=np.int64)]).reshape(-1, K)
-    for q in primes:
-        w = pow(2, 32, q)
-        W = np.empty(K, dtype=np.int64)
-        x = 1
-        for k in range(K):
-            W[k] = x
-            x = x * w % q
-        S = ((hb % q) * W % q).sum(axis=1) % q
-        wk = pow(w, K, q)
-        r = 0
-        for s in S[::-1]:
-            r = (r * wk + int(s)) % q
-        out.append(r)
-    return out
-
-
-PRIMES = [2147483647, 2147483629, 2147483587]
-
-
-@pytest.mark.parametrize("bits_a,bits_b", [(1 << 28, 1 << 28), (1 << 30, 1 << 30), (1 << 30, 1 << 20)])
-def test_full_size_residues(bits_a, bits_b):
+# The isolated-multiply sweep's sizes, compared with the oracle bit for bit
+# (the oracle runs a 2^30 x 2^30-bit product in a few seconds on all host
+# cores): balanced 2^24, 2^28 and 2^30 bits, the unbalanced 2^30 x 2^20,
+# and squares at 2^24, 2^28 and 2^30 bits.
+@pytest.mark.parametrize("bits_a,bits_b", [(1 << 24, 1 << 24), (1 << 28, 1 << 28), (1 << 30, 1 << 30),
+                                           (1 << 30, 1 << 20), (1 << 20, 1 << 30)])
+def test_full_size_exact_vs_oracle(bits_a, bits_b):
     la, lb = bits_a // 64, bits_b // 64
-    a, b = rand_limbs(la, 101), rand_limbs(lb, 202)
-    got = pm.mul_mag_ntt(a, b)
+    got = check(rand_limbs(la, 101 + la), rand_limbs(lb, 202 + lb))
     assert got.size == la + lb or got.size == la + lb - 1
-    ra, rb, rc = residues(a, PRIMES), residues(b, PRIMES), residues(got, PRIMES)
-    for q, x, y, z in zip(PRIMES, ra, rb, rc):
-        assert x * y % q == z
-    # exact low limbs: product mod 2^(64*k) from the low limbs of the operands
-    k = 64
-    lowa, lowb = O.limbs_to_int(a[:k]), O.limbs_to_int(b[:k])
-    assert O.limbs_to_int(got[:k]) == (lowa * lowb) % (1 << (64 * k))
 
 
-def test_full_size_square_residues():
-    la = (1 << 30) // 64
-    a = rand_limbs(la, 303)
-    got = pm.mul_mag_ntt(a, a)
-    ra, rc = residues(a, PRIMES), residues(got, PRIMES)
-    for q, x, z in zip(PRIMES, ra, rc):
-        assert x * x % q == z
-
-
-def test_2e28_bits_exact_vs_oracle():
-    la = (1 << 28) // 64
-    a, b = rand_limbs(la, 11), rand_limbs(la, 12)
-    check(a, b)
+@pytest.mark.parametrize("bits", [1 << 24, 1 << 28, 1 << 30])
+def test_full_size_square_exact_vs_oracle(bits):
+    n = bits // 64
+    got = check(rand_limbs(n, 303 + n), None, square=True)
+    assert got.size in (2 * n, 2 * n - 1)
