@@ -249,6 +249,12 @@ typedef int (*pimul_mul_fn)(const uint64_t* a, size_t la, const uint64_t* b, siz
  * conversion wall times; ntt_products = number of backend calls;
  * ntt_hist33[L] = backend calls with transform length 2^L.
  *
+ * Re-entrant: the backend, the threshold, the error state and the
+ * statistics belong to the call (the pi drivers below and pimul_to_decimal
+ * alike), so calls from different host threads may run at the same time.
+ * The first backend error stops the run: no later product is issued, and
+ * the call returns that backend's code.
+ *
  * Replaces: crates/pi-core/src/algorithm/chudnovsky.rs:75 Chudnovsky::compute
  * with crates/pi-core/src/algorithm/util.rs:25 write_decimal_digits, whose
  * multiplies all reach crates/bignum/src/ntt.rs:806 through

@@ -24,7 +24,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <exception>
 #include <functional>
+#include <list>
 #include <map>
 #include <condition_variable>
 #include <mutex>
@@ -154,17 +156,103 @@ static Limbs copy_limbs(const uint64_t* src, size_t n) {
 
 // ------------------------------------------------------------------ config
 static size_t g_karatsuba_threshold = 32;   // config.rs:101
-static size_t g_ntt_threshold = 8192;       // config.rs:103
 static size_t g_newton_div_threshold = 64;  // config.rs:104
 static size_t g_to_string_dc_threshold = 32;  // config.rs:105
 static const uint64_t PARALLEL_SPLIT = 64;  // pi-core config.rs:61
 
 typedef int (*mul_fn)(const uint64_t*, size_t, const uint64_t*, size_t, uint64_t*, size_t, size_t*);
-static mul_fn g_backend = nullptr;
-static std::atomic<uint64_t> g_ntt_calls{0};
-static std::atomic<uint64_t> g_ntt_hist[33];
-static std::atomic<int> g_error{0};
-static std::string g_errmsg;
+
+// ------------------------------------------------------------------ per-call state
+// Every driver call (pimul_pi_*, pimul_to_decimal) runs with a context of its
+// own: the multiply backend, the NTT threshold, the first backend error and
+// the call's statistics.  The calling thread holds it in t_ctx and every
+// helper thread the pipeline starts (Worker, parallel_for) inherits it, so
+// calls from different host threads share no mutable state.
+struct PiCtx {
+  mul_fn backend = nullptr;
+  size_t ntt_threshold = 8192;  // config.rs:103
+  std::atomic<int> error{0};
+  std::atomic<uint64_t> ntt_calls{0};
+  std::atomic<uint64_t> ntt_hist[33];
+  std::atomic<uint64_t> batch_levels{0};
+  double bt[5] = {0, 0, 0, 0, 0};  // level-batched splitting: time per step (PIMUL_PI_TIMING)
+  double leaf_ms = 0;
+  PiCtx() {
+    for (auto& h : ntt_hist) h.store(0);
+  }
+};
+static thread_local PiCtx* t_ctx = nullptr;
+static PiCtx& C() {
+  static thread_local PiCtx idle;  // only reached outside a driver call
+  return t_ctx ? *t_ctx : idle;
+}
+
+// A backend error stops the pipeline at once: mul_ntt throws PiAbort, which
+// unwinds to the driver's entry point (threads hand it on at join).
+struct PiAbort {
+  int rc;
+};
+
+// A helper thread that runs with the caller's context and hands an
+// exception thrown inside it to whoever joins it.  The destructor joins too,
+// so a thread is never left running when its parent unwinds.
+class Worker {
+ public:
+  Worker() = default;
+  template <class F>
+  explicit Worker(F&& f) {
+    start(std::forward<F>(f));
+  }
+  template <class F>
+  void start(F&& f) {
+    PiCtx* c = t_ctx;
+    th_ = std::thread([this, c, fn = std::forward<F>(f)]() mutable {
+      t_ctx = c;
+      try {
+        fn();
+      } catch (...) {
+        ex_ = std::current_exception();
+      }
+    });
+  }
+  void join() {
+    if (th_.joinable()) th_.join();
+    if (ex_) {
+      std::exception_ptr e = ex_;
+      ex_ = nullptr;
+      std::rethrow_exception(e);
+    }
+  }
+  ~Worker() {
+    if (th_.joinable()) th_.join();
+  }
+  Worker(const Worker&) = delete;
+  Worker& operator=(const Worker&) = delete;
+
+ private:
+  std::exception_ptr ex_;
+  std::thread th_;
+};
+
+// Runs a driver body with ctx as the calling thread's context: returns the
+// body's code, the first backend error, or PIMUL_ENOMEM for a failed host
+// allocation.
+template <class F>
+static int with_ctx(PiCtx& ctx, F&& body) {
+  PiCtx* prev = t_ctx;
+  t_ctx = &ctx;
+  int rc;
+  try {
+    rc = body();
+    if (!rc && ctx.error.load()) rc = ctx.error.load();
+  } catch (const PiAbort& e) {
+    rc = e.rc;
+  } catch (const std::bad_alloc&) {
+    rc = PIMUL_ENOMEM;
+  }
+  t_ctx = prev;
+  return rc;
+}
 
 // ------------------------------------------------------------------ magnitudes
 static void trim(Limbs& a) {
@@ -384,16 +472,19 @@ static Limbs mul_karatsuba(const Limbs& a, const Limbs& b) {  // integer.rs:552-
 static Limbs mul_ntt(const Limbs& a, const Limbs& b) {
   Limbs out(a.size() + b.size());
   size_t n = 0;
-  int rc = g_backend ? g_backend(a.data(), a.size(), b.data(), b.size(), out.data(), out.size(), &n)
+  PiCtx& c = C();
+  if (int e = c.error.load()) throw PiAbort{e};
+  int rc = c.backend ? c.backend(a.data(), a.size(), b.data(), b.size(), out.data(), out.size(), &n)
                      : pimul_mul(a.data(), a.size(), b.data(), b.size(), out.data(), out.size(), &n);
   if (rc) {
-    g_error.store(rc);
-    return {};
+    int none = 0;
+    c.error.compare_exchange_strong(none, rc);
+    throw PiAbort{rc};
   }
   uint64_t L = 0;
   while ((1ull << L) < 4 * (a.size() + b.size()) - 1) L++;
-  g_ntt_calls.fetch_add(1, std::memory_order_relaxed);
-  g_ntt_hist[L].fetch_add(1, std::memory_order_relaxed);
+  C().ntt_calls.fetch_add(1, std::memory_order_relaxed);
+  C().ntt_hist[L].fetch_add(1, std::memory_order_relaxed);
   out.resize(n);
   return out;
 }
@@ -403,7 +494,7 @@ static Limbs mul_mag(const Limbs& a0, const Limbs& b0) {
   if (a0.empty() || b0.empty()) return {};
   size_t smaller = std::min(a0.size(), b0.size());
   bool fits = (a0.size() + b0.size()) * 4 <= (1ull << 32);
-  if (fits && smaller >= g_ntt_threshold) return mul_ntt(a0, b0);
+  if (fits && smaller >= C().ntt_threshold) return mul_ntt(a0, b0);
   if (smaller < g_karatsuba_threshold) return mul_schoolbook(a0, b0);
   return mul_karatsuba(a0, b0);
 }
@@ -960,7 +1051,7 @@ static std::string to_decimal_top(const Int& n) {  // integer.rs:892-930
   divrem(n, sp, hi, lo);
   std::string hs, ls;
   if (n.m.size() >= 4096) {
-    std::thread t([&] { ls = to_decimal_padded(lo, m); });
+    Worker t([&] { ls = to_decimal_padded(lo, m); });
     hs = to_decimal_top(hi);
     t.join();
   } else {
@@ -981,7 +1072,7 @@ static std::string to_decimal_padded(const Int& n, size_t want) {  // integer.rs
   divrem(n, sp, hi, lo);
   std::string hs, ls;
   if (n.m.size() >= 4096) {
-    std::thread t([&] { ls = to_decimal_padded(lo, m); });
+    Worker t([&] { ls = to_decimal_padded(lo, m); });
     hs = to_decimal_padded(hi, want - m);
     t.join();
   } else {
@@ -1174,7 +1265,7 @@ static PQT split(uint64_t a, uint64_t b, int depth) {
   uint64_t m = (a + b) / 2;
   PQT L, R;
   if (b - a >= PARALLEL_SPLIT && depth < 4) {
-    std::thread th([&] { R = split(m, b, depth + 1); });
+    Worker th([&] { R = split(m, b, depth + 1); });
     L = split(a, m, depth + 1);
     th.join();
   } else {
@@ -1198,7 +1289,7 @@ static void split_root(uint64_t a, uint64_t b, Int& q, Int& t) {
   }
   uint64_t m = (a + b) / 2;
   PQT L, R;
-  std::thread th([&] { R = split(m, b, 1); });
+  Worker th([&] { R = split(m, b, 1); });
   L = split(a, m, 1);
   th.join();
   t = add(mul(L.t, R.q), mul(L.p, R.t));
@@ -1272,13 +1363,21 @@ static void parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn
   }
   const size_t parts = std::min(n, nt);
   const size_t per = (n + parts - 1) / parts;
-  std::vector<std::thread> th;
+  std::list<Worker> th;  // Workers do not move: a list constructs them in place
   for (size_t i = 1; i < parts; i++) {
     size_t lo = i * per, hi = std::min(n, lo + per);
-    if (lo < hi) th.emplace_back(fn, lo, hi);
+    if (lo < hi) th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
   }
   fn(0, std::min(n, per));
-  for (auto& t : th) t.join();
+  std::exception_ptr first;
+  for (auto& t : th) {
+    try {
+      t.join();
+    } catch (...) {
+      if (!first) first = std::current_exception();
+    }
+  }
+  if (first) std::rethrow_exception(first);
 }
 
 // Pinned host staging, a device buffer and a stream, grown on demand.
@@ -1323,10 +1422,8 @@ struct LevelStaging {
   }
 };
 
-static std::atomic<uint64_t> g_batch_levels{0};
 // Wall-time split of the batched drivers (ms): host staging, GPU round trip
 // (copies + batch), host unpacking, host-side products, node combine.
-static double g_bt[5];
 
 // Products a[i] * b[i] of magnitudes.  Those whose smaller operand has at
 // least gpu_min limbs go to the GPU in one pimul_mul_batch call: operands
@@ -1376,9 +1473,9 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
       jobs[g] = pimul_job{d_in + off[a], a->size(), d_in + off[b], b->size(), d_out + ooff[g]};
       uint64_t L2 = 0;
       while ((1ull << L2) < 4 * (a->size() + b->size()) - 1) L2++;
-      g_ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
+      C().ntt_hist[L2].fetch_add(1, std::memory_order_relaxed);
     }
-    g_ntt_calls.fetch_add(gi.size(), std::memory_order_relaxed);
+    C().ntt_calls.fetch_add(gi.size(), std::memory_order_relaxed);
     double t1 = now_ms();
     if (cudaMemcpyAsync(d_in, S.h, in_w * 8, cudaMemcpyHostToDevice, S.st) != cudaSuccess) return PIMUL_ECUDA;
     rc = pimul_mul_batch(jobs.data(), jobs.size(), S.st);
@@ -1394,16 +1491,16 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
       }
     });
     double t3 = now_ms();
-    g_bt[0] += t1 - t0;
-    g_bt[1] += t2 - t1;
-    g_bt[2] += t3 - t2;
+    C().bt[0] += t1 - t0;
+    C().bt[1] += t2 - t1;
+    C().bt[2] += t3 - t2;
   }
   double t4 = now_ms();
   parallel_for(ci.size(), [&](size_t lo, size_t hi) {
     for (size_t c = lo; c < hi; c++) out[ci[c]] = mul_mag(*A[ci[c]], *B[ci[c]]);
   });
-  g_bt[3] += now_ms() - t4;
-  return g_error.load();
+  C().bt[3] += now_ms() - t4;
+  return C().error.load();
 }
 
 // One level: nodes[2i], nodes[2i+1] -> next[i]; an odd last node moves up as
@@ -1442,19 +1539,18 @@ static int merge_level(std::vector<PQT>& nodes, LevelStaging& S) {
   });
   if (nodes.size() & 1) next[np] = std::move(nodes.back());
   nodes.swap(next);
-  g_bt[4] += now_ms() - t0;
-  g_batch_levels.fetch_add(1, std::memory_order_relaxed);
+  C().bt[4] += now_ms() - t0;
+  C().batch_levels.fetch_add(1, std::memory_order_relaxed);
   return PIMUL_OK;
 }
 
-static double g_leaf_ms = 0;
 
 static void report_split(const char* what) {
   if (!getenv("PIMUL_PI_TIMING")) return;
   fprintf(stderr, "[pimul] %s: leaves %.1f ms, staging %.1f, gpu %.1f, unpack %.1f, host products %.1f, "
-          "bookkeeping %.1f\n", what, g_leaf_ms, g_bt[0], g_bt[1], g_bt[2], g_bt[3], g_bt[4]);
-  for (double& x : g_bt) x = 0;
-  g_leaf_ms = 0;
+          "bookkeeping %.1f\n", what, C().leaf_ms, C().bt[0], C().bt[1], C().bt[2], C().bt[3], C().bt[4]);
+  for (double& x : C().bt) x = 0;
+  C().leaf_ms = 0;
 }
 
 // ---------------------------------------------- device-resident splitting
@@ -1571,9 +1667,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
       cu(cudaMemcpyAsync(z.q, o.q, o.qn * 8, cudaMemcpyDeviceToDevice, st));
       cu(cudaMemcpyAsync(z.t, o.t, o.tn * 8, cudaMemcpyDeviceToDevice, st));
     }
-    g_ntt_calls.fetch_add(nprod, std::memory_order_relaxed);
+    C().ntt_calls.fetch_add(nprod, std::memory_order_relaxed);
     for (int L2 = 0; L2 < 33; L2++)
-      if (hist[L2]) g_ntt_hist[L2].fetch_add(hist[L2], std::memory_order_relaxed);
+      if (hist[L2]) C().ntt_hist[L2].fetch_add(hist[L2], std::memory_order_relaxed);
     double t1 = now_ms();
     if (!rc) rc = pimul_sum_batch(sj.data(), sj.size(), st);
     const double t_sum = now_ms();
@@ -1608,9 +1704,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
               "subtract %.1f, lengths %.1f + %.1f)\n", np, nprod, next[0].qn, t2 - t1, t1 - t0, t_sum - t1,
               t_as - t_sum, t_arr - t_as, t2 - t_arr);
     nodes.swap(next);
-    g_batch_levels.fetch_add(1, std::memory_order_relaxed);
-    g_bt[1] += t2 - t1;
-    g_bt[4] += (t1 - t0);
+    C().batch_levels.fetch_add(1, std::memory_order_relaxed);
+    C().bt[1] += t2 - t1;
+    C().bt[4] += (t1 - t0);
   }
   return rc;
 }
@@ -1668,7 +1764,7 @@ static int dev_root_truncated(DLevel& Lv, cudaStream_t st, uint64_t top_limbs, D
     sj.push_back(pimul_sum_job{L.t + dx1, L.tn - dx1, R.q + dyq, R.qn - dyq, nullptr, 0, nullptr, 0, tmp, n1});
     sj.push_back(pimul_sum_job{L.p + dx2, L.pn - dx2, R.t + dy2, R.tn - dy2, nullptr, 0, nullptr, 0, tmp + n1, n2});
   }
-  g_ntt_calls.fetch_add(3, std::memory_order_relaxed);
+  C().ntt_calls.fetch_add(3, std::memory_order_relaxed);
   rc = pimul_sum_batch(sj.data(), sj.size(), st);
   if (!rc && diff) {
     pimul_addsub_job aj{tmp, n1, tmp + n1, n2, z.t, tn, 1};
@@ -1779,7 +1875,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     }
     if (!rc) rc = dev_reduce(roots[sgi], st, true);
   }
-  g_leaf_ms += tl;
+  C().leaf_ms += tl;
   DLevel top;
   for (DLevel& r : roots) {
     for (const DNode& n : r.nodes) top.nodes.push_back(n);
@@ -1806,7 +1902,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
       rc = PIMUL_ECUDA;
     q = Int(std::move(qm), false);
     t = Int(std::move(tm), true);
-    g_bt[2] += now_ms() - t0;
+    C().bt[2] += now_ms() - t0;
   }
   dev_free(top, st);
   cudaStreamSynchronize(st);
@@ -1816,8 +1912,8 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
 
 static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int& t, DevRoot* keep = nullptr) {
   const uint64_t nleaf = (b - a + (leaf == LEAF_AUTO ? 32 : leaf) - 1) / (leaf == LEAF_AUTO ? 32 : leaf);
-  for (double& x : g_bt) x = 0;
-  g_leaf_ms = 0;
+  for (double& x : C().bt) x = 0;
+  C().leaf_ms = 0;
   // device-resident levels (every range obeys the static signs; a leaf that
   // did not would send the splitting down the host-staged path below)
   if (nleaf > 1) {
@@ -1831,7 +1927,7 @@ static int split_root_batched(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int
   parallel_for(nleaf, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; i++) nodes[i] = split(a + i * leaf, std::min(b, a + (i + 1) * leaf), 4);
   });
-  g_leaf_ms = now_ms() - t0;
+  C().leaf_ms = now_ms() - t0;
   LevelStaging S;
   int rc = S.init();
   while (!rc && nodes.size() > 1) rc = merge_level(nodes, S);
@@ -1915,7 +2011,7 @@ static int to_decimal_core(const uint64_t* x, size_t n, bool on_dev, uint64_t xb
     own = make_dec_plan(ndig);
     plan = &own;
   }
-  if (g_error.load()) return g_error.load();
+  if (C().error.load()) return C().error.load();
   if (plan->kmin != pidec::LEAF_K) return PIMUL_EINVAL;
   const size_t total = (size_t)19 << plan->K;
   if (want > total) {
@@ -1943,7 +2039,7 @@ static int to_decimal_batched_into(const Int& X, char* out, size_t want, const D
     if (s.size() > want) return PIMUL_EINVAL;
     memset(out, '0', want - s.size());
     memcpy(out + want - s.size(), s.data(), s.size());
-    return g_error.load();
+    return C().error.load();
   }
   return to_decimal_core(X.m.data(), X.m.size(), false, bits_of(X.m), out, want, plan);
 }
@@ -1982,36 +2078,28 @@ static int finish_digits(Flt pi, const Flt& scale, uint64_t digits, char* out, d
   if (device_plan) {
     int rc = to_decimal_batched_into(ip, out, digits, device_plan);
     if (t_phase) *t_phase = now_ms() - t0;
-    return rc ? rc : g_error.load();
+    return rc ? rc : C().error.load();
   }
   std::string s = to_decimal_top(ip);
   if (t_phase) *t_phase = now_ms() - t0;
-  if (g_error.load()) return g_error.load();
+  if (C().error.load()) return C().error.load();
   if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
   memcpy(out, s.data(), digits);
   return PIMUL_OK;
 }
 
 // Digits of pi by Gauss-Legendre (see pimul.h).
-extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
-                                          uint64_t ntt_threshold, uint32_t flags, double* phase_ms,
-                                          uint64_t* ntt_products) {
-  if (digits == 0) return PIMUL_OK;
-  if (!out || cap < digits) return PIMUL_EINVAL;
-  g_backend = reinterpret_cast<mul_fn>(backend);
-  g_ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
-  g_ntt_calls.store(0);
-  for (auto& h : g_ntt_hist) h.store(0);
-  g_error.store(0);
+static int gauss_legendre_body(uint64_t digits, char* out, uint32_t flags, double* phase_ms,
+                               uint64_t* ntt_products) {
   const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
   double t0 = now_ms();
   if (flags & PIMUL_PI_DEVICE_AGM) {
     // the AGM, the quotient and the conversion on the device; the decimal
     // scale and the conversion's divisors on threads beside the iteration
     Flt scale;
-    std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
+    Worker scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
     DecPlan dplan;
-    std::thread plan_th([&] { dplan = make_dec_plan(digits + 1); });
+    Worker plan_th([&] { dplan = make_dec_plan(digits + 1); });
     piagm::AgmOut A;
     int rc = piagm::agm_device(prec, &A, nullptr);
     const double t1 = now_ms();
@@ -2019,7 +2107,7 @@ extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap
     plan_th.join();
     uint64_t* d_ip = nullptr;
     size_t ipn = 0;
-    if (!rc && g_error.load()) rc = g_error.load();
+    if (!rc && C().error.load()) rc = C().error.load();
     if (!rc) {
       // pi 10^(D-1) = scale (a + b)^2 / (4 t)
       const size_t nl = (prec + 192 + 63) / 64, lq = std::min(A.num_limbs, nl);
@@ -2036,17 +2124,17 @@ extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap
       phase_ms[1] = 0;
       phase_ms[2] = now_ms() - t1;
     }
-    if (ntt_products) *ntt_products = g_ntt_calls.load();
+    if (ntt_products) *ntt_products = C().ntt_calls.load();
     return rc;
   }
   // the decimal scale 10^(D-1) at the working precision runs beside the
   // iterations (it depends on nothing else)
   Flt scale;
-  std::thread scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
+  Worker scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
   // the device conversion's divisors and reciprocals too
   const bool device_dec = (flags & PIMUL_PI_DEVICE_DECIMAL) != 0;
   DecPlan dplan;
-  std::thread plan_th([&] {
+  Worker plan_th([&] {
     if (device_dec) dplan = make_dec_plan(digits + 1);
   });
   Flt pi = gauss_legendre(prec, (flags & PIMUL_PI_FAST_SQRT) != 0);
@@ -2060,8 +2148,19 @@ extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap
     phase_ms[1] = 0;
     phase_ms[2] = tdc;
   }
-  if (ntt_products) *ntt_products = g_ntt_calls.load();
+  if (ntt_products) *ntt_products = C().ntt_calls.load();
   return rc;
+}
+
+extern "C" int pimul_pi_gauss_legendre_ex(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
+                                          uint64_t ntt_threshold, uint32_t flags, double* phase_ms,
+                                          uint64_t* ntt_products) {
+  if (digits == 0) return PIMUL_OK;
+  if (!out || cap < digits) return PIMUL_EINVAL;
+  PiCtx ctx;
+  ctx.backend = reinterpret_cast<mul_fn>(backend);
+  ctx.ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
+  return with_ctx(ctx, [&] { return gauss_legendre_body(digits, out, flags, phase_ms, ntt_products); });
 }
 
 extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
@@ -2073,16 +2172,8 @@ extern "C" int pimul_pi_gauss_legendre(uint64_t digits, char* out, size_t cap, p
 // writes `digits` characters ("31415...", no decimal point) to out.
 // phase_ms (optional, 3 entries): binary splitting, final assembly,
 // decimal conversion.  backend NULL = the GPU engine (pimul_mul).
-static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
-                      uint64_t leaf_terms, double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33) {
-  if (digits == 0) return PIMUL_OK;
-  if (!out || cap < digits) return PIMUL_EINVAL;
-  g_backend = reinterpret_cast<mul_fn>(backend);
-  g_ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
-  g_ntt_calls.store(0);
-  g_batch_levels.store(0);
-  for (auto& h : g_ntt_hist) h.store(0);
-  g_error.store(0);
+static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, double* phase_ms,
+                           uint64_t* ntt_products, uint64_t* ntt_hist33) {
   // precision.rs:64: bits = ceil(D log2 10) + 256
   const uint64_t prec = (uint64_t)std::ceil((double)digits * 3.321928094887362) + 256;
   const uint64_t n_terms = (uint64_t)std::ceil((double)digits / DIGITS_PER_TERM) + SAFETY_TERMS;
@@ -2092,7 +2183,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   // depends on nothing else (util.rs:25-83 computes it after pi).
   Flt sq, scale;
   double t_sqrt = 0, t_scale = 0;
-  std::thread sqrt_th([&] {
+  Worker sqrt_th([&] {
     double ts = now_ms();
     Flt p;
     if (leaf_terms) {
@@ -2104,7 +2195,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
     t_sqrt = now_ms() - ts;
   });
-  std::thread scale_th([&] {
+  Worker scale_th([&] {
     double ts = now_ms();
     scale = pow_int(flt_from_u64(10, prec), Int(digits - 1));
     t_scale = now_ms() - ts;
@@ -2113,13 +2204,13 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   // and W = 426880 sqrt(10005) 10^(D-1) for the device final assembly (this
   // thread alone joins the two above; the main thread joins it)
   DecPlan dplan;
-  std::thread plan_th([&] {
+  Worker plan_th([&] {
     if (leaf_terms) dplan = make_dec_plan(digits + 1);
   });
   Flt W;
-  std::thread w_th;
+  Worker w_th;
   if (leaf_terms)
-    w_th = std::thread([&] {
+    w_th.start([&] {
       sqrt_th.join();
       scale_th.join();
       W = mul_at_prec(sq, scale, prec + 64);
@@ -2130,6 +2221,13 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   };
   Int q, t;
   DevRoot droot;  // the root's Q and |T| when they stay on the device
+  struct ArenaGuard {  // returns the root's arenas when a backend error unwinds this call
+    DLevel& L;
+    ~ArenaGuard() {
+      for (uint64_t* ar : L.arenas) cudaFree(ar);
+      L.arenas.clear();
+    }
+  } arena_guard{droot.lvl};
   droot.top_limbs = pidec::final_assembly_top_limbs(prec);
   int brc = PIMUL_OK;
   if (leaf_terms)
@@ -2138,6 +2236,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     split_root(1, n_terms + 1, q, t);
   if (brc) {
     for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
+    droot.lvl.arenas.clear();
     join_sqrt();
     join_scale();
     plan_th.join();
@@ -2154,6 +2253,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     int frc = pidec::final_assembly_device(r.q, r.qn, droot.q_off, r.t, r.tn, droot.t_off, CH_A, W.mant.data(),
                                            W.mant.size(), W.exp, prec, &d_ip, &ipn, fms);
     for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
+    droot.lvl.arenas.clear();
     double t2 = now_ms();
     plan_th.join();
     if (!frc) frc = to_decimal_batched_into_dev(d_ip, ipn, out, digits, &dplan);
@@ -2163,15 +2263,15 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
       fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms, final assembly on the device: "
               "reciprocal %.1f ms, products %.1f ms\n", t_sqrt, t_scale, fms[0], fms[1]);
     if (frc) return frc;
-    if (g_error.load()) return g_error.load();
+    if (C().error.load()) return C().error.load();
     if (phase_ms) {
       phase_ms[0] = t1 - t0;
       phase_ms[1] = t2 - t1;
       phase_ms[2] = t3 - t2;
     }
-    if (ntt_products) *ntt_products = g_ntt_calls.load();
+    if (ntt_products) *ntt_products = C().ntt_calls.load();
     if (ntt_hist33)
-      for (int i = 0; i < 33; i++) ntt_hist33[i] = g_ntt_hist[i].load();
+      for (int i = 0; i < 33; i++) ntt_hist33[i] = C().ntt_hist[i].load();
     return PIMUL_OK;
   }
   // final assembly (chudnovsky.rs:146-204)
@@ -2202,7 +2302,7 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   if (getenv("PIMUL_PI_TIMING"))
     fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms (waited %.1f), reciprocal %.1f ms\n", t_sqrt,
             t_scale, t_join, t_recip);
-  if (g_error.load()) return g_error.load();
+  if (C().error.load()) return C().error.load();
   if (!written) {
     if (s.size() < digits) s = std::string(digits - s.size(), '0') + s;
     memcpy(out, s.data(), digits);
@@ -2212,40 +2312,52 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
     phase_ms[1] = t2 - t1;
     phase_ms[2] = t3 - t2;
   }
-  if (ntt_products) *ntt_products = g_ntt_calls.load();
+  if (ntt_products) *ntt_products = C().ntt_calls.load();
   if (ntt_hist33)
-    for (int i = 0; i < 33; i++) ntt_hist33[i] = g_ntt_hist[i].load();
+    for (int i = 0; i < 33; i++) ntt_hist33[i] = C().ntt_hist[i].load();
   return PIMUL_OK;
+}
+
+static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
+                      uint64_t leaf_terms, double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33,
+                      uint64_t* levels) {
+  if (digits == 0) return PIMUL_OK;
+  if (!out || cap < digits) return PIMUL_EINVAL;
+  PiCtx ctx;
+  ctx.backend = reinterpret_cast<mul_fn>(backend);
+  ctx.ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
+  int rc = with_ctx(ctx, [&] { return chudnovsky_body(digits, out, leaf_terms, phase_ms, ntt_products, ntt_hist33); });
+  if (levels) *levels = ctx.batch_levels.load();
+  return rc;
 }
 
 extern "C" int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend,
                                    uint64_t ntt_threshold, double* phase_ms, uint64_t* ntt_products,
                                    uint64_t* ntt_hist33) {
-  return chudnovsky(digits, out, cap, backend, ntt_threshold, 0, phase_ms, ntt_products, ntt_hist33);
+  return chudnovsky(digits, out, cap, backend, ntt_threshold, 0, phase_ms, ntt_products, ntt_hist33, nullptr);
 }
 
 // Decimal string of a non-negative integer (see pimul.h).
 extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size_t cap, size_t* len,
                                 int batched) {
   if (!len || (n && !limbs)) return PIMUL_EINVAL;
-  g_backend = nullptr;
-  g_ntt_threshold = 8192;
-  g_error.store(0);
-  Int x(Limbs(limbs, limbs + n), false);
-  std::string s;
-  if (x.zero()) {
-    s = "0";
-  } else if (batched) {
-    int rc = to_decimal_batched(x, s);
-    if (rc) return rc;
-  } else {
-    s = to_decimal_top(x);
-    if (g_error.load()) return g_error.load();
-  }
-  *len = s.size();
-  if (!out || cap < s.size()) return PIMUL_EINVAL;
-  memcpy(out, s.data(), s.size());
-  return PIMUL_OK;
+  PiCtx ctx;
+  return with_ctx(ctx, [&]() -> int {
+    Int x(Limbs(limbs, limbs + n), false);
+    std::string s;
+    if (x.zero()) {
+      s = "0";
+    } else if (batched) {
+      int rc = to_decimal_batched(x, s);
+      if (rc) return rc;
+    } else {
+      s = to_decimal_top(x);
+    }
+    *len = s.size();
+    if (!out || cap < s.size()) return PIMUL_EINVAL;
+    memcpy(out, s.data(), s.size());
+    return PIMUL_OK;
+  });
 }
 
 // Batched form (see pimul.h): binary splitting level by level through
@@ -2253,8 +2365,6 @@ extern "C" int pimul_to_decimal(const uint64_t* limbs, size_t n, char* out, size
 extern "C" int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms,
                                            double* phase_ms, uint64_t* gpu_products, uint64_t* levels,
                                            uint64_t* ntt_hist33) {
-  int rc = chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : LEAF_AUTO, phase_ms, gpu_products,
-                      ntt_hist33);
-  if (levels) *levels = g_batch_levels.load();
-  return rc;
+  return chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : LEAF_AUTO, phase_ms, gpu_products,
+                    ntt_hist33, levels);
 }
