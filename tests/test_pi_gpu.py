@@ -112,3 +112,19 @@ def test_batched_small_and_odd_shapes(digits, leaf):
         ref = f.read().strip()
     s, _ = pm.pi_chudnovsky_batched(digits, leaf)
     assert s == ref[:digits]
+
+
+def test_1e8_digits_batched_and_device_agm_match_cpu_restatement():
+    # 10^8 digits against the CPU pipeline's digits (the host restatement of
+    # pi-core's Chudnovsky with every product through the oracle, recorded by
+    # tests/golden/make_pi_cpu_digits.py): the level-batched device-resident
+    # Chudnovsky run and the device Gauss-Legendre AGM both match it.
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["100000000"]
+    assert want["source"] == "cpu-restatement"
+    s, info = pm.pi_chudnovsky_batched(100_000_000)
+    assert s[-20:] == want["last20"]
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+    del s
+    g, _ = pm.pi_gauss_legendre(100_000_000, device_agm=True)
+    assert hashlib.sha256(g.encode()).hexdigest() == want["sha256"]
