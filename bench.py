@@ -43,7 +43,7 @@ BITS_B = 1 << 30
 # DRAM traffic of the dominant kernel class (forward passes) per transform
 # word: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
 # k_col_mid<9,fwd> (x2) and k_fwd_last<8> at N = 2^26 (mean 1023.2 MB per
-# launch = 15.25 bytes per word; profiles/ntt_pass_kernels_2e29_full.md).
+# launch = 15.25 bytes per word).
 # Traffic grows in proportion to N, so a launch moves 15.25 N bytes.
 NCU_TRAFFIC_BYTES_PER_WORD = 15.25
 
@@ -54,6 +54,12 @@ def b_mul(n, la, lb, square=False):
 
 def next_pow2_log(x):
     return (x - 1).bit_length()
+
+
+def mul_workload(la, lb, L):
+    """config.workload of the isolated multiply (the same string in both arms)."""
+    return (f"isolated multiply, balanced 2^{(64 * la).bit_length() - 1} x 2^{(64 * lb).bit_length() - 1} bits "
+            f"({la} x {lb} limbs), N = 2^{L}")
 
 
 def make_operands(la, lb, seed=20241203):
@@ -322,7 +328,7 @@ def run_gpu(args):
             "dtype": "u64",
             "data": "synthetic: seeded uniform u64 limbs, top limb bit 63 set (numpy PCG64)",
             "config": {
-                "workload": f"isolated multiply, balanced 2^{BITS_A.bit_length()-1} x 2^{BITS_B.bit_length()-1} bits ({la} x {lb} limbs), N = 2^{L}",
+                "workload": mul_workload(la, lb, L),
                 "bits_a": BITS_A, "bits_b": BITS_B, "la": la, "lb": lb, "transform_len": N,
                 "bytes_per_step_model": "B_mul(N) = 96N + 16(la+lb)",
                 "bytes_per_step": bytes_step,
@@ -343,7 +349,7 @@ def run_gpu(args):
                          "step_achieved": round(step_achieved, 1),
                          "step_frac": round(step_achieved / peak, 4),
                          "binding_unit": "integer ALU pipe, not HBM (ncu: ALU 62-70 % busy, issue 59-67 %, "
-                                         "DRAM 13-35 % of peak; profiles/ntt_pass_kernels_2e29_full.md)",
+                                         "DRAM 13-35 % of peak, from ncu captures of the pass kernels)",
                          "io_effective_gbs": round(16 * (la + lb) / (ms_step * 1e-3) / 1e9, 1),
                          "integer_model": {
                              "butterflies": 3 * (N // 2) * L, "pointwise_mulmods": 2 * N,
@@ -355,9 +361,167 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
+        if ws == 1:
+            run_extras(line, args, peak)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------- extras
+# The other configurations, measured in the same default run and reported
+# as keys of the headline line: the isolated-multiply sweep, the batched
+# uneven products, the served stream at several offered loads, pi runs and
+# a BBP sample.
+SWEEP = [("mul", 16, 16), ("mul", 20, 20), ("mul", 24, 24), ("mul", 28, 28), ("mul", 30, 30), ("mul", 30, 20),
+         ("sqr", 16, 16), ("sqr", 20, 20), ("sqr", 24, 24), ("sqr", 28, 28), ("sqr", 30, 30)]
+L2_FLUSH_BYTES = 512 << 20  # written between timed calls: larger than the 129 MB L2
+
+
+def sweep_measure(peak):
+    """Config 2's sweep: balanced 2^16..2^30-bit products, 2^30 x 2^20 and
+    squares, operands resident in HBM.  Every call is timed alone with CUDA
+    events on its stream after a 512 MiB write that flushes L2; the median
+    over the repetitions is reported, with GB/s on the two-pass bytes model
+    and a SHA-256 prefix of the product."""
+    import hashlib
+    import torch
+    import pi_gb300 as pm
+    lib = pm.lib()
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    rows = []
+    for kind, ba, bb in SWEEP:
+        sq = kind == "sqr"
+        la, lb = (1 << ba) // 64, (1 << bb) // 64
+        a, b = make_operands(la, lb, seed=1000 + ba + 64 * bb)
+        with torch.cuda.stream(stream):
+            da = torch.from_numpy(a.view(np.int64)).cuda()
+            db = da if sq else torch.from_numpy(b.view(np.int64)).cuda()
+            dout = torch.empty(la + (la if sq else lb), dtype=torch.int64, device="cuda")
+        stream.synchronize()
+        lb_eff = la if sq else lb
+
+        def one():
+            rc = lib.pimul_mul_device(ctypes.c_void_p(da.data_ptr()), la, ctypes.c_void_p(db.data_ptr()), lb_eff,
+                                      ctypes.c_void_p(dout.data_ptr()), sp)
+            if rc:
+                raise RuntimeError(lib.pimul_last_error().decode())
+
+        for _ in range(3):
+            one()
+        stream.synchronize()
+        L = next_pow2_log(4 * la + 4 * lb_eff - 1)
+        n = 1 << L
+        reps = 20 if L >= 25 else 50
+        times = []
+        with torch.cuda.stream(stream):
+            for _ in range(reps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                one()
+                e1.record(stream)
+                times.append((e0, e1))
+        stream.synchronize()
+        ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in times)
+        by = b_mul(n, la, lb_eff, square=sq)
+        gbs = by / (ms * 1e-3) / 1e9
+        digest = hashlib.sha256(dout.cpu().numpy().tobytes()).hexdigest()[:16]
+        rows.append({"case": f"square 2^{ba} bits" if sq else f"2^{ba} x 2^{bb} bits", "la": la, "lb": lb_eff,
+                     "transform_len": f"2^{L}", "ms": round(ms, 4), "gbs": round(gbs, 1),
+                     "hbm_frac": round(gbs / peak, 4), "io_gbs": round(16 * (la + lb_eff) / (ms * 1e-3) / 1e9, 1),
+                     "reps": reps, "product_sha256_16": digest})
+        del da, db, dout
+    del flush
+    torch.cuda.empty_cache()
+    return {"model": "B_mul(N) = 96N + 16(la+lb), B_sqr(N) = 64N + 24la bytes; hbm_frac of measured HBM GB/s",
+            "timing": "each call alone: CUDA events around one pimul_mul_device after a 512 MiB L2 flush; median",
+            "parity": "bit-exact vs the oracle in tests/test_mul_gpu.py (full sizes included)",
+            "rows": rows}
+
+
+def pi_measure():
+    """Chudnovsky pi to 10^9 digits through the level-batched, device-resident
+    splitting, and 10^8 digits both batched and plain (one GPU call per
+    product); wall times, phase splits and SHA-256 of the digits, compared
+    with the recorded hashes (10^8: the CPU restatement's digits)."""
+    import hashlib
+    import pi_gb300 as pm
+    pm.init(0)
+    golden = {}
+    path = os.path.join(ROOT, "tests", "golden", "pi_digits_hashes.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            golden = json.load(f)
+    out = {}
+    pm.pi_chudnovsky_batched(100_000)  # warm-up (tables, pools, kernels)
+    pm.pi_chudnovsky(100_000)
+    for D in (10 ** 9, 10 ** 8):
+        t0 = time.perf_counter()
+        s, info = pm.pi_chudnovsky_batched(D)
+        wall = time.perf_counter() - t0
+        h = hashlib.sha256(s.encode()).hexdigest()
+        rec = golden.get(str(D))
+        key = "pi_1e9" if D == 10 ** 9 else "pi_1e8_plain_vs_batched"
+        out[key] = {"digits": D, "batched_wall_s": round(wall, 3),
+                    "phases_ms": {k: round(v, 1) for k, v in info.items() if k.endswith("_ms")},
+                    "gpu_products": info["ntt_products"], "sha256": h, "last20": s[-20:],
+                    "matches_recorded": None if rec is None else (h == rec["sha256"]),
+                    "recorded_source": None if rec is None else rec.get("source", "mpmath")}
+        if D == 10 ** 8:
+            t1 = time.perf_counter()
+            sp_, _ = pm.pi_chudnovsky(D)
+            pwall = time.perf_counter() - t1
+            out[key].update({"plain_wall_s": round(pwall, 3), "speedup_batched_vs_plain": round(pwall / wall, 2),
+                             "plain_identical": sp_ == s})
+            del sp_
+        del s
+    return out
+
+
+def bbp_measure(positions=64, max_pos=8e8):
+    """A seeded sample of config 5's BBP spot checks, one batched launch."""
+    import pi_gb300 as pm
+    rng = np.random.default_rng(2025)
+    pos = rng.integers(0, int(max_pos), size=positions, dtype=np.uint64)
+    pm.bbp_hex_digits(np.arange(64, dtype=np.uint64))
+    t0 = time.perf_counter()
+    d = pm.bbp_hex_digits(pos)
+    dt = time.perf_counter() - t0
+    terms = 4.0 * float((pos.astype(np.float64) + 1).sum())
+    return {"positions": positions, "range": f"[0, {int(max_pos)})", "wall_s": round(dt, 3),
+            "positions_per_s": round(positions / dt, 3), "terms_per_s": round(terms / dt, 1),
+            "extrapolated_65536_positions_s": round(dt * 65536 / positions, 1),
+            "first_digits": [f"{int(x):08x}" for x in d[:4]]}
+
+
+def run_extras(line, args, peak):
+    """Adds the other configurations to the headline line (rank 0, one GPU)."""
+    import torch
+    steps = [("sweep", lambda: sweep_measure(peak)),
+             ("batch4096", lambda: batch_measure(10, 3, tune=True, cpu=not args.no_cpu_baseline)),
+             ("served", lambda: served_measure(args.requests, [0.8, 1.0, 1.5, 2.0])),
+             ("pi", pi_measure),
+             ("bbp", bbp_measure)]
+    only = set(args.extras.split(",")) if args.extras not in ("all", "none") else None
+    for name, fn in steps:
+        if args.extras == "none" or (only is not None and name not in only):
+            continue
+        t0 = time.perf_counter()
+        try:
+            r = fn()
+        except Exception as e:  # noqa: BLE001 - one failing extra must not lose the headline
+            r = {"error": f"{type(e).__name__}: {e}"}
+        torch.cuda.empty_cache()
+        if name == "pi" and "error" not in r:
+            line.update(r)
+        else:
+            for k in ("project_metric", "n_gpus", "vs_baseline", "dtype", "scaling"):
+                r.pop(k, None)
+            line[name] = r
+        line.setdefault("extras_wall_s", {})[name] = round(time.perf_counter() - t0, 1)
 
 
 # ----------------------------------------------------------------- batched form
@@ -378,6 +542,11 @@ def make_exact_bits(rng, bits):
 
 
 def run_batch(args):
+    print(json.dumps(batch_measure(args.steps, args.warmup, tune=not args.no_tune, cpu=not args.no_cpu_baseline)),
+          flush=True)
+
+
+def batch_measure(steps, warmup, tune=True, cpu=True):
     """Config 3: 4,096 independent products of uneven sizes; the graph-planned
     batch vs the direct batch vs one pimul_mul_device call per product."""
     import torch
@@ -401,7 +570,7 @@ def run_batch(args):
     jobs = [(base + 8 * int(offs_a[i]), int(la[i]), base + 8 * int(offs_b[i]), int(lb[i]),
              obase + 8 * int(out_off[i])) for i in range(len(la))]
     rjobs = [(a, x, b, y, rbase + 8 * int(out_off[i])) for i, (a, x, b, y, _) in enumerate(jobs)]
-    tune = pm.autotune(7, 19, 4) if not args.no_tune else {}
+    tune = pm.autotune(7, 19, 4) if tune else {}
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     plan = pm.BatchPlan(la, lb)
@@ -433,9 +602,9 @@ def run_batch(args):
         e1.synchronize()
         return e0.elapsed_time(e1) / steps
 
-    ms_plan = timeit(step_plan, args.steps, args.warmup)
-    ms_direct = timeit(step_direct, args.steps, args.warmup)
-    ms_plain = timeit(step_plain, max(2, args.steps // 4), 1)
+    ms_plan = timeit(step_plan, steps, warmup)
+    ms_direct = timeit(step_direct, steps, warmup)
+    ms_plain = timeit(step_plain, max(2, steps // 4), 1)
     step_plan()
     step_plain()
     stream.synchronize()
@@ -451,7 +620,7 @@ def run_batch(args):
         "project_metric": PROJECT_METRIC,
         "value": round(nprod / (ms_plan * 1e-3), 1),
         "unit": "products/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": round(ms_plan, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic: operand bit lengths log-uniform in [2^10, 2^22], uniform limbs (seeded)",
@@ -465,10 +634,10 @@ def run_batch(args):
         "model_gbs": round(bytes_model / (ms_plan * 1e-3) / 1e9, 1),
         "bit_exact_vs_plain": exact,
         "autotune": tune,
-        "cpu_baseline": None if args.no_cpu_baseline else batch_cpu_baseline(ops_a, ops_b, d_out, out_off),
+        "cpu_baseline": batch_cpu_baseline(ops_a, ops_b, d_out, out_off) if cpu else None,
     }
     plan.close()
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def batch_cpu_baseline(ops_a, ops_b, d_out, out_off):
@@ -541,15 +710,21 @@ def served_stream(n, seed=20241204, lo=12, hi=28, chain=0.3, sq=0.25):
 
 
 def run_served(args):
+    loads = [float(x) for x in str(args.load).split(",")]
+    print(json.dumps(served_measure(args.requests, loads)), flush=True)
+
+
+def served_measure(n, loads):
     """Config 4: Poisson request stream through the device-resident service
     (continuous batching, chained handles, HBM budget) vs the plain per-call
-    path fed by one worker in arrival order.  Latency = completion - arrival."""
-    import threading
+    path fed by one worker in arrival order, at each offered load (a multiple
+    of the plain path's measured capacity; above 1 the plain path saturates).
+    Latency = completion - arrival.  Results are compared bit for bit with
+    the plain path's at the first load."""
     import torch
     import pi_gb300 as pm
     pm.init(0)
     lib = pm.lib()
-    n = args.requests
     base, reqs = served_stream(n)
     pm.set_budget(120 << 30)
     # ---- plain path: device operands as torch tensors, results kept
@@ -577,66 +752,76 @@ def run_served(args):
         res.append(plain_one(k, res))
     t_serial = time.perf_counter() - t0
     capacity = n / t_serial
-    lam = args.load * capacity
-    rng = np.random.default_rng(99)
-    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
-    # ---- plain path under the arrival process (one worker, FIFO)
     del res
     torch.cuda.empty_cache()
-    res = []
-    lat_plain = []
-    t0 = time.perf_counter()
-    for k in range(n):
-        while time.perf_counter() - t0 < arrivals[k]:
-            pass
-        res.append(plain_one(k, res))
-        lat_plain.append(time.perf_counter() - t0 - arrivals[k])
-    span_plain = time.perf_counter() - t0
-    plain_host = [np.trim_zeros(r.cpu().numpy().view(np.uint64), "b") for r in res]
-    del res
-    torch.cuda.empty_cache()
-    # ---- served path
     hb = [pm.upload(x) for x in base]
-    pm.service_reset_stats()
-    outs, tickets = [], []
-    t0 = time.perf_counter()
-    for k, (op, x, y) in enumerate(reqs):
-        while time.perf_counter() - t0 < arrivals[k]:
-            pass
-        ha = hb[x] if x >= 0 else outs[-x - 1]
-        if op == "sqr":
-            h, t = pm.submit(ha)
-        else:
-            h, t = pm.submit(ha, hb[y] if y >= 0 else outs[-y - 1])
-        outs.append(h)
-        tickets.append(t)
-    for t in tickets:
-        pm.wait(t)
-    span_served = time.perf_counter() - t0
-    st = pm.service_stats()
-    served_host = [pm.download(h) for h in outs]
-    exact = all(np.array_equal(a, b) for a, b in zip(served_host, plain_host))
-    for h in outs + hb:
+    runs = []
+    exact = None
+    for li, load in enumerate(loads):
+        lam = load * capacity
+        rng = np.random.default_rng(99)
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
+        # ---- plain path under the arrival process (one worker, FIFO)
+        res = []
+        lat_plain = []
+        t0 = time.perf_counter()
+        for k in range(n):
+            while time.perf_counter() - t0 < arrivals[k]:
+                pass
+            res.append(plain_one(k, res))
+            lat_plain.append(time.perf_counter() - t0 - arrivals[k])
+        span_plain = time.perf_counter() - t0
+        plain_host = [np.trim_zeros(r.cpu().numpy().view(np.uint64), "b") for r in res] if li == 0 else None
+        del res
+        torch.cuda.empty_cache()
+        # ---- served path
+        pm.service_reset_stats()
+        outs, tickets = [], []
+        t0 = time.perf_counter()
+        for k, (op, x, y) in enumerate(reqs):
+            while time.perf_counter() - t0 < arrivals[k]:
+                pass
+            ha = hb[x] if x >= 0 else outs[-x - 1]
+            if op == "sqr":
+                h, t = pm.submit(ha)
+            else:
+                h, t = pm.submit(ha, hb[y] if y >= 0 else outs[-y - 1])
+            outs.append(h)
+            tickets.append(t)
+        for t in tickets:
+            pm.wait(t)
+        span_served = time.perf_counter() - t0
+        st = pm.service_stats()
+        if plain_host is not None:
+            served_host = [pm.download(h) for h in outs]
+            exact = all(np.array_equal(a, b) for a, b in zip(served_host, plain_host))
+            del served_host, plain_host
+        for h in outs:
+            pm.free(h)
+        lp = np.array(lat_plain) * 1e3
+        runs.append({
+            "offered_load": load, "lambda_rps": round(lam, 1),
+            "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                       "ops_per_s": round(n / span_served, 1), "batches": st["batches"]},
+            "plain": {"p50_ms": round(float(np.percentile(lp, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lp, 99)), 3), "ops_per_s": round(n / span_plain, 1)},
+            "throughput_served_over_plain": round(span_plain / span_served, 3)})
+    for h in hb:
         pm.free(h)
-    lp = np.array(lat_plain) * 1e3
-    line = {
+    first = runs[0]
+    return {
         "metric": "served request stream: p50/p99 latency and ops/s vs plain per-call",
         "project_metric": PROJECT_METRIC,
-        "value": round(n / span_served, 1), "unit": "requests/s",
-        "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * span_served, 1),
+        "value": first["served"]["ops_per_s"], "unit": "requests/s",
+        "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * n / first["served"]["ops_per_s"], 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic: Poisson arrivals (seeded), operand bits log-uniform in [2^12, 2^28], "
                 "30% chained on earlier results, 25% squares",
-        "config": {"workload": f"{n} requests, offered load {args.load} of the plain path's capacity",
-                   "plain_capacity_rps": round(capacity, 1), "lambda_rps": round(lam, 1),
-                   "hbm_budget_bytes": 120 << 30},
-        "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                   "ops_per_s": round(n / span_served, 1), "batches": st["batches"]},
-        "plain": {"p50_ms": round(float(np.percentile(lp, 50)), 3), "p99_ms": round(float(np.percentile(lp, 99)), 3),
-                  "ops_per_s": round(n / span_plain, 1)},
+        "config": {"workload": f"{n} requests per offered load, loads {loads} of the plain path's capacity",
+                   "plain_capacity_rps": round(capacity, 1), "hbm_budget_bytes": 120 << 30},
+        "served": first["served"], "plain": first["plain"], "loads": runs,
         "bit_exact_served_vs_plain": bool(exact),
     }
-    print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------- pi runs
@@ -914,7 +1099,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: seeded uniform u64 limbs, top limb bit 63 set (numpy PCG64)",
-        "config": {"workload": "isolated multiply, balanced 2^30 x 2^30 bits (2^24 x 2^24 limbs), N = 2^27",
+        "config": {"workload": mul_workload(la, lb, L),
                    "bits_a": BITS_A, "bits_b": BITS_B, "la": la, "lb": lb, "transform_len": N,
                    "bytes_per_step_model": "B_mul(N) = 96N + 16(la+lb)"},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port",
@@ -956,11 +1141,15 @@ def main():
                     help="mul: the 2^30-bit product (headline); batch: 4096 uneven products; "
                          "served: Poisson request stream through the multiply service")
     ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--extras", default="all",
+                    help="other configurations added to the headline line: all, none, or a comma-separated "
+                         "subset of sweep,batch4096,served,pi,bbp")
     ap.add_argument("--hex-checks", type=int, default=8, help="BBP spot checks of the hex conversion")
     ap.add_argument("--hex-cpu-digits", type=int, default=1_000_000)
     ap.add_argument("--hex-input", choices=["pi", "random"], default="pi",
                     help="text to convert: pi's digits (BBP-checked) or seeded random digits")
-    ap.add_argument("--load", type=float, default=0.8)
+    ap.add_argument("--load", default="0.8,1.0,1.5,2.0",
+                    help="offered loads of the served workload, comma-separated multiples of plain capacity")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--bits", type=int, default=30,
                     help="log2 bits per operand (30 = the headline workload; smaller for profiling)")

@@ -1,13 +1,14 @@
 """Generate tests/golden/*.json from the reference's own unit tests.
 
-Reads the reference's Rust test sources as text (joelodom/pi, mounted at
-/root/reference in the build container) and records, for every known-answer
+Reads the reference's Rust test sources as text (a checkout of joelodom/pi,
+given as the first argument or in PI_REFERENCE) and records, for every known-answer
 test on the multiply path, the inputs and the exact expected output.
 Expected products come from Python's exact integer multiply, which is
 independent of both the CPU oracle and the CUDA engine.  Known constants
 (digits of pi, BBP hex values) are parsed out of the reference source text.
 
-Run:  python tests/golden/make_golden.py [/path/to/reference]
+Run:  python tests/golden/make_golden.py /path/to/joelodom-pi
+  or: PI_REFERENCE=/path/to/joelodom-pi python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -17,7 +18,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PI_REFERENCE", "")
+if __name__ == "__main__" and not os.path.isdir(REF):
+    sys.exit("usage: make_golden.py <path to a joelodom/pi checkout> (or set PI_REFERENCE)")
 HERE = os.path.dirname(os.path.abspath(__file__))
 P = 0xFFFFFFFF00000001
 M64 = (1 << 64) - 1
