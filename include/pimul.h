@@ -193,6 +193,23 @@ int pimul_autotune(int log_n_min, int log_n_max, int reps, char* report, size_t 
 int pimul_tuning_set(int log_n, int passes, int small_ctas_per_sm);
 
 /*
+ * Twiddle-table cache.  The first and middle passes of a transform read
+ * their twiddles from tables laid out like the data (one coalesced load per
+ * element; the inverse first pass's table also carries the 1/N scaling),
+ * built on first use per transform shape and kept until pimul_shutdown.
+ * First passes use tables up to transform length 2^28 (8 N bytes per
+ * direction); longer transforms, and shapes past the cap, compute their
+ * twiddles.  pimul_twiddle_cache sets the cap in bytes (default 8 GiB;
+ * 0: build no more tables) for tables built from then on and reports the
+ * bytes already held in *held (may be NULL).  The cache is device memory
+ * outside the served form's HBM budget.
+ *
+ * Replaces: the twiddle cache of crates/bignum/src/ntt.rs:571-611 (the
+ * reference caches its per-length twiddles up to a 2^28 cap too).
+ */
+int pimul_twiddle_cache(uint64_t max_bytes, uint64_t* held);
+
+/*
  * Served form: a device-resident multiply service.
  *
  * Integers live on the device as handles.  pimul_submit queues a product

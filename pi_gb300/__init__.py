@@ -75,6 +75,7 @@ def load(build_if_stale: bool = True):
     L.pimul_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _sz]
     L.pimul_tuning_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.pimul_set_budget.argtypes = [ctypes.c_uint64]
+    L.pimul_twiddle_cache.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_upload.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_submit.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
                                ctypes.POINTER(ctypes.c_uint64)]
@@ -305,6 +306,15 @@ OP_MUL, OP_SQR = 0, 1
 def set_budget(nbytes: int):
     """HBM admission budget of the multiply service (default 120 GiB)."""
     _check(lib().pimul_set_budget(int(nbytes)))
+
+
+def twiddle_cache(max_bytes: int) -> int:
+    """Cap of the pass-twiddle table cache in bytes (0: build no more
+    tables; tables already built stay until shutdown).  Returns the bytes
+    held."""
+    held = ctypes.c_uint64(0)
+    _check(lib().pimul_twiddle_cache(int(max_bytes), ctypes.byref(held)))
+    return held.value
 
 
 def upload(limbs) -> int:

@@ -229,8 +229,10 @@ __device__ __forceinline__ uint64_t* job_array(const Job& J, int which) {
 // coefficient n = i * 2^S + j0 + j, i.e. 16-bit slice n % 4 of limb n / 4;
 // limbs past nl are zero (the reference's zero tail).  which = 0: operand a,
 // 1: operand b (squares skip b).
+// twf: the pass's twiddle table (tw_first), or null to compute the twiddles.
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const Job* jobs, Job one, int which, int L, Roots RT,
+                                                                           const uint64_t* __restrict__ twf) {
   constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   if (which == 1 && skips_b(J)) return;
@@ -262,6 +264,19 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
   constexpr int TL = 8 - T;
   const uint32_t tlo = tid >> T, jj = tid & ((1u << T) - 1);
   const uint64_t gbase = ((uint64_t)tlo << S) + j0 + jj;
+  if (twf) {
+    // twiddles laid out like the data: one coalesced load each
+#pragma unroll 2
+    for (int g = 0; g < PER_THREAD; g += 8) {
+      uint64_t t8[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) t8[q] = __ldg(twf + gbase + ((uint64_t)((g + q) << TL) << S));
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        data[gbase + ((uint64_t)((g + q) << TL) << S)] = gl::mul(sm[spad((g + q) * PASS_THREADS + tid)], t8[q]);
+    }
+    return;
+  }
   if (L > LVL_MAX) {
     // w^(f (j0 + jj)) = w^(f j0) w^(f jj): the first factor for the tile's
     // 2^R frequencies replaces the round twiddles in tw (the rounds are
@@ -299,8 +314,10 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
 
 // Middle column pass: 2^(9-R) blocks x 2^R rows x 2^T columns; forward pass
 // twiddles w_M^(f*j) after the rounds, inverse ones before.
+// twm: the pass's twiddle table (tw_mid), or null to compute the twiddles.
 template <int R, bool FWD>
-__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const Job* jobs, Job one, int which, int S, Roots RT,
+                                                                         const uint64_t* __restrict__ twm) {
   constexpr int T = TILE_LOG - 9, BC = 9 - R;
   constexpr int TL = 8 - T;  // row bits covered by tid >> T
   static_assert(R >= TL, "thread index must stay inside one block's rows");
@@ -333,18 +350,27 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
     tile_fwd_t<R, T, BC, PASS_THREADS>(sm, tw, tid);
     // outgoing pass twiddles w_M^(f*j)
     const uint32_t eJ = row_freq_t<R>(tlo) * Jc;
+    // table: twm[r 2^S + j] for row r of the block and column j
+    const uint64_t tbase = ((uint64_t)tlo << S) + j0 + jj;
 #pragma unroll 1
     for (int g = 0; g < PER_THREAD; g += 8) {
       uint64_t t8[8];
+      if (twm) {
 #pragma unroll
-      for (int q = 0; q < 8; q++)
-        t8[q] = root_pow32(RT, mlog, eJ + row_freq_t<R>(((g + q) << TL) & RM) * Jc, false);
+        for (int q = 0; q < 8; q++) t8[q] = __ldg(twm + tbase + ((uint64_t)(((g + q) << TL) & RM) << S));
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          t8[q] = root_pow32(RT, mlog, eJ + row_freq_t<R>(((g + q) << TL) & RM) * Jc, false);
+      }
 #pragma unroll
       for (int q = 0; q < 8; q++) data[gaddr(g + q)] = gl::mul(sm[spad((g + q) * PASS_THREADS + tid)], t8[q]);
     }
   } else {
     // incoming pass twiddles w_M^-(f*j), applied by the first inverse round
+    // (tile row row0 + k is row (row0 + k) & RM of its block)
     auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+      if (twm) return __ldg(twm + ((uint64_t)((row0 & RM) + (uint32_t)k) << S) + j0 + j);
       const uint32_t f = row_freq_t<R>(row0 & RM) + row_freq_t<R>((uint32_t)k);
       return root_pow32(RT, mlog, f * (uint32_t)(j0 + j), true);
     };
@@ -360,24 +386,25 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_col_mid(const J
 template <int R>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const Job* jobs, Job one, int which,
                                                                           Roots RT) {
-  constexpr int BC = TILE_LOG - R;
+  static_assert(R <= 9 && PASS_THREADS == 256 && TILE_LOG == 12, "eight warps, one 512-word chunk each");
   const Job J = job_of(jobs, one);
   if (is_square(J)) return;
   if (which == 1 && !(J.flags & JF_B_FULL)) return;
   extern __shared__ uint64_t sm[];
   uint64_t* tw = sm + spad(1u << TILE_LOG);
-  const int tid = threadIdx.x;
-  uint64_t* base = (which ? J.B : J.A) + ((uint64_t)blockIdx.x << TILE_LOG);
+  // warp w owns the tile's 512-word chunk w (whole blocks): after the round
+  // twiddles are staged, only __syncwarp separates its rounds
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* chunk = (which ? J.B : J.A) + ((uint64_t)blockIdx.x << TILE_LOG) + ((uint32_t)warp << 9);
+  uint64_t* smc = sm + spad((uint32_t)warp << 9);
 #pragma unroll
-  for (int q = 0; q < PER_THREAD; q++) {
-    const uint32_t lin = q * PASS_THREADS + tid;
-    cp_async8(sm + spad(lin), base + lin);
-  }
+  for (int q = 0; q < 16; q++) cp_async8(smc + spad(q * 32 + lane), chunk + q * 32 + lane);
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();
-  tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) base[lin] = sm[spad(lin)];
+  chunk_fwd_t<R>(smc, tw, lane);
+#pragma unroll
+  for (int q = 0; q < 16; q++) chunk[q * 32 + lane] = smc[spad(q * 32 + lane)];
 }
 
 // Fused middle of the multiply on one contiguous tile: last forward pass of
@@ -388,9 +415,10 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_last(const 
 // in B (shared or owned) the last pass is skipped and the result goes to A.
 // EXT = false: plain products only (no shared spectrum, no addend), the
 // form every single product and every batch without those roles uses.
+// ninv = 0: no scaling here (the inverse first pass's twiddle table carries N^-1).
 template <int R, bool EXT>
 __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* jobs, Job one, uint64_t ninv, Roots RT) {
-  constexpr int BC = TILE_LOG - R;
+  static_assert(R <= 9 && PASS_THREADS == 256 && TILE_LOG == 12, "eight warps, one 512-word chunk each");
   const Job J = job_of(jobs, one);
   if (EXT && (J.flags & JF_ADDEND)) return;
   const bool sq = is_square(J), spec = EXT && b_spectrum(J);
@@ -402,11 +430,12 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
   uint64_t* tw = sm + spad(1u << TILE_LOG);
   const int tid = threadIdx.x;
   const uint64_t off = (uint64_t)blockIdx.x << TILE_LOG;
+  // warp w owns the tile's 512-word chunk w (whole blocks) from load to store
+  const int warp = tid >> 5, lane = tid & 31;
+  const uint64_t coff = off + ((uint32_t)warp << 9);
+  uint64_t* smc = sm + spad((uint32_t)warp << 9);
 #pragma unroll
-  for (int q = 0; q < PER_THREAD; q++) {
-    const uint32_t lin = q * PASS_THREADS + tid;
-    cp_async8(sm + spad(lin), cin + off + lin);
-  }
+  for (int q = 0; q < 16; q++) cp_async8(smc + spad(q * 32 + lane), cin + coff + q * 32 + lane);
   // a's (and the addend's) tile is read after b's rounds: start it towards
   // L2 now (tiles are 32 KB at 32 KB offsets of 256-byte aligned arrays)
   if (tid == 0) {
@@ -416,17 +445,20 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
   load_tw512(tw, RT);
   cp_async_wait_all();
   __syncthreads();
-  if (!spec) tile_fwd_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) {
-    uint64_t x = sm[spad(lin)];
-    uint64_t y = sq ? x : a[off + lin];
+  if (!spec) chunk_fwd_t<R>(smc, tw, lane);
+#pragma unroll 4
+  for (int q = 0; q < 16; q++) {
+    const uint32_t lin = q * 32 + lane;
+    uint64_t x = smc[spad(lin)];
+    uint64_t y = sq ? x : a[coff + lin];
     uint64_t p = gl::mul(x, y);
-    if (EXT && X) p = gl::add(p, X[off + lin]);
-    sm[spad(lin)] = gl::mul(p, ninv);
+    if (EXT && X) p = gl::add(p, X[coff + lin]);
+    smc[spad(lin)] = ninv ? gl::mul(p, ninv) : p;
   }
-  __syncthreads();
-  tile_inv_t<R, 0, BC, PASS_THREADS>(sm, tw, tid);
-  for (uint32_t lin = tid; lin < (1u << TILE_LOG); lin += PASS_THREADS) cout[off + lin] = sm[spad(lin)];
+  __syncwarp();
+  chunk_inv_t<R>(smc, tw, lane);
+#pragma unroll
+  for (int q = 0; q < 16; q++) cout[coff + q * 32 + lane] = smc[spad(q * 32 + lane)];
 }
 
 // Addends: A <- A * B (spectra, element by element), read later as X.
@@ -509,8 +541,11 @@ __host__ __device__ __forceinline__ uint64_t aux_bytes_for(uint64_t nwin) {
 // Inverse pass 0 (natural order out) fused with the window fold: each tile
 // row holds 2^T consecutive coefficients = 2^(T-3) windows; every window
 // writes its low 2 limbs to the output and its high part to H.
+// twi: the pass's twiddle table (tw_first, inverse, with N^-1), or null to
+// compute the twiddles (the caller then scales by N^-1 in k_mid).
 template <int R>
-__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT) {
+__global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry(const Job* jobs, Job one, int L, Roots RT,
+                                                                                 const uint64_t* __restrict__ twi) {
   constexpr int T = TILE_LOG - R;
   const Job J = job_of(jobs, one);
   if (J.flags & JF_ADDEND) return;
@@ -528,7 +563,16 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
 #pragma unroll
   for (int q = 0; q < PER_THREAD; q++)
     cp_async8(sm + spad(q * PASS_THREADS + tid), data + gbase + ((uint64_t)(q << TL) << S));
-  if (L > LVL_MAX) {
+  if (twi) {
+    load_tw512(tw, RT);
+    cp_async_wait_all();
+    __syncthreads();
+    // inverse pass twiddles (times N^-1) from the table, laid out like the data
+    auto ptw = [&](uint32_t row0, int k, uint32_t j) {
+      return __ldg(twi + ((uint64_t)(row0 + (uint32_t)k) << S) + j0 + j);
+    };
+    tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
+  } else if (L > LVL_MAX) {
     // inverse pass twiddles w^-(f (j0 + j)) = w^-(f j0) w^-(f j): the first
     // factor for the tile's 2^R frequencies is staged in tw, which the
     // first inverse round does not need for round twiddles (its sub-problems
@@ -1247,7 +1291,132 @@ struct Launcher {
   bool stats;  // count and (optionally) time launches
   const Roots& R;
   cudaEvent_t b_ready = nullptr;  // operand b's upload (plain host-buffer call): waited on before its first pass
+  bool tables = true;             // read pass twiddles from the cached tables (false: compute them)
 };
+
+// ---------------------------------------------------------------- twiddle tables
+// Pass twiddles can be read from tables laid out like the data they
+// multiply, one coalesced load per element, instead of being computed from
+// the root tables (a product of two table entries per element in the first
+// passes, a scattered lookup in a 2^(R+S)-entry level table in the middle
+// ones).  With f_R the digit-reversed row frequency (row_freq_t<R>):
+//   first pass of length N = 2^L, radix 2^R, S = L - R:
+//     forward  tw[i 2^S + J] = w_N^(f_R(i) J)
+//     inverse  tw[i 2^S + J] = w_N^-(f_R(i) J) N^-1   (the inverse's 1/N for free)
+//   middle pass of radix 2^R and stride 2^S, M = 2^(R+S):
+//     tw[r 2^S + j] = w_M^(+-f_R(r) j)
+// Tables are built once per shape, on first use, and kept until
+// pimul_shutdown (the reference keeps its twiddles in a cache too,
+// crates/bignum/src/ntt.rs:571-611), up to a byte cap; first passes longer
+// than 2^TW_LOG_MAX compute their twiddles.
+constexpr int TW_LOG_MAX = 28;
+
+template <int R>
+__global__ void k_tw_first(uint64_t* tw, int L, int inv, uint64_t scale, Roots RT) {
+  const int S = L - R;
+  const uint64_t n = 1ull << L, smask = (1ull << S) - 1;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(e >> S), J = (uint32_t)(e & smask);
+    uint64_t t = root_pow32(RT, L, row_freq_t<R>(i) * J, inv != 0);
+    if (inv) t = gl::mul(t, scale);
+    tw[e] = gl::canon(t);
+  }
+}
+
+template <int R>
+__global__ void k_tw_mid(uint64_t* tw, int S, int inv, Roots RT) {
+  const int M = R + S;
+  const uint64_t n = 1ull << M, smask = (1ull << S) - 1;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = (uint32_t)(e >> S), j = (uint32_t)(e & smask);
+    tw[e] = gl::canon(root_pow32(RT, M, row_freq_t<R>(r) * j, inv != 0));
+  }
+}
+
+struct TwCache {
+  std::mutex mu;
+  std::unordered_map<uint64_t, uint64_t*> tables;
+  uint64_t bytes = 0;
+  uint64_t cap = 8ull << 30;
+  cudaStream_t st = nullptr;
+};
+static TwCache& tw_cache() {
+  static TwCache* c = new TwCache;  // never destroyed: usable during static destruction
+  return *c;
+}
+
+// The table of one pass (kind 0: first pass, R + S = L; kind 1: middle pass),
+// built on first use.  Null (compute the twiddles) when the shape is above
+// TW_LOG_MAX or the cap, while `caller` is capturing a graph (a table is
+// never built inside a capture), or when allocating it fails.
+static const uint64_t* tw_table(int kind, int R, int S, bool inv, cudaStream_t caller) {
+  if (kind == 0 && R + S > TW_LOG_MAX) return nullptr;
+  const uint64_t key = ((uint64_t)kind << 24) | ((uint64_t)R << 16) | ((uint64_t)S << 8) | (inv ? 1u : 0u);
+  TwCache& c = tw_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  auto it = c.tables.find(key);
+  if (it != c.tables.end()) return it->second;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (caller && (cudaStreamIsCapturing(caller, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)) return nullptr;
+  const uint64_t words = 1ull << (R + S);
+  if (c.bytes + 8 * words > c.cap) return nullptr;
+  if (!c.st && cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    c.st = nullptr;
+    return nullptr;
+  }
+  uint64_t* d = nullptr;
+  if (cudaMalloc(&d, 8 * words) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(words / 256, 152 * 16));
+  const Roots& RT = g_dev.roots;
+  if (kind == 0) {
+    const uint64_t ninv = hf::pow(hf::pow(2, 191), (uint64_t)(R + S));  // 2^-L (2^192 = 1)
+    PIMUL_DISPATCH_R(R, (k_tw_first<RR><<<blocks, 256, 0, c.st>>>(d, R + S, inv ? 1 : 0, ninv, RT)));
+  } else {
+    PIMUL_DISPATCH_R(R, (k_tw_mid<RR><<<blocks, 256, 0, c.st>>>(d, S, inv ? 1 : 0, RT)));
+  }
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c.st) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
+  c.tables[key] = d;
+  c.bytes += 8 * words;
+  return d;
+}
+
+// Pointers of every pass table of a length-2^L plan (null entries: compute).
+struct PassTables {
+  const uint64_t* first_fwd = nullptr;
+  const uint64_t* first_inv = nullptr;  // carries N^-1: k_mid then skips its scaling
+  const uint64_t* mid_fwd[5] = {};
+  const uint64_t* mid_inv[5] = {};
+};
+static PassTables pass_tables(const Plan& pl, cudaStream_t caller) {
+  PassTables t;
+  const int L = pl.L;
+  t.first_fwd = tw_table(0, pl.r[0], L - pl.r[0], false, caller);
+  t.first_inv = tw_table(0, pl.r[0], L - pl.r[0], true, caller);
+  int consumed = pl.r[0];
+  for (int p = 1; p < pl.np - 1; p++) {
+    consumed += pl.r[p];
+    t.mid_fwd[p] = tw_table(1, pl.r[p], L - consumed, false, caller);
+    t.mid_inv[p] = tw_table(1, pl.r[p], L - consumed, true, caller);
+  }
+  return t;
+}
+
+static void tw_release_all() {
+  TwCache& c = tw_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  for (auto& kv : c.tables) cudaFree(kv.second);
+  c.tables.clear();
+  c.bytes = 0;
+  if (c.st) cudaStreamDestroy(c.st);
+  c.st = nullptr;
+}
 
 // All launches of the large-product pipeline for `nj` products sharing the
 // transform length 2^L: the products come from the device array `jobs`
@@ -1258,19 +1427,23 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
   const Plan pl = make_plan(L);
   const dim3 grid((unsigned)(1ull << (L - TILE_LOG)), nj);
   const size_t smem = pass_smem_bytes(TILE_LOG);
-  const uint64_t ninv = hf::pow(hf::pow(2, 191), L);  // 2^-L (2^192 = 1)
+  const PassTables tw = X.tables ? pass_tables(pl, X.st) : PassTables{};
+  // 2^-L (2^192 = 1); 0 when the inverse first pass's table applies it
+  const uint64_t ninv = tw.first_inv ? 0 : hf::pow(hf::pow(2, 191), L);
   const int rl = pl.r[pl.np - 1];
   for (int which = 0; which < 2; which++) {
     if (which == 1 && X.b_ready) cudaStreamWaitEvent(X.st, X.b_ready, 0);
     {
       KTimer kt(K_PACK, X.st, X.stats);
-      PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L, X.R)));
+      PIMUL_DISPATCH_R(pl.r[0], (k_fwd_first<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L, X.R,
+                                                                                                   tw.first_fwd)));
     }
     int consumed = pl.r[0];
     for (int p = 1; p < pl.np - 1; p++) {
       consumed += pl.r[p];
       KTimer kt(K_PASS_FWD, X.st, X.stats);
-      PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L - consumed, X.R)));
+      PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, true><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, which, L - consumed, X.R,
+                                                                                        tw.mid_fwd[p])));
     }
     if (which == 0 || any_b_full) {
       KTimer kt(K_PASS_FWD, X.st, X.stats);
@@ -1295,11 +1468,12 @@ static void run_large(const Launcher& X, const Job* jobs, const Job& one, uint32
     int S = L - consumed;
     consumed -= pl.r[p];
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, 2, S, X.R)));
+    PIMUL_DISPATCH_R(pl.r[p], (k_col_mid<RR, false><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, 2, S, X.R, tw.mid_inv[p])));
   }
   {
     KTimer kt(K_PASS_INV, X.st, X.stats);
-    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, L, X.R)));
+    PIMUL_DISPATCH_R(pl.r[0], (k_inv_first_carry<(RR < 7 ? 7 : RR)><<<grid, PASS_THREADS, smem, X.st>>>(jobs, one, L, X.R,
+                                                                                                         tw.first_inv)));
   }
   {
     KTimer kt(K_CARRY, X.st, X.stats);
@@ -1665,6 +1839,11 @@ static int plan_create(const size_t* la, const size_t* lb, size_t n, BatchPlan**
   cudaStream_t cs = nullptr;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
+    // twiddle tables are never built inside a capture: build them first
+    for (size_t i = 0; i < n; i++) {
+      const int L = log2_ceil(4 * (uint64_t)la[i] + 4 * (uint64_t)lb[i] - 1);
+      if (la[i] && lb[i] && L > SMALL_LOG_MAX) pass_tables(make_plan(L), nullptr);
+    }
     uint8_t* desc = P->dev + round256(P->B.arena_bytes);
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -2100,6 +2279,7 @@ int pimul_shutdown(void) {
   cudaSetDevice(g_dev.device);
   cudaDeviceSynchronize();
   release_host_staging();
+  tw_release_all();
   cudaFree(g_dev.d_roots);
   if (g_dev.pool) cudaMemPoolTrimTo(g_dev.pool, 0);
   g_dev = DeviceState{};
@@ -2201,6 +2381,14 @@ int pimul_tuning_set(int log_n, int passes, int small_ctas_per_sm) {
     g_tuned_np[log_n].store(passes);
   }
   if (small_ctas_per_sm > 0) g_small_ctas_per_sm.store(small_ctas_per_sm);
+  return PIMUL_OK;
+}
+
+int pimul_twiddle_cache(uint64_t max_bytes, uint64_t* held) {
+  TwCache& c = tw_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  c.cap = max_bytes;
+  if (held) *held = c.bytes;
   return PIMUL_OK;
 }
 
@@ -2961,6 +3149,7 @@ static int mul_device_noalloc(const uint64_t* d_a, uint64_t la, const uint64_t* 
   J.H = nd->scratch + 2 * NOALLOC_N_MAX;
   J.aux = reinterpret_cast<uint8_t*>(nd->scratch + 2 * NOALLOC_N_MAX + NOALLOC_WIN_MAX);
   Launcher X{st, false, R};  // no statistics hook: its event timing would create CUDA events
+  X.tables = false;          // nor the twiddle tables, which are allocated on first use
   run_large(X, nullptr, J, 1, z.L, z.nchunk);
   CU(cudaGetLastError());
   return PIMUL_OK;

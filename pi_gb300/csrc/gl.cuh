@@ -210,66 +210,61 @@ __device__ __forceinline__ Lz lz_mul(uint64_t a, uint64_t b) {
   return z;
 }
 
-// x * 2^S for S in {24, 48, 72} on a lazy value with |k| < 2^6 -> weak.
-template <int S>
-__device__ __forceinline__ uint64_t lz_shl(Lz x) {
-  static_assert(S == 24 || S == 48 || S == 72, "lazy shifts are 24, 48 or 72 bits");
-  if constexpr (S == 24) {
-    // (h:l) 2^24 = (w2:w1:w0), w2 < 2^24; k 2^88 adds k 2^24 to w2
-    uint32_t w0 = x.l << 24;
-    uint32_t w1 = __funnelshift_l(x.l, x.h, 24);
-    int32_t w2 = (int32_t)(x.h >> 8) + (int32_t)((uint32_t)x.k << 24);
-    return fold_words(w0, w1, w2);
-  } else if constexpr (S == 48) {
-    // (h:l) 2^48 = words (0, l << 16, w2, h >> 16) and k 2^112 = -k 2^16 (2^96 = -1):
-    // value = (w1:0) + w2 EPS - w3 with w3 = (h >> 16) + k 2^16
-    uint32_t w1 = x.l << 16;
-    uint32_t w2 = __funnelshift_l(x.l, x.h, 16);
-    int32_t w3 = (int32_t)(x.h >> 16) + (int32_t)((uint32_t)x.k << 16);
-    uint64_t u;
-    asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(w2));
-    uint32_t z0, z1;
-    asm("{\n\t.reg .u32 k, nk, hk, u0, u1, w3h;\n\t"
-        "mov.b64 {u0, u1}, %4;\n\t"
-        "shr.s32 w3h, %3, 31;\n\t"
-        "sub.cc.u32 %0, 0, %3;\n\t"
-        "subc.cc.u32 %1, %2, w3h;\n\t"
-        "subc.u32 k, 0, w3h;\n\t"
-        "add.cc.u32 %0, %0, u0;\n\t"
-        "addc.cc.u32 %1, %1, u1;\n\t"
-        "addc.u32 k, k, 0;\n\t"
-        "neg.s32 nk, k;\n\t"
-        "shr.s32 hk, k, 31;\n\t"
-        "add.cc.u32 %0, %0, nk;\n\t"
-        "addc.u32 %1, %1, hk;\n\t"
-        "}"
-        : "=&r"(z0), "=&r"(z1)
-        : "r"(w1), "r"(w3), "l"(u));
-    return mk64(z0, z1);
-  } else {
-    // y = (h:l) 2^8 = (y2:y1:y0); y 2^64 = y0 EPS - y1 - y2 2^32 (2^128 = -2^32)
-    // and k 2^136 = -k 2^40: value = y0 EPS - ((y2 + k 2^8) : y1)
-    uint32_t y0 = x.l << 8;
-    uint32_t y1 = __funnelshift_l(x.l, x.h, 8);
-    int32_t y2 = (int32_t)(x.h >> 24) + (int32_t)((uint32_t)x.k << 8);
-    uint64_t u;
-    asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(y0));
-    uint32_t z0, z1;
-    asm("{\n\t.reg .u32 k, nk, hk, u0, u1, y2h;\n\t"
-        "mov.b64 {u0, u1}, %4;\n\t"
-        "shr.s32 y2h, %3, 31;\n\t"
-        "sub.cc.u32 %0, u0, %2;\n\t"
-        "subc.cc.u32 %1, u1, %3;\n\t"
-        "subc.u32 k, 0, y2h;\n\t"
-        "neg.s32 nk, k;\n\t"
-        "shr.s32 hk, k, 31;\n\t"
-        "add.cc.u32 %0, %0, nk;\n\t"
-        "addc.u32 %1, %1, hk;\n\t"
-        "}"
-        : "=&r"(z0), "=&r"(z1)
-        : "r"(y1), "r"(y2), "l"(u));
-    return mk64(z0, z1);
-  }
+// Shifts that leave their result lazy (no fold), for the radix-8 / radix-4
+// butterflies.  Derivations, with x = l + h 2^32 + k 2^64:
+//  * x 2^24 = (l << 24) + funnel(l, h, 24) 2^32 + ((h >> 8) + k 2^24) 2^64: the
+//    overflow count grows to |k| < 2^28 (|x.k| < 2^6 in), which lz_add,
+//    lz_sub and fold accept but another shift does not;
+//  * x 2^48 = w1 2^32 + w2 2^64 + w3 2^96 with w1 = l << 16, w2 = funnel(l, h, 16),
+//    w3 = (h >> 16) + k 2^16; with 2^64 = 2^32 - 1 and 2^96 = -1 this is
+//    w2 EPS + w1 2^32 - w3, a 96-bit value with k in {-1 .. 2} (|x.k| < 2^15 in);
+//  * x 2^72 = y 2^64 for y = x 2^8 = y0 + y1 2^32 + y2 2^64 (y0 = l << 8,
+//    y1 = funnel(l, h, 8), y2 = (h >> 24) + k 2^8); with 2^128 = -2^32 this is
+//    y0 EPS - y1 - y2 2^32, k in {-1 .. 1} (|x.k| < 2^23 in).
+__device__ __forceinline__ Lz lz_shl24_wide(Lz x) {
+  Lz z;
+  z.l = x.l << 24;
+  z.h = __funnelshift_l(x.l, x.h, 24);
+  z.k = (int32_t)(x.h >> 8) + (int32_t)((uint32_t)x.k << 24);
+  return z;
+}
+
+__device__ __forceinline__ Lz lz_shl48_n(Lz x) {
+  const uint32_t w1 = x.l << 16, w2 = __funnelshift_l(x.l, x.h, 16);
+  const int32_t w3 = (int32_t)(x.h >> 16) + (int32_t)((uint32_t)x.k << 16);
+  uint64_t u;
+  asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(w2));
+  Lz z;
+  asm("{\n\t.reg .u32 sh, u0, u1;\n\t"
+      "mov.b64 {u0, u1}, %5;\n\t"
+      "shr.s32 sh, %4, 31;\n\t"
+      "sub.cc.u32 %0, u0, %4;\n\t"
+      "subc.cc.u32 %1, u1, sh;\n\t"
+      "subc.u32 %2, 0, sh;\n\t"
+      "add.cc.u32 %1, %1, %3;\n\t"
+      "addc.u32 %2, %2, 0;\n\t"
+      "}"
+      : "=&r"(z.l), "=&r"(z.h), "=&r"(z.k)
+      : "r"(w1), "r"(w3), "l"(u));
+  return z;
+}
+
+__device__ __forceinline__ Lz lz_shl72_n(Lz x) {
+  const uint32_t y0 = x.l << 8, y1 = __funnelshift_l(x.l, x.h, 8);
+  const int32_t y2 = (int32_t)(x.h >> 24) + (int32_t)((uint32_t)x.k << 8);
+  uint64_t u;
+  asm("mul.wide.u32 %0, %1, 0xFFFFFFFF;" : "=l"(u) : "r"(y0));
+  Lz z;
+  asm("{\n\t.reg .u32 sh, u0, u1;\n\t"
+      "mov.b64 {u0, u1}, %5;\n\t"
+      "shr.s32 sh, %4, 31;\n\t"
+      "sub.cc.u32 %0, u0, %3;\n\t"
+      "subc.cc.u32 %1, u1, %4;\n\t"
+      "subc.u32 %2, 0, sh;\n\t"
+      "}"
+      : "=&r"(z.l), "=&r"(z.h), "=&r"(z.k)
+      : "r"(y1), "r"(y2), "l"(u));
+  return z;
 }
 
 // base^e mod p (canonical result).

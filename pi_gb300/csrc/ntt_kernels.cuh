@@ -115,8 +115,9 @@ __device__ __forceinline__ void bfly_dif(uint64_t& a, uint64_t& b) {
 
 // Forward DFT of 2^B values in registers: v[k] <- sum_m v[m] w^(m k), with
 // w = 2^(192 / 2^B) (the 8th root of unity is 2^24).  Natural-order output.
-// Radix 4 and 8 run on lazy values (see gl.cuh) and fold once at the end.
-// Forward DFT on lazy inputs (|k| <= 1, e.g. products from lz_mul).
+// Radix 4 and 8 run on lazy values (see gl.cuh) and fold once per output;
+// the internal twiddles are the lazy shifts of gl.cuh.  Inputs are lazy
+// with |k| <= 1 (e.g. products from lz_mul).
 template <int B>
 __device__ __forceinline__ void dft_fwd_lz(const gl::Lz* x, uint64_t* v) {
   using namespace gl;
@@ -126,29 +127,33 @@ __device__ __forceinline__ void dft_fwd_lz(const gl::Lz* x, uint64_t* v) {
   } else if constexpr (B == 2) {
     Lz a0 = lz_add(x[0], x[2]), c = lz_sub(x[0], x[2]);
     Lz a1 = lz_add(x[1], x[3]);
-    Lz d = lz(lz_shl<48>(lz_sub(x[1], x[3])));
+    Lz d = lz_shl48_n(lz_sub(x[1], x[3]));
     v[0] = fold(lz_add(a0, a1));
     v[1] = fold(lz_add(c, d));
     v[2] = fold(lz_sub(a0, a1));
     v[3] = fold(lz_sub(c, d));
   } else {
     static_assert(B == 3, "radix 2, 4 or 8");
-    // stage 1: x_k +- x_(k+4), differences times w^k = 2^(24k)
+    // stage 1: x_m +- x_(m+4); the differences d_m carry the twiddle w^m
     Lz a0 = lz_add(x[0], x[4]), d0 = lz_sub(x[0], x[4]);
     Lz a1 = lz_add(x[1], x[5]), d1 = lz_sub(x[1], x[5]);
     Lz a2 = lz_add(x[2], x[6]), d2 = lz_sub(x[2], x[6]);
     Lz a3 = lz_add(x[3], x[7]), d3 = lz_sub(x[3], x[7]);
-    Lz b1 = lz(lz_shl<24>(d1)), b2 = lz(lz_shl<48>(d2)), b3 = lz(lz_shl<72>(d3));
-    // stage 2: radix-4 halves, the odd difference times w^2 = 2^48
+    // even outputs: radix 4 on the sums
     Lz c0 = lz_add(a0, a2), c2 = lz_sub(a0, a2);
-    Lz c1 = lz_add(a1, a3), c3 = lz(lz_shl<48>(lz_sub(a1, a3)));
-    Lz e0 = lz_add(d0, b2), e2 = lz_sub(d0, b2);
-    Lz e1 = lz_add(b1, b3), e3 = lz(lz_shl<48>(lz_sub(b1, b3)));
-    // stage 3 with the output bit reversal folded into the stores
+    Lz c1 = lz_add(a1, a3), c3 = lz_shl48_n(lz_sub(a1, a3));
     v[0] = fold(lz_add(c0, c1));
     v[4] = fold(lz_sub(c0, c1));
     v[2] = fold(lz_add(c2, c3));
     v[6] = fold(lz_sub(c2, c3));
+    // odd outputs: radix 4 on b_m = w^m d_m.  With g = w^2 d3,
+    // b1 + b3 = w (d1 + g) and (b1 - b3) w^2 = w^3 (d1 - g), so every shift
+    // acts on a value with a small overflow count and the one by w (24 bits)
+    // can stay lazy
+    Lz b2 = lz_shl48_n(d2);
+    Lz e0 = lz_add(d0, b2), e2 = lz_sub(d0, b2);
+    Lz g = lz_shl48_n(d3);
+    Lz e1 = lz_shl24_wide(lz_add(d1, g)), e3 = lz_shl72_n(lz_sub(d1, g));
     v[1] = fold(lz_add(e0, e1));
     v[5] = fold(lz_sub(e0, e1));
     v[3] = fold(lz_add(e2, e3));
@@ -181,7 +186,7 @@ __device__ __forceinline__ void dft_inv_lz(const gl::Lz* x, uint64_t* v) {
     // inputs in bit-reversed order (x0, x2, x1, x3)
     Lz s = lz_add(x[0], x[2]), d = lz_sub(x[0], x[2]);
     Lz t = lz_add(x[1], x[3]);
-    Lz e = lz(lz_shl<48>(lz_sub(x[1], x[3])));
+    Lz e = lz_shl48_n(lz_sub(x[1], x[3]));
     v[0] = fold(lz_add(s, t));
     v[2] = fold(lz_sub(s, t));
     v[1] = fold(lz_sub(d, e));
@@ -193,12 +198,12 @@ __device__ __forceinline__ void dft_inv_lz(const gl::Lz* x, uint64_t* v) {
     Lz s23 = lz_add(x[2], x[6]), d23 = lz_sub(x[2], x[6]);
     Lz s45 = lz_add(x[1], x[5]), d45 = lz_sub(x[1], x[5]);
     Lz s67 = lz_add(x[3], x[7]), d67 = lz_sub(x[3], x[7]);
-    Lz t23 = lz(lz_shl<48>(d23)), t67 = lz(lz_shl<48>(d67));
+    Lz t23 = lz_shl48_n(d23), t67 = lz_shl48_n(d67);
     Lz v0 = lz_add(s01, s23), v2 = lz_sub(s01, s23);
     Lz v1 = lz_sub(d01, t23), v3 = lz_add(d01, t23);
     Lz v4 = lz_add(s45, s67), v6 = lz_sub(s45, s67);
     Lz v5 = lz_sub(d45, t67), v7 = lz_add(d45, t67);
-    Lz t5 = lz(lz_shl<72>(v5)), t6 = lz(lz_shl<48>(v6)), t7 = lz(lz_shl<24>(v7));
+    Lz t5 = lz_shl72_n(v5), t6 = lz_shl48_n(v6), t7 = lz_shl24_wide(v7);
     v[0] = fold(lz_add(v0, v4));
     v[4] = fold(lz_sub(v0, v4));
     v[1] = fold(lz_sub(v1, t5));
@@ -388,6 +393,29 @@ __device__ __forceinline__ void tile_inv_t(uint64_t* sm, const uint64_t* tw512, 
     round_inv_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT>(sm, tw512, tid, ptw);
     __syncthreads();
     tile_inv_t<R, T, BC, NT, Q - 1>(sm, tw512, tid);
+  }
+}
+
+// Rounds of a contiguous pass with one warp per 512-word chunk of the tile
+// (2^(9-R) blocks of 2^R words): a chunk's data never leaves its warp, so the
+// rounds synchronise with __syncwarp instead of the whole CTA.  smc is the
+// chunk's base in shared memory (its words at smc + spad(i), i < 512).
+template <int R, int Q = 0>
+__device__ __forceinline__ void chunk_fwd_t(uint64_t* smc, const uint64_t* tw512, int lane) {
+  if constexpr (Q < rp_count(R)) {
+    round_fwd_t<R, 0, 9 - R, rp_bits(R, Q), rp_mlog(R, Q), 32, (Q > 0 ? rp_bits(R, Q - 1) : 0),
+                (Q > 0 ? rp_mlog(R, Q - 1) : 0)>(smc, tw512, lane);
+    __syncwarp();
+    chunk_fwd_t<R, Q + 1>(smc, tw512, lane);
+  }
+}
+
+template <int R, int Q = rp_count(R) - 1>
+__device__ __forceinline__ void chunk_inv_t(uint64_t* smc, const uint64_t* tw512, int lane) {
+  if constexpr (Q >= 0) {
+    round_inv_t<R, 0, 9 - R, rp_bits(R, Q), rp_mlog(R, Q), 32>(smc, tw512, lane, NoPassTw());
+    __syncwarp();
+    chunk_inv_t<R, Q - 1>(smc, tw512, lane);
   }
 }
 

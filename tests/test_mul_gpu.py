@@ -3,6 +3,7 @@
 Bit-exact integer equality is the bar: every product must equal the
 reference's CPU multiply on the same operands.
 """
+import os
 import threading
 
 import numpy as np
@@ -14,6 +15,7 @@ from conftest import hexlimbs, rand_limbs, splitmix64_limbs
 
 pytestmark = pytest.mark.gpu
 M64 = (1 << 64) - 1
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def check(a, b, square=False):
@@ -173,3 +175,39 @@ def test_full_size_square_exact_vs_oracle(bits):
     n = bits // 64
     got = check(rand_limbs(n, 303 + n), None, square=True)
     assert got.size in (2 * n, 2 * n - 1)
+
+
+def test_computed_twiddles_match_oracle_in_fresh_process():
+    # With the twiddle-table cache capped at 0 before the first product, every
+    # pass computes its twiddles from the root tables (the path transforms
+    # longer than 2^28 take, and the no-alloc entry point's): products at
+    # N = 2^21, 2^24 and 2^27 must still equal the oracle's.
+    import subprocess
+    import sys
+    code = r"""
+import sys, numpy as np
+sys.path.insert(0, %r)
+import pi_gb300 as pm, oracle as O
+from conftest import rand_limbs
+pm.init(0)
+assert pm.twiddle_cache(0) == 0
+for la, lb in ((1 << 18, 1 << 18), (1 << 21, 1 << 21), (1 << 24, 1 << 24), (1 << 21, 3)):
+    a, b = rand_limbs(la, la + 5), rand_limbs(lb, lb + 6)
+    assert np.array_equal(pm.mul_mag_ntt(a, b), O.mul_mag_ntt(a, b)), (la, lb)
+assert pm.twiddle_cache(0) == 0
+print("ok")
+""" % (os.path.dirname(os.path.abspath(__file__)),)
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join([ROOT, env.get("PYTHONPATH", "")])
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+
+
+def test_twiddle_tables_are_cached():
+    # the first product at a length builds its tables; later ones reuse them
+    before = pm.twiddle_cache(8 << 30)
+    a, b = rand_limbs(5000, 1), rand_limbs(7000, 2)
+    check(a, b)
+    mid = pm.twiddle_cache(8 << 30)
+    check(a, b)
+    assert pm.twiddle_cache(8 << 30) == mid >= before
