@@ -117,6 +117,32 @@ __device__ __forceinline__ uint32_t mont_mul32(uint32_t a, uint32_t b, uint32_t 
   return r;
 }
 
+// The same product for m < 2^31: t + u m < 2^62 + 2^63 cannot carry out of
+// 64 bits and r = th + hi(u m) + (tl != 0) < 2m < 2^32, so the reduction is
+// min(r, r - m) (r - m wraps above r exactly when r < m).
+__device__ __forceinline__ uint32_t mont_mul31(uint32_t a, uint32_t b, uint32_t m, uint32_t minv) {
+  uint32_t r;
+  asm("{\n\t.reg .u32 tl, th, u, uh, z, s, d;\n\t"
+      "mul.lo.u32 tl, %1, %2;\n\t"
+      "mul.hi.u32 th, %1, %2;\n\t"
+      "mul.lo.u32 u, tl, %4;\n\t"
+      "mul.hi.u32 uh, u, %3;\n\t"
+      "add.cc.u32 z, tl, 0xFFFFFFFF;\n\t"
+      "addc.u32 s, th, uh;\n\t"
+      "sub.u32 d, s, %3;\n\t"
+      "min.u32 %0, s, d;\n\t"
+      "}"
+      : "=r"(r)
+      : "r"(a), "r"(b), "r"(m), "r"(minv));
+  return r;
+}
+
+// 2x mod m for x < m < 2^31: 2x < 2^32, min(2x, 2x - m).
+__device__ __forceinline__ uint32_t dbl_mod31(uint32_t x, uint32_t m) {
+  const uint32_t y = x + x;
+  return min(y, y - m);
+}
+
 // 2x mod m for x < m < 2^32 (the same carry and borrow test).
 __device__ __forceinline__ uint32_t dbl_mod32(uint32_t x, uint32_t m) {
   uint32_t r;
@@ -195,6 +221,20 @@ __device__ __forceinline__ uint64_t pow16_mod(uint64_t e, uint64_t d) {
 // arithmetic (R = 2^32): x runs through the Montgomery forms of 2^(prefix
 // of E), one square per bit and one doubling per set bit.  R mod m comes
 // from a 32-bit remainder; nothing converts 64-bit integers to floats.
+// SMALL: m < 2^31, where the Montgomery product and the doubling need no
+// carry out of 32 bits (mont_mul31, dbl_mod31).
+template <bool SMALL>
+__device__ __forceinline__ uint32_t mm32(uint32_t a, uint32_t b, uint32_t m, uint32_t minv) {
+  if constexpr (SMALL) return mont_mul31(a, b, m, minv);
+  else return mont_mul32(a, b, m, minv);
+}
+template <bool SMALL>
+__device__ __forceinline__ uint32_t dbl32(uint32_t x, uint32_t m) {
+  if constexpr (SMALL) return dbl_mod31(x, m);
+  else return dbl_mod32(x, m);
+}
+
+template <bool SMALL>
 __device__ __forceinline__ uint32_t pow2_mod_odd32(uint64_t E, uint32_t m, uint32_t minv) {
   uint32_t x = (0u - m) % m;  // R mod m: the Montgomery form of 1
   // bits 32 and up (E < 2^40) first, then the low word's 32 bits unrolled
@@ -203,20 +243,20 @@ __device__ __forceinline__ uint32_t pow2_mod_odd32(uint64_t E, uint32_t m, uint3
   const uint32_t eh = (uint32_t)(E >> 32);
   if (eh) {
     const int top = 31 - __clz((int)eh);
-    x = dbl_mod32(x, m);
+    x = dbl32<SMALL>(x, m);
     for (int b = top - 1; b >= 0; b--) {
-      x = mont_mul32(x, x, m, minv);
-      if ((eh >> b) & 1) x = dbl_mod32(x, m);
+      x = mm32<SMALL>(x, x, m, minv);
+      if ((eh >> b) & 1) x = dbl32<SMALL>(x, m);
     }
   }
   uint32_t el = (uint32_t)E;
 #pragma unroll
   for (int b = 0; b < 32; b++) {
-    x = mont_mul32(x, x, m, minv);
-    if ((int32_t)el < 0) x = dbl_mod32(x, m);
+    x = mm32<SMALL>(x, x, m, minv);
+    if ((int32_t)el < 0) x = dbl32<SMALL>(x, m);
     el <<= 1;
   }
-  return mont_mul32(x, 1, m, minv);
+  return mm32<SMALL>(x, 1, m, minv);
 }
 
 // The same for odd 2^32 <= m < 2^34 in 64-bit Montgomery arithmetic.
@@ -247,8 +287,9 @@ __device__ __forceinline__ uint64_t bbp_term(uint64_t e, uint64_t d) {
   if (m == 1) return lo;
   const uint64_t E = 4 * e + 64 - (uint64_t)t;
   const uint64_t minv = neg_inv64(m);  // -m^-1 mod 2^64
-  const uint64_t r = m < (1ull << 32) ? (uint64_t)pow2_mod_odd32(E, (uint32_t)m, (uint32_t)minv)
-                                      : pow2_mod_odd64(E, m, minv);
+  const uint64_t r = m < (1ull << 31)   ? (uint64_t)pow2_mod_odd32<true>(E, (uint32_t)m, (uint32_t)minv)
+                     : m < (1ull << 32) ? (uint64_t)pow2_mod_odd32<false>(E, (uint32_t)m, (uint32_t)minv)
+                                        : pow2_mod_odd64(E, m, minv);
   return (lo - r) * (0 - minv);
 }
 
