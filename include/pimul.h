@@ -246,6 +246,13 @@ int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uin
                         uint64_t* bytes_in_use);
 int pimul_service_reset_stats(void);
 
+/* Admission policy of the service: requests whose transform length is
+ * 2^big_log_n or more run alone on the high-priority stream (default 24),
+ * smaller ones are grouped, at most max_batch per group (default 4096);
+ * values <= 0 leave a setting unchanged.  No counterpart in the reference
+ * (it has no multiply service). */
+int pimul_service_config(int big_log_n, int max_batch);
+
 /* pimul_mul's contract (host buffers, trimmed result, squares when a == b)
  * carried out through the served form: upload, submit, wait, download,
  * free.  Same signature as pimul_mul, so it can be a pimul_mul_fn backend. */

@@ -76,6 +76,7 @@ def load(build_if_stale: bool = True):
     L.pimul_tuning_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.pimul_set_budget.argtypes = [ctypes.c_uint64]
     L.pimul_twiddle_cache.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_service_config.argtypes = [ctypes.c_int, ctypes.c_int]
     L.pimul_upload.argtypes = [_u64p, _sz, ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_submit.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
                                ctypes.POINTER(ctypes.c_uint64)]
@@ -306,6 +307,12 @@ OP_MUL, OP_SQR = 0, 1
 def set_budget(nbytes: int):
     """HBM admission budget of the multiply service (default 120 GiB)."""
     _check(lib().pimul_set_budget(int(nbytes)))
+
+
+def service_config(big_log_n: int = 0, max_batch: int = 0):
+    """Service admission policy: transforms of 2^big_log_n and longer run
+    alone; groups hold at most max_batch requests (0 leaves a value)."""
+    _check(lib().pimul_service_config(int(big_log_n), int(max_batch)))
 
 
 def twiddle_cache(max_bytes: int) -> int:

@@ -446,17 +446,27 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_mid(const Job* 
   cp_async_wait_all();
   __syncthreads();
   if (!spec) chunk_fwd_t<R>(smc, tw, lane);
+  if (EXT && X) {
+    // sum of two products: a b + X, then the inverse rounds
 #pragma unroll 4
-  for (int q = 0; q < 16; q++) {
-    const uint32_t lin = q * 32 + lane;
-    uint64_t x = smc[spad(lin)];
-    uint64_t y = sq ? x : a[coff + lin];
-    uint64_t p = gl::mul(x, y);
-    if (EXT && X) p = gl::add(p, X[coff + lin]);
-    smc[spad(lin)] = ninv ? gl::mul(p, ninv) : p;
+    for (int q = 0; q < 16; q++) {
+      const uint32_t lin = q * 32 + lane;
+      uint64_t x = smc[spad(lin)];
+      uint64_t p = gl::add(gl::mul(x, sq ? x : a[coff + lin]), X[coff + lin]);
+      smc[spad(lin)] = ninv ? gl::mul(p, ninv) : p;
+    }
+    __syncwarp();
+    chunk_inv_t<R>(smc, tw, lane);
+  } else {
+    // the pointwise product (times N^-1 when the inverse first pass's table
+    // does not carry it) enters the first inverse round as lazy products
+    auto pw = [&](uint32_t row0, int k, uint32_t) {
+      const uint32_t lin = row0 + (uint32_t)k;
+      const uint64_t y = sq ? smc[spad(lin)] : a[coff + lin];
+      return ninv ? gl::mul(y, ninv) : y;
+    };
+    chunk_inv_t<R>(smc, tw, lane, pw);
   }
-  __syncwarp();
-  chunk_inv_t<R>(smc, tw, lane);
 #pragma unroll
   for (int q = 0; q < 16; q++) cout[coff + q * 32 + lane] = smc[spad(q * 32 + lane)];
 }
@@ -674,40 +684,65 @@ __global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, 
 // walks a contiguous segment of chunks, the segment results are chained by
 // thread 0.
 constexpr int SCAN_THREADS = 1024;
+// Carry function of a run of chunks as two bits: bit 0 = carry out for carry
+// in 0, bit 1 = carry out for carry in 1 (the chunk's (g, p) byte has the
+// same layout).  Identity: 0b10.  Running `first`, then `then`:
+__device__ __forceinline__ uint32_t cf_then(uint32_t first, uint32_t then) {
+  const uint32_t o0 = (then >> (first & 1)) & 1;
+  const uint32_t o1 = (then >> ((first >> 1) & 1)) & 1;
+  return o0 | (o1 << 1);
+}
+
+// Carry pass 2 (one CTA per product): the carry into every chunk, as an
+// exclusive scan of the chunks' carry functions.  Each thread composes a
+// contiguous run (16-byte loads), the CTA scans the runs with warp shuffles,
+// and each thread writes its run's carries in.
 __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
   if (J.flags & JF_ADDEND) return;
   const uint64_t nchunk = n_chunks(n_windows_out(job_nout(J)));
-  const uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;
+  const uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;  // 64-byte aligned
   uint8_t* chunk_cin = const_cast<uint8_t*>(chunk_gp) + nchunk;
-  __shared__ uint8_t seg_g[SCAN_THREADS], seg_p[SCAN_THREADS], seg_cin[SCAN_THREADS];
-  const uint64_t per = (nchunk + SCAN_THREADS - 1) / SCAN_THREADS;
+  __shared__ uint32_t warp_f[SCAN_THREADS / 32];
+  const uint64_t per = ((nchunk + SCAN_THREADS - 1) / SCAN_THREADS + 15) & ~15ull;  // a multiple of 16
   const uint64_t lo = threadIdx.x * per, hi = lo + per < nchunk ? lo + per : nchunk;
-  uint8_t cg = 0, cp = 1;  // segment carry out for carry in 0 / 1
-  for (uint64_t k = lo; k < hi; k++) {
-    uint8_t gp = chunk_gp[k];
-    uint8_t o0 = gp & 1, o1 = (gp >> 1) & 1;
-    cg = cg ? o1 : o0;
-    cp = cp ? o1 : o0;
+  uint32_t f = 2;  // identity
+  uint64_t k = lo;
+  for (; k + 16 <= hi; k += 16) {
+    const uint4 v = *reinterpret_cast<const uint4*>(chunk_gp + k);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 16; q++) f = cf_then(f, (w[q >> 2] >> (8 * (q & 3))) & 3);
   }
-  seg_g[threadIdx.x] = cg;
-  seg_p[threadIdx.x] = cp;
+  for (; k < hi; k++) f = cf_then(f, chunk_gp[k] & 3);
+  // exclusive scan of the threads' functions
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = f;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= o) inc = cf_then(prev, inc);
+  }
+  if (lane == 31) warp_f[warp] = inc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // only the first ceil(nchunk / per) segments hold chunks
-    const int used = (int)((nchunk + per - 1) / per);
-    uint8_t cin = 0;
-    for (int k = 0; k < used; k++) {
-      seg_cin[k] = cin;
-      cin = cin ? seg_p[k] : seg_g[k];
+  if (warp == 0) {
+    uint32_t winc = lane < SCAN_THREADS / 32 ? warp_f[lane] : 2;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, winc, o);
+      if (lane >= o) winc = cf_then(prev, winc);
     }
+    const uint32_t wexc = __shfl_up_sync(0xFFFFFFFFu, winc, 1);
+    __syncwarp();
+    if (lane < SCAN_THREADS / 32) warp_f[lane] = lane ? wexc : 2;
   }
   __syncthreads();
-  uint8_t cin = seg_cin[threadIdx.x];
-  for (uint64_t k = lo; k < hi; k++) {
-    chunk_cin[k] = cin;
-    uint8_t gp = chunk_gp[k];
-    cin = cin ? ((gp >> 1) & 1) : (gp & 1);
+  const uint32_t in_warp = __shfl_up_sync(0xFFFFFFFFu, inc, 1);
+  const uint32_t before = cf_then(warp_f[warp], lane ? in_warp : 2);
+  uint32_t cin = before & 1;  // carry into this run (the product's carry in is 0)
+  for (k = lo; k < hi; k++) {
+    chunk_cin[k] = (uint8_t)cin;
+    cin = (chunk_gp[k] >> cin) & 1;
   }
 }
 
@@ -2052,6 +2087,7 @@ struct Service {
   std::vector<double> latencies;  // seconds, completed requests
   uint64_t completed = 0, batches = 0;
   int max_batch = 4096;
+  int big_log_n = 24;  // requests with transforms of 2^big_log_n and longer run alone on stream 0
 };
 // Heap-allocated and never destroyed: its thread is joined by an atexit
 // handler (registered after the CUDA runtime's, so it runs first).
@@ -2115,11 +2151,10 @@ static int svc_req_L(const SvcRequest& r) {
   return log2_ceil(4 * la + 4 * lb - 1);
 }
 
-static const int SVC_BIG_L = 20;  // transforms of 2^20 and longer run alone
 
 static void svc_admit(std::unique_lock<std::mutex>& lk) {
   if (g_svc.queue.empty()) return;
-  const bool big_head = svc_req_L(g_svc.requests[g_svc.queue.front()]) >= SVC_BIG_L;
+  const bool big_head = svc_req_L(g_svc.requests[g_svc.queue.front()]) >= g_svc.big_log_n;
   int si = -1;
   if (big_head) {
     if (!g_svc.stream_busy[0]) si = 0;
@@ -2133,7 +2168,7 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
   while (!g_svc.queue.empty() && (int)take.size() < g_svc.max_batch) {
     uint64_t t = g_svc.queue.front();
     SvcRequest& r = g_svc.requests[t];
-    const bool big = svc_req_L(r) >= SVC_BIG_L;
+    const bool big = svc_req_L(r) >= g_svc.big_log_n;
     if (big != big_head || (big && !take.empty())) break;  // a big request forms its own group
     SvcHandle& A = g_svc.handles[r.a];
     SvcHandle& B = g_svc.handles[r.b];
@@ -2574,6 +2609,13 @@ int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uin
   if (completed) *completed = g_svc.completed;
   if (batches) *batches = g_svc.batches;
   if (in_use) *in_use = g_svc.in_use;
+  return PIMUL_OK;
+}
+
+int pimul_service_config(int big_log_n, int max_batch) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  if (big_log_n > 0) g_svc.big_log_n = big_log_n;
+  if (max_batch > 0) g_svc.max_batch = max_batch;
   return PIMUL_OK;
 }
 

@@ -410,10 +410,12 @@ __device__ __forceinline__ void chunk_fwd_t(uint64_t* smc, const uint64_t* tw512
   }
 }
 
-template <int R, int Q = rp_count(R) - 1>
-__device__ __forceinline__ void chunk_inv_t(uint64_t* smc, const uint64_t* tw512, int lane) {
+// ptw: factors multiplied into the first inverse round's inputs as lazy
+// products (ptw(row0, k, 0) for chunk word row0 + k), e.g. a pointwise product.
+template <int R, int Q = rp_count(R) - 1, class F = NoPassTw>
+__device__ __forceinline__ void chunk_inv_t(uint64_t* smc, const uint64_t* tw512, int lane, const F& ptw = F()) {
   if constexpr (Q >= 0) {
-    round_inv_t<R, 0, 9 - R, rp_bits(R, Q), rp_mlog(R, Q), 32>(smc, tw512, lane, NoPassTw());
+    round_inv_t<R, 0, 9 - R, rp_bits(R, Q), rp_mlog(R, Q), 32>(smc, tw512, lane, ptw);
     __syncwarp();
     chunk_inv_t<R, Q - 1>(smc, tw512, lane);
   }
