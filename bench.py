@@ -42,10 +42,10 @@ BITS_B = 1 << 30
 
 # DRAM traffic of the dominant kernel class (forward passes) per transform
 # word: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
-# k_col_mid<9,fwd> (x2) and k_fwd_last<8> at N = 2^26 (mean 1023.2 MB per
-# launch = 15.25 bytes per word).
-# Traffic grows in proportion to N, so a launch moves 15.25 N bytes.
-NCU_TRAFFIC_BYTES_PER_WORD = 15.25
+# each of k_col_mid<9,fwd> (15.60 bytes per word) and k_fwd_last<9> (15.53)
+# of a 2^30 x 2^30-bit product (N = 2^27); the class runs the first twice
+# and the second once per transform: 15.58 N bytes per launch.
+NCU_TRAFFIC_BYTES_PER_WORD = 15.58
 
 
 def b_mul(n, la, lb, square=False):
@@ -197,6 +197,28 @@ def stats(lib):
     return out
 
 
+# ALU-pipe warp instructions per transform word, per launch of each pass
+# kernel (smsp__inst_executed_pipe_alu.sum / N from one ncu capture per
+# kernel of a 2^30 x 2^30-bit product, N = 2^27, plan 2^9 x 2^9 x 2^9);
+# "carry" is the three carry kernels together.  Instruction counts do not
+# depend on the clock or on timing.
+NCU_ALU_PER_WORD = {
+    "k_fwd_first": 2.87, "k_col_mid_fwd": 2.82, "k_fwd_last": 2.22, "k_mid": 4.36,
+    "k_col_mid_inv": 2.66, "k_inv_first_carry": 3.04, "carry": 0.47,
+}
+# The integer ALU pipe retires 16 lanes per clock per SM sub-partition:
+# half a warp instruction per clock, four sub-partitions per SM.
+ALU_WARP_INSTR_PER_CLK_PER_SM = 4 * 0.5
+
+
+def alu_per_word(kind):
+    """Mean ALU warp instructions per word of one launch of a kernel class."""
+    a = NCU_ALU_PER_WORD
+    return {"pack": a["k_fwd_first"], "pass_fwd": (2 * a["k_col_mid_fwd"] + a["k_fwd_last"]) / 3,
+            "pass_inv": (a["k_col_mid_inv"] + a["k_inv_first_carry"]) / 2, "pointwise": a["k_mid"],
+            "carry": a["carry"] / 3}.get(kind, 0.0)
+
+
 def kernel_bytes_per_launch(kind, n, la, lb):
     """Algorithmic bytes of one launch of each kernel class."""
     if kind in ("pass_fwd", "pass_inv"):
@@ -307,6 +329,15 @@ def run_gpu(args):
     achieved = per_launch / (avg_ms * 1e-3) / 1e9
     step_achieved = bytes_step / (ms_step * 1e-3) / 1e9
     launches = sum(v["launches"] for v in ks.values())
+    # integer-pipe roofline: ALU warp instructions (ncu counts per word) over
+    # the pipe's capacity at the SM clock sampled during the timed region
+    clocks = clk.summary()
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    f_sm = (clocks["sm_mhz"] or clocks["sm_max_mhz"] or 2070.0) * 1e6
+    alu_cap = n_sm * ALU_WARP_INSTR_PER_CLK_PER_SM * f_sm  # warp instructions / s
+    int_frac = alu_per_word(dom) * N / (avg_ms * 1e-3) / alu_cap
+    step_alu = sum(alu_per_word(k) * N * ks[k]["launches"] / args.steps for k in ks)
+    int_frac_step = step_alu / (ms_step * 1e-3) / alu_cap
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -348,8 +379,14 @@ def run_gpu(args):
                          "bytes_per_launch": per_launch, "avg_launch_ms": round(avg_ms, 4),
                          "step_achieved": round(step_achieved, 1),
                          "step_frac": round(step_achieved / peak, 4),
-                         "binding_unit": "integer ALU pipe, not HBM (ncu: ALU 62-70 % busy, issue 59-67 %, "
-                                         "DRAM 13-35 % of peak, from ncu captures of the pass kernels)",
+                         "int_frac": round(int_frac, 4), "int_frac_step": round(int_frac_step, 4),
+                         "int_model": {"alu_warp_instr_per_word": round(alu_per_word(dom), 3),
+                                       "alu_warp_instr_per_step": round(step_alu),
+                                       "peak_warp_instr_per_s": round(alu_cap),
+                                       "sms": n_sm, "sm_mhz": f_sm / 1e6,
+                                       "model": "ALU-pipe warp instructions per word from ncu x N, over "
+                                                "SMs x 4 sub-partitions x 0.5 warp instr/clk x sampled SM clock"},
+                         "binding_unit": "integer ALU pipe (int_frac), not HBM (frac)",
                          "io_effective_gbs": round(16 * (la + lb) / (ms_step * 1e-3) / 1e9, 1),
                          "integer_model": {
                              "butterflies": 3 * (N // 2) * L, "pointwise_mulmods": 2 * N,
@@ -358,7 +395,7 @@ def run_gpu(args):
                                       "products per multiply"}},
             "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ks.items()},
             "gpu_launches": launches,
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "cpu_baseline": cpu,
         }
         if ws == 1:
@@ -757,7 +794,12 @@ def served_measure(n, loads):
     hb = [pm.upload(x) for x in base]
     runs = []
     exact = None
-    for li, load in enumerate(loads):
+    # every load with the default admission policy (transforms of 2^24 and
+    # longer run alone, smaller ones are batched), then the highest load
+    # again with 2^20 and longer alone (mid-size products one at a time)
+    plan = [(load, 24) for load in loads] + [(max(loads), 20)]
+    for li, (load, big) in enumerate(plan):
+        pm.service_config(big_log_n=big)
         lam = load * capacity
         rng = np.random.default_rng(99)
         arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
@@ -800,12 +842,13 @@ def served_measure(n, loads):
             pm.free(h)
         lp = np.array(lat_plain) * 1e3
         runs.append({
-            "offered_load": load, "lambda_rps": round(lam, 1),
+            "offered_load": load, "lambda_rps": round(lam, 1), "alone_from_log_n": big,
             "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
                        "ops_per_s": round(n / span_served, 1), "batches": st["batches"]},
             "plain": {"p50_ms": round(float(np.percentile(lp, 50)), 3),
                       "p99_ms": round(float(np.percentile(lp, 99)), 3), "ops_per_s": round(n / span_plain, 1)},
             "throughput_served_over_plain": round(span_plain / span_served, 3)})
+    pm.service_config(big_log_n=24)
     for h in hb:
         pm.free(h)
     first = runs[0]
