@@ -21,6 +21,7 @@ not shard): value = all ranks' bytes / max rank time.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import ctypes
 import json
 import os
@@ -204,7 +205,7 @@ def stats(lib):
 # depend on the clock or on timing.
 NCU_ALU_PER_WORD = {
     "k_fwd_first": 2.87, "k_col_mid_fwd": 2.82, "k_fwd_last": 2.22, "k_mid": 4.36,
-    "k_col_mid_inv": 2.66, "k_inv_first_carry": 3.04, "carry": 0.47,
+    "k_col_mid_inv": 2.66, "k_inv_first_carry": 3.04, "carry": 0.46,
 }
 # The integer ALU pipe retires 16 lanes per clock per SM sub-partition:
 # half a warp instruction per clock, four sub-partitions per SM.
@@ -1042,10 +1043,35 @@ def run_bbp(args):
     rng = np.random.default_rng(2025)
     pos = rng.integers(0, int(args.max_pos), size=args.positions, dtype=np.uint64)
     pm.bbp_hex_digits(np.arange(64, dtype=np.uint64))  # warm-up
+    # launches of at most --bbp-batch positions (a full 65,536-position run
+    # takes tens of minutes; each launch is bounded)
+    bs = max(1, args.bbp_batch)
     t0 = time.perf_counter()
-    d = pm.bbp_hex_digits(pos)
+    d = np.concatenate([pm.bbp_hex_digits(pos[i:i + bs]) for i in range(0, pos.size, bs)])
     dt = time.perf_counter() - t0
     terms = 4.0 * float((pos.astype(np.float64) + 1).sum())
+    digest = hashlib.sha256("".join(f"{int(p)} {int(x):08x}\n" for p, x in zip(pos, d)).encode()).hexdigest()
+    check = None
+    if args.check_digits:
+        # every position against the hex digits of pi computed independently:
+        # batched Chudnovsky to D decimal digits, then verify-hex's conversion
+        D = int(args.check_digits)
+        t1 = time.perf_counter()
+        sdig, _ = pm.pi_chudnovsky_batched(D)
+        hx = pm.decimal_to_hex("3." + sdig[1:])
+        del sdig
+        frac = hx[2:]
+        limit = len(frac) - 40  # verify-hex leaves its last 32 hex digits unchecked
+        ok = bad = 0
+        for p_, x in zip(pos, d):
+            if int(p_) + 8 <= limit:
+                if frac[int(p_): int(p_) + 8] == f"{int(x):08x}":
+                    ok += 1
+                else:
+                    bad += 1
+        check = {"decimal_digits": D, "hex_digits": len(frac), "checked_below": limit, "positions_checked": ok + bad,
+                 "matches": ok, "mismatches": bad, "seconds": round(time.perf_counter() - t1, 1)}
+        del hx, frac
     line = {
         "metric": "BBP hex-digit spot checks (positions/s)", "project_metric": PROJECT_METRIC,
         "value": round(args.positions / dt, 3), "unit": "positions/s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -1055,6 +1081,8 @@ def run_bbp(args):
         "terms_per_s": round(terms / dt, 1),
         "extrapolated_65536_positions_s": round(dt * 65536 / args.positions, 1),
         "first_digits": [f"{int(x):08x}" for x in d[:4]],
+        "digits_sha256": digest, "digits_format": "one line per position in seeded order: '<position> <8 hex>'",
+        "cross_check": check,
     }
     if not args.no_cpu_baseline:
         import oracle
@@ -1180,6 +1208,9 @@ def main():
     ap.add_argument("--max-pos", type=float, default=8e8)
     ap.add_argument("--cpu-positions", type=int, default=16)
     ap.add_argument("--cpu-depth", type=float, default=2e6)
+    ap.add_argument("--bbp-batch", type=int, default=8192, help="BBP positions per launch")
+    ap.add_argument("--check-digits", type=float, default=0,
+                    help="BBP: also compute pi to this many decimal digits, convert to hex and compare every position")
     ap.add_argument("--workload", choices=["mul", "batch", "served", "pi", "bbp", "hex"], default="mul",
                     help="mul: the 2^30-bit product (headline); batch: 4096 uneven products; "
                          "served: Poisson request stream through the multiply service")
