@@ -515,6 +515,16 @@ def pi_measure():
             out[key].update({"plain_wall_s": round(pwall, 3), "speedup_batched_vs_plain": round(pwall / wall, 2),
                              "plain_identical": sp_ == s})
             del sp_
+            # the splitting tree's upper levels through the multiply service
+            # (chained handles submitted as the recursion unfolds)
+            pm.pi_chudnovsky_served(100_000)
+            t2 = time.perf_counter()
+            ss_, sinfo = pm.pi_chudnovsky_served(D)
+            swall = time.perf_counter() - t2
+            out[key].update({"served_wall_s": round(swall, 3), "served_identical": ss_ == s,
+                             "served_service_requests": sinfo["service_requests"],
+                             "served_phases_ms": {k: round(v, 1) for k, v in sinfo.items() if k.endswith("_ms")}})
+            del ss_
         del s
     return out
 

@@ -213,19 +213,30 @@ int pimul_twiddle_cache(uint64_t max_bytes, uint64_t* held);
  * Served form: a device-resident multiply service.
  *
  * Integers live on the device as handles.  pimul_submit queues a product
- * (op PIMUL_OP_MUL: a * b; PIMUL_OP_SQR: a * a) and returns its result
+ * (op PIMUL_OP_MUL: a * b; PIMUL_OP_SQR: a * a), a sum (PIMUL_OP_ADD:
+ * a + b, stored in max(la, lb) + 1 limbs) or a difference (PIMUL_OP_SUB:
+ * a - b for values a >= b, stored in max(la, lb) limbs; a smaller a gives
+ * the difference modulo 2^(64 max(la, lb))) and returns its result
  * handle and a ticket at once; the result handle may be an input of later
  * submits before it is computed (the dependency is a CUDA event: no host
- * round trip).  A service thread admits queued requests in order while
- * their result and scratch memory fit the HBM budget (pimul_set_budget,
+ * round trip).  A service thread admits queued requests whose inputs are
+ * launched, in order, while their result and scratch memory fit the HBM
+ * budget (pimul_set_budget,
  * default 120 GiB; handles count against it until freed), launches each
  * admitted group as one batch, and releases the scratch when the group
  * completes; requests that arrive meanwhile join the next group (continuous
- * batching).  Groups of small requests run on four streams; a request with a
- * transform of 2^20 or more forms its own group on a high-priority stream.  pimul_wait blocks until a ticket's
- * product is done (timeout_us < 0: no limit) or returns PIMUL_ETIMEDOUT.
- * pimul_free waits for the handle's producer and readers.  A result handle
- * stores la + lb limbs; pimul_download returns the trimmed value.
+ * batching).  Groups run on four streams (products and sums in separate
+ * groups); a request with a transform of 2^24 or more (pimul_service_config)
+ * forms its own group on a high-priority stream.  pimul_wait blocks until a
+ * ticket's result is done (timeout_us < 0: no limit) or returns
+ * PIMUL_ETIMEDOUT.  pimul_free waits for the handle's producer and readers;
+ * pimul_release returns at once and the handle is freed when they are done
+ * (a tree of chained requests releases its inner nodes this way).
+ * pimul_adopt makes a handle of device memory the caller owns and keeps
+ * (never freed by the service, not counted in the budget); pimul_handle_device
+ * waits for a handle's producer and gives its device address and stored
+ * length.  A product handle stores la + lb limbs; pimul_download returns the
+ * trimmed value.
  * pimul_service_stats reports submit-to-completion latency percentiles.
  *
  * Replaces: the per-level products of the binary-splitting tree with their
@@ -235,6 +246,8 @@ int pimul_twiddle_cache(uint64_t max_bytes, uint64_t* held);
  */
 #define PIMUL_OP_MUL 0
 #define PIMUL_OP_SQR 1
+#define PIMUL_OP_ADD 2
+#define PIMUL_OP_SUB 3
 int pimul_set_budget(uint64_t bytes);
 int pimul_upload(const uint64_t* host, size_t n, uint64_t* handle);
 int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t* ticket);
@@ -242,6 +255,9 @@ int pimul_wait(uint64_t ticket, int64_t timeout_us);
 int pimul_handle_size(uint64_t handle, size_t* limbs);
 int pimul_download(uint64_t handle, uint64_t* host, size_t cap, size_t* len);
 int pimul_free(uint64_t handle);
+int pimul_release(uint64_t handle);
+int pimul_adopt(const uint64_t* d, size_t n, uint64_t* handle);
+int pimul_handle_device(uint64_t handle, const uint64_t** d, size_t* limbs);
 int pimul_service_stats(double* p50_ms, double* p99_ms, uint64_t* completed, uint64_t* batches,
                         uint64_t* bytes_in_use);
 int pimul_service_reset_stats(void);
@@ -313,6 +329,24 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
  */
 int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t cap, uint64_t leaf_terms, double* phase_ms,
                                 uint64_t* gpu_products, uint64_t* levels, uint64_t* ntt_hist33);
+
+/*
+ * pimul_pi_chudnovsky_batched with the splitting tree's upper levels driven
+ * through the multiply service: the level-batched device splitting stops at
+ * about serve_nodes nodes (0: 512), which become handles (pimul_adopt), and
+ * the rest of the tree is submitted as the recursion unfolds, five chained
+ * requests per merge (the three products, the T cross products' sum or
+ * difference), inner nodes released as their parents are queued; only the
+ * root's Q and |T| are read, by the device final assembly.  Same digits.
+ * Optional outputs as pimul_pi_chudnovsky_batched; requests = service
+ * requests submitted.
+ *
+ * Replaces: the binary splitting's recursion of
+ * crates/pi-core/src/algorithm/chudnovsky.rs:377-413, whose products and
+ * sums of one level run as independent rayon tasks.
+ */
+int pimul_pi_chudnovsky_served(uint64_t digits, char* out, size_t cap, uint64_t serve_nodes, double* phase_ms,
+                               uint64_t* gpu_products, uint64_t* requests);
 
 /*
  * Decimal string of the non-negative integer limbs[0..n) (little-endian u64,

@@ -26,7 +26,7 @@ __all__ = [
     "PimulError", "lib", "load", "version", "init", "mul_mag_ntt", "mul_device", "sum_batch", "SumJob",
     "plan", "sync", "bbp_hex_digits", "mul_batch", "BatchPlan", "autotune",
     "tuning_apply", "PimulJob", "set_budget", "upload", "submit", "wait", "download", "free",
-    "handle_size", "pi_chudnovsky", "pi_gauss_legendre", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "LIB_PATH",
+    "handle_size", "pi_chudnovsky", "pi_gauss_legendre", "service_stats", "service_reset_stats", "OP_MUL", "OP_SQR", "OP_ADD", "OP_SUB", "release", "adopt", "handle_device", "pi_chudnovsky_served", "LIB_PATH",
     "decimal_to_hex", "convert_decimal_to_hex",
 ]
 
@@ -84,6 +84,12 @@ def load(build_if_stale: bool = True):
     L.pimul_handle_size.argtypes = [ctypes.c_uint64, ctypes.POINTER(_sz)]
     L.pimul_download.argtypes = [ctypes.c_uint64, _u64p, _sz, ctypes.POINTER(_sz)]
     L.pimul_free.argtypes = [ctypes.c_uint64]
+    L.pimul_release.argtypes = [ctypes.c_uint64]
+    L.pimul_adopt.argtypes = [ctypes.c_void_p, _sz, ctypes.POINTER(ctypes.c_uint64)]
+    L.pimul_handle_device.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(_sz)]
+    L.pimul_pi_chudnovsky_served.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_uint64,
+                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                             ctypes.POINTER(ctypes.c_uint64)]
     L.pimul_service_stats.argtypes = [ctypes.POINTER(ctypes.c_double)] * 2 + [ctypes.POINTER(ctypes.c_uint64)] * 3
     L.pimul_service_reset_stats.argtypes = []
     L.pimul_pi_chudnovsky.argtypes = [ctypes.c_uint64, ctypes.c_char_p, _sz, ctypes.c_void_p, ctypes.c_uint64,
@@ -301,7 +307,7 @@ def tuning_apply(choices: dict):
 
 
 # ----------------------------------------------------------------- served form
-OP_MUL, OP_SQR = 0, 1
+OP_MUL, OP_SQR, OP_ADD, OP_SUB = 0, 1, 2, 3
 
 
 def set_budget(nbytes: int):
@@ -362,6 +368,42 @@ def download(h: int) -> np.ndarray:
 
 def free(h: int):
     _check(lib().pimul_free(h))
+
+
+def release(h: int):
+    """Free the handle once its producer and the requests reading it are done
+    (returns at once)."""
+    _check(lib().pimul_release(h))
+
+
+def adopt(device_ptr: int, n: int) -> int:
+    """A handle for n limbs of device memory the caller owns and keeps."""
+    h = ctypes.c_uint64(0)
+    _check(lib().pimul_adopt(ctypes.c_void_p(device_ptr), n, ctypes.byref(h)))
+    return h.value
+
+
+def handle_device(h: int):
+    """(device address, stored limbs) of a handle; waits for its producer."""
+    d = ctypes.c_void_p(0)
+    n = _sz(0)
+    _check(lib().pimul_handle_device(h, ctypes.byref(d), ctypes.byref(n)))
+    return d.value, n.value
+
+
+def pi_chudnovsky_served(digits: int, serve_nodes: int = 0):
+    """Digits of pi by Chudnovsky with the splitting tree's upper levels
+    (above about serve_nodes nodes, 0: 512) submitted to the multiply service
+    as chained handles (pimul_pi_chudnovsky_served).  Returns (digits_str, info)."""
+    buf = ctypes.create_string_buffer(digits + 1)
+    ph = (ctypes.c_double * 3)()
+    n = ctypes.c_uint64(0)
+    req = ctypes.c_uint64(0)
+    _check(lib().pimul_pi_chudnovsky_served(digits, buf, digits + 1, serve_nodes, ph, ctypes.byref(n),
+                                            ctypes.byref(req)))
+    info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
+            "ntt_products": n.value, "service_requests": req.value}
+    return ctypes.string_at(buf, digits).decode("ascii"), info
 
 
 def service_stats() -> dict:

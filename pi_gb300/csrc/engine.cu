@@ -2050,11 +2050,13 @@ struct SvcHandle {
   bool freed = false;
   uint64_t bytes = 0;
   int readers = 0;           // queued or running requests that read this handle
+  bool borrowed = false;     // the caller's device memory (pimul_adopt): never freed here
+  bool release = false;      // pimul_release: free once its producer and readers are done
 };
 
 struct SvcRequest {
   uint64_t ticket;
-  int op;  // 0 multiply, 1 square
+  int op;  // 0 multiply, 1 square, 2 add, 3 subtract (PIMUL_OP_*)
   uint64_t a, b, out;  // handle ids
   double t_submit;
   double t_done = 0;
@@ -2146,17 +2148,70 @@ static int svc_start() {
 // not fit the budget.
 // Transform length (log2) of a queued request.
 static int svc_req_L(const SvcRequest& r) {
+  if (r.op >= 2) return 0;  // additions and subtractions: one linear pass
   uint64_t la = g_svc.handles[r.a].limbs, lb = g_svc.handles[r.b].limbs;
   if (!la || !lb) return 0;
   return log2_ceil(4 * la + 4 * lb - 1);
 }
 
+// Free a handle whose producer has been launched and whose readers are done
+// (the free is ordered after the producer's batch on stream 0).
+static void svc_free_now(uint64_t id) {
+  auto it = g_svc.handles.find(id);
+  if (it == g_svc.handles.end()) return;
+  SvcHandle& h = it->second;
+  if (h.ready) {
+    cudaStreamWaitEvent(g_svc.streams[0], h.ready, 0);
+    cudaEventDestroy(h.ready);
+  }
+  if (!h.borrowed && h.d) cudaFreeAsync(h.d, g_svc.streams[0]);
+  g_svc.in_use -= h.bytes;
+  g_svc.handles.erase(it);
+}
+
+// Released handles that have become free.
+static void svc_free_released() {
+  std::vector<uint64_t> done;
+  for (auto& kv : g_svc.handles)
+    if (kv.second.release && !kv.second.pending && kv.second.readers <= 0) done.push_back(kv.first);
+  for (uint64_t id : done) svc_free_now(id);
+}
+
+
+int svc_addsub(const pimul_addsub_job* jobs, size_t n, cudaStream_t st);  // unchecked, asynchronous (below)
+
+// Group kind of a request: 0 a product below the big length, 1 a big
+// product (alone on stream 0), 2 an addition or subtraction.
+static int svc_kind(const SvcRequest& r) {
+  if (r.op >= 2) return 2;
+  return svc_req_L(r) >= g_svc.big_log_n ? 1 : 0;
+}
+
+static bool svc_ready(const SvcRequest& r) {
+  return !g_svc.handles[r.a].pending && !g_svc.handles[r.b].pending;
+}
+
+// One group: the kind of the first ready request in the queue, then every
+// ready request of that kind among the first SVC_SCAN queued (in order),
+// within the budget.  A request whose input is not launched yet waits
+// without holding back the ready ones behind it (continuous batching of
+// whatever is ready).
+constexpr size_t SVC_SCAN = 1 << 14;
 
 static void svc_admit(std::unique_lock<std::mutex>& lk) {
   if (g_svc.queue.empty()) return;
-  const bool big_head = svc_req_L(g_svc.requests[g_svc.queue.front()]) >= g_svc.big_log_n;
+  int kind = -1;
+  size_t scanned = 0;
+  for (auto it = g_svc.queue.begin(); it != g_svc.queue.end() && scanned < SVC_SCAN; ++it, ++scanned) {
+    const SvcRequest& r = g_svc.requests[*it];
+    if (svc_ready(r)) {
+      kind = svc_kind(r);
+      break;
+    }
+  }
+  if (kind < 0) return;
   int si = -1;
-  if (big_head) {
+  if (kind == 1) {
     if (!g_svc.stream_busy[0]) si = 0;
   } else {
     for (size_t i = 1; i < g_svc.streams.size(); i++)
@@ -2165,27 +2220,25 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
   if (si < 0) return;
   std::vector<uint64_t> take;
   uint64_t add = 0;
-  while (!g_svc.queue.empty() && (int)take.size() < g_svc.max_batch) {
-    uint64_t t = g_svc.queue.front();
-    SvcRequest& r = g_svc.requests[t];
-    const bool big = svc_req_L(r) >= g_svc.big_log_n;
-    if (big != big_head || (big && !take.empty())) break;  // a big request forms its own group
-    SvcHandle& A = g_svc.handles[r.a];
-    SvcHandle& B = g_svc.handles[r.b];
-    bool inputs_launched = !A.pending && !B.pending;
-    if (!inputs_launched) {
-      // a producer inside this same group is fine only if launched before:
-      // keep it simple and start a new group at that point
-      break;
+  scanned = 0;
+  for (auto it = g_svc.queue.begin();
+       it != g_svc.queue.end() && scanned < SVC_SCAN && (int)take.size() < g_svc.max_batch; scanned++) {
+    SvcRequest& r = g_svc.requests[*it];
+    if (!svc_ready(r) || svc_kind(r) != kind) {
+      ++it;
+      continue;
     }
     if (g_svc.in_use + add + r.scratch > g_svc.budget && !(take.empty() && g_svc.inflight.empty())) break;
-    take.push_back(t);
+    take.push_back(*it);
     add += r.scratch;
-    g_svc.queue.pop_front();
+    it = g_svc.queue.erase(it);
+    if (kind == 1) break;  // a big request forms its own group
   }
   if (take.empty()) return;
   cudaStream_t st = g_svc.streams[si];
+  const bool linear = g_svc.requests[take.front()].op >= 2;
   std::vector<pimul_job> jobs;
+  std::vector<pimul_addsub_job> asj;
   jobs.reserve(take.size());
   for (uint64_t t : take) {
     SvcRequest& r = g_svc.requests[t];
@@ -2193,12 +2246,18 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
     SvcHandle& B = g_svc.handles[r.b];
     SvcHandle& O = g_svc.handles[r.out];
     if (A.ready) cudaStreamWaitEvent(st, A.ready, 0);
-    if (r.op == 0 && B.ready) cudaStreamWaitEvent(st, B.ready, 0);
+    if (r.op != 1 && B.ready) cudaStreamWaitEvent(st, B.ready, 0);
     if (O.ready) cudaStreamWaitEvent(st, O.ready, 0);  // result buffer allocated
-    const uint64_t* pa = A.d;
-    const uint64_t* pb = r.op == 1 ? A.d : B.d;
-    uint64_t lb = r.op == 1 ? A.limbs : B.limbs;
-    jobs.push_back(pimul_job{pa, A.limbs, pb, lb, O.d});
+    if (linear) {
+      // out = a + b (max + 1 limbs) or a - b (a's limbs; a >= b): no carry
+      // or borrow can leave the output, so nothing is checked
+      asj.push_back(pimul_addsub_job{A.d, A.limbs, B.d, B.limbs, O.d, O.limbs, r.op == 3 ? PIMUL_SUB_MOD : 0});
+    } else {
+      const uint64_t* pa = A.d;
+      const uint64_t* pb = r.op == 1 ? A.d : B.d;
+      uint64_t lb = r.op == 1 ? A.limbs : B.limbs;
+      jobs.push_back(pimul_job{pa, A.limbs, pb, lb, O.d});
+    }
     r.state = 1;
   }
   SvcBatch bt;
@@ -2207,7 +2266,7 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
   bt.tickets = take;
   g_svc.in_use += add;
   lk.unlock();
-  int rc = mul_batch(jobs.data(), jobs.size(), st);
+  int rc = linear ? svc_addsub(asj.data(), asj.size(), st) : mul_batch(jobs.data(), jobs.size(), st);
   cudaEventCreateWithFlags(&bt.done, cudaEventDisableTiming);
   cudaEventRecord(bt.done, st);
   lk.lock();
@@ -2247,6 +2306,7 @@ static void svc_reap(std::unique_lock<std::mutex>& lk) {
       }
       g_svc.in_use -= bt.scratch;
       g_svc.stream_busy[bt.stream] = 0;
+      svc_free_released();
       cudaEventDestroy(bt.done);
       g_svc.inflight.erase(g_svc.inflight.begin() + i);
       g_svc.done_cv.notify_all();
@@ -2466,7 +2526,7 @@ int pimul_upload(const uint64_t* host, size_t n, uint64_t* handle) {
 }
 
 int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t* ticket) {
-  if (!out_handle || !ticket || (op != PIMUL_OP_MUL && op != PIMUL_OP_SQR)) return fail(PIMUL_EINVAL, "bad argument");
+  if (!out_handle || !ticket || op < PIMUL_OP_MUL || op > PIMUL_OP_SUB) return fail(PIMUL_EINVAL, "bad argument");
   int rc = svc_start();
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_svc.mu);
@@ -2475,10 +2535,13 @@ int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t*
   if (ia == g_svc.handles.end() || ib == g_svc.handles.end() || ia->second.freed || ib->second.freed)
     return fail(PIMUL_ENOTFOUND, "unknown or freed handle");
   uint64_t la = ia->second.limbs, lb = ib->second.limbs;
-  uint64_t outl = la + lb;
+  const bool linear = op == PIMUL_OP_ADD || op == PIMUL_OP_SUB;
+  // a sum keeps every carry in max + 1 limbs; a difference (a >= b) fits in max
+  uint64_t outl = op == PIMUL_OP_ADD ? std::max(la, lb) + 1 : op == PIMUL_OP_SUB ? std::max(la, lb) : la + lb;
   uint64_t obytes = round256(std::max<uint64_t>(outl, 1) * 8);
-  uint64_t scratch = (la && lb && sizes_for(la, lb).L > SMALL_LOG_MAX) ? scratch_bytes(la, lb, false) : 0;
-  if (la && lb && sizes_for(la, lb).L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
+  uint64_t scratch =
+      (!linear && la && lb && sizes_for(la, lb).L > SMALL_LOG_MAX) ? scratch_bytes(la, lb, false) : 0;
+  if (!linear && la && lb && sizes_for(la, lb).L > 32) return fail(PIMUL_EINVAL, "transform length above 2^32");
   if (obytes + scratch > g_svc.budget) return fail(PIMUL_ENOMEM, "request larger than the HBM budget");
   uint64_t* d = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync((void**)&d, obytes, g_dev.pool, g_svc.streams[0]);
@@ -2497,7 +2560,7 @@ int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t*
   uint64_t t = g_svc.next_ticket++;
   SvcRequest r;
   r.ticket = t;
-  r.op = op == PIMUL_OP_SQR ? 1 : 0;
+  r.op = op;
   r.a = a;
   r.b = op == PIMUL_OP_SQR ? a : b;
   r.out = oid;
@@ -2586,16 +2649,49 @@ int pimul_free(uint64_t handle) {
   });
   auto f = g_svc.handles.find(handle);
   if (f == g_svc.handles.end()) return fail(PIMUL_ENOTFOUND, "handle freed concurrently");
-  SvcHandle& h = f->second;
-  if (h.ready) {
-    cudaStreamWaitEvent(g_svc.streams[0], h.ready, 0);
-    cudaEventDestroy(h.ready);
+  svc_free_now(handle);
+  return PIMUL_OK;
+}
+
+int pimul_release(uint64_t handle) {
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  auto it = g_svc.handles.find(handle);
+  if (it == g_svc.handles.end() || it->second.freed || it->second.release)
+    return fail(PIMUL_ENOTFOUND, "unknown, freed or released handle");
+  it->second.release = true;
+  if (!it->second.pending && it->second.readers <= 0) svc_free_now(handle);
+  return PIMUL_OK;
+}
+
+int pimul_adopt(const uint64_t* d, size_t n, uint64_t* handle) {
+  if (!handle || (n && !d)) return fail(PIMUL_EINVAL, "null argument");
+  int rc = svc_start();
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  uint64_t id = svc_new_handle(n, const_cast<uint64_t*>(d), false, 0);
+  g_svc.handles[id].borrowed = true;
+  *handle = id;
+  return PIMUL_OK;
+}
+
+int pimul_handle_device(uint64_t handle, const uint64_t** d, size_t* limbs) {
+  if (!d || !limbs) return fail(PIMUL_EINVAL, "null argument");
+  int64_t producer;
+  {
+    std::lock_guard<std::mutex> lk(g_svc.mu);
+    auto it = g_svc.handles.find(handle);
+    if (it == g_svc.handles.end() || it->second.freed) return fail(PIMUL_ENOTFOUND, "unknown handle");
+    producer = it->second.producer;
   }
-  cudaFreeAsync(h.d, g_svc.streams[0]);
-  g_svc.in_use -= h.bytes;
-  h.freed = true;
-  h.d = nullptr;
-  g_svc.handles.erase(handle);
+  if (producer >= 0) {
+    int rc = pimul_wait((uint64_t)producer, -1);
+    if (rc) return rc;
+  }
+  std::lock_guard<std::mutex> lk(g_svc.mu);
+  auto it = g_svc.handles.find(handle);
+  if (it == g_svc.handles.end()) return fail(PIMUL_ENOTFOUND, "handle freed concurrently");
+  *d = it->second.d;
+  *limbs = it->second.limbs;
   return PIMUL_OK;
 }
 
@@ -2809,7 +2905,7 @@ __global__ void __launch_bounds__(256) k_top_limb(const uint64_t* const* arrs, c
 
 // Batched add/subtract on `st` (asynchronous); *d_overflow (device int,
 // zeroed by the caller) is set when a carry or borrow leaves a top limb.
-static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st, int* d_overflow) {
+static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st, int* d_overflow, bool unchecked) {
   if (n == 0) return PIMUL_OK;
   uint64_t aux_total = 0, max_chunk = 0;
   for (size_t i = 0; i < n; i++) {
@@ -2827,7 +2923,7 @@ static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st
   uint64_t off = desc;
   for (size_t i = 0; i < n; i++) {
     h[i] = AsJob{jobs[i].x, jobs[i].y, jobs[i].out, jobs[i].nx, jobs[i].ny, jobs[i].nout, dev + off,
-                 (uint32_t)(jobs[i].sub != 0), (uint32_t)(jobs[i].sub != PIMUL_SUB_MOD)};
+                 (uint32_t)(jobs[i].sub != 0), (uint32_t)(!unchecked && jobs[i].sub != PIMUL_SUB_MOD)};
     off += as_aux_bytes(jobs[i].nout);
   }
   if (host_to_device(dev, h.data(), n * sizeof(AsJob), st)) e = cudaErrorUnknown;
@@ -2864,7 +2960,7 @@ int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
   CU(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
   bool all_mod = true;
   for (size_t i = 0; i < n && all_mod; i++) all_mod = jobs[i].sub == PIMUL_SUB_MOD;
-  rc = addsub_launch(jobs, n, st, d_flag);
+  rc = addsub_launch(jobs, n, st, d_flag, false);
   if (all_mod) {  // nothing to check: stay asynchronous
     cudaFreeAsync(d_flag, st);
     return rc;
@@ -2942,7 +3038,7 @@ int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream) {
   if (!rc) rc = run_units(units.data(), units.size(), st, true);
   if (!rc && !aj.empty()) {
     cudaError_t e = cudaMemsetAsync(tmp, 0, sizeof(int), st);
-    if (e == cudaSuccess) rc = addsub_launch(aj.data(), aj.size(), st, reinterpret_cast<int*>(tmp));
+    if (e == cudaSuccess) rc = addsub_launch(aj.data(), aj.size(), st, reinterpret_cast<int*>(tmp), false);
     else rc = fail(PIMUL_ECUDA, std::string("sum batch: ") + cudaGetErrorString(e));
   }
   if (tmp) cudaFreeAsync(tmp, st);
@@ -3118,6 +3214,15 @@ int pimul_mul(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64
 //    pimul_shutdown forgets the set-up, so a call after a cudaDeviceReset
 //    (made after pimul_shutdown) resolves the addresses and copies the
 //    tables again.
+namespace pimul {
+// The service's additions and subtractions: no carry or borrow can leave
+// their outputs (sums get max + 1 limbs, differences are of a >= b), so the
+// batch is launched unchecked and stays asynchronous.
+int svc_addsub(const pimul_addsub_job* jobs, size_t n, cudaStream_t st) {
+  return ::addsub_launch(jobs, n, st, nullptr, true);
+}
+}  // namespace pimul
+
 namespace pimul {
 constexpr int NOALLOC_LOG_MAX = 20;
 constexpr uint64_t NOALLOC_N_MAX = 1ull << NOALLOC_LOG_MAX;

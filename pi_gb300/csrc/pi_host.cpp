@@ -177,6 +177,8 @@ struct PiCtx {
   std::atomic<uint64_t> batch_levels{0};
   double bt[5] = {0, 0, 0, 0, 0};  // level-batched splitting: time per step (PIMUL_PI_TIMING)
   double leaf_ms = 0;
+  uint64_t serve_nodes = 0;  // > 0: the splitting tree above this many nodes goes through the multiply service
+  uint64_t served_requests = 0;
   PiCtx() {
     for (auto& h : ntt_hist) h.store(0);
   }
@@ -1719,7 +1721,92 @@ struct DevRoot {
   DLevel lvl;
   uint64_t top_limbs = 0;
   uint64_t q_off = 0, t_off = 0;
+  std::vector<uint64_t> svc_handles;  // the served tree's root handles (freed after the final assembly)
 };
+
+// ---------------------------------------------------- served splitting tree
+// The upper levels of the splitting tree driven through the multiply service
+// (pimul_submit) as the recursion unfolds, the way the reference's
+// recursion issues them (crates/pi-core/src/algorithm/chudnovsky.rs:377-413):
+// every node's |P|, Q, |T| is a handle, each merge is five chained requests
+// (P_L P_R, Q_L Q_R, |T_L| Q_R, |P_L| |T_R|, and their sum or difference
+// with the static signs of the level-batched form), and a node's handles are
+// released as soon as its parent's requests are queued.  Nothing returns to
+// the host between levels; the service batches whatever is ready.
+struct HNode {
+  uint64_t p = 0, q = 0, t = 0;
+  uint64_t terms = 0;
+};
+
+static int svc_req(int op, uint64_t a, uint64_t b, uint64_t* out) {
+  uint64_t tk = 0;
+  C().served_requests++;
+  return pimul_submit(op, a, b, out, &tk);
+}
+
+static int serve_tree(const std::vector<HNode>& v, size_t lo, size_t hi, bool need_p, HNode& out) {
+  if (hi - lo == 1) {
+    out = v[lo];
+    return PIMUL_OK;
+  }
+  const size_t m = (lo + hi) / 2;
+  HNode L, R;
+  int rc = serve_tree(v, lo, m, true, L);  // P_L enters T
+  if (!rc) rc = serve_tree(v, m, hi, need_p, R);
+  if (rc) return rc;
+  uint64_t t1 = 0, t2 = 0;
+  if (need_p) rc = svc_req(PIMUL_OP_MUL, L.p, R.p, &out.p);
+  if (!rc) rc = svc_req(PIMUL_OP_MUL, L.q, R.q, &out.q);
+  if (!rc) rc = svc_req(PIMUL_OP_MUL, L.t, R.q, &t1);
+  if (!rc) rc = svc_req(PIMUL_OP_MUL, L.p, R.t, &t2);
+  // |T| = |T_L| Q_R + (-1)^m_L |P_L| |T_R|  (P of m terms has sign (-1)^m, T < 0)
+  if (!rc) rc = svc_req((L.terms & 1) ? PIMUL_OP_SUB : PIMUL_OP_ADD, t1, t2, &out.t);
+  out.terms = L.terms + R.terms;
+  for (uint64_t h : {t1, t2, L.p, L.q, L.t, R.p, R.q, R.t})
+    if (h) pimul_release(h);
+  return rc;
+}
+
+// Runs the served tree over the nodes of `top` (device arrays the caller
+// keeps until the root is done) and puts the root's Q and |T| (trimmed) in
+// keep->lvl as one node; their handles go to keep->svc_handles.
+static int serve_root(const DLevel& top, cudaStream_t st, DevRoot* keep) {
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PIMUL_ECUDA;  // the service streams read the nodes
+  std::vector<HNode> v(top.nodes.size());
+  int rc = PIMUL_OK;
+  for (size_t i = 0; i < v.size() && !rc; i++) {
+    const DNode& n = top.nodes[i];
+    rc = pimul_adopt(n.p, n.pn, &v[i].p);
+    if (!rc) rc = pimul_adopt(n.q, n.qn, &v[i].q);
+    if (!rc) rc = pimul_adopt(n.t, n.tn, &v[i].t);
+    v[i].terms = n.terms;
+  }
+  HNode root;
+  if (!rc) rc = serve_tree(v, 0, v.size(), false, root);
+  if (rc) return rc;
+  const uint64_t* dq = nullptr;
+  const uint64_t* dt = nullptr;
+  size_t qn = 0, tn = 0;
+  rc = pimul_handle_device(root.q, &dq, &qn);
+  if (!rc) rc = pimul_handle_device(root.t, &dt, &tn);
+  keep->svc_handles = {root.q, root.t};
+  if (root.p) pimul_release(root.p);
+  if (rc) return rc;
+  const uint64_t* arrs[2] = {dq, dt};
+  const size_t lens[2] = {qn, tn};
+  size_t trimmed[2] = {0, 0};
+  rc = pimul_top_limbs(arrs, lens, 2, trimmed, st);
+  if (rc) return rc;
+  DNode r{};
+  r.q = const_cast<uint64_t*>(dq);
+  r.t = const_cast<uint64_t*>(dt);
+  r.qn = trimmed[0];
+  r.tn = trimmed[1];
+  r.terms = root.terms;
+  keep->lvl.nodes = {r};
+  keep->q_off = keep->t_off = 0;
+  return PIMUL_OK;
+}
 
 // Root merge from the operands' top m + 2 limbs (m = top_limbs + 2): the
 // cut parts move Q = Q_L Q_R and T = T_L Q_R +- P_L T_R by less than
@@ -1873,13 +1960,22 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
       nd.pn = lens[3 * i], nd.qn = lens[3 * i + 1], nd.tn = lens[3 * i + 2];
       nd.terms = terms;
     }
-    if (!rc) rc = dev_reduce(roots[sgi], st, true);
+    // served mode: each segment stops at its share of the nodes handed to the service
+    const size_t stop = C().serve_nodes && keep ? std::max<size_t>(1, C().serve_nodes / nseg) : 1;
+    if (!rc) rc = dev_reduce(roots[sgi], st, true, stop);
   }
   C().leaf_ms += tl;
   DLevel top;
   for (DLevel& r : roots) {
     for (const DNode& n : r.nodes) top.nodes.push_back(n);
     top.arenas.insert(top.arenas.end(), r.arenas.begin(), r.arenas.end());
+  }
+  if (keep && C().serve_nodes && !rc) {
+    rc = serve_root(top, st, keep);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    keep->lvl.arenas = std::move(top.arenas);  // the handed-over nodes: freed after the final assembly
+    return rc;
   }
   if (keep && keep->top_limbs && !rc) {
     rc = dev_reduce(top, st, true, 2);
@@ -2221,13 +2317,15 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
   };
   Int q, t;
   DevRoot droot;  // the root's Q and |T| when they stay on the device
-  struct ArenaGuard {  // returns the root's arenas when a backend error unwinds this call
-    DLevel& L;
+  struct ArenaGuard {  // returns the root's arenas and service handles when an error ends this call
+    DevRoot& R;
     ~ArenaGuard() {
-      for (uint64_t* ar : L.arenas) cudaFree(ar);
-      L.arenas.clear();
+      for (uint64_t h : R.svc_handles) pimul_free(h);
+      R.svc_handles.clear();
+      for (uint64_t* ar : R.lvl.arenas) cudaFree(ar);
+      R.lvl.arenas.clear();
     }
-  } arena_guard{droot.lvl};
+  } arena_guard{droot};
   droot.top_limbs = pidec::final_assembly_top_limbs(prec);
   int brc = PIMUL_OK;
   if (leaf_terms)
@@ -2252,6 +2350,8 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
     double fms[2] = {0, 0};
     int frc = pidec::final_assembly_device(r.q, r.qn, droot.q_off, r.t, r.tn, droot.t_off, CH_A, W.mant.data(),
                                            W.mant.size(), W.exp, prec, &d_ip, &ipn, fms);
+    for (uint64_t h : droot.svc_handles) pimul_free(h);
+    droot.svc_handles.clear();
     for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
     droot.lvl.arenas.clear();
     double t2 = now_ms();
@@ -2320,14 +2420,16 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
 
 static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backend, uint64_t ntt_threshold,
                       uint64_t leaf_terms, double* phase_ms, uint64_t* ntt_products, uint64_t* ntt_hist33,
-                      uint64_t* levels) {
+                      uint64_t* levels, uint64_t serve_nodes = 0, uint64_t* served_requests = nullptr) {
   if (digits == 0) return PIMUL_OK;
   if (!out || cap < digits) return PIMUL_EINVAL;
   PiCtx ctx;
   ctx.backend = reinterpret_cast<mul_fn>(backend);
   ctx.ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
+  ctx.serve_nodes = serve_nodes;
   int rc = with_ctx(ctx, [&] { return chudnovsky_body(digits, out, leaf_terms, phase_ms, ntt_products, ntt_hist33); });
   if (levels) *levels = ctx.batch_levels.load();
+  if (served_requests) *served_requests = ctx.served_requests;
   return rc;
 }
 
@@ -2367,4 +2469,11 @@ extern "C" int pimul_pi_chudnovsky_batched(uint64_t digits, char* out, size_t ca
                                            uint64_t* ntt_hist33) {
   return chudnovsky(digits, out, cap, nullptr, 0, leaf_terms ? leaf_terms : LEAF_AUTO, phase_ms, gpu_products,
                     ntt_hist33, levels);
+}
+
+// The splitting's upper levels through the multiply service (see pimul.h).
+extern "C" int pimul_pi_chudnovsky_served(uint64_t digits, char* out, size_t cap, uint64_t serve_nodes,
+                                          double* phase_ms, uint64_t* gpu_products, uint64_t* requests) {
+  return chudnovsky(digits, out, cap, nullptr, 0, LEAF_AUTO, phase_ms, gpu_products, nullptr, nullptr,
+                    serve_nodes ? serve_nodes : 512, requests);
 }

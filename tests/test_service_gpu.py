@@ -145,3 +145,68 @@ def test_free_waits_for_readers():
     assert np.array_equal(got, O.mul_mag_ntt(rand_limbs(1 << 18, 6), rand_limbs(1 << 18, 7)))
     pm.free(b)
     pm.free(h)
+
+
+def _int(x):
+    return O.limbs_to_int(x)
+
+
+def test_add_and_subtract_requests_chained():
+    # sums and differences as service requests, chained on products without
+    # a host round trip: s = a b + c, d = s - c (= a b), e = d - a b = 0,
+    # with operands of different stored lengths in both orders
+    cases = [(300, 200, 5), (5, 300, 200), (4000, 4000, 4001), (1, 1, 1), (70000, 3000, 65000)]
+    for la, lb, lc in cases:
+        a, b, c = rand_limbs(la, la + 1), rand_limbs(lb, lb + 2), rand_limbs(lc, lc + 3)
+        ha, hb, hc = pm.upload(a), pm.upload(b), pm.upload(c)
+        p, _ = pm.submit(ha, hb)
+        s, _ = pm.submit(p, hc, op=pm.OP_ADD)
+        d, _ = pm.submit(s, hc, op=pm.OP_SUB)
+        e, t = pm.submit(d, p, op=pm.OP_SUB)
+        pm.wait(t)
+        want = _int(a) * _int(b)
+        assert _int(pm.download(s)) == want + _int(c)
+        assert _int(pm.download(d)) == want
+        assert pm.download(e).size == 0
+        for h in (ha, hb, hc, p, s, d, e):
+            pm.free(h)
+
+
+def test_release_frees_after_readers_and_adopt_keeps_caller_memory():
+    import torch
+    a, b = rand_limbs(5000, 11), rand_limbs(7000, 12)
+    ta = torch.from_numpy(a.view(np.int64)).cuda()
+    torch.cuda.synchronize()
+    ha = pm.adopt(ta.data_ptr(), a.size)
+    hb = pm.upload(b)
+    p, _ = pm.submit(ha, hb)
+    q, t = pm.submit(p, ha)  # reads p and the adopted a
+    pm.release(p)            # freed once q has read it
+    pm.release(ha)           # the adopted memory stays the caller's
+    pm.wait(t)
+    assert _int(pm.download(q)) == _int(a) * _int(b) * _int(a)
+    dq, nq = pm.handle_device(q)
+    assert dq != 0 and nq == 2 * a.size + b.size
+    assert np.array_equal(ta.cpu().numpy().view(np.uint64), a)
+    with pytest.raises(pm.PimulError):
+        pm.download(p)       # released and freed
+    pm.free(q)
+    pm.free(hb)
+
+
+def test_served_chudnovsky_matches_golden():
+    import hashlib
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    for d, nodes in ((1000, 0), (100_000, 0), (100_000, 7), (100_000, 4096)):
+        s, info = pm.pi_chudnovsky_served(d, nodes)
+        assert s == ref[:d], (d, nodes)
+    assert info["service_requests"] > 0
+    with open(os.path.join(here, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000"]
+    s, info = pm.pi_chudnovsky_served(1_000_000)
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]
+    assert info["service_requests"] >= 5 * 100
