@@ -30,6 +30,7 @@
 #include "../../include/pimul.h"
 #include "agm.h"
 #include "dec.h"
+#include "hostcopy.h"
 
 namespace piagm {
 namespace {
@@ -45,6 +46,16 @@ __global__ void k_shift(const uint64_t* __restrict__ src, uint64_t src_len, int6
     const uint64_t lo = i >= 0 && (uint64_t)i < src_len ? src[i] : 0;
     const uint64_t hi = i + 1 >= 0 && (uint64_t)(i + 1) < src_len ? src[i + 1] : 0;
     dst[j] = bs ? (lo >> bs) | (hi << (64 - bs)) : lo;
+  }
+}
+
+// lo[i] = low word of x[i] c, hi[i] = high word of x[i - 1] c, for
+// i in [0, n] (lo[n] = hi[0] = 0): x c = lo + hi.
+__global__ void k_mul_word_split(const uint64_t* __restrict__ x, uint64_t n, uint64_t c, uint64_t* __restrict__ lo,
+                                 uint64_t* __restrict__ hi) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x) {
+    lo[i] = i < n ? x[i] * c : 0;
+    hi[i] = i > 0 ? __umul64hi(x[i - 1], c) : 0;
   }
 }
 
@@ -85,6 +96,17 @@ struct Agm {
     const unsigned blocks = (unsigned)std::min<size_t>((dst_len + 255) / 256, 1u << 16);
     k_shift<<<std::max(1u, blocks), 256, 0, st>>>(src, src_len, sh, dst, dst_len);
     cu(cudaGetLastError());
+  }
+  // z[0..n+1) = x[0..n) c for a one-word c (lo, hi: n + 1 limbs of
+  // scratch; z may not alias x), asynchronous
+  void mul_word(const uint64_t* x, size_t n, uint64_t c, uint64_t* z, uint64_t* lo, uint64_t* hi) {
+    if (rc) return;
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 256) / 256, 1u << 16);
+    k_mul_word_split<<<std::max(1u, blocks), 256, 0, st>>>(x, n, c, lo, hi);
+    cu(cudaGetLastError());
+    if (rc) return;
+    pimul_addsub_job j{lo, n + 1, hi, n + 1, z, n + 1, 0};  // x c < 2^(64 (n + 1)): no carry out
+    rc = pimul::svc_addsub(&j, 1, st);
   }
   // z = x + y or x - y (x >= y; sub = PIMUL_SUB_MOD: modulo, asynchronous)
   // over W limbs (in place allowed)
@@ -265,6 +287,142 @@ int agm_device(uint64_t prec, AgmOut* out, double* ms) {
     return G.rc;
   }
   *out = AgmOut{num, 2 * W, -128 * (int64_t)nf, den, W, -64 * (int64_t)nf};
+  if (ms) ms[0] = now_ms() - t0;
+  return PIMUL_OK;
+}
+
+namespace {
+
+// 5^e into a cudaMalloc'd buffer: r = 5, then for each bit of e below the
+// top one r = r^2 (and r = 5 r when the bit is set), each product exact and
+// trimmed to its length (read back: a few dozen steps).
+int pow5(Agm& G, uint64_t e, DevNum* out) {
+  const size_t cap = (size_t)((double)e * 2.321928094887362 / 64.0) + 4;  // limbs of 5^e, plus room
+  uint64_t* A = G.alloc(cap);
+  uint64_t* B = G.alloc(cap);
+  uint64_t* lo = G.alloc(cap);
+  uint64_t* hi = G.alloc(cap);
+  if (G.rc) return G.rc;
+  const uint64_t start = e ? 5 : 1;
+  G.cu(cudaMemcpyAsync(A, &start, 8, cudaMemcpyHostToDevice, G.st));
+  G.cu(cudaStreamSynchronize(G.st));  // start is a local
+  size_t L = 1;
+  const int nb = e ? 64 - __builtin_clzll(e) : 0;
+  for (int i = nb - 2; i >= 0 && !G.rc; i--) {
+    if (2 * L + 1 > cap) return G.rc = PIMUL_EINVAL;  // not reached: cap bounds 5^e with room
+    G.rc = pimul_mul_device(A, L, A, L, B, G.st);  // a square (same operand)
+    size_t L2 = 2 * L;
+    if ((e >> i) & 1) {
+      G.mul_word(B, L2, 5, A, lo, hi);
+      L2++;
+    } else {
+      std::swap(A, B);
+    }
+    L = G.trimmed(A, L2);
+  }
+  if (G.rc) return G.rc;
+  uint64_t* m = nullptr;
+  if (cudaMalloc((void**)&m, L * 8) != cudaSuccess) {
+    cudaGetLastError();
+    return G.rc = PIMUL_ENOMEM;
+  }
+  G.cu(cudaMemcpyAsync(m, A, L * 8, cudaMemcpyDeviceToDevice, G.st));
+  G.cu(cudaStreamSynchronize(G.st));
+  if (G.rc) {
+    cudaFree(m);
+    return G.rc;
+  }
+  *out = DevNum{m, L, 0};
+  return PIMUL_OK;
+}
+
+}  // namespace
+
+int pow5_device(uint64_t e, DevNum* out) {
+  if (!out) return PIMUL_EINVAL;
+  *out = DevNum{};
+  Agm G;
+  if (cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  return pow5(G, e, out);
+}
+
+// sqrt(10005) = 2^7 sqrt(x) with x = 10005 / 2^14 in (1/2, 1); y ~ 1/sqrt(x)
+// in fixed point (nf fraction limbs below one integer limb) by
+// y' = y (3 - x y^2) / 2 at the planned precisions (x y^2 is a one-word
+// multiplication and a shift, not a product), three steps at three limbs
+// from an f64 start first.  From y = (1 + e)/sqrt(x) a step gives
+// (1 - 3e^2/2 - e^3/2)/sqrt(x), and the truncations cost a few units of the
+// step's last limb, so a step at m limbs from an input right to m' limbs,
+// 2 m' >= m + 2, leaves y right to 64 m - 4 bits.  Then
+// W = 426880 sqrt(10005) 5^(D-1) 2^(D-1) = (426880 * 10005 y) 5^(D-1) 2^(D-8).
+int chudnovsky_w_device(uint64_t digits, uint64_t prec, DevNum* out, double* ms) {
+  if (!out || !digits || prec < 64) return PIMUL_EINVAL;
+  *out = DevNum{};
+  const double t0 = now_ms();
+  Agm G;
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&G.st, cudaStreamNonBlocking, prio_hi) != cudaSuccess) return PIMUL_ECUDA;
+  G.nf = (prec + 128 + 63) / 64 + 1;
+  G.W = G.nf + 1;
+  const size_t nf = G.nf, W = G.W;
+  constexpr uint64_t N = 10005, SH = 14, C2 = 426880ull * 10005ull;
+  uint64_t* y = G.alloc(W);
+  uint64_t* u = G.alloc(W);
+  uint64_t* v = G.alloc(W);
+  uint64_t* d = G.alloc(W);
+  uint64_t* three = G.alloc(W);
+  uint64_t* s = G.alloc(W + 2);
+  uint64_t* lo = G.alloc(W + 2);
+  uint64_t* hi = G.alloc(W + 2);
+  uint64_t* tmp = G.alloc(2 * W + 2);
+  if (G.rc) return G.rc;
+  const uint64_t h_three = 3;
+  const double frac = std::ldexp(1.0, (int)(SH / 2)) / std::sqrt((double)N) - 1.0;  // 1/sqrt(x) - 1
+  const uint64_t h_y[2] = {(uint64_t)std::ldexp(frac, 64), 1};
+  G.cu(cudaMemcpyAsync(three + nf, &h_three, 8, cudaMemcpyHostToDevice, G.st));
+  G.cu(cudaMemcpyAsync(y + nf - 1, h_y, 16, cudaMemcpyHostToDevice, G.st));
+  G.cu(cudaStreamSynchronize(G.st));  // host constants are locals
+  auto step = [&](size_t m) {
+    const size_t off = nf - m;
+    G.mul(y, y, u, m, tmp);                      // y^2
+    G.mul_word(u + off, m + 1, N, s, lo, hi);    // y^2 N (m + 2 limbs)
+    G.shift(s, m + 2, (int64_t)SH, v + off, m + 1);  // x y^2
+    G.addsub(three, v, d, PIMUL_SUB_MOD);        // 3 - x y^2 > 0
+    G.mul(y, d, u, m, tmp);
+    G.shift(u, W, 1, y, W);
+  };
+  std::vector<size_t> plan{nf};
+  // m -> (m + 1) / 2 + 1 decreases strictly above 3
+  while (plan.back() > 3) plan.push_back((plan.back() + 1) / 2 + 1);
+  std::reverse(plan.begin(), plan.end());
+  for (int k = 0; k < 3; k++) step(std::min<size_t>(3, nf));
+  for (size_t m : plan)
+    if (m > 3) step(m);
+  // 426880 * 10005 y (W + 1 limbs, nf fraction limbs), then times 5^(D-1)
+  G.mul_word(y, W, C2, s, lo, hi);
+  DevNum p5;
+  if (!G.rc) G.rc = pow5(G, digits - 1, &p5);
+  if (G.rc) {
+    if (p5.mant) cudaFree(p5.mant);
+    return G.rc;
+  }
+  const size_t full = W + 1 + p5.limbs, keep = std::min(full, nf + 2);
+  uint64_t* prod = G.alloc(full);
+  if (!G.rc) G.rc = pimul_mul_device(s, W + 1, p5.mant, p5.limbs, prod, G.st);
+  uint64_t* m = nullptr;
+  if (!G.rc && cudaMalloc((void**)&m, keep * 8) != cudaSuccess) {
+    cudaGetLastError();
+    G.rc = PIMUL_ENOMEM;
+  }
+  if (m) G.cu(cudaMemcpyAsync(m, prod + (full - keep), keep * 8, cudaMemcpyDeviceToDevice, G.st));
+  G.cu(cudaStreamSynchronize(G.st));
+  cudaFree(p5.mant);
+  if (G.rc) {
+    if (m) cudaFree(m);
+    return G.rc;
+  }
+  *out = DevNum{m, keep, (int64_t)digits - 8 - 64 * (int64_t)nf + 64 * (int64_t)(full - keep)};
   if (ms) ms[0] = now_ms() - t0;
   return PIMUL_OK;
 }

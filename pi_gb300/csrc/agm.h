@@ -21,4 +21,23 @@ struct AgmOut {
 // (a + b)^2 and t after ceil(log2 prec) + 2 steps.  ms (optional): time.
 int agm_device(uint64_t prec, AgmOut* out, double* ms);
 
+// A number in device memory: mant[0..limbs) 2^exp (cudaMalloc; the caller
+// frees mant with cudaFree).
+struct DevNum {
+  uint64_t* mant = nullptr;
+  size_t limbs = 0;
+  int64_t exp = 0;
+};
+
+// 5^e exactly (exp = 0), by left-to-right binary powering on the device.
+int pow5_device(uint64_t e, DevNum* out);
+
+// Chudnovsky's constant times the decimal scale, W = 426880 sqrt(10005)
+// 10^(D-1) (chudnovsky.rs:118-126 and util.rs:25-83), on the device with a
+// relative error below 2^-(prec + 128): sqrt(10005) from Newton's iteration
+// for an inverse square root, 10^(D-1) = 5^(D-1) 2^(D-1) with 5^(D-1)
+// exact.  The stream has the device's highest priority.  ms (optional):
+// time.
+int chudnovsky_w_device(uint64_t digits, uint64_t prec, DevNum* out, double* ms);
+
 }  // namespace piagm

@@ -245,8 +245,8 @@ struct Arena {
 
 }  // namespace
 
-int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, const Level* lv, char* out, size_t want,
-                      double* ms) {
+int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, const Level* lv, bool lv_on_device,
+                      char* out, size_t want, double* ms) {
   if (!x || !nx || !lv || !out || K <= LEAF_K || K > 40) return PIMUL_EINVAL;
   if (lv[LEAF_K].lp + 1 != (size_t)LEAF_W) return PIMUL_EINVAL;
   const size_t total = (size_t)19 << K;
@@ -261,8 +261,9 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
     if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
     return rc == PIMUL_OK;
   };
-  // divisors and reciprocals, one buffer
+  // divisors and reciprocals: in place on the device, or uploaded into one buffer
   std::vector<size_t> poff(K), voff(K);
+  std::vector<const uint64_t*> dPk(K, nullptr), dVk(K, nullptr);
   size_t pv = 0;
   for (int k = LEAF_K; k < K; k++) {
     if (!lv[k].P || !lv[k].V || !lv[k].lp || !lv[k].lv) return PIMUL_EINVAL;
@@ -272,10 +273,17 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
   uint64_t* dpv = nullptr;
   uint64_t* cur = nullptr;
   uint64_t* one = nullptr;
-  if ((rc = A.get(&dpv, pv)) || (rc = A.get(&cur, nx)) || (rc = A.get(&one, 1))) return rc;
+  if ((!lv_on_device && (rc = A.get(&dpv, pv))) || (rc = A.get(&cur, nx)) || (rc = A.get(&one, 1))) return rc;
   for (int k = LEAF_K; k < K && !rc; k++) {
+    if (lv_on_device) {
+      dPk[k] = lv[k].P;
+      dVk[k] = lv[k].V;
+      continue;
+    }
     rc = pimul::host_to_device(dpv + poff[k], lv[k].P, lv[k].lp * 8, st);
     if (!rc) rc = pimul::host_to_device(dpv + voff[k], lv[k].V, lv[k].lv * 8, st);
+    dPk[k] = dpv + poff[k];
+    dVk[k] = dpv + voff[k];
   }
   if (!rc && x_on_device) cu(cudaMemcpyAsync(cur, x, nx * 8, cudaMemcpyDeviceToDevice, st));
   if (!rc && !x_on_device) rc = pimul::host_to_device(cur, x, nx * 8, st);
@@ -290,8 +298,8 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
   std::vector<uint8_t> hflag;
   for (int k = K - 1; k >= LEAF_K && !rc; k--) {
     const Level& L = lv[k];
-    const uint64_t* dP = dpv + poff[k];
-    const uint64_t* dV = dpv + voff[k];
+    const uint64_t* dP = dPk[k];
+    const uint64_t* dV = dVk[k];
     // t low limbs of x left out of the quotient estimate (x_hi keeps one)
     const size_t t = std::min(L.lp >= 3 ? L.lp - 2 : 0, w_in - 1);
     const size_t w = L.lp + 1, hi_w = w_in - t, prod_w = hi_w + L.lv, qp_w = w + L.lp;
@@ -434,84 +442,23 @@ std::vector<uint64_t> host_recip_pow2(const std::vector<uint64_t>& d, size_t s) 
 
 }  // namespace
 
-static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
-                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip,
-                         size_t* ipn, double* ms, double t0);
-
-int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const uint64_t* dT, size_t tn,
-                          uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec,
-                          uint64_t** d_ip, size_t* ipn, double* ms) {
-  if (!dQ || !qn || (tn && !dT) || !wm || !wl || !d_ip || !ipn || !A) return PIMUL_EINVAL;
-  *d_ip = nullptr;
-  *ipn = 0;
-  const double t0 = now_ms();
-  Arena Ar;
-  if (cudaStreamCreateWithFlags(&Ar.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+// Y ~ 2^(128 nl) / dn for dn = dnorm[0..nl) (device, top bit set, nl >= 3):
+// Newton's iteration with precision doubling from Y_(64 m0) found on the
+// host from the top limbs of dn; each step h -> c = 2h - 64 bits computes
+// E = 2^(h+c) - D_c Y_h from the low limbs of one product and
+// Y_c = Y_h 2^(c-h) + floor(Y_h E / 2^(2h)) - 4, so Y stays an underestimate
+// and lands within 4 units.  *Yout (nl + 1 limbs) comes from Ar.
+static int recip_newton(Arena& Ar, const uint64_t* dnorm, size_t nl, uint64_t** Yout) {
   const cudaStream_t st = Ar.st;
   int rc = PIMUL_OK;
   auto cu = [&](cudaError_t e) {
     if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
     return rc == PIMUL_OK;
   };
-  const size_t nl = (prec + 192 + 63) / 64;
-  // den window: limbs [s0, qt + 1) of A Q - |T| (qt = Q's length with its
-  // offset; carries from below s0 are dropped: a relative error below
-  // 2^-(64 nl)); the stored parts of Q and |T| must reach down to s0
-  const size_t qt = qn + q_off, tt = tn + t_off;
-  const size_t dn = qt + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
-  if (tt > dn || s0 < q_off || (tt > s0 && s0 < t_off) || qn < std::min(qt, nl)) return PIMUL_EINVAL;
-  uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr;
-  if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn))) return rc;
-  k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(
-      dQ + (s0 - q_off), qt - s0, A, lo, hi);
-  if (!cu(cudaGetLastError())) return rc;
-  pimul_addsub_job j1{lo, wn, hi, wn, den, wn, 0};
-  if ((rc = pimul_addsub_batch(&j1, 1, st))) return rc;
-  if (tt > s0) {
-    pimul_addsub_job j2{den, wn, dT + (s0 - t_off), tt - s0, den, wn, 1};
-    if ((rc = pimul_addsub_batch(&j2, 1, st))) return rc;
-  }
-  Ar.put(lo);
-  Ar.put(hi);
-  // W Q / den with Q's top lq = min(qt, nl) limbs
-  const size_t lq = std::min(qt, nl);
-  return quotient_tail(Ar, den, wn, 64 * (int64_t)s0, dQ + (qn - lq), lq, 64 * (int64_t)(qt - lq), wm, wl, we, prec,
-                       d_ip, ipn, ms, t0);
-}
-
-// floor(W N / D): D = den[0..wn) 2^den_exp on the device, N = n_top[0..lq)
-// 2^n_exp (lq <= nl, its top limbs), W = wm 2^we on the host.  D's top
-// 64 nl bits are normalised, R ~ 2^(128 nl) / D comes from Newton's
-// iteration (precision doubling from 576 bits found on the host), and the
-// quotient is floor(W (N_top R >> 64 lq) 2^e).
-static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
-                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip,
-                         size_t* ipn, double* ms, double t0) {
-  const cudaStream_t st = Ar.st;
-  int rc = PIMUL_OK;
-  auto cu = [&](cudaError_t e) {
-    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
-    return rc == PIMUL_OK;
-  };
-  const size_t nl = (prec + 192 + 63) / 64;
-  if (!den || !wn || !n_top || !lq || lq > nl || !wm || !wl || !d_ip || !ipn) return PIMUL_EINVAL;
-  uint64_t *dnorm = nullptr, *consts = nullptr;
-  if ((rc = Ar.get(&dnorm, nl)) || (rc = Ar.get(&consts, 1))) return rc;
-  // bit length of the window, then dn = its top 64 nl bits
-  uint64_t top[3] = {0, 0, 0};
-  const size_t nt = std::min<size_t>(3, wn);
-  cu(cudaMemcpyAsync(top, den + (wn - nt), nt * 8, cudaMemcpyDeviceToHost, st));
-  cu(cudaStreamSynchronize(st));
-  if (rc) return rc;
-  int64_t B = 0;
-  for (size_t i = nt; i-- > 0 && !B;)
-    if (top[i]) B = 64 * (int64_t)(wn - nt + i) + 64 - __builtin_clzll(top[i]);
-  if (B <= 64 * (int64_t)(wn - nt)) return PIMUL_EINVAL;  // the divisor vanishes in its top limbs
-  const int64_t shn = B - 64 * (int64_t)nl;
-  k_shr_slots<<<slot_grid(nl, 1), 256, 0, st>>>(den, 0, wn, shn, dnorm, 0, nl, 1);
-  if (!cu(cudaGetLastError())) return rc;
-  const int64_t ed = den_exp + shn;  // D ~ dn 2^ed
-  // Newton: Y_(64 m0) from the top limbs of dn on the host
+  *Yout = nullptr;
+  if (nl < 3) return PIMUL_EINVAL;
+  uint64_t* consts = nullptr;
+  if ((rc = Ar.get(&consts, 1))) return rc;
   const size_t m0 = std::min<size_t>(8, nl - 2), k0 = m0 + 2;
   std::vector<uint64_t> dtop(k0);
   cu(cudaMemcpyAsync(dtop.data(), dnorm + (nl - k0), k0 * 8, cudaMemcpyDeviceToHost, st));
@@ -554,16 +501,105 @@ static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_
     Y = Yn;
     m = mp;
   }
+  Ar.put(consts);
   if (rc) return rc;
+  *Yout = Y;
+  return PIMUL_OK;
+}
+
+static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
+                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, bool w_dev, uint64_t prec,
+                         uint64_t** d_ip, size_t* ipn, double* ms, double t0);
+
+int final_assembly_device(const uint64_t* dQ, size_t qn, uint64_t q_off, const uint64_t* dT, size_t tn,
+                          uint64_t t_off, uint64_t A, const uint64_t* wm, size_t wl, int64_t we, bool w_dev,
+                          uint64_t prec, uint64_t** d_ip, size_t* ipn, double* ms) {
+  if (!dQ || !qn || (tn && !dT) || !wm || !wl || !d_ip || !ipn || !A) return PIMUL_EINVAL;
+  *d_ip = nullptr;
+  *ipn = 0;
+  const double t0 = now_ms();
+  Arena Ar;
+  if (cudaStreamCreateWithFlags(&Ar.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
+  const cudaStream_t st = Ar.st;
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
+    return rc == PIMUL_OK;
+  };
+  const size_t nl = (prec + 192 + 63) / 64;
+  // den window: limbs [s0, qt + 1) of A Q - |T| (qt = Q's length with its
+  // offset; carries from below s0 are dropped: a relative error below
+  // 2^-(64 nl)); the stored parts of Q and |T| must reach down to s0
+  const size_t qt = qn + q_off, tt = tn + t_off;
+  const size_t dn = qt + 1, s0 = dn > nl + 2 ? dn - (nl + 2) : 0, wn = dn - s0;
+  if (tt > dn || s0 < q_off || (tt > s0 && s0 < t_off) || qn < std::min(qt, nl)) return PIMUL_EINVAL;
+  uint64_t *lo = nullptr, *hi = nullptr, *den = nullptr;
+  if ((rc = Ar.get(&lo, wn)) || (rc = Ar.get(&hi, wn)) || (rc = Ar.get(&den, wn))) return rc;
+  k_mul_small_split<<<(unsigned)std::min<uint64_t>((wn + 255) / 256, 1u << 20), 256, 0, st>>>(
+      dQ + (s0 - q_off), qt - s0, A, lo, hi);
+  if (!cu(cudaGetLastError())) return rc;
+  pimul_addsub_job j1{lo, wn, hi, wn, den, wn, 0};
+  if ((rc = pimul_addsub_batch(&j1, 1, st))) return rc;
+  if (tt > s0) {
+    pimul_addsub_job j2{den, wn, dT + (s0 - t_off), tt - s0, den, wn, 1};
+    if ((rc = pimul_addsub_batch(&j2, 1, st))) return rc;
+  }
+  Ar.put(lo);
+  Ar.put(hi);
+  // W Q / den with Q's top lq = min(qt, nl) limbs
+  const size_t lq = std::min(qt, nl);
+  return quotient_tail(Ar, den, wn, 64 * (int64_t)s0, dQ + (qn - lq), lq, 64 * (int64_t)(qt - lq), wm, wl, we, w_dev,
+                       prec, d_ip, ipn, ms, t0);
+}
+
+// floor(W N / D): D = den[0..wn) 2^den_exp on the device, N = n_top[0..lq)
+// 2^n_exp (lq <= nl, its top limbs), W = wm 2^we on the host (in device
+// memory when w_dev).  D's top
+// 64 nl bits are normalised, R ~ 2^(128 nl) / D comes from Newton's
+// iteration (precision doubling from 576 bits found on the host), and the
+// quotient is floor(W (N_top R >> 64 lq) 2^e).
+static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq,
+                         int64_t n_exp, const uint64_t* wm, size_t wl, int64_t we, bool w_dev, uint64_t prec,
+                         uint64_t** d_ip, size_t* ipn, double* ms, double t0) {
+  const cudaStream_t st = Ar.st;
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
+    return rc == PIMUL_OK;
+  };
+  const size_t nl = (prec + 192 + 63) / 64;
+  if (!den || !wn || !n_top || !lq || lq > nl || !wm || !wl || !d_ip || !ipn) return PIMUL_EINVAL;
+  uint64_t* dnorm = nullptr;
+  if ((rc = Ar.get(&dnorm, nl))) return rc;
+  // bit length of the window, then dn = its top 64 nl bits
+  uint64_t top[3] = {0, 0, 0};
+  const size_t nt = std::min<size_t>(3, wn);
+  cu(cudaMemcpyAsync(top, den + (wn - nt), nt * 8, cudaMemcpyDeviceToHost, st));
+  cu(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  int64_t B = 0;
+  for (size_t i = nt; i-- > 0 && !B;)
+    if (top[i]) B = 64 * (int64_t)(wn - nt + i) + 64 - __builtin_clzll(top[i]);
+  if (B <= 64 * (int64_t)(wn - nt)) return PIMUL_EINVAL;  // the divisor vanishes in its top limbs
+  const int64_t shn = B - 64 * (int64_t)nl;
+  k_shr_slots<<<slot_grid(nl, 1), 256, 0, st>>>(den, 0, wn, shn, dnorm, 0, nl, 1);
+  if (!cu(cudaGetLastError())) return rc;
+  const int64_t ed = den_exp + shn;  // D ~ dn 2^ed
+  uint64_t* Y = nullptr;
+  if ((rc = recip_newton(Ar, dnorm, nl, &Y))) return rc;
   const double t1 = now_ms();
   // ip = floor(W N_top R 2^e2)
   uint64_t *X1 = nullptr, *X2 = nullptr, *dW = nullptr;
   if ((rc = Ar.get(&X1, lq + nl + 1))) return rc;
   if ((rc = pimul_mul_device(n_top, lq, Y, nl + 1, X1, st))) return rc;
   Ar.put(Y);
-  if ((rc = Ar.get(&dW, wl)) || (rc = Ar.get(&X2, wl + nl + 1))) return rc;
-  if ((rc = pimul::host_to_device(dW, wm, wl * 8, st))) return rc;
-  if ((rc = pimul_mul_device(dW, wl, X1 + lq, nl + 1, X2, st))) return rc;
+  const uint64_t* Wd = wm;
+  if (!w_dev) {
+    if ((rc = Ar.get(&dW, wl)) || (rc = pimul::host_to_device(dW, wm, wl * 8, st))) return rc;
+    Wd = dW;
+  }
+  if ((rc = Ar.get(&X2, wl + nl + 1))) return rc;
+  if ((rc = pimul_mul_device(Wd, wl, X1 + lq, nl + 1, X2, st))) return rc;
   // W N / D ~ X2 2^(64 lq) * 2^(we + n_exp - 128 nl - ed)
   const int64_t e2 = we + 64 * (int64_t)lq + n_exp - 128 * (int64_t)nl - ed;
   const int64_t ip_bits = 64 * (int64_t)(wl + nl + 1) + e2;
@@ -605,14 +641,125 @@ static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_
 }
 
 int quotient_device(const uint64_t* den, size_t wn, int64_t den_exp, const uint64_t* n_top, size_t lq, int64_t n_exp,
-                    const uint64_t* wm, size_t wl, int64_t we, uint64_t prec, uint64_t** d_ip, size_t* ipn,
-                    double* ms) {
+                    const uint64_t* wm, size_t wl, int64_t we, bool w_dev, uint64_t prec, uint64_t** d_ip,
+                    size_t* ipn, double* ms) {
   if (!d_ip || !ipn) return PIMUL_EINVAL;
   *d_ip = nullptr;
   *ipn = 0;
   Arena Ar;
   if (cudaStreamCreateWithFlags(&Ar.st, cudaStreamNonBlocking) != cudaSuccess) return PIMUL_ECUDA;
-  return quotient_tail(Ar, den, wn, den_exp, n_top, lq, n_exp, wm, wl, we, prec, d_ip, ipn, ms, now_ms());
+  return quotient_tail(Ar, den, wn, den_exp, n_top, lq, n_exp, wm, wl, we, w_dev, prec, d_ip, ipn, ms, now_ms());
+}
+
+void free_levels_device(DevLevels* L) {
+  if (!L) return;
+  for (uint64_t* p : L->bufs) cudaFree(p);
+  L->bufs.clear();
+  L->lv.clear();
+  L->K = 0;
+}
+
+// P_0 = 10^19, P_k = P_(k-1)^2 (exact; the length and bit count of each read
+// back from its top two limbs), s_k = 2 bits(P_k) + 64.  At the top level
+// T = K - 1, with nl = |P_T| + 1 limbs and dn = P_T 2^(64 nl - bits(P_T)),
+// Newton's Y ~ 2^(128 nl) / dn (an underestimate within 4 units) gives
+// V_T = Y >> (64 |P_T| - bits(P_T)) <= floor(2^(s_T) / P_T); below it
+// V_(k-1) = (P_(k-1) V_k) >> (s_k - s_(k-1)), also an underestimate
+// (P_k = P_(k-1)^2) within a few units.  A quotient estimate
+// floor(x V_k / 2^(s_k)) for x < P_k^2 then falls short of x div P_k by
+// less than one plus a few times 2^-64, which the conversion's correction
+// rounds take.
+int build_levels_device(int K, DevLevels* out, double* ms) {
+  if (!out || K <= LEAF_K || K > 40) return PIMUL_EINVAL;
+  free_levels_device(out);
+  const double t0 = now_ms();
+  Arena A;
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&A.st, cudaStreamNonBlocking, prio_hi) != cudaSuccess) return PIMUL_ECUDA;
+  const cudaStream_t st = A.st;
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = e == cudaErrorMemoryAllocation ? PIMUL_ENOMEM : PIMUL_ECUDA;
+    return rc == PIMUL_OK;
+  };
+  auto keep = [&](uint64_t** p, size_t limbs) {
+    *p = nullptr;
+    if (rc) return;
+    if (cudaMalloc((void**)p, std::max<size_t>(limbs, 1) * 8) != cudaSuccess) {
+      cudaGetLastError();
+      rc = PIMUL_ENOMEM;
+      return;
+    }
+    out->bufs.push_back(*p);
+  };
+  auto trimmed = [&](const uint64_t* x, size_t n) -> size_t {
+    size_t len = 0;
+    if (rc) return 0;
+    const uint64_t* arr[1] = {x};
+    size_t lens[1] = {n};
+    rc = pimul_top_limbs(arr, lens, 1, &len, st);
+    return len;
+  };
+  std::vector<uint64_t*> P(K, nullptr), V(K, nullptr);
+  std::vector<size_t> lp(K, 0), lv(K, 0);
+  std::vector<uint64_t> bits(K, 0), sh(K, 0);
+  keep(&P[0], 1);
+  const uint64_t chunk = CHUNK;
+  if (!rc) cu(cudaMemcpyAsync(P[0], &chunk, 8, cudaMemcpyHostToDevice, st));
+  lp[0] = 1;
+  bits[0] = 64;
+  for (int k = 1; k < K && !rc; k++) {
+    keep(&P[k], 2 * lp[k - 1]);
+    if (rc) break;
+    rc = pimul_mul_device(P[k - 1], lp[k - 1], P[k - 1], lp[k - 1], P[k], st);  // a square
+    uint64_t top2[2] = {0, 0};
+    if (!rc) cu(cudaMemcpyAsync(top2, P[k] + 2 * lp[k - 1] - 2, 16, cudaMemcpyDeviceToHost, st));
+    cu(cudaStreamSynchronize(st));
+    if (rc) break;
+    lp[k] = top2[1] ? 2 * lp[k - 1] : 2 * lp[k - 1] - 1;
+    const uint64_t tw = top2[1] ? top2[1] : top2[0];
+    bits[k] = 64 * (lp[k] - 1) + 64 - __builtin_clzll(tw);
+  }
+  for (int k = 0; k < K; k++) sh[k] = 2 * bits[k] + 64;
+  if (rc) return rc;
+  // the top level's reciprocal
+  const int T = K - 1;
+  const size_t nl = lp[T] + 1;
+  uint64_t* dnorm = nullptr;
+  if ((rc = A.get(&dnorm, nl))) return rc;
+  k_shr_slots<<<slot_grid(nl, 1), 256, 0, st>>>(P[T], 0, lp[T], -(int64_t)(64 * nl - bits[T]), dnorm, 0, nl, 1);
+  if (!cu(cudaGetLastError())) return rc;
+  uint64_t* Y = nullptr;
+  if ((rc = recip_newton(A, dnorm, nl, &Y))) return rc;
+  keep(&V[T], nl + 1);
+  if (rc) return rc;
+  k_shr_slots<<<slot_grid(nl + 1, 1), 256, 0, st>>>(Y, 0, nl + 1, (int64_t)(64 * lp[T] - bits[T]), V[T], 0, nl + 1, 1);
+  if (!cu(cudaGetLastError())) return rc;
+  lv[T] = trimmed(V[T], nl + 1);
+  A.put(Y);
+  A.put(dnorm);
+  for (int k = T - 1; k >= LEAF_K && !rc; k--) {
+    const size_t pw = lp[k] + lv[k + 1];
+    const uint64_t d = sh[k + 1] - sh[k];
+    const size_t vw = pw - d / 64;
+    uint64_t* prod = nullptr;
+    if ((rc = A.get(&prod, pw))) break;
+    if ((rc = pimul_mul_device(P[k], lp[k], V[k + 1], lv[k + 1], prod, st))) break;
+    keep(&V[k], vw);
+    if (rc) break;
+    k_shr_slots<<<slot_grid(vw, 1), 256, 0, st>>>(prod, 0, pw, (int64_t)d, V[k], 0, vw, 1);
+    if (!cu(cudaGetLastError())) break;
+    lv[k] = trimmed(V[k], vw);
+    A.put(prod);
+  }
+  cu(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  out->K = K;
+  out->lv.assign(K, Level{nullptr, 0, nullptr, 0, 0});
+  for (int k = LEAF_K; k < K; k++) out->lv[k] = Level{P[k], lp[k], V[k], lv[k], sh[k]};
+  if (ms) ms[0] = now_ms() - t0;
+  return PIMUL_OK;
 }
 
 }  // namespace pidec

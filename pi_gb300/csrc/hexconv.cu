@@ -334,7 +334,7 @@ extern "C" int pimul_decimal_to_hex(const char* text, size_t len, char* out, siz
   const uint64_t one_h = 1;
   uint64_t* ip = nullptr;
   size_t nip = 0;
-  if ((rc = pidec::quotient_device(dQ, nQ, 0, cur, nN, 0, &one_h, 1, (int64_t)(4 * h), prec, &ip, &nip, nullptr)))
+  if ((rc = pidec::quotient_device(dQ, nQ, 0, cur, nN, 0, &one_h, 1, (int64_t)(4 * h), false, prec, &ip, &nip, nullptr)))
     return rc;
   const size_t nm = (4 * h + 2 + 63) / 64 + 1;  // m < 2^(4h + 2), and a limb for an estimate above it
   uint64_t *dm = nullptr, *d_one = nullptr;

@@ -176,6 +176,7 @@ struct PiCtx {
   std::atomic<uint64_t> ntt_hist[33];
   std::atomic<uint64_t> batch_levels{0};
   double bt[5] = {0, 0, 0, 0, 0};  // level-batched splitting: time per step (PIMUL_PI_TIMING)
+  std::mutex bt_mu;                  // segments of the splitting run on two host threads
   double leaf_ms = 0;
   uint64_t serve_nodes = 0;  // > 0: the splitting tree above this many nodes goes through the multiply service
   uint64_t served_requests = 0;
@@ -187,6 +188,12 @@ static thread_local PiCtx* t_ctx = nullptr;
 static PiCtx& C() {
   static thread_local PiCtx idle;  // only reached outside a driver call
   return t_ctx ? *t_ctx : idle;
+}
+
+static void bt_add(int i, double ms) {
+  PiCtx& c = C();
+  std::lock_guard<std::mutex> lk(c.bt_mu);
+  c.bt[i] += ms;
 }
 
 // A backend error stops the pipeline at once: mul_ntt throws PiAbort, which
@@ -1493,15 +1500,15 @@ static int batch_mul(const std::vector<const Limbs*>& A, const std::vector<const
       }
     });
     double t3 = now_ms();
-    C().bt[0] += t1 - t0;
-    C().bt[1] += t2 - t1;
-    C().bt[2] += t3 - t2;
+    bt_add(0, t1 - t0);
+    bt_add(1, t2 - t1);
+    bt_add(2, t3 - t2);
   }
   double t4 = now_ms();
   parallel_for(ci.size(), [&](size_t lo, size_t hi) {
     for (size_t c = lo; c < hi; c++) out[ci[c]] = mul_mag(*A[ci[c]], *B[ci[c]]);
   });
-  C().bt[3] += now_ms() - t4;
+  bt_add(3, now_ms() - t4);
   return C().error.load();
 }
 
@@ -1541,7 +1548,7 @@ static int merge_level(std::vector<PQT>& nodes, LevelStaging& S) {
   });
   if (nodes.size() & 1) next[np] = std::move(nodes.back());
   nodes.swap(next);
-  C().bt[4] += now_ms() - t0;
+  bt_add(4, now_ms() - t0);
   C().batch_levels.fetch_add(1, std::memory_order_relaxed);
   return PIMUL_OK;
 }
@@ -1600,7 +1607,9 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
     // new level: Q, P, T per pair (and the odd node).  T = T_L Q_R + P_L T_R
     // is one fused sum (its spectra added before one inverse transform);
     // a difference goes through the temporaries T_L Q_R, P_L T_R and a
-    // batched subtraction.  Q_L Q_R and T_L Q_R share Q_R's spectrum.
+    // batched subtraction.  Q_L Q_R and T_L Q_R share Q_R's spectrum, and
+    // P_R P_L and T_R P_L share P_L's (the batch shares the second factor's
+    // spectrum among products of one transform length).
     size_t lvl_w = 0, tmp_w = 0;
     for (size_t i = 0; i < np; i++) {
       const DNode& L = nodes[2 * i];
@@ -1637,7 +1646,7 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
       count(L.qn, R.qn);
       if (need_p) {
         z.p = nxt + lo, z.pn = L.pn + R.pn, lo += z.pn;
-        sj.push_back(pimul_sum_job{L.p, L.pn, R.p, R.pn, nullptr, 0, nullptr, 0, z.p, z.pn});
+        sj.push_back(pimul_sum_job{R.p, R.pn, L.p, L.pn, nullptr, 0, nullptr, 0, z.p, z.pn});
         count(L.pn, R.pn);
       } else {
         z.p = nullptr, z.pn = 0;
@@ -1647,14 +1656,14 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
       count(L.tn, R.qn);
       count(L.pn, R.tn);
       if (!(L.terms & 1)) {
-        sj.push_back(pimul_sum_job{L.t, L.tn, R.q, R.qn, L.p, L.pn, R.t, R.tn, z.t, z.tn});
+        sj.push_back(pimul_sum_job{L.t, L.tn, R.q, R.qn, R.t, R.tn, L.p, L.pn, z.t, z.tn});
       } else {
         uint64_t* tq = tmp + to;
         to += L.tn + R.qn;
         uint64_t* pt = tmp + to;
         to += L.pn + R.tn;
         sj.push_back(pimul_sum_job{L.t, L.tn, R.q, R.qn, nullptr, 0, nullptr, 0, tq, L.tn + R.qn});
-        sj.push_back(pimul_sum_job{L.p, L.pn, R.t, R.tn, nullptr, 0, nullptr, 0, pt, L.pn + R.tn});
+        sj.push_back(pimul_sum_job{R.t, R.tn, L.p, L.pn, nullptr, 0, nullptr, 0, pt, L.pn + R.tn});
         aj.push_back(pimul_addsub_job{tq, L.tn + R.qn, pt, L.pn + R.tn, z.t, z.tn, 1});
       }
     }
@@ -1707,8 +1716,8 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
               t_as - t_sum, t_arr - t_as, t2 - t_arr);
     nodes.swap(next);
     C().batch_levels.fetch_add(1, std::memory_order_relaxed);
-    C().bt[1] += t2 - t1;
-    C().bt[4] += (t1 - t0);
+    bt_add(1, t2 - t1);
+    bt_add(4, (t1 - t0));
   }
   return rc;
 }
@@ -1919,14 +1928,12 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_hi) != cudaSuccess) return PIMUL_ECUDA;
   std::vector<DLevel> roots(nseg);
-  int rc = PIMUL_OK;
-  double tl = 0;
-  for (size_t sgi = 0; sgi < nseg && !rc; sgi++) {
+  std::vector<double> seg_tl(nseg, 0.0);
+  // one segment: leaves on the device, then its levels (stopping at `stop`
+  // nodes), all on stream sw
+  auto run_segment = [&](size_t sgi, cudaStream_t sw) -> int {
     const uint64_t k0 = seg_k[sgi], k1 = seg_k[sgi + 1], lf = seg_leaf[sgi];
-    if (lf > pileaf::MAX_TERMS) {
-      rc = PIMUL_EINVAL;
-      break;
-    }
+    if (lf > pileaf::MAX_TERMS) return PIMUL_EINVAL;
     const uint64_t nl = (k1 - k0 + lf - 1) / lf;
     double t0 = now_ms();
     // slots sized from the segment's last full leaf (the largest values),
@@ -1936,17 +1943,16 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     const uint32_t sp = (uint32_t)big.p.m.size() + 2, sq = (uint32_t)big.q.m.size() + 2,
                    stt = (uint32_t)big.t.m.size() + 2;
     uint64_t* arena = nullptr;
-    if (cudaMallocAsync((void**)&arena, std::max<uint64_t>(nl * (sp + sq + stt), 1) * 8, st) != cudaSuccess) {
+    if (cudaMallocAsync((void**)&arena, std::max<uint64_t>(nl * (sp + sq + stt), 1) * 8, sw) != cudaSuccess) {
       cudaGetLastError();
-      rc = PIMUL_ENOMEM;
-      break;
+      return PIMUL_ENOMEM;
     }
     roots[sgi].arenas.push_back(arena);
     std::vector<uint32_t> lens(3 * nl);
     std::vector<uint8_t> signs(nl);
-    rc = pileaf::leaves_device(k0, k1, (uint32_t)lf, (uint32_t)nl, sp, sq, stt, arena, lens.data(), signs.data(), st);
-    tl += now_ms() - t0;
-    if (rc) break;
+    int rc = pileaf::leaves_device(k0, k1, (uint32_t)lf, (uint32_t)nl, sp, sq, stt, arena, lens.data(), signs.data(), sw);
+    seg_tl[sgi] = now_ms() - t0;
+    if (rc) return rc;
     std::vector<DNode>& nodes = roots[sgi].nodes;
     nodes.resize(nl);
     for (uint64_t i = 0; i < nl && !rc; i++) {
@@ -1962,8 +1968,41 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     }
     // served mode: each segment stops at its share of the nodes handed to the service
     const size_t stop = C().serve_nodes && keep ? std::max<size_t>(1, C().serve_nodes / nseg) : 1;
-    if (!rc) rc = dev_reduce(roots[sgi], st, true, stop);
+    if (!rc) rc = dev_reduce(roots[sgi], sw, true, stop);
+    return rc;
+  };
+  // segments on two host threads with a stream each: one segment's host work
+  // (leaf slots, descriptors, the level lengths read back) overlaps the
+  // other's kernels
+  const size_t nwork = nseg >= 2 ? 2 : 1;
+  std::vector<cudaStream_t> wst(nwork, st);
+  for (size_t w = 1; w < nwork; w++)
+    if (cudaStreamCreateWithPriority(&wst[w], cudaStreamNonBlocking, prio_hi) != cudaSuccess) wst[w] = nullptr;
+  std::atomic<size_t> next_seg{0};
+  std::atomic<int> seg_rc{0};
+  auto work = [&](size_t w) {
+    for (;;) {
+      const size_t sgi = next_seg.fetch_add(1);
+      if (sgi >= nseg || seg_rc.load()) break;
+      const int r = wst[w] ? run_segment(sgi, wst[w]) : PIMUL_ECUDA;
+      int none = 0;
+      if (r) seg_rc.compare_exchange_strong(none, r);
+    }
+  };
+  {
+    std::list<Worker> helpers;
+    for (size_t w = 1; w < nwork; w++) helpers.emplace_back([&work, w] { work(w); });
+    work(0);
+    for (Worker& h : helpers) h.join();
   }
+  for (size_t w = 1; w < nwork; w++)
+    if (wst[w]) {
+      cudaStreamSynchronize(wst[w]);
+      cudaStreamDestroy(wst[w]);
+    }
+  int rc = seg_rc.load();
+  double tl = 0;
+  for (double x : seg_tl) tl += x;
   C().leaf_ms += tl;
   DLevel top;
   for (DLevel& r : roots) {
@@ -1998,7 +2037,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
       rc = PIMUL_ECUDA;
     q = Int(std::move(qm), false);
     t = Int(std::move(tm), true);
-    C().bt[2] += now_ms() - t0;
+    bt_add(2, now_ms() - t0);
   }
   dev_free(top, st);
   cudaStreamSynchronize(st);
@@ -2050,6 +2089,7 @@ struct DecPlan {
   std::vector<Int> P;       // P_k = (10^19)^(2^k)
   std::vector<Int> V;       // V_k ~ 2^(s_k) / P_k, k >= kmin
   std::vector<uint64_t> sh; // s_k = 2 bits(P_k) + 64
+  pidec::DevLevels dev;     // or: levels kmin..K-1 built in device memory (dev.K == K)
 };
 
 // Plan for integers of at most ndig decimal digits.  V_k: Newton once at the
@@ -2096,6 +2136,25 @@ static DecPlan make_dec_plan(uint64_t ndig) {
   return D;
 }
 
+// The same plan with its levels built on the device (pidec::build_levels_device:
+// every V_k an underestimate within a few units of floor(2^(s_k) / P_k),
+// which the conversion's correction rounds absorb); a small plan is built on
+// the host.
+static DecPlan make_dec_plan_device(uint64_t ndig) {
+  DecPlan D;
+  const uint64_t nch = (ndig + 18) / 19;
+  while ((1ull << D.K) < nch) D.K++;
+  if (D.K <= pidec::LEAF_K) return make_dec_plan(ndig);
+  D.kmin = pidec::LEAF_K;
+  const int rc = pidec::build_levels_device(D.K, &D.dev, nullptr);
+  if (rc) {
+    int none = 0;
+    C().error.compare_exchange_strong(none, rc);
+    throw PiAbort{rc};
+  }
+  return D;
+}
+
 // Exactly `want` decimal digits of x < 10^want (zero-padded on the left),
 // written straight into out; x: n limbs on the host, or in device memory
 // (on_dev), of bit length xbits.
@@ -2115,12 +2174,15 @@ static int to_decimal_core(const uint64_t* x, size_t n, bool on_dev, uint64_t xb
     out += want - total;
     want = total;
   }
+  const bool lv_dev = plan->dev.K == plan->K;
   std::vector<pidec::Level> lv(plan->K);
-  for (int k = plan->kmin; k < plan->K; k++)
-    lv[k] = pidec::Level{plan->P[k].m.data(), plan->P[k].m.size(), plan->V[k].m.data(), plan->V[k].m.size(),
-                         plan->sh[k]};
+  if (!lv_dev)
+    for (int k = plan->kmin; k < plan->K; k++)
+      lv[k] = pidec::Level{plan->P[k].m.data(), plan->P[k].m.size(), plan->V[k].m.data(), plan->V[k].m.size(),
+                           plan->sh[k]};
   double ms[3] = {0, 0, 0};
-  int rc = pidec::to_decimal_device(x, n, on_dev, plan->K, lv.data(), out, want, ms);
+  int rc = pidec::to_decimal_device(x, n, on_dev, plan->K, lv_dev ? plan->dev.lv.data() : lv.data(), lv_dev, out,
+                                    want, ms);
   if (getenv("PIMUL_PI_TIMING"))
     fprintf(stderr, "[pimul] decimal conversion on the device: upload %.1f ms, levels %.1f, leaves + download %.1f\n",
             ms[0], ms[1], ms[2]);
@@ -2191,11 +2253,13 @@ static int gauss_legendre_body(uint64_t digits, char* out, uint32_t flags, doubl
   double t0 = now_ms();
   if (flags & PIMUL_PI_DEVICE_AGM) {
     // the AGM, the quotient and the conversion on the device; the decimal
-    // scale and the conversion's divisors on threads beside the iteration
-    Flt scale;
-    Worker scale_th([&] { scale = pow_int(flt_from_u64(10, prec), Int(digits - 1)); });
+    // scale 10^(D-1) = 5^(D-1) 2^(D-1) (5^(D-1) exact, on the device) and the
+    // conversion's divisors on threads beside the iteration
+    piagm::DevNum p5;
+    int p5rc = PIMUL_OK;
+    Worker scale_th([&] { p5rc = piagm::pow5_device(digits - 1, &p5); });
     DecPlan dplan;
-    Worker plan_th([&] { dplan = make_dec_plan(digits + 1); });
+    Worker plan_th([&] { dplan = make_dec_plan_device(digits + 1); });
     piagm::AgmOut A;
     int rc = piagm::agm_device(prec, &A, nullptr);
     const double t1 = now_ms();
@@ -2203,14 +2267,16 @@ static int gauss_legendre_body(uint64_t digits, char* out, uint32_t flags, doubl
     plan_th.join();
     uint64_t* d_ip = nullptr;
     size_t ipn = 0;
+    if (!rc) rc = p5rc;
     if (!rc && C().error.load()) rc = C().error.load();
     if (!rc) {
-      // pi 10^(D-1) = scale (a + b)^2 / (4 t)
+      // pi 10^(D-1) = 5^(D-1) 2^(D-3) (a + b)^2 / t
       const size_t nl = (prec + 192 + 63) / 64, lq = std::min(A.num_limbs, nl);
       rc = pidec::quotient_device(A.den, A.den_limbs, A.den_exp, A.num + (A.num_limbs - lq), lq,
-                                  A.num_exp + 64 * (int64_t)(A.num_limbs - lq), scale.mant.data(), scale.mant.size(),
-                                  scale.exp - 2, prec, &d_ip, &ipn, nullptr);
+                                  A.num_exp + 64 * (int64_t)(A.num_limbs - lq), p5.mant, p5.limbs,
+                                  (int64_t)digits - 3, true, prec, &d_ip, &ipn, nullptr);
     }
+    if (p5.mant) cudaFree(p5.mant);
     if (A.num) cudaFree(A.num);
     if (A.den) cudaFree(A.den);
     if (!rc) rc = to_decimal_batched_into_dev(d_ip, ipn, out, digits, &dplan);
@@ -2276,10 +2342,14 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
   double t0 = now_ms();
   // sqrt(10005) * 426880 runs beside the binary splitting (chudnovsky.rs:118-126),
   // and so does the decimal scale 10^(D-1) at the working precision, which
-  // depends on nothing else (util.rs:25-83 computes it after pi).
+  // depends on nothing else (util.rs:25-83 computes it after pi).  The plain
+  // form computes both on the host (sqrt_mut restates the reference's
+  // iteration); the batched form computes their product
+  // W = 426880 sqrt(10005) 10^(D-1) on the device for the device final
+  // assembly, and both host values only if the splitting ends on the host.
   Flt sq, scale;
-  double t_sqrt = 0, t_scale = 0;
-  Worker sqrt_th([&] {
+  double t_sqrt = 0, t_scale = 0, t_w = 0, t_plan = 0;
+  auto host_sqrt = [&] {
     double ts = now_ms();
     Flt p;
     if (leaf_terms) {
@@ -2290,28 +2360,55 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
     }
     sq = mul_at_prec(p, flt_from_u64(426880, 64), p.prec);
     t_sqrt = now_ms() - ts;
-  });
-  Worker scale_th([&] {
+  };
+  auto host_scale = [&] {
     double ts = now_ms();
     scale = pow_int(flt_from_u64(10, prec), Int(digits - 1));
     t_scale = now_ms() - ts;
-  });
-  // batched form: the decimal conversion's divisors and reciprocals too,
-  // and W = 426880 sqrt(10005) 10^(D-1) for the device final assembly (this
-  // thread alone joins the two above; the main thread joins it)
+  };
+  Worker sqrt_th, scale_th;
+  if (!leaf_terms) {
+    sqrt_th.start(host_sqrt);
+    scale_th.start(host_scale);
+  }
+  // batched form: the decimal conversion's divisors and reciprocals too
   DecPlan dplan;
   Worker plan_th([&] {
-    if (leaf_terms) dplan = make_dec_plan(digits + 1);
+    double ts = now_ms();
+    if (leaf_terms) dplan = make_dec_plan_device(digits + 1);
+    t_plan = now_ms() - ts;
   });
-  Flt W;
+  piagm::DevNum W;
+  int w_rc = PIMUL_OK;
   Worker w_th;
   if (leaf_terms)
     w_th.start([&] {
-      sqrt_th.join();
-      scale_th.join();
-      W = mul_at_prec(sq, scale, prec + 64);
+      double ts = now_ms();
+      w_rc = piagm::chudnovsky_w_device(digits, prec, &W, nullptr);
+      t_w = now_ms() - ts;
     });
-  auto join_sqrt = [&] { leaf_terms ? w_th.join() : sqrt_th.join(); };
+  struct WGuard {  // the device W, whichever way this call ends
+    Worker& th;
+    piagm::DevNum& w;
+    ~WGuard() {
+      try {
+        th.join();
+      } catch (...) {
+      }
+      if (w.mant) cudaFree(w.mant);
+      w.mant = nullptr;
+    }
+  } w_guard{w_th, W};
+  // the host values, for the plain form or a batched splitting that ended on the host
+  auto join_sqrt = [&] {
+    if (!leaf_terms) {
+      sqrt_th.join();
+    } else if (sq.zero()) {
+      Worker sc(host_scale);
+      host_sqrt();
+      sc.join();
+    }
+  };
   auto join_scale = [&] {
     if (!leaf_terms) scale_th.join();
   };
@@ -2335,21 +2432,25 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
   if (brc) {
     for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
     droot.lvl.arenas.clear();
-    join_sqrt();
-    join_scale();
+    if (!leaf_terms) {
+      sqrt_th.join();
+      scale_th.join();
+    }
     plan_th.join();
     return brc;
   }
   double t1 = now_ms();
   if (!droot.lvl.nodes.empty()) {
     // final assembly and decimal conversion without leaving the device
-    join_sqrt();
+    w_th.join();
     const DNode& r = droot.lvl.nodes[0];
     uint64_t* d_ip = nullptr;
     size_t ipn = 0;
     double fms[2] = {0, 0};
-    int frc = pidec::final_assembly_device(r.q, r.qn, droot.q_off, r.t, r.tn, droot.t_off, CH_A, W.mant.data(),
-                                           W.mant.size(), W.exp, prec, &d_ip, &ipn, fms);
+    int frc = w_rc;
+    if (!frc)
+      frc = pidec::final_assembly_device(r.q, r.qn, droot.q_off, r.t, r.tn, droot.t_off, CH_A, W.mant, W.limbs, W.exp,
+                                         true, prec, &d_ip, &ipn, fms);
     for (uint64_t h : droot.svc_handles) pimul_free(h);
     droot.svc_handles.clear();
     for (uint64_t* ar : droot.lvl.arenas) cudaFree(ar);
@@ -2360,8 +2461,8 @@ static int chudnovsky_body(uint64_t digits, char* out, uint64_t leaf_terms, doub
     if (d_ip) cudaFree(d_ip);
     double t3 = now_ms();
     if (getenv("PIMUL_PI_TIMING"))
-      fprintf(stderr, "[pimul] sqrt thread %.1f ms, scale thread %.1f ms, final assembly on the device: "
-              "reciprocal %.1f ms, products %.1f ms\n", t_sqrt, t_scale, fms[0], fms[1]);
+      fprintf(stderr, "[pimul] W thread %.1f ms, conversion plan thread %.1f ms, final assembly on the device: "
+              "reciprocal %.1f ms, products %.1f ms\n", t_w, t_plan, fms[0], fms[1]);
     if (frc) return frc;
     if (C().error.load()) return C().error.load();
     if (phase_ms) {
