@@ -27,6 +27,7 @@
 #include "ntt_kernels.cuh"
 #include "../../include/pimul.h"
 #include "hostcopy.h"
+#include "splitmerge.h"
 
 namespace pimul {
 
@@ -915,6 +916,287 @@ __global__ void __launch_bounds__(SMALL_THREADS, 4) k_small_mul(const SmallJob* 
   }
 }
 
+// ---- merged binary-splitting levels (one node pair per thread group) ------
+// The lowest levels of a Chudnovsky splitting segment hold hundreds of
+// thousands of node pairs whose products all fit one CTA's shared memory.
+// A group of G = N/8 threads merges one pair (L, R) into
+//   P = P_L P_R,  Q = Q_L Q_R,  T = T_L Q_R + P_L T_R
+// (magnitudes; crates/pi-core/src/algorithm/chudnovsky.rs:377-413).  The
+// spectra of Q_R and P_L serve two products each and T's two products are
+// added in the transform domain: six forward and three inverse transforms
+// per pair instead of eight and four, no temporaries in HBM and no separate
+// addition.  Three padded arrays per group; every CTA holds 512 threads and
+// 3 * 2^12 padded words whatever the level's length (2^L / 8 threads and
+// 3 * 2^L words per group).
+constexpr int MERGE_THREADS = 512;
+
+struct MergeLevel {
+  const uint64_t* in;
+  const uint32_t* in_len;
+  uint64_t* out;
+  uint32_t* out_len;
+  uint32_t sp, sq, st, op, oq, ot;
+  uint32_t n_in;
+  int L;
+  int* bad;
+};
+
+__host__ __device__ __forceinline__ int merge_group_threads(int L) {
+  const int g = (1 << L) / 8;
+  return g < 32 ? 32 : g;
+}
+__host__ __device__ __forceinline__ size_t merge_cta_smem(int L) {
+  return (size_t)(MERGE_THREADS / merge_group_threads(L)) * 3 * spad(1u << L) * 8;
+}
+
+// One round of radix 2^B over the sub-problems of 2^mlog words of na (1..3)
+// arrays of 2^L words, by the nth threads of a group (tid >= nth: no work).
+template <int B, bool FWD>
+__device__ __forceinline__ void mround(uint64_t* a0, uint64_t* a1, uint64_t* a2, int na, int L, int mlog,
+                                       const Roots& R, int tid, int nth) {
+  const int slog = mlog - B, ilog = L - B;
+  const uint32_t smask = (1u << slog) - 1, imask = (1u << ilog) - 1;
+  for (uint32_t w = tid; w < ((uint32_t)na << ilog); w += nth) {
+    const uint32_t ai = w >> ilog;
+    uint64_t* sm = ai == 0 ? a0 : (ai == 1 ? a1 : a2);
+    const uint32_t rest = w & imask;
+    const uint32_t jp = rest & smask;
+    const uint32_t row0 = ((rest >> slog) << mlog) + jp;
+    uint64_t v[1 << B];
+#pragma unroll
+    for (int m = 0; m < (1 << B); m++) v[m] = sm[spad(row0 + (m << slog))];
+    if constexpr (FWD) {
+      dft_fwd<B>(v);
+      if (slog > 0) {
+#pragma unroll
+        for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], round_tw(R, mlog, k * jp, false));
+      }
+    } else {
+      gl::Lz x[1 << B];
+      x[0] = gl::lz(v[0]);
+#pragma unroll
+      for (int k = 1; k < (1 << B); k++)
+        x[k] = slog > 0 ? gl::lz_mul(v[k], round_tw(R, mlog, k * jp, true)) : gl::lz(v[k]);
+      dft_inv_lz<B>(x, v);
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << B); k++) sm[spad(row0 + (k << slog))] = v[k];
+  }
+}
+
+// Forward (or unscaled inverse) transforms of na arrays of 2^Lp words by one
+// group, then CTA barriers up to the round count of 2^Lmax: the groups of a
+// CTA may hold different lengths and must pass the same barriers.
+template <bool FWD>
+__device__ void group_dft(uint64_t* a0, uint64_t* a1, uint64_t* a2, int na, int Lp, int Lmax, const Roots& R,
+                          int tid, int G) {
+  int bits[8], n = 0, rem = Lp;
+  while (rem > 0) {
+    int b = rem >= 3 ? 3 : rem;
+    if (rem == 4) b = 2;
+    bits[n++] = b;
+    rem -= b;
+  }
+  int mlog = FWD ? Lp : 0;
+  for (int i = 0; i < n; i++) {
+    const int b = bits[FWD ? i : n - 1 - i];
+    if (!FWD) mlog += b;
+    if (b == 3) mround<3, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
+    else if (b == 2) mround<2, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
+    else mround<1, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
+    if (FWD) mlog -= b;
+    __syncthreads();
+  }
+  for (int i = n; i < rp_count(Lmax); i++) __syncthreads();
+}
+
+// Limbs x[0..n) -> 16-bit coefficients of an array of 2^Lp words (zero tail).
+__device__ __forceinline__ void group_pack(uint64_t* sm, const uint64_t* x, uint32_t n, int Lp, int tid, int G) {
+  for (uint32_t l = tid; l < (1u << Lp) / 4; l += G) {
+    const uint64_t v = l < n ? x[l] : 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) sm[spad(4 * l + q)] = (v >> (16 * q)) & 0xFFFF;
+  }
+}
+
+// Carry normalisation of a group's inverse-transformed array (exact
+// convolution values, below 2^45) into nl limbs at out, one 16-coefficient
+// window per thread (nl <= 2^Lp / 4 + 1, so the windows fit G = 2^Lp / 8
+// threads); sH (a free array) holds the windows' high parts.  Returns the
+// trimmed length to every thread of the group.  Same window arithmetic as
+// the one-CTA multiply above.
+__device__ uint32_t group_carry_store(const uint64_t* smX, int Lp, uint32_t nl, uint64_t* out, uint64_t* sH,
+                                      bool active, int gtid, int G, int gw0, uint32_t* sA, uint32_t* sBm,
+                                      uint32_t* sTop) {
+  const int tid = threadIdx.x;
+  const uint32_t N = 1u << Lp;
+  const uint32_t n_out = active && nl ? 4 * nl - 1 : 0;
+  const uint32_t nwin = (n_out + 15) / 16;
+  const uint32_t w = gtid;
+  Win v{{0, 0, 0, 0}, 0};
+  if (w < nwin) {
+    uint64_t c[16];
+#pragma unroll
+    for (int t = 0; t < 16; t++) {
+      const uint32_t idx = 16 * w + t;
+      c[t] = idx < N ? gl::canon(smX[spad(idx)]) : 0;
+    }
+    v = fold16(c, 1);
+  }
+  __syncthreads();
+  if (w < nwin) sH[w] = v.hi;
+  __syncthreads();
+  const uint64_t hprev = (w > 0 && w - 1 < nwin) ? sH[w - 1] : 0;
+  uint64_t s0 = v.l[0] + hprev;
+  uint64_t c = s0 < hprev;
+  uint64_t s1 = v.l[1] + c;  c = c && s1 == 0;
+  uint64_t s2 = v.l[2] + c;  c = c && s2 == 0;
+  uint64_t s3 = v.l[3] + c;  c = c && s3 == 0;
+  const bool gg = w < nwin && c;
+  const bool pp = w < nwin && (s0 & s1 & s2 & s3) == ~0ull;
+  const uint32_t A = __ballot_sync(0xFFFFFFFFu, gg || pp), Bm = __ballot_sync(0xFFFFFFFFu, gg);
+  if ((tid & 31) == 0) {
+    sA[tid >> 5] = A;
+    sBm[tid >> 5] = Bm;
+  }
+  __syncthreads();
+  uint32_t cin = 0;
+  for (int k = gw0; k < (tid >> 5); k++) {
+    const uint64_t s = (uint64_t)sA[k] + sBm[k] + cin;
+    cin = (uint32_t)(s >> 32);
+  }
+  const uint32_t carries = (A + Bm + cin) ^ A ^ Bm;
+  if ((carries >> (tid & 31)) & 1) {
+    if (++s0 == 0) if (++s1 == 0) if (++s2 == 0) ++s3;
+  }
+  uint32_t top = 0;
+  if (w < nwin) {
+    const uint32_t base = 4 * w;
+    const uint64_t s[4] = {s0, s1, s2, s3};
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (base + q < nl) {
+        out[base + q] = s[q];
+        if (s[q]) top = base + q + 1;
+      }
+  }
+  top = __reduce_max_sync(0xFFFFFFFFu, top);
+  if ((tid & 31) == 0) sTop[tid >> 5] = top;
+  __syncthreads();
+  uint32_t t = 0;
+  for (int k = gw0; k < gw0 + G / 32; k++) t = max(t, sTop[k]);
+  __syncthreads();  // sTop is reused by the next call
+  return t;
+}
+
+// One node pair (pair = true) or the copy of an odd last node (copy = true)
+// by one group; an idle group passes the same barriers.
+__device__ void merge_item(const MergeLevel& M, const Roots& R, uint32_t item, bool pair, bool copy, uint64_t* X1,
+                           uint64_t* X2, uint64_t* X3, int gtid, int G, int gw0, uint32_t* sA, uint32_t* sBm,
+                           uint32_t* sTop) {
+  const size_t in_stride = (size_t)M.sp + M.sq + M.st, out_stride = (size_t)M.op + M.oq + M.ot;
+  uint64_t* zp = M.out + (size_t)item * out_stride;
+  uint64_t* zq = zp + M.op;
+  uint64_t* zt = zq + M.oq;
+  if (copy) {
+    const uint32_t i = M.n_in - 1;
+    const uint64_t* p = M.in + (size_t)i * in_stride;
+    const uint32_t pn = M.in_len[3 * i], qn = M.in_len[3 * i + 1], tn = M.in_len[3 * i + 2];
+    for (uint32_t k = gtid; k < pn; k += G) zp[k] = p[k];
+    for (uint32_t k = gtid; k < qn; k += G) zq[k] = p[M.sp + k];
+    for (uint32_t k = gtid; k < tn; k += G) zt[k] = p[M.sp + M.sq + k];
+    if (gtid == 0) {
+      M.out_len[3 * item] = pn;
+      M.out_len[3 * item + 1] = qn;
+      M.out_len[3 * item + 2] = tn;
+    }
+  }
+  uint32_t pl = 0, ql = 0, tl = 0, pr = 0, qr = 0, tr = 0;
+  const uint64_t *PL = nullptr, *QL = nullptr, *TL = nullptr, *PR = nullptr, *QR = nullptr, *TR = nullptr;
+  if (pair) {
+    const uint32_t l = 2 * item, r = l + 1;
+    pl = M.in_len[3 * l], ql = M.in_len[3 * l + 1], tl = M.in_len[3 * l + 2];
+    pr = M.in_len[3 * r], qr = M.in_len[3 * r + 1], tr = M.in_len[3 * r + 2];
+    PL = M.in + (size_t)l * in_stride, QL = PL + M.sp, TL = QL + M.sq;
+    PR = M.in + (size_t)r * in_stride, QR = PR + M.sp, TR = QR + M.sq;
+  }
+  const uint32_t n_p = pl + pr, n_q = ql + qr, n_t = max(tl + qr, pl + tr) + 1;
+  const uint32_t need = max(max(4 * n_p, 4 * n_q), 4 * max(tl + qr, pl + tr));  // coefficients + 1
+  int Lp = 4;
+  while ((1u << Lp) + 1 < need && Lp < 31) Lp++;  // 2^Lp >= need - 1 output coefficients
+  const bool fits = Lp <= M.L && n_p <= M.op && n_q <= M.oq && n_t <= M.ot;
+  if (pair && !fits && gtid == 0) atomicExch(M.bad, 1);
+  const bool act = pair && fits;
+  if (!act) Lp = M.L;  // an idle group keeps the level's barrier schedule
+  const int rt = act ? gtid : (1 << 30);
+  const uint32_t N = 1u << Lp;
+  // N^-1 = 2^-Lp = p - (2^(64-Lp) - 2^(32-Lp))  (2^96 = -1, 2^64 = 2^32 - 1)
+  const uint64_t ninv = gl::P - ((1ull << (64 - Lp)) - (1ull << (32 - Lp)));
+
+  // Q_R, T_L, Q_L: X2 <- T_L Q_R, X3 <- Q_L Q_R N^-1
+  if (act) {
+    group_pack(X1, QR, qr, Lp, gtid, G);
+    group_pack(X2, TL, tl, Lp, gtid, G);
+    group_pack(X3, QL, ql, Lp, gtid, G);
+  }
+  __syncthreads();
+  group_dft<true>(X1, X2, X3, 3, Lp, M.L, R, rt, G);
+  for (uint32_t i = gtid; act && i < N; i += G) {
+    const uint64_t y = X1[spad(i)];
+    X2[spad(i)] = gl::mul(X2[spad(i)], y);
+    X3[spad(i)] = gl::mul(gl::mul(X3[spad(i)], y), ninv);
+  }
+  __syncthreads();
+  group_dft<false>(X3, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
+  const uint32_t q_len = group_carry_store(X3, Lp, n_q, zq, X1, act, gtid, G, gw0, sA, sBm, sTop);
+  // P_L, T_R: X2 <- (T_L Q_R + P_L T_R) N^-1, X1 keeps P_L's spectrum
+  if (act) {
+    group_pack(X1, PL, pl, Lp, gtid, G);
+    group_pack(X3, TR, tr, Lp, gtid, G);
+  }
+  __syncthreads();
+  group_dft<true>(X1, X3, nullptr, 2, Lp, M.L, R, rt, G);
+  for (uint32_t i = gtid; act && i < N; i += G)
+    X2[spad(i)] = gl::mul(gl::add(X2[spad(i)], gl::mul(X1[spad(i)], X3[spad(i)])), ninv);
+  __syncthreads();
+  group_dft<false>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
+  const uint32_t t_len = group_carry_store(X2, Lp, n_t, zt, X3, act, gtid, G, gw0, sA, sBm, sTop);
+  // P_R: X2 <- P_L P_R N^-1
+  if (act) group_pack(X2, PR, pr, Lp, gtid, G);
+  __syncthreads();
+  group_dft<true>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
+  for (uint32_t i = gtid; act && i < N; i += G) X2[spad(i)] = gl::mul(gl::mul(X2[spad(i)], X1[spad(i)]), ninv);
+  __syncthreads();
+  group_dft<false>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
+  const uint32_t p_len = group_carry_store(X2, Lp, n_p, zp, X3, act, gtid, G, gw0, sA, sBm, sTop);
+  if (act && gtid == 0) {
+    M.out_len[3 * item] = p_len;
+    M.out_len[3 * item + 1] = q_len;
+    M.out_len[3 * item + 2] = t_len;
+  }
+}
+
+// Persistent over the level's items (pairs, then the odd last node): each
+// CTA runs MERGE_THREADS / G groups side by side.
+__global__ void __launch_bounds__(MERGE_THREADS, 2) k_split_merge(MergeLevel M, Roots R) {
+  extern __shared__ uint64_t sm[];
+  __shared__ uint32_t sA[MERGE_THREADS / 32], sBm[MERGE_THREADS / 32], sTop[MERGE_THREADS / 32];
+  const int G = merge_group_threads(M.L);
+  const uint32_t gpc = MERGE_THREADS / G;
+  const uint32_t grp = threadIdx.x / G;
+  const int gtid = (int)(threadIdx.x % G);
+  const uint32_t np = M.n_in / 2, items = np + (M.n_in & 1);
+  const uint32_t nchunks = (items + gpc - 1) / gpc;
+  const uint32_t words = spad(1u << M.L);
+  uint64_t* X1 = sm + (size_t)grp * 3 * words;
+  for (uint32_t k = blockIdx.x; k < nchunks; k += gridDim.x) {
+    const uint32_t item = k * gpc + grp;
+    merge_item(M, R, item, item < np, item == np && (M.n_in & 1), X1, X1 + words, X1 + 2 * words, gtid, G,
+               (int)(grp * G / 32), sA, sBm, sTop);
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ host side
 static int log2_ceil(uint64_t x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
 
@@ -997,6 +1279,9 @@ static cudaError_t set_smem_attrs() {
   if (e == cudaSuccess) e = set_smem_attrs_r<9>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_cta_smem(SMALL_LOG_MAX));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_split_merge, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)merge_cta_smem(pimerge::MAX_LOG));
   return e;
 }
 
@@ -3314,3 +3599,32 @@ extern "C" int pimul_mul_device_noalloc(const uint64_t* d_a, size_t la, const ui
                               "(transform length <= 2^20)");
   return mul_device_noalloc(d_a, la, d_b, lb, d_out, (cudaStream_t)stream);
 }
+
+// ---------------------------------------- merged splitting levels (internal)
+namespace pimerge {
+
+int prepare() { return pimul::ensure_init(-1); }
+
+int merge_level(const Level& lv, int* d_bad, cudaStream_t stream) {
+  using namespace pimul;
+  if (lv.L < 1 || lv.L > MAX_LOG || !d_bad || lv.op < lv.sp || lv.oq < lv.sq || lv.ot < lv.st)
+    return PIMUL_EINVAL;
+  if (lv.n_in < 2) return PIMUL_OK;
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  const MergeLevel M{lv.in, lv.in_len, lv.out, lv.out_len, lv.sp, lv.sq, lv.st, lv.op, lv.oq, lv.ot,
+                     lv.n_in, lv.L, d_bad};
+  const uint32_t gpc = MERGE_THREADS / merge_group_threads(lv.L);
+  const uint32_t items = lv.n_in / 2 + (lv.n_in & 1);
+  const uint32_t nchunks = (items + gpc - 1) / gpc;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_dev.device);
+  const uint32_t grid = std::min<uint32_t>(nchunks, (uint32_t)sms * 2);
+  k_split_merge<<<grid, MERGE_THREADS, merge_cta_smem(lv.L), stream>>>(M, g_dev.roots);
+  g_launch[K_SMALL].fetch_add(1, std::memory_order_relaxed);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("merged splitting level: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+}  // namespace pimerge

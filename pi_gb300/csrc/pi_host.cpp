@@ -45,6 +45,7 @@
 #include "../../include/pimul.h"
 #include "dec.h"
 #include "leaves.h"
+#include "splitmerge.h"
 #include "agm.h"
 
 namespace pihost {
@@ -1901,6 +1902,168 @@ static uint64_t auto_leaf(uint64_t k_hi) {
   return std::max<uint64_t>(8, std::min<uint64_t>(32, (uint64_t)(4096.0 / bits)));
 }
 
+// The lowest levels of a segment merged by the one-CTA kernel (splitmerge.h),
+// as one schedule captured in a CUDA graph: every level whose node pairs all
+// need transforms of at most 2^12 points, stopping above `stop` nodes.  The
+// leaves sit in fixed slots (sp, sq, st words); each merged level gets slots
+// sized by the largest untrimmed product of the level, computed here from
+// the leaves' exact lengths, and the trimmed lengths stay on the device until
+// the last merged level, whose lengths are the only ones read back.  Lv
+// becomes that level (its arena replaces the leaves').  Left nodes must hold
+// an even number of terms (T a sum); otherwise, or when no level qualifies,
+// Lv is left as it is.  PIMUL_EINVAL if a pair outgrew its planned transform
+// (the caller then takes the host-staged path).
+// PIMUL_PI_MERGED_LEVELS=0 runs those levels through pimul_sum_batch instead.
+static bool merged_levels_on() {
+  const char* e = getenv("PIMUL_PI_MERGED_LEVELS");
+  return !e || atoi(e) != 0;
+}
+
+static int merge_low_levels(DLevel& Lv, uint32_t sp, uint32_t sq, uint32_t st, size_t stop, cudaStream_t sw) {
+  std::vector<DNode>& nodes = Lv.nodes;
+  const size_t n0 = nodes.size();
+  if (n0 < 2 || n0 > 0xFFFFFFFFull) return PIMUL_OK;
+  for (size_t i = 0; i + 1 < n0; i++)
+    if (nodes[i].terms & 1) return PIMUL_OK;
+  // plan: per-node upper bounds of the lengths, level by level
+  struct B3 {
+    uint64_t p, q, t;
+  };
+  std::vector<B3> bnd(n0);
+  for (size_t i = 0; i < n0; i++) bnd[i] = B3{nodes[i].pn, nodes[i].qn, nodes[i].tn};
+  struct Plan {
+    uint32_t n_in, op, oq, ot;
+    int L;
+  };
+  std::vector<Plan> plan;
+  uint64_t cp = sp, cq = sq, ct = st;
+  size_t n = n0;
+  while (n > std::max<size_t>(stop, 1) && n >= 2) {
+    const size_t np = n / 2;
+    std::vector<B3> nb(np + (n & 1));
+    uint64_t need = 0;
+    for (size_t i = 0; i < np; i++) {
+      const B3& l = bnd[2 * i];
+      const B3& r = bnd[2 * i + 1];
+      const uint64_t tm = std::max(l.t + r.q, l.p + r.t);
+      nb[i] = B3{l.p + r.p, l.q + r.q, tm + 1};
+      need = std::max(need, 4 * std::max(std::max(l.p + r.p, l.q + r.q), tm) - 1);
+    }
+    if (n & 1) nb[np] = bnd[n - 1];
+    int L = 6;
+    while ((1ull << L) < need) L++;
+    if (L > pimerge::MAX_LOG) break;
+    uint64_t op = cp, oq = cq, ot = ct;
+    for (const B3& z : nb) op = std::max(op, z.p), oq = std::max(oq, z.q), ot = std::max(ot, z.t);
+    plan.push_back(Plan{(uint32_t)n, (uint32_t)op, (uint32_t)oq, (uint32_t)ot, L});
+    cp = op, cq = oq, ct = ot;
+    bnd.swap(nb);
+    n = bnd.size();
+  }
+  if (plan.empty()) return PIMUL_OK;
+  const double t0 = now_ms();
+  int rc = PIMUL_OK;
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = PIMUL_ECUDA;
+    return e == cudaSuccess;
+  };
+  // device lengths of the leaves, and per merged level its slots and lengths
+  const size_t K = plan.size();
+  std::vector<uint64_t*> arena(K + 1, nullptr);
+  std::vector<uint32_t*> lens(K + 1, nullptr);
+  arena[0] = nodes[0].p;
+  int* d_bad = nullptr;
+  std::vector<uint32_t> h0(3 * n0);
+  for (size_t i = 0; i < n0; i++) {
+    h0[3 * i] = (uint32_t)nodes[i].pn;
+    h0[3 * i + 1] = (uint32_t)nodes[i].qn;
+    h0[3 * i + 2] = (uint32_t)nodes[i].tn;
+  }
+  cu(cudaMallocAsync((void**)&d_bad, 256, sw));
+  cu(cudaMallocAsync((void**)&lens[0], 3 * n0 * 4, sw));
+  if (!rc) cu(cudaMemcpyAsync(lens[0], h0.data(), 3 * n0 * 4, cudaMemcpyHostToDevice, sw));
+  for (size_t j = 0; j < K && !rc; j++) {
+    const Plan& P = plan[j];
+    const size_t nn = P.n_in / 2 + (P.n_in & 1);
+    if (!cu(cudaMallocAsync((void**)&arena[j + 1], nn * ((size_t)P.op + P.oq + P.ot) * 8, sw))) break;
+    cu(cudaMallocAsync((void**)&lens[j + 1], 3 * nn * 4, sw));
+  }
+  // the schedule: every merged level back to back, captured once as a graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (!rc) rc = pimerge::prepare();
+  if (!rc && cu(cudaStreamBeginCapture(sw, cudaStreamCaptureModeThreadLocal))) {
+    int crc = cudaMemsetAsync(d_bad, 0, sizeof(int), sw) == cudaSuccess ? PIMUL_OK : PIMUL_ECUDA;
+    uint32_t s_p = sp, s_q = sq, s_t = st;
+    for (size_t j = 0; j < K && !crc; j++) {
+      const Plan& P = plan[j];
+      pimerge::Level lv{arena[j], lens[j], arena[j + 1], lens[j + 1], s_p, s_q, s_t, P.op, P.oq, P.ot, P.n_in, P.L};
+      crc = pimerge::merge_level(lv, d_bad, sw);
+      s_p = P.op, s_q = P.oq, s_t = P.ot;
+    }
+    const bool ended = cu(cudaStreamEndCapture(sw, &graph));
+    if (!rc && crc) rc = crc;
+    if (!rc && ended) cu(cudaGraphInstantiate(&exec, graph, 0));
+    if (!rc) cu(cudaGraphLaunch(exec, sw));
+  }
+  // the last merged level's lengths and the error flag come back once
+  const size_t nK = bnd.size();
+  std::vector<uint32_t> hK(3 * nK);
+  int h_bad = 0;
+  if (!rc) cu(cudaMemcpyAsync(hK.data(), lens[K], 3 * nK * 4, cudaMemcpyDeviceToHost, sw));
+  if (!rc) cu(cudaMemcpyAsync(&h_bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, sw));
+  cu(cudaStreamSynchronize(sw));
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (size_t j = 0; j <= K; j++)
+    if (lens[j]) cudaFreeAsync(lens[j], sw);
+  if (d_bad) cudaFreeAsync(d_bad, sw);
+  for (size_t j = 1; j < K; j++)
+    if (arena[j]) cudaFreeAsync(arena[j], sw);
+  if (!rc && h_bad) rc = PIMUL_EINVAL;
+  if (rc) {
+    if (arena[K]) cudaFreeAsync(arena[K], sw);
+    return rc;
+  }
+  // the new level: slots of the last plan, terms summed pairwise
+  std::vector<uint64_t> terms(n0);
+  for (size_t i = 0; i < n0; i++) terms[i] = nodes[i].terms;
+  for (size_t j = 0; j < K; j++) {
+    std::vector<uint64_t> nt(terms.size() / 2 + (terms.size() & 1));
+    for (size_t i = 0; i + 1 < terms.size(); i += 2) nt[i / 2] = terms[i] + terms[i + 1];
+    if (terms.size() & 1) nt.back() = terms.back();
+    terms.swap(nt);
+  }
+  const Plan& PK = plan.back();
+  const size_t stride = (size_t)PK.op + PK.oq + PK.ot;
+  std::vector<DNode> next(nK);
+  for (size_t i = 0; i < nK; i++) {
+    DNode& z = next[i];
+    z.p = arena[K] + i * stride;
+    z.q = z.p + PK.op;
+    z.t = z.q + PK.oq;
+    z.pn = hK[3 * i], z.qn = hK[3 * i + 1], z.tn = hK[3 * i + 2];
+    z.terms = terms[i];
+  }
+  for (uint64_t* a : Lv.arenas) cudaFreeAsync(a, sw);
+  Lv.arenas.assign(1, arena[K]);
+  nodes.swap(next);
+  uint64_t npairs = 0;
+  for (size_t j = 0; j < K; j++) {
+    const uint64_t pairs = plan[j].n_in / 2;
+    npairs += pairs;
+    C().ntt_hist[plan[j].L].fetch_add(4 * pairs, std::memory_order_relaxed);
+  }
+  C().ntt_calls.fetch_add(4 * npairs, std::memory_order_relaxed);
+  C().batch_levels.fetch_add(K, std::memory_order_relaxed);
+  const double t1 = now_ms();
+  bt_add(1, t1 - t0);
+  if (getenv("PIMUL_PI_TIMING"))
+    fprintf(stderr, "[pimul]   merged levels: %zu (from %zu nodes to %zu, transforms 2^%d..2^%d), %.1f ms\n", K, n0,
+            nK, plan.front().L, plan.back().L, t1 - t0);
+  return PIMUL_OK;
+}
+
 // Device-resident splitting over terms [a, b): segment by segment, the
 // leaves are computed on the device (leaves.cu) into fixed slots and the
 // segment is reduced to its root; the segment roots are then merged on the
@@ -1968,6 +2131,7 @@ static int split_root_device(uint64_t a, uint64_t b, uint64_t leaf, Int& q, Int&
     }
     // served mode: each segment stops at its share of the nodes handed to the service
     const size_t stop = C().serve_nodes && keep ? std::max<size_t>(1, C().serve_nodes / nseg) : 1;
+    if (!rc && merged_levels_on()) rc = merge_low_levels(roots[sgi], sp, sq, stt, stop, sw);
     if (!rc) rc = dev_reduce(roots[sgi], sw, true, stop);
     return rc;
   };

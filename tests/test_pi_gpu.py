@@ -128,3 +128,19 @@ def test_1e8_digits_batched_and_device_agm_match_cpu_restatement():
     del s
     g, _ = pm.pi_gauss_legendre(100_000_000, device_agm=True)
     assert hashlib.sha256(g.encode()).hexdigest() == want["sha256"]
+
+
+@pytest.mark.parametrize("digits,leaf", [(3000, 2), (20000, 4), (100_000, 6), (100_000, 64), (1_000_000, 0),
+                                         (3_000_000, 0)])
+def test_merged_splitting_levels_match_batched_levels(digits, leaf, monkeypatch):
+    # the lowest splitting levels merged pair by pair in one CTA (fused
+    # P, Q, T products, graph-captured schedule) against the same levels
+    # through pimul_sum_batch; even leaf sizes, odd node counts on the way up
+    with open(os.path.join(HERE, "golden", "pi_digits_100k.txt")) as f:
+        ref = f.read().strip()
+    monkeypatch.setenv("PIMUL_PI_MERGED_LEVELS", "0")
+    plain, _ = pm.pi_chudnovsky_batched(digits, leaf)
+    monkeypatch.setenv("PIMUL_PI_MERGED_LEVELS", "1")
+    merged, info = pm.pi_chudnovsky_batched(digits, leaf)
+    assert merged == plain
+    assert merged[:100_000] == ref[:min(digits, 100_000)]
