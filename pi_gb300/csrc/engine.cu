@@ -949,65 +949,35 @@ __host__ __device__ __forceinline__ size_t merge_cta_smem(int L) {
   return (size_t)(MERGE_THREADS / merge_group_threads(L)) * 3 * spad(1u << L) * 8;
 }
 
-// One round of radix 2^B over the sub-problems of 2^mlog words of na (1..3)
-// arrays of 2^L words, by the nth threads of a group (tid >= nth: no work).
-template <int B, bool FWD>
-__device__ __forceinline__ void mround(uint64_t* a0, uint64_t* a1, uint64_t* a2, int na, int L, int mlog,
-                                       const Roots& R, int tid, int nth) {
-  const int slog = mlog - B, ilog = L - B;
-  const uint32_t smask = (1u << slog) - 1, imask = (1u << ilog) - 1;
-  for (uint32_t w = tid; w < ((uint32_t)na << ilog); w += nth) {
-    const uint32_t ai = w >> ilog;
-    uint64_t* sm = ai == 0 ? a0 : (ai == 1 ? a1 : a2);
-    const uint32_t rest = w & imask;
-    const uint32_t jp = rest & smask;
-    const uint32_t row0 = ((rest >> slog) << mlog) + jp;
-    uint64_t v[1 << B];
-#pragma unroll
-    for (int m = 0; m < (1 << B); m++) v[m] = sm[spad(row0 + (m << slog))];
-    if constexpr (FWD) {
-      dft_fwd<B>(v);
-      if (slog > 0) {
-#pragma unroll
-        for (int k = 1; k < (1 << B); k++) v[k] = gl::mul(v[k], round_tw(R, mlog, k * jp, false));
-      }
-    } else {
-      gl::Lz x[1 << B];
-      x[0] = gl::lz(v[0]);
-#pragma unroll
-      for (int k = 1; k < (1 << B); k++)
-        x[k] = slog > 0 ? gl::lz_mul(v[k], round_tw(R, mlog, k * jp, true)) : gl::lz(v[k]);
-      dft_inv_lz<B>(x, v);
+// Forward (or unscaled inverse) transforms of NA arrays of 2^L words by one
+// group of 2^L / 8 threads: the pass kernels' rounds (radix 8, then 4) with
+// compile-time geometry, each round's twiddles applied as lazy products by
+// the next one, from the 4096-entry table of 4096th roots; one CTA barrier
+// per round (idle groups pass the barriers only).
+template <int L, int NA, int Q = 0>
+__device__ __forceinline__ void group_fwd_c(uint64_t* a0, uint64_t* a1, uint64_t* a2, const uint64_t* tw, int tid,
+                                            bool act) {
+  if constexpr (Q < rp_count(L)) {
+    constexpr int NT = (1 << L) / 8, B = rp_bits(L, Q), MLOG = rp_mlog(L, Q);
+    constexpr int PB = Q > 0 ? rp_bits(L, Q - 1) : 0, PMLOG = Q > 0 ? rp_mlog(L, Q - 1) : 0;
+    if (act) {
+      round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a0, tw, tid);
+      if constexpr (NA > 1) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a1, tw, tid);
+      if constexpr (NA > 2) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a2, tw, tid);
     }
-#pragma unroll
-    for (int k = 0; k < (1 << B); k++) sm[spad(row0 + (k << slog))] = v[k];
+    __syncthreads();
+    group_fwd_c<L, NA, Q + 1>(a0, a1, a2, tw, tid, act);
   }
 }
 
-// Forward (or unscaled inverse) transforms of na arrays of 2^Lp words by one
-// group, then CTA barriers up to the round count of 2^Lmax: the groups of a
-// CTA may hold different lengths and must pass the same barriers.
-template <bool FWD>
-__device__ void group_dft(uint64_t* a0, uint64_t* a1, uint64_t* a2, int na, int Lp, int Lmax, const Roots& R,
-                          int tid, int G) {
-  int bits[8], n = 0, rem = Lp;
-  while (rem > 0) {
-    int b = rem >= 3 ? 3 : rem;
-    if (rem == 4) b = 2;
-    bits[n++] = b;
-    rem -= b;
-  }
-  int mlog = FWD ? Lp : 0;
-  for (int i = 0; i < n; i++) {
-    const int b = bits[FWD ? i : n - 1 - i];
-    if (!FWD) mlog += b;
-    if (b == 3) mround<3, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
-    else if (b == 2) mround<2, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
-    else mround<1, FWD>(a0, a1, a2, na, Lp, mlog, R, tid, G);
-    if (FWD) mlog -= b;
+template <int L, int Q = rp_count(L) - 1>
+__device__ __forceinline__ void group_inv_c(uint64_t* a0, const uint64_t* tw, int tid, bool act) {
+  if constexpr (Q >= 0) {
+    constexpr int NT = (1 << L) / 8;
+    if (act) round_inv_t<L, 0, 0, rp_bits(L, Q), rp_mlog(L, Q), NT, NoPassTw, 12>(a0, tw, tid, NoPassTw());
     __syncthreads();
+    group_inv_c<L, Q - 1>(a0, tw, tid, act);
   }
-  for (int i = n; i < rp_count(Lmax); i++) __syncthreads();
 }
 
 // Limbs x[0..n) -> 16-bit coefficients of an array of 2^Lp words (zero tail).
@@ -1090,10 +1060,15 @@ __device__ uint32_t group_carry_store(const uint64_t* smX, int Lp, uint32_t nl, 
 }
 
 // One node pair (pair = true) or the copy of an odd last node (copy = true)
-// by one group; an idle group passes the same barriers.
-__device__ void merge_item(const MergeLevel& M, const Roots& R, uint32_t item, bool pair, bool copy, uint64_t* X1,
-                           uint64_t* X2, uint64_t* X3, int gtid, int G, int gw0, uint32_t* sA, uint32_t* sBm,
+// by one group of G = 2^L / 8 threads; an idle group passes the same
+// barriers.  Every pair of the level runs transforms of 2^L points (a pair
+// that needs fewer gets a longer transform, which changes nothing).
+template <int L>
+__device__ void merge_item(const MergeLevel& M, const uint64_t* tw, uint32_t item, bool pair, bool copy,
+                           uint64_t* X1, uint64_t* X2, uint64_t* X3, int gtid, int gw0, uint32_t* sA, uint32_t* sBm,
                            uint32_t* sTop) {
+  constexpr int G = (1 << L) / 8;
+  constexpr uint32_t N = 1u << L;
   const size_t in_stride = (size_t)M.sp + M.sq + M.st, out_stride = (size_t)M.op + M.oq + M.ot;
   uint64_t* zp = M.out + (size_t)item * out_stride;
   uint64_t* zq = zp + M.op;
@@ -1121,54 +1096,50 @@ __device__ void merge_item(const MergeLevel& M, const Roots& R, uint32_t item, b
     PR = M.in + (size_t)r * in_stride, QR = PR + M.sp, TR = QR + M.sq;
   }
   const uint32_t n_p = pl + pr, n_q = ql + qr, n_t = max(tl + qr, pl + tr) + 1;
-  const uint32_t need = max(max(4 * n_p, 4 * n_q), 4 * max(tl + qr, pl + tr));  // coefficients + 1
-  int Lp = 4;
-  while ((1u << Lp) + 1 < need && Lp < 31) Lp++;  // 2^Lp >= need - 1 output coefficients
-  const bool fits = Lp <= M.L && n_p <= M.op && n_q <= M.oq && n_t <= M.ot;
+  // output coefficients of the longest product: 4 len - 1 <= 2^L
+  const uint32_t need = max(max(n_p, n_q), max(tl + qr, pl + tr));
+  const bool fits = 4ull * need <= N + 1ull && n_p <= M.op && n_q <= M.oq && n_t <= M.ot;
   if (pair && !fits && gtid == 0) atomicExch(M.bad, 1);
   const bool act = pair && fits;
-  if (!act) Lp = M.L;  // an idle group keeps the level's barrier schedule
-  const int rt = act ? gtid : (1 << 30);
-  const uint32_t N = 1u << Lp;
-  // N^-1 = 2^-Lp = p - (2^(64-Lp) - 2^(32-Lp))  (2^96 = -1, 2^64 = 2^32 - 1)
-  const uint64_t ninv = gl::P - ((1ull << (64 - Lp)) - (1ull << (32 - Lp)));
+  // N^-1 = 2^-L = p - (2^(64-L) - 2^(32-L))  (2^96 = -1, 2^64 = 2^32 - 1)
+  constexpr uint64_t ninv = gl::P - ((1ull << (64 - L)) - (1ull << (32 - L)));
 
   // Q_R, T_L, Q_L: X2 <- T_L Q_R, X3 <- Q_L Q_R N^-1
   if (act) {
-    group_pack(X1, QR, qr, Lp, gtid, G);
-    group_pack(X2, TL, tl, Lp, gtid, G);
-    group_pack(X3, QL, ql, Lp, gtid, G);
+    group_pack(X1, QR, qr, L, gtid, G);
+    group_pack(X2, TL, tl, L, gtid, G);
+    group_pack(X3, QL, ql, L, gtid, G);
   }
   __syncthreads();
-  group_dft<true>(X1, X2, X3, 3, Lp, M.L, R, rt, G);
+  group_fwd_c<L, 3>(X1, X2, X3, tw, gtid, act);
   for (uint32_t i = gtid; act && i < N; i += G) {
     const uint64_t y = X1[spad(i)];
     X2[spad(i)] = gl::mul(X2[spad(i)], y);
     X3[spad(i)] = gl::mul(gl::mul(X3[spad(i)], y), ninv);
   }
   __syncthreads();
-  group_dft<false>(X3, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
-  const uint32_t q_len = group_carry_store(X3, Lp, n_q, zq, X1, act, gtid, G, gw0, sA, sBm, sTop);
+  group_inv_c<L>(X3, tw, gtid, act);
+  const uint32_t q_len = group_carry_store(X3, L, n_q, zq, X1, act, gtid, G, gw0, sA, sBm, sTop);
   // P_L, T_R: X2 <- (T_L Q_R + P_L T_R) N^-1, X1 keeps P_L's spectrum
   if (act) {
-    group_pack(X1, PL, pl, Lp, gtid, G);
-    group_pack(X3, TR, tr, Lp, gtid, G);
+    group_pack(X1, PL, pl, L, gtid, G);
+    group_pack(X3, TR, tr, L, gtid, G);
   }
   __syncthreads();
-  group_dft<true>(X1, X3, nullptr, 2, Lp, M.L, R, rt, G);
+  group_fwd_c<L, 2>(X1, X3, nullptr, tw, gtid, act);
   for (uint32_t i = gtid; act && i < N; i += G)
     X2[spad(i)] = gl::mul(gl::add(X2[spad(i)], gl::mul(X1[spad(i)], X3[spad(i)])), ninv);
   __syncthreads();
-  group_dft<false>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
-  const uint32_t t_len = group_carry_store(X2, Lp, n_t, zt, X3, act, gtid, G, gw0, sA, sBm, sTop);
+  group_inv_c<L>(X2, tw, gtid, act);
+  const uint32_t t_len = group_carry_store(X2, L, n_t, zt, X3, act, gtid, G, gw0, sA, sBm, sTop);
   // P_R: X2 <- P_L P_R N^-1
-  if (act) group_pack(X2, PR, pr, Lp, gtid, G);
+  if (act) group_pack(X2, PR, pr, L, gtid, G);
   __syncthreads();
-  group_dft<true>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
+  group_fwd_c<L, 1>(X2, nullptr, nullptr, tw, gtid, act);
   for (uint32_t i = gtid; act && i < N; i += G) X2[spad(i)] = gl::mul(gl::mul(X2[spad(i)], X1[spad(i)]), ninv);
   __syncthreads();
-  group_dft<false>(X2, nullptr, nullptr, 1, Lp, M.L, R, rt, G);
-  const uint32_t p_len = group_carry_store(X2, Lp, n_p, zp, X3, act, gtid, G, gw0, sA, sBm, sTop);
+  group_inv_c<L>(X2, tw, gtid, act);
+  const uint32_t p_len = group_carry_store(X2, L, n_p, zp, X3, act, gtid, G, gw0, sA, sBm, sTop);
   if (act && gtid == 0) {
     M.out_len[3 * item] = p_len;
     M.out_len[3 * item + 1] = q_len;
@@ -1177,22 +1148,22 @@ __device__ void merge_item(const MergeLevel& M, const Roots& R, uint32_t item, b
 }
 
 // Persistent over the level's items (pairs, then the odd last node): each
-// CTA runs MERGE_THREADS / G groups side by side.
+// CTA runs MERGE_THREADS / G groups side by side.  8 <= L <= 12.
+template <int L>
 __global__ void __launch_bounds__(MERGE_THREADS, 2) k_split_merge(MergeLevel M, Roots R) {
   extern __shared__ uint64_t sm[];
   __shared__ uint32_t sA[MERGE_THREADS / 32], sBm[MERGE_THREADS / 32], sTop[MERGE_THREADS / 32];
-  const int G = merge_group_threads(M.L);
-  const uint32_t gpc = MERGE_THREADS / G;
+  constexpr int G = (1 << L) / 8;
+  constexpr uint32_t gpc = MERGE_THREADS / G, words = spad(1u << L);
   const uint32_t grp = threadIdx.x / G;
   const int gtid = (int)(threadIdx.x % G);
   const uint32_t np = M.n_in / 2, items = np + (M.n_in & 1);
   const uint32_t nchunks = (items + gpc - 1) / gpc;
-  const uint32_t words = spad(1u << M.L);
   uint64_t* X1 = sm + (size_t)grp * 3 * words;
   for (uint32_t k = blockIdx.x; k < nchunks; k += gridDim.x) {
     const uint32_t item = k * gpc + grp;
-    merge_item(M, R, item, item < np, item == np && (M.n_in & 1), X1, X1 + words, X1 + 2 * words, gtid, G,
-               (int)(grp * G / 32), sA, sBm, sTop);
+    merge_item<L>(M, R.w12, item, item < np, item == np && (M.n_in & 1), X1, X1 + words, X1 + 2 * words, gtid,
+                  (int)(grp * G / 32), sA, sBm, sTop);
     __syncthreads();
   }
 }
@@ -1279,9 +1250,11 @@ static cudaError_t set_smem_attrs() {
   if (e == cudaSuccess) e = set_smem_attrs_r<9>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_small_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_cta_smem(SMALL_LOG_MAX));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_split_merge, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)merge_cta_smem(pimerge::MAX_LOG));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_split_merge<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_cta_smem(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_split_merge<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_cta_smem(9));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_split_merge<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_cta_smem(10));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_split_merge<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_cta_smem(11));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_split_merge<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_cta_smem(12));
   return e;
 }
 
@@ -3607,7 +3580,7 @@ int prepare() { return pimul::ensure_init(-1); }
 
 int merge_level(const Level& lv, int* d_bad, cudaStream_t stream) {
   using namespace pimul;
-  if (lv.L < 1 || lv.L > MAX_LOG || !d_bad || lv.op < lv.sp || lv.oq < lv.sq || lv.ot < lv.st)
+  if (lv.L < MIN_LOG || lv.L > MAX_LOG || !d_bad || lv.op < lv.sp || lv.oq < lv.sq || lv.ot < lv.st)
     return PIMUL_EINVAL;
   if (lv.n_in < 2) return PIMUL_OK;
   int rc = ensure_init(-1);
@@ -3620,7 +3593,14 @@ int merge_level(const Level& lv, int* d_bad, cudaStream_t stream) {
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_dev.device);
   const uint32_t grid = std::min<uint32_t>(nchunks, (uint32_t)sms * 2);
-  k_split_merge<<<grid, MERGE_THREADS, merge_cta_smem(lv.L), stream>>>(M, g_dev.roots);
+  const size_t smem = merge_cta_smem(lv.L);
+  switch (lv.L) {
+    case 8: k_split_merge<8><<<grid, MERGE_THREADS, smem, stream>>>(M, g_dev.roots); break;
+    case 9: k_split_merge<9><<<grid, MERGE_THREADS, smem, stream>>>(M, g_dev.roots); break;
+    case 10: k_split_merge<10><<<grid, MERGE_THREADS, smem, stream>>>(M, g_dev.roots); break;
+    case 11: k_split_merge<11><<<grid, MERGE_THREADS, smem, stream>>>(M, g_dev.roots); break;
+    default: k_split_merge<12><<<grid, MERGE_THREADS, smem, stream>>>(M, g_dev.roots); break;
+  }
   g_launch[K_SMALL].fetch_add(1, std::memory_order_relaxed);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("merged splitting level: ") + cudaGetErrorString(e));

@@ -297,7 +297,9 @@ __device__ __forceinline__ uint32_t round_item(uint32_t w) {
 // are applied here, to the inputs, as lazy products that feed the DFT
 // directly: element row r had position jp' = r mod 2^MLOG and output index
 // k' = (r >> MLOG) mod 2^PB there, twiddle w_(2^PMLOG)^(k' jp').
-template <int R, int T, int BC, int B, int MLOG, int NT, int PB, int PMLOG>
+// tw512 holds the 2^TWLOG roots w^t of one fixed length (512 in the pass
+// kernels, 4096 in the one-CTA merge of whole transforms).
+template <int R, int T, int BC, int B, int MLOG, int NT, int PB, int PMLOG, int TWLOG = 9>
 __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
   constexpr int SLOG = MLOG - B;
   constexpr int ITEMS = 1 << (BC + R + T - B);
@@ -317,7 +319,7 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
     if constexpr (PB > 0) {
       static_assert(PMLOG - PB == MLOG, "rounds must nest");
       const uint32_t kp = (rest >> SLOG) & ((1u << PB) - 1);
-      const uint32_t base = (kp * jp) << (9 - PMLOG), step = (kp << SLOG) << (9 - PMLOG);
+      const uint32_t base = (kp * jp) << (TWLOG - PMLOG), step = (kp << SLOG) << (TWLOG - PMLOG);
 #pragma unroll
       for (int m = 0; m < (1 << B); m++) x[m] = gl::lz_mul(v[m], tw512[base + m * step]);
     } else {
@@ -337,7 +339,7 @@ struct NoPassTw {};
 // multiplies its inputs by the pass twiddles of the tile when a functor is
 // given (ptw(row0, k, col) for tile row row0 + k, row0 a multiple of 2^B),
 // feeding the lazy products straight into the DFT.
-template <int R, int T, int BC, int B, int MLOG, int NT, class F>
+template <int R, int T, int BC, int B, int MLOG, int NT, class F, int TWLOG = 9>
 __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512, int tid, const F& ptw) {
   constexpr int SLOG = MLOG - B;
   constexpr int ITEMS = 1 << (BC + R + T - B);
@@ -361,11 +363,11 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
       for (int k = 0; k < (1 << B); k++) x[k] = gl::lz_mul(v[k], ptw(row0, k, j));
     } else {
       x[0] = gl::lz(v[0]);
-      const uint32_t jps = jp << (9 - MLOG);
+      const uint32_t jps = jp << (TWLOG - MLOG);
 #pragma unroll
       for (int k = 1; k < (1 << B); k++) {
         if constexpr (SLOG > 0) {
-          x[k] = gl::lz_mul(v[k], tw512[(512 - k * jps) & 511]);
+          x[k] = gl::lz_mul(v[k], tw512[((1u << TWLOG) - k * jps) & ((1u << TWLOG) - 1)]);
         } else {
           x[k] = gl::lz(v[k]);
         }

@@ -1913,9 +1913,16 @@ static uint64_t auto_leaf(uint64_t k_hi) {
 // an even number of terms (T a sum); otherwise, or when no level qualifies,
 // Lv is left as it is.  PIMUL_EINVAL if a pair outgrew its planned transform
 // (the caller then takes the host-staged path).
-// PIMUL_PI_MERGED_LEVELS=0 runs those levels through pimul_sum_batch instead.
+// PIMUL_PI_MERGED_LEVELS=0 runs those levels through pimul_sum_batch instead;
+// PIMUL_PI_LEVEL_GRAPH=0 launches the merged levels one by one on the stream
+// instead of through the captured graph (same kernels, for profilers that
+// do not follow graph capture on several host threads).
 static bool merged_levels_on() {
   const char* e = getenv("PIMUL_PI_MERGED_LEVELS");
+  return !e || atoi(e) != 0;
+}
+static bool level_graph_on() {
+  const char* e = getenv("PIMUL_PI_LEVEL_GRAPH");
   return !e || atoi(e) != 0;
 }
 
@@ -1950,7 +1957,7 @@ static int merge_low_levels(DLevel& Lv, uint32_t sp, uint32_t sq, uint32_t st, s
       need = std::max(need, 4 * std::max(std::max(l.p + r.p, l.q + r.q), tm) - 1);
     }
     if (n & 1) nb[np] = bnd[n - 1];
-    int L = 6;
+    int L = pimerge::MIN_LOG;
     while ((1ull << L) < need) L++;
     if (L > pimerge::MAX_LOG) break;
     uint64_t op = cp, oq = cq, ot = ct;
@@ -1992,7 +1999,7 @@ static int merge_low_levels(DLevel& Lv, uint32_t sp, uint32_t sq, uint32_t st, s
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   if (!rc) rc = pimerge::prepare();
-  if (!rc && cu(cudaStreamBeginCapture(sw, cudaStreamCaptureModeThreadLocal))) {
+  auto enqueue = [&]() -> int {
     int crc = cudaMemsetAsync(d_bad, 0, sizeof(int), sw) == cudaSuccess ? PIMUL_OK : PIMUL_ECUDA;
     uint32_t s_p = sp, s_q = sq, s_t = st;
     for (size_t j = 0; j < K && !crc; j++) {
@@ -2001,6 +2008,12 @@ static int merge_low_levels(DLevel& Lv, uint32_t sp, uint32_t sq, uint32_t st, s
       crc = pimerge::merge_level(lv, d_bad, sw);
       s_p = P.op, s_q = P.oq, s_t = P.ot;
     }
+    return crc;
+  };
+  if (!rc && !level_graph_on()) {
+    rc = enqueue();
+  } else if (!rc && cu(cudaStreamBeginCapture(sw, cudaStreamCaptureModeThreadLocal))) {
+    const int crc = enqueue();
     const bool ended = cu(cudaStreamEndCapture(sw, &graph));
     if (!rc && crc) rc = crc;
     if (!rc && ended) cu(cudaGraphInstantiate(&exec, graph, 0));

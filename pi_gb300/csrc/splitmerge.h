@@ -11,6 +11,8 @@ namespace pimerge {
 // Longest transform (log2) a merged level takes: every product of a node
 // pair stays inside one CTA's shared memory.
 constexpr int MAX_LOG = 12;
+// Shortest transform (log2) of a merged level: shorter pairs run at 2^8.
+constexpr int MIN_LOG = 8;
 
 // One level of the splitting tree in fixed slots.  Node i of the level is
 // |P| at in + i (sp + sq + st), Q at + sp, |T| at + sp + sq, with its
@@ -38,7 +40,7 @@ int prepare();
 // synchronisation, so a run of levels can be captured in a CUDA graph.
 // *d_bad (device memory) is set to 1 if a pair needs a longer transform than
 // lv.L or outgrows its slot (that pair is then not written).  PIMUL_EINVAL
-// for L > MAX_LOG or a slot smaller than the level below it.
+// for L outside [MIN_LOG, MAX_LOG] or a slot smaller than the level below it.
 int merge_level(const Level& lv, int* d_bad, cudaStream_t stream);
 
 }  // namespace pimerge
