@@ -791,7 +791,7 @@ struct SmallJob {
 // Threads per product: an eighth of the transform length (one radix-8
 // butterfly per thread and round), at least a warp; SMALL_THREADS / G
 // products of one length run side by side in a CTA.
-__host__ __device__ __forceinline__ int small_group_threads(int L) {
+__host__ __device__ __forceinline__ constexpr int small_group_threads(int L) {
   const int g = (1 << L) / 8;
   return g < 32 ? 32 : (g > SMALL_THREADS ? SMALL_THREADS : g);
 }
@@ -805,6 +805,35 @@ struct SmallChunk {
   uint32_t first, count;
   int L;
 };
+
+// Forward (or unscaled inverse) transforms of NA arrays of 2^L words by a
+// group of NT threads: the pass kernels' rounds (radix 8, then 4) with
+// compile-time geometry, each round's twiddles applied as lazy products by
+// the next one, from the 4096-entry table of 4096th roots; one CTA barrier
+// per round.  Bit i of act: array i is transformed (idle groups and skipped
+// arrays pass the barriers only).
+template <int L, int NT, int NA, int Q = 0>
+__device__ __forceinline__ void group_fwd_c(uint64_t* a0, uint64_t* a1, uint64_t* a2, const uint64_t* tw, int tid,
+                                            unsigned act) {
+  if constexpr (Q < rp_count(L)) {
+    constexpr int B = rp_bits(L, Q), MLOG = rp_mlog(L, Q);
+    constexpr int PB = Q > 0 ? rp_bits(L, Q - 1) : 0, PMLOG = Q > 0 ? rp_mlog(L, Q - 1) : 0;
+    if (act & 1) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a0, tw, tid);
+    if constexpr (NA > 1) if (act & 2) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a1, tw, tid);
+    if constexpr (NA > 2) if (act & 4) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a2, tw, tid);
+    __syncthreads();
+    group_fwd_c<L, NT, NA, Q + 1>(a0, a1, a2, tw, tid, act);
+  }
+}
+
+template <int L, int NT, int Q = rp_count(L) - 1>
+__device__ __forceinline__ void group_inv_c(uint64_t* a0, const uint64_t* tw, int tid, bool act) {
+  if constexpr (Q >= 0) {
+    if (act) round_inv_t<L, 0, 0, rp_bits(L, Q), rp_mlog(L, Q), NT, NoPassTw, 12>(a0, tw, tid, NoPassTw());
+    __syncthreads();
+    group_inv_c<L, NT, Q - 1>(a0, tw, tid, act);
+  }
+}
 
 // One product by the G threads of a group (gtid = thread in the group, gw0
 // = the CTA-wide index of the group's first warp).  Inactive groups run
@@ -830,8 +859,19 @@ __device__ void small_multiply(const SmallJob& job, bool active, int L, const Ro
   __syncthreads();
   TileGeom g{L, 0, 0};
   const int rt = active ? gtid : (1 << 30);  // an inactive group's rounds do no work
-  tile_dft_fwd(smA, g, R, rt, G);
-  tile_dft_fwd(smB, g, R, square ? (1 << 30) : rt, G);
+  // lengths 2^8 .. 2^12 (G = min(2^L / 8, SMALL_THREADS) threads): rounds with
+  // compile-time geometry; shorter ones: runtime geometry
+  const unsigned act2 = active ? (square ? 1u : 3u) : 0u;
+  switch (L) {
+    case 8: group_fwd_c<8, small_group_threads(8), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
+    case 9: group_fwd_c<9, small_group_threads(9), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
+    case 10: group_fwd_c<10, small_group_threads(10), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
+    case 11: group_fwd_c<11, small_group_threads(11), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
+    case 12: group_fwd_c<12, small_group_threads(12), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
+    default:
+      tile_dft_fwd(smA, g, R, rt, G);
+      tile_dft_fwd(smB, g, R, square ? (1 << 30) : rt, G);
+  }
   // times N^-1 = 2^(-L): with 2^96 = -1 and 2^64 = 2^32 - 1 (mod p),
   // 2^(-L) = -2^(96-L) = p - (2^(64-L) - 2^(32-L)) for 1 <= L <= 32
   const uint64_t ninv = gl::P - ((1ull << (64 - L)) - (1ull << (32 - L)));
@@ -841,7 +881,14 @@ __device__ void small_multiply(const SmallJob& job, bool active, int L, const Ro
     smA[spad(i)] = gl::mul(gl::mul(x, y), ninv);
   }
   __syncthreads();
-  tile_dft_inv(smA, g, R, rt, G);
+  switch (L) {
+    case 8: group_inv_c<8, small_group_threads(8)>(smA, R.w12, gtid, active); break;
+    case 9: group_inv_c<9, small_group_threads(9)>(smA, R.w12, gtid, active); break;
+    case 10: group_inv_c<10, small_group_threads(10)>(smA, R.w12, gtid, active); break;
+    case 11: group_inv_c<11, small_group_threads(11)>(smA, R.w12, gtid, active); break;
+    case 12: group_inv_c<12, small_group_threads(12)>(smA, R.w12, gtid, active); break;
+    default: tile_dft_inv(smA, g, R, rt, G);
+  }
   // carry: windows of 16 coefficients, one per thread (N/16 <= G)
   const uint32_t nwin = (n_out + 15) / 16, nl = la + lb;
   uint64_t* sH = smB;  // reuse: B no longer needed
@@ -947,37 +994,6 @@ __host__ __device__ __forceinline__ int merge_group_threads(int L) {
 }
 __host__ __device__ __forceinline__ size_t merge_cta_smem(int L) {
   return (size_t)(MERGE_THREADS / merge_group_threads(L)) * 3 * spad(1u << L) * 8;
-}
-
-// Forward (or unscaled inverse) transforms of NA arrays of 2^L words by one
-// group of 2^L / 8 threads: the pass kernels' rounds (radix 8, then 4) with
-// compile-time geometry, each round's twiddles applied as lazy products by
-// the next one, from the 4096-entry table of 4096th roots; one CTA barrier
-// per round (idle groups pass the barriers only).
-template <int L, int NA, int Q = 0>
-__device__ __forceinline__ void group_fwd_c(uint64_t* a0, uint64_t* a1, uint64_t* a2, const uint64_t* tw, int tid,
-                                            bool act) {
-  if constexpr (Q < rp_count(L)) {
-    constexpr int NT = (1 << L) / 8, B = rp_bits(L, Q), MLOG = rp_mlog(L, Q);
-    constexpr int PB = Q > 0 ? rp_bits(L, Q - 1) : 0, PMLOG = Q > 0 ? rp_mlog(L, Q - 1) : 0;
-    if (act) {
-      round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a0, tw, tid);
-      if constexpr (NA > 1) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a1, tw, tid);
-      if constexpr (NA > 2) round_fwd_t<L, 0, 0, B, MLOG, NT, PB, PMLOG, 12>(a2, tw, tid);
-    }
-    __syncthreads();
-    group_fwd_c<L, NA, Q + 1>(a0, a1, a2, tw, tid, act);
-  }
-}
-
-template <int L, int Q = rp_count(L) - 1>
-__device__ __forceinline__ void group_inv_c(uint64_t* a0, const uint64_t* tw, int tid, bool act) {
-  if constexpr (Q >= 0) {
-    constexpr int NT = (1 << L) / 8;
-    if (act) round_inv_t<L, 0, 0, rp_bits(L, Q), rp_mlog(L, Q), NT, NoPassTw, 12>(a0, tw, tid, NoPassTw());
-    __syncthreads();
-    group_inv_c<L, Q - 1>(a0, tw, tid, act);
-  }
 }
 
 // Limbs x[0..n) -> 16-bit coefficients of an array of 2^Lp words (zero tail).
@@ -1111,14 +1127,14 @@ __device__ void merge_item(const MergeLevel& M, const uint64_t* tw, uint32_t ite
     group_pack(X3, QL, ql, L, gtid, G);
   }
   __syncthreads();
-  group_fwd_c<L, 3>(X1, X2, X3, tw, gtid, act);
+  group_fwd_c<L, G, 3>(X1, X2, X3, tw, gtid, act ? 7u : 0u);
   for (uint32_t i = gtid; act && i < N; i += G) {
     const uint64_t y = X1[spad(i)];
     X2[spad(i)] = gl::mul(X2[spad(i)], y);
     X3[spad(i)] = gl::mul(gl::mul(X3[spad(i)], y), ninv);
   }
   __syncthreads();
-  group_inv_c<L>(X3, tw, gtid, act);
+  group_inv_c<L, G>(X3, tw, gtid, act);
   const uint32_t q_len = group_carry_store(X3, L, n_q, zq, X1, act, gtid, G, gw0, sA, sBm, sTop);
   // P_L, T_R: X2 <- (T_L Q_R + P_L T_R) N^-1, X1 keeps P_L's spectrum
   if (act) {
@@ -1126,19 +1142,19 @@ __device__ void merge_item(const MergeLevel& M, const uint64_t* tw, uint32_t ite
     group_pack(X3, TR, tr, L, gtid, G);
   }
   __syncthreads();
-  group_fwd_c<L, 2>(X1, X3, nullptr, tw, gtid, act);
+  group_fwd_c<L, G, 2>(X1, X3, nullptr, tw, gtid, act ? 3u : 0u);
   for (uint32_t i = gtid; act && i < N; i += G)
     X2[spad(i)] = gl::mul(gl::add(X2[spad(i)], gl::mul(X1[spad(i)], X3[spad(i)])), ninv);
   __syncthreads();
-  group_inv_c<L>(X2, tw, gtid, act);
+  group_inv_c<L, G>(X2, tw, gtid, act);
   const uint32_t t_len = group_carry_store(X2, L, n_t, zt, X3, act, gtid, G, gw0, sA, sBm, sTop);
   // P_R: X2 <- P_L P_R N^-1
   if (act) group_pack(X2, PR, pr, L, gtid, G);
   __syncthreads();
-  group_fwd_c<L, 1>(X2, nullptr, nullptr, tw, gtid, act);
+  group_fwd_c<L, G, 1>(X2, nullptr, nullptr, tw, gtid, act ? 1u : 0u);
   for (uint32_t i = gtid; act && i < N; i += G) X2[spad(i)] = gl::mul(gl::mul(X2[spad(i)], X1[spad(i)]), ninv);
   __syncthreads();
-  group_inv_c<L>(X2, tw, gtid, act);
+  group_inv_c<L, G>(X2, tw, gtid, act);
   const uint32_t p_len = group_carry_store(X2, L, n_p, zp, X3, act, gtid, G, gw0, sA, sBm, sTop);
   if (act && gtid == 0) {
     M.out_len[3 * item] = p_len;
@@ -2315,6 +2331,7 @@ struct SvcHandle {
 struct SvcRequest {
   uint64_t ticket;
   int op;  // 0 multiply, 1 square, 2 add, 3 subtract (PIMUL_OP_*)
+  int L = 0;  // transform length (log2) of a product, from the input lengths at submit
   uint64_t a, b, out;  // handle ids
   double t_submit;
   double t_done = 0;
@@ -2348,6 +2365,7 @@ struct Service {
   uint64_t completed = 0, batches = 0;
   int max_batch = 4096;
   int big_log_n = 24;  // requests with transforms of 2^big_log_n and longer run alone on stream 0
+  bool dirty = true;   // something admission depends on changed since the last admission pass
 };
 // Heap-allocated and never destroyed: its thread is joined by an atexit
 // handler (registered after the CUDA runtime's, so it runs first).
@@ -2401,17 +2419,6 @@ static int svc_start() {
   return PIMUL_OK;
 }
 
-// One iteration's worth of admission: FIFO, stop at the first request whose
-// inputs are not launched yet (its producer is still queued) or that does
-// not fit the budget.
-// Transform length (log2) of a queued request.
-static int svc_req_L(const SvcRequest& r) {
-  if (r.op >= 2) return 0;  // additions and subtractions: one linear pass
-  uint64_t la = g_svc.handles[r.a].limbs, lb = g_svc.handles[r.b].limbs;
-  if (!la || !lb) return 0;
-  return log2_ceil(4 * la + 4 * lb - 1);
-}
-
 // Free a handle whose producer has been launched and whose readers are done
 // (the free is ordered after the producer's batch on stream 0).
 static void svc_free_now(uint64_t id) {
@@ -2442,40 +2449,43 @@ int svc_addsub(const pimul_addsub_job* jobs, size_t n, cudaStream_t st);  // unc
 // product (alone on stream 0), 2 an addition or subtraction.
 static int svc_kind(const SvcRequest& r) {
   if (r.op >= 2) return 2;
-  return svc_req_L(r) >= g_svc.big_log_n ? 1 : 0;
+  return r.L >= g_svc.big_log_n ? 1 : 0;
 }
 
 static bool svc_ready(const SvcRequest& r) {
   return !g_svc.handles[r.a].pending && !g_svc.handles[r.b].pending;
 }
 
-// One group: the kind of the first ready request in the queue, then every
-// ready request of that kind among the first SVC_SCAN queued (in order),
-// within the budget.  A request whose input is not launched yet waits
-// without holding back the ready ones behind it (continuous batching of
-// whatever is ready).
+// One group: the kind of the first ready request in the queue whose stream
+// is free (stream 0 for a big product, a free batch stream otherwise), then
+// every ready request of that kind among the first SVC_SCAN queued (in
+// order), within the budget.  A request whose input is not launched yet
+// waits without holding back the ready ones behind it (continuous batching
+// of whatever is ready).  Returns whether a group was launched.
 constexpr size_t SVC_SCAN = 1 << 14;
 
-static void svc_admit(std::unique_lock<std::mutex>& lk) {
-  if (g_svc.queue.empty()) return;
+static bool svc_admit(std::unique_lock<std::mutex>& lk) {
+  if (g_svc.queue.empty()) return false;
+  // the free streams first: with none, nothing can be admitted and the
+  // queue is not scanned (the submitting threads share this mutex)
+  int batch_si = -1;
+  for (size_t i = 1; i < g_svc.streams.size(); i++)
+    if (!g_svc.stream_busy[i]) { batch_si = (int)i; break; }
+  const bool big_free = !g_svc.stream_busy[0];
+  if (batch_si < 0 && !big_free) return false;
   int kind = -1;
   size_t scanned = 0;
   for (auto it = g_svc.queue.begin(); it != g_svc.queue.end() && scanned < SVC_SCAN; ++it, ++scanned) {
     const SvcRequest& r = g_svc.requests[*it];
-    if (svc_ready(r)) {
-      kind = svc_kind(r);
+    if (!svc_ready(r)) continue;
+    const int k = svc_kind(r);
+    if (k == 1 ? big_free : batch_si >= 0) {
+      kind = k;
       break;
     }
   }
-  if (kind < 0) return;
-  int si = -1;
-  if (kind == 1) {
-    if (!g_svc.stream_busy[0]) si = 0;
-  } else {
-    for (size_t i = 1; i < g_svc.streams.size(); i++)
-      if (!g_svc.stream_busy[i]) { si = (int)i; break; }
-  }
-  if (si < 0) return;
+  if (kind < 0) return false;
+  const int si = kind == 1 ? 0 : batch_si;
   std::vector<uint64_t> take;
   uint64_t add = 0;
   scanned = 0;
@@ -2492,7 +2502,7 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
     it = g_svc.queue.erase(it);
     if (kind == 1) break;  // a big request forms its own group
   }
-  if (take.empty()) return;
+  if (take.empty()) return false;
   cudaStream_t st = g_svc.streams[si];
   const bool linear = g_svc.requests[take.front()].op >= 2;
   std::vector<pimul_job> jobs;
@@ -2542,9 +2552,11 @@ static void svc_admit(std::unique_lock<std::mutex>& lk) {
   g_svc.stream_busy[si] = 1;
   g_svc.inflight.push_back(std::move(bt));
   g_svc.batches++;
+  return true;
 }
 
-static void svc_reap(std::unique_lock<std::mutex>& lk) {
+static bool svc_reap(std::unique_lock<std::mutex>& lk) {
+  bool any = false;
   for (size_t i = 0; i < g_svc.inflight.size();) {
     SvcBatch& bt = g_svc.inflight[i];
     if (cudaEventQuery(bt.done) == cudaSuccess) {
@@ -2568,18 +2580,22 @@ static void svc_reap(std::unique_lock<std::mutex>& lk) {
       cudaEventDestroy(bt.done);
       g_svc.inflight.erase(g_svc.inflight.begin() + i);
       g_svc.done_cv.notify_all();
+      any = true;
     } else {
       i++;
     }
   }
+  return any;
 }
 
 static void svc_loop() {
   cudaSetDevice(g_dev.device);
   std::unique_lock<std::mutex> lk(g_svc.mu);
   while (!g_svc.stop) {
-    svc_reap(lk);
-    svc_admit(lk);
+    if (svc_reap(lk)) g_svc.dirty = true;  // streams and budget freed
+    // admission only after a change (a submission, a completion, a release,
+    // a new budget or policy), and again after every group it launched
+    if (g_svc.dirty) g_svc.dirty = svc_admit(lk);
     if (g_svc.inflight.empty() && g_svc.queue.empty()) {
       g_svc.cv.wait_for(lk, std::chrono::milliseconds(50));
     } else {
@@ -2748,6 +2764,7 @@ int pimul_twiddle_cache(uint64_t max_bytes, uint64_t* held) {
 int pimul_set_budget(uint64_t bytes) {
   std::lock_guard<std::mutex> lk(g_svc.mu);
   g_svc.budget = bytes;
+  g_svc.dirty = true;
   return PIMUL_OK;
 }
 
@@ -2819,6 +2836,7 @@ int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t*
   SvcRequest r;
   r.ticket = t;
   r.op = op;
+  r.L = (!linear && la && lb) ? log2_ceil(4 * la + 4 * lb - 1) : 0;
   r.a = a;
   r.b = op == PIMUL_OP_SQR ? a : b;
   r.out = oid;
@@ -2829,6 +2847,7 @@ int pimul_submit(int op, uint64_t a, uint64_t b, uint64_t* out_handle, uint64_t*
   if (r.b != r.a) g_svc.handles[r.b].readers++;
   g_svc.requests[t] = r;
   g_svc.queue.push_back(t);
+  g_svc.dirty = true;
   *out_handle = oid;
   *ticket = t;
   g_svc.cv.notify_one();
@@ -2908,6 +2927,7 @@ int pimul_free(uint64_t handle) {
   auto f = g_svc.handles.find(handle);
   if (f == g_svc.handles.end()) return fail(PIMUL_ENOTFOUND, "handle freed concurrently");
   svc_free_now(handle);
+  g_svc.dirty = true;
   return PIMUL_OK;
 }
 
@@ -2917,7 +2937,10 @@ int pimul_release(uint64_t handle) {
   if (it == g_svc.handles.end() || it->second.freed || it->second.release)
     return fail(PIMUL_ENOTFOUND, "unknown, freed or released handle");
   it->second.release = true;
-  if (!it->second.pending && it->second.readers <= 0) svc_free_now(handle);
+  if (!it->second.pending && it->second.readers <= 0) {
+    svc_free_now(handle);
+    g_svc.dirty = true;
+  }
   return PIMUL_OK;
 }
 
@@ -2970,6 +2993,7 @@ int pimul_service_config(int big_log_n, int max_batch) {
   std::lock_guard<std::mutex> lk(g_svc.mu);
   if (big_log_n > 0) g_svc.big_log_n = big_log_n;
   if (max_batch > 0) g_svc.max_batch = max_batch;
+  g_svc.dirty = true;
   return PIMUL_OK;
 }
 

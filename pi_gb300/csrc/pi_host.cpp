@@ -1781,6 +1781,7 @@ static int serve_tree(const std::vector<HNode>& v, size_t lo, size_t hi, bool ne
 // keeps until the root is done) and puts the root's Q and |T| (trimmed) in
 // keep->lvl as one node; their handles go to keep->svc_handles.
 static int serve_root(const DLevel& top, cudaStream_t st, DevRoot* keep) {
+  const double t0 = now_ms();
   if (cudaStreamSynchronize(st) != cudaSuccess) return PIMUL_ECUDA;  // the service streams read the nodes
   std::vector<HNode> v(top.nodes.size());
   int rc = PIMUL_OK;
@@ -1792,13 +1793,18 @@ static int serve_root(const DLevel& top, cudaStream_t st, DevRoot* keep) {
     v[i].terms = n.terms;
   }
   HNode root;
+  const double t1 = now_ms();
   if (!rc) rc = serve_tree(v, 0, v.size(), false, root);
   if (rc) return rc;
+  const double t2 = now_ms();
   const uint64_t* dq = nullptr;
   const uint64_t* dt = nullptr;
   size_t qn = 0, tn = 0;
   rc = pimul_handle_device(root.q, &dq, &qn);
   if (!rc) rc = pimul_handle_device(root.t, &dt, &tn);
+  if (getenv("PIMUL_PI_TIMING"))
+    fprintf(stderr, "[pimul] served tree: %zu nodes handed over (sync + adopt %.1f ms), requests queued in %.1f ms, "
+            "root ready after %.1f ms\n", v.size(), t1 - t0, t2 - t1, now_ms() - t2);
   keep->svc_handles = {root.q, root.t};
   if (root.p) pimul_release(root.p);
   if (rc) return rc;
