@@ -309,10 +309,17 @@ int pimul_pi_chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn bac
  * eighth of the terms, at most 64, so that each level's products fill
  * their transform lengths; at most 64 in any case) are computed on the
  * device;
- * every level above keeps P, Q and T in HBM, with all of the level's
- * products in one pimul_sum_batch call (Q_L Q_R, P_L P_R, and T_L Q_R +
- * P_L T_R as one fused sum; Q_L Q_R and T_L Q_R share Q_R's transform) and
- * the trimmed lengths from pimul_top_limbs.  The root's Q and T stay in HBM
+ * the lowest levels (every node pair's products within 2^12 points) merge
+ * one pair per thread group in shared memory (P, Q and the fused T sum from
+ * six forward and three inverse transforms), with the levels' schedule
+ * captured as one CUDA graph per segment and the trimmed lengths kept on
+ * the device; every level above keeps P, Q and T in HBM, with all of the
+ * level's products in one pimul_sum_batch call (Q_L Q_R, P_L P_R, and
+ * T_L Q_R + P_L T_R as one fused sum; Q_L Q_R and T_L Q_R share Q_R's
+ * transform) and the trimmed lengths from pimul_top_limbs.  Environment:
+ * PIMUL_PI_MERGED_LEVELS=0 runs the lowest levels through pimul_sum_batch
+ * too, PIMUL_PI_LEVEL_GRAPH=0 launches the merged levels one by one instead
+ * of through the graph (same kernels; for profilers).  The root's Q and T stay in HBM
  * for the final assembly (a Newton reciprocal of A Q + T on the device) and
  * the decimal conversion (level-batched with its nodes in HBM, as
  * pimul_to_decimal); only the digits return to the host.  The conversion's
