@@ -1,16 +1,19 @@
 // Binary-splitting leaves on the device.
 //
 // P, Q, T of short runs of consecutive Chudnovsky terms
-// (crates/pi-core/src/algorithm/chudnovsky.rs:377-413), one thread per run:
+// (crates/pi-core/src/algorithm/chudnovsky.rs:377-413), one warp per run:
 //   p_k = -(6k-5)(2k-1)(6k-1),  q_k = (C^3/24) k^3,  t_k = p_k (A + B k)
 // then the run's terms merged pairwise level by level,
 //   P = P_L P_R,  Q = Q_L Q_R,  T = T_L Q_R + P_L T_R,
-// with schoolbook products on the thread's local buffers (the same
-// arithmetic as the host's flat leaf path in pi_host.cpp, and an integer
-// result is unique, so the values are the host's).  A level of m terms
-// holds about 12 limbs per term, so a 64-term run needs two 960-limb level
-// buffers and two product temporaries: about 24 KB of local memory per
-// thread, which stays in L1/L2.
+// with every level in the warp's shared memory.  Magnitudes are stored and
+// the signs are the static ones of the splitting (P of m terms has sign
+// (-1)^m, every T < 0), so |T| = |T_L| Q_R + (-1)^(m_L) |P_L| |T_R|; a
+// merge whose |T| would come out negative is reported (the caller then
+// takes the host path).  A product is computed by a group of lanes, each
+// owning a run of output columns: 192-bit signed column sums (T's two
+// products go into the same sums), the carries propagated along the lane's
+// run and then from lane to lane.  An integer result is unique, so the
+// values are those of the host's leaf path.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,214 +28,204 @@ namespace {
 
 constexpr uint64_t CH_A = 13591409, CH_B = 545140134;  // chudnovsky.rs:57-58
 constexpr uint64_t C3_OVER_24 = 10939058860032000ull;  // chudnovsky.rs:61
-constexpr uint32_t BUF = 14 * MAX_TERMS + 64;          // limbs of one level
-constexpr uint32_t TMP = 8 * MAX_TERMS + 16;           // limbs of one product temporary
+constexpr int LW_WARPS = 4;                            // leaves (warps) per CTA
 
-struct Node {
-  uint16_t po, qo, to;  // offsets of |P|, Q, |T| in the level buffer
-  uint16_t pn, qn, tn;  // trimmed lengths
-  bool ps, ts;          // P < 0, T < 0
+// Fixed slots of a level whose nodes hold at most m terms (k < 2^31):
+// |p_k| < 2^100, q_k < 2^147, |t_k| < 2^161, so |P| < 2^(100 m) fits 2m
+// limbs, Q 3m, and |T| < m 2^(146.3 (m - 1) + 161) fits 3m + 2 limbs; the
+// T slot holds 3m + 3, the untrimmed length of the merge that makes it.
+__device__ __forceinline__ uint32_t slot_words(uint32_t m) { return 8 * m + 3; }
+__device__ __forceinline__ uint32_t q_at(uint32_t m) { return 2 * m; }
+__device__ __forceinline__ uint32_t t_at(uint32_t m) { return 5 * m; }
+constexpr uint32_t LEVEL_WORDS = 11 * MAX_TERMS;  // the largest level: MAX_TERMS single terms
+
+struct Lens {
+  uint16_t p, q, t;
 };
 
-__device__ __forceinline__ uint32_t trim(const uint64_t* x, uint32_t n) {
-  while (n && x[n - 1] == 0) n--;
-  return n;
-}
-
-// z[0..nx+ny) = x y (schoolbook); returns the trimmed length.
-__device__ uint32_t mulw(const uint64_t* x, uint32_t nx, const uint64_t* y, uint32_t ny, uint64_t* z) {
-  if (!nx || !ny) return 0;
-  for (uint32_t i = 0; i < nx + ny; i++) z[i] = 0;
-  for (uint32_t i = 0; i < nx; i++) {
-    const uint64_t xi = x[i];
-    uint64_t carry = 0;
-    for (uint32_t j = 0; j < ny; j++) {
-      const uint64_t lo = xi * y[j];
-      uint64_t hi = __umul64hi(xi, y[j]);
-      uint64_t s = z[i + j] + lo;
-      hi += s < lo;
-      s += carry;
-      hi += s < carry;  // the 128-bit sum z + x y + carry fits: no overflow of hi
-      z[i + j] = s;
-      carry = hi;
-    }
-    z[i + ny] = carry;
-  }
-  return trim(z, nx + ny);
-}
-
-__device__ int cmpw(const uint64_t* x, uint32_t nx, const uint64_t* y, uint32_t ny) {
-  if (nx != ny) return nx < ny ? -1 : 1;
-  for (uint32_t i = nx; i-- > 0;)
-    if (x[i] != y[i]) return x[i] < y[i] ? -1 : 1;
-  return 0;
-}
-
-// z = (sx ? -|x| : |x|) + (sy ? -|y| : |y|); returns |z|'s length, sign in sz.
-__device__ uint32_t add_signed(const uint64_t* x, uint32_t nx, bool sx, const uint64_t* y, uint32_t ny, bool sy,
-                               uint64_t* z, bool& sz) {
-  if (sx == sy) {
-    if (nx < ny) {
-      const uint64_t* t = x;
-      x = y;
-      y = t;
-      uint32_t tn = nx;
-      nx = ny;
-      ny = tn;
-    }
-    uint64_t c = 0;
-    for (uint32_t i = 0; i < nx; i++) {
-      const uint64_t yi = i < ny ? y[i] : 0;
-      const uint64_t s = x[i] + yi;
-      const uint64_t c1 = s < yi;
-      z[i] = s + c;
-      c = c1 | (z[i] < s);
-    }
-    z[nx] = c;
-    sz = sx;
-    return trim(z, nx + 1);
-  }
-  const int c = cmpw(x, nx, y, ny);
-  if (c == 0) {
-    sz = false;
+// z[0..nz) = x1 y1 + (sub ? -1 : +1) x2 y2 (x2 == nullptr: x1 y1 only), with
+// nz = x1y1's untrimmed length, plus one limb for a sum of two, by the G
+// lanes of a group (gl = lane in the group, gmask = the group's lanes).
+// Returns the trimmed length to every lane of the group; *bad = 1 (and
+// nothing written) if nz > cap, and *bad = 1 if the result is negative.
+__device__ uint32_t grp_mul(const uint64_t* x1, uint32_t nx1, const uint64_t* y1, uint32_t ny1, const uint64_t* x2,
+                            uint32_t nx2, const uint64_t* y2, uint32_t ny2, bool sub, uint64_t* z, uint32_t cap,
+                            uint32_t gl, uint32_t G, unsigned gmask, uint32_t src0, int* bad) {
+  const uint32_t n1 = (nx1 && ny1) ? nx1 + ny1 : 0;
+  const uint32_t n2 = (x2 && nx2 && ny2) ? nx2 + ny2 : 0;
+  const uint32_t nz = n2 ? max(n1, n2) + 1 : n1;
+  if (nz > cap) {
+    if (gl == 0) *bad = 1;
     return 0;
   }
-  if (c < 0) {
-    const uint64_t* t = x;
-    x = y;
-    y = t;
-    uint32_t tn = nx;
-    nx = ny;
-    ny = tn;
-    sx = sy;
+  const uint32_t c = (nz + G - 1) / G;
+  const uint32_t k0 = min(nz, gl * c), k1 = min(nz, k0 + c);
+  __int128 carry = 0;  // signed carry into column k, in units of 2^(64 k)
+  for (uint32_t k = k0; k < k1; k++) {
+    uint64_t lo = 0;
+    __int128 hi = 0;  // the column sum is lo + hi 2^64
+    if (n1) {
+      const uint32_t i0 = k + 1 > ny1 ? k + 1 - ny1 : 0, i1 = min(k, nx1 - 1);
+      for (uint32_t i = i0; i <= i1; i++) {
+        const unsigned __int128 pr = (unsigned __int128)x1[i] * y1[k - i];
+        const uint64_t plo = (uint64_t)pr;
+        lo += plo;
+        hi += (__int128)(pr >> 64) + (lo < plo ? 1 : 0);
+      }
+    }
+    if (n2) {
+      const uint32_t i0 = k + 1 > ny2 ? k + 1 - ny2 : 0, i1 = min(k, nx2 - 1);
+      for (uint32_t i = i0; i <= i1; i++) {
+        const unsigned __int128 pr = (unsigned __int128)x2[i] * y2[k - i];
+        const uint64_t plo = (uint64_t)pr;
+        if (sub) {
+          hi -= (__int128)(pr >> 64) + (lo < plo ? 1 : 0);
+          lo -= plo;
+        } else {
+          lo += plo;
+          hi += (__int128)(pr >> 64) + (lo < plo ? 1 : 0);
+        }
+      }
+    }
+    const uint64_t clo = (uint64_t)carry;
+    const uint64_t nlo = lo + clo;
+    carry = hi + (carry >> 64) + (nlo < clo ? 1 : 0);
+    z[k] = nlo;
   }
-  uint64_t borrow = 0;
-  for (uint32_t i = 0; i < nx; i++) {
-    const uint64_t yi = i < ny ? y[i] : 0;
-    const uint64_t d = x[i] - yi - borrow;
-    borrow = (x[i] < yi || (x[i] == yi && borrow)) ? 1 : 0;
-    z[i] = d;
+  // carries from lane to lane: lane s adds the final carry out of lane s - 1
+  for (uint32_t s = 1; s < G; s++) {
+    const uint64_t vlo = __shfl_sync(gmask, (uint64_t)carry, src0 + s - 1);
+    const uint64_t vhi = __shfl_sync(gmask, (uint64_t)((unsigned __int128)carry >> 64), src0 + s - 1);
+    if (gl == s) {
+      __int128 v = (__int128)(((unsigned __int128)vhi << 64) | vlo);
+      for (uint32_t k = k0; k < k1 && v != 0; k++) {
+        const uint64_t wlo = (uint64_t)v;
+        const uint64_t nlo = z[k] + wlo;
+        v = (v >> 64) + (nlo < wlo ? 1 : 0);
+        z[k] = nlo;
+      }
+      carry += v;
+    }
   }
-  sz = sx;
-  return trim(z, nx);
+  // the carry out of the top column must vanish (a negative |T| shows here)
+  if (gl == G - 1 && carry != 0) *bad = 1;
+  __syncwarp(gmask);
+  uint32_t top = 0;
+  for (uint32_t k = k0; k < k1; k++)
+    if (z[k]) top = k + 1;
+  for (uint32_t o = 1; o < G; o <<= 1) top = max(top, __shfl_xor_sync(gmask, top, o));
+  return top;
 }
 
-// *bad = 1 and no further writes when a leaf's buffers or slot are too small.
-__global__ void __launch_bounds__(64) k_leaves(uint64_t a0, uint64_t b, uint32_t m, uint32_t nleaf, uint64_t* out,
-                                               uint32_t sp, uint32_t sq, uint32_t st, uint32_t* lens,
-                                               uint8_t* signs, int* bad) {
-  const uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+// p_k, q_k, t_k (magnitudes) into the term slot at z (P at 0, Q at 2, T at 5).
+__device__ Lens term_values(uint64_t k, uint64_t* z) {
+  const unsigned __int128 f = (unsigned __int128)(6 * k - 5) * (2 * k - 1);
+  const unsigned __int128 p = f * (6 * k - 1);  // < 2^100
+  const unsigned __int128 k2 = (unsigned __int128)k * k;
+  const unsigned __int128 k3 = k2 * k;  // < 2^93
+  // q = C^3/24 k^3 and t = p (A + B k): 128 x 64 -> 192 bits
+  auto mul192 = [](unsigned __int128 a, uint64_t b, uint64_t* out) {
+    const unsigned __int128 lo = (unsigned __int128)(uint64_t)a * b;
+    const unsigned __int128 hi = (unsigned __int128)(uint64_t)(a >> 64) * b + (lo >> 64);
+    out[0] = (uint64_t)lo;
+    out[1] = (uint64_t)hi;
+    out[2] = (uint64_t)(hi >> 64);
+  };
+  Lens L;
+  z[0] = (uint64_t)p;
+  z[1] = (uint64_t)(p >> 64);
+  L.p = z[1] ? 2 : 1;
+  mul192(k3, C3_OVER_24, z + 2);
+  L.q = z[4] ? 3 : (z[3] ? 2 : 1);
+  mul192(p, CH_A + CH_B * k, z + 5);
+  L.t = z[7] ? 3 : (z[6] ? 2 : 1);
+  return L;
+}
+
+// One warp per leaf; *bad = 1 when a value breaks the static signs or
+// outgrows its slot (nothing past a slot is written).
+__global__ void __launch_bounds__(32 * LW_WARPS) k_leaves(uint64_t a0, uint64_t b, uint32_t m, uint32_t nleaf,
+                                                         uint64_t* out, uint32_t sp, uint32_t sq, uint32_t st,
+                                                         uint32_t* lens, uint8_t* signs, int* bad) {
+  __shared__ uint64_t s_buf[LW_WARPS][2][LEVEL_WORDS];
+  __shared__ Lens s_len[LW_WARPS][2][MAX_TERMS];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t leaf = blockIdx.x * LW_WARPS + warp;
   if (leaf >= nleaf) return;
   const uint64_t ka = a0 + (uint64_t)leaf * m;
   const uint64_t kb = ka + m < b ? ka + m : b;
   uint32_t n = (uint32_t)(kb - ka);
-  uint64_t buf0[BUF], buf1[BUF], tq[TMP], pt[TMP];
-  Node nodes[MAX_TERMS], next[MAX_TERMS / 2 + 1];
-  uint64_t* cur = buf0;
-  uint64_t* nxt = buf1;
-  uint32_t off = 0;
-  for (uint32_t i = 0; i < n; i++) {
-    const uint64_t k = ka + i;
-    // p = -(6k-5)(2k-1)(6k-1), q = (C^3/24) k^3, t = p (A + B k)
-    const uint64_t f1 = 6 * k - 5, f2 = 2 * k - 1, f3 = 6 * k - 1;
-    uint64_t pm[2] = {f1 * f2, __umul64hi(f1, f2)};
-    uint64_t p3[3], k2[2] = {k * k, __umul64hi(k, k)}, kk[1] = {k}, k3[3], c3[1] = {C3_OVER_24}, q4[4];
-    uint64_t ff[1] = {f3};
-    const uint32_t pn = mulw(pm, trim(pm, 2), ff, 1, p3);
-    const uint32_t k3n = mulw(k2, trim(k2, 2), kk, 1, k3);
-    const uint32_t qn = mulw(k3, k3n, c3, 1, q4);
-    uint64_t ab[2];
-    ab[0] = CH_B * k;
-    ab[1] = __umul64hi(CH_B, k);
-    ab[0] += CH_A;
-    ab[1] += ab[0] < CH_A;
-    uint64_t t5[5];
-    const uint32_t tn = mulw(p3, pn, ab, trim(ab, 2), t5);
-    Node& nd = nodes[i];
-    nd.po = (uint16_t)off, nd.pn = (uint16_t)pn;
-    for (uint32_t j = 0; j < pn; j++) cur[off + j] = p3[j];
-    off += pn;
-    nd.qo = (uint16_t)off, nd.qn = (uint16_t)qn;
-    for (uint32_t j = 0; j < qn; j++) cur[off + j] = q4[j];
-    off += qn;
-    nd.to = (uint16_t)off, nd.tn = (uint16_t)tn;
-    for (uint32_t j = 0; j < tn; j++) cur[off + j] = t5[j];
-    off += tn;
-    nd.ps = true;
-    nd.ts = true;
-  }
+  uint64_t* cur = s_buf[warp][0];
+  uint64_t* nxt = s_buf[warp][1];
+  Lens* lc = s_len[warp][0];
+  Lens* ln = s_len[warp][1];
+  for (uint32_t i = lane; i < n; i += 32) lc[i] = term_values(ka + i, cur + i * slot_words(1));
+  __syncwarp();
+  uint32_t tm = 1;  // terms per full node of the current level
   while (n > 1) {
-    const uint32_t np = n / 2;
-    uint32_t o = 0;
-    for (uint32_t i = 0; i < np; i++) {
-      const Node L = nodes[2 * i];
-      const Node R = nodes[2 * i + 1];
-      Node z;
-      if (o + L.pn + R.pn + L.qn + R.qn + (L.tn + R.qn > L.pn + R.tn ? L.tn + R.qn : L.pn + R.tn) + 1 > BUF ||
-          L.tn + R.qn > TMP || L.pn + R.tn > TMP) {
-        *bad = 1;
-        return;
-      }
-      z.po = (uint16_t)o;
-      z.pn = (uint16_t)mulw(cur + L.po, L.pn, cur + R.po, R.pn, nxt + o);
-      z.ps = L.ps != R.ps;
-      o += z.pn;
-      z.qo = (uint16_t)o;
-      z.qn = (uint16_t)mulw(cur + L.qo, L.qn, cur + R.qo, R.qn, nxt + o);
-      o += z.qn;
-      const uint32_t a1 = mulw(cur + L.to, L.tn, cur + R.qo, R.qn, tq);
-      const uint32_t a2 = mulw(cur + L.po, L.pn, cur + R.to, R.tn, pt);
-      bool zs = false;
-      z.to = (uint16_t)o;
-      z.tn = (uint16_t)add_signed(tq, a1, L.ts, pt, a2, L.ps != R.ts, nxt + o, zs);
-      z.ts = zs;
-      o += z.tn;
-      next[i] = z;
+    const uint32_t np = n / 2, m2 = 2 * tm;
+    uint32_t G = 1;
+    while (G * 2 * np <= 32) G *= 2;  // lanes per pair
+    const uint32_t gi = lane / G, gl = lane % G, src0 = gi * G;
+    const unsigned gmask = G == 32 ? 0xFFFFFFFFu : ((1u << G) - 1) << src0;
+    const uint32_t si = slot_words(tm), so = slot_words(m2);
+    for (uint32_t pr = gi; pr < np; pr += 32 / G) {
+      const uint64_t* L = cur + (2 * pr) * si;
+      const uint64_t* R = L + si;
+      const Lens a = lc[2 * pr], c = lc[2 * pr + 1];
+      uint64_t* z = nxt + pr * so;
+      Lens zl;
+      zl.p = (uint16_t)grp_mul(L, a.p, R, c.p, nullptr, 0, nullptr, 0, false, z, q_at(m2), gl, G, gmask, src0, bad);
+      zl.q = (uint16_t)grp_mul(L + q_at(tm), a.q, R + q_at(tm), c.q, nullptr, 0, nullptr, 0, false, z + q_at(m2),
+                               t_at(m2) - q_at(m2), gl, G, gmask, src0, bad);
+      // |T| = |T_L| Q_R + (-1)^(m_L) |P_L| |T_R|: a left node holds tm terms
+      zl.t = (uint16_t)grp_mul(L + t_at(tm), a.t, R + q_at(tm), c.q, L, a.p, R + t_at(tm), c.t, (tm & 1) != 0,
+                               z + t_at(m2), slot_words(m2) - t_at(m2), gl, G, gmask, src0, bad);
+      if (zl.t > 3 * m2 + 2 && gl == 0) *bad = 1;
+      if (gl == 0) ln[pr] = zl;
     }
-    if (n & 1) {
-      const Node L = nodes[n - 1];
-      if (o + L.pn + L.qn + L.tn > BUF) {
-        *bad = 1;
-        return;
-      }
-      Node z = L;
-      z.po = (uint16_t)o;
-      for (uint32_t j = 0; j < L.pn; j++) nxt[o + j] = cur[L.po + j];
-      o += L.pn;
-      z.qo = (uint16_t)o;
-      for (uint32_t j = 0; j < L.qn; j++) nxt[o + j] = cur[L.qo + j];
-      o += L.qn;
-      z.to = (uint16_t)o;
-      for (uint32_t j = 0; j < L.tn; j++) nxt[o + j] = cur[L.to + j];
-      o += L.tn;
-      next[np] = z;
+    if (n & 1) {  // the odd last node moves up unchanged
+      const uint64_t* o = cur + (n - 1) * si;
+      uint64_t* z = nxt + np * so;
+      const Lens a = lc[n - 1];
+      for (uint32_t j = lane; j < a.p; j += 32) z[j] = o[j];
+      for (uint32_t j = lane; j < a.q; j += 32) z[q_at(m2) + j] = o[q_at(tm) + j];
+      for (uint32_t j = lane; j < a.t; j += 32) z[t_at(m2) + j] = o[t_at(tm) + j];
+      if (lane == 0) ln[np] = a;
     }
+    __syncwarp();
     n = np + (n & 1);
-    for (uint32_t i = 0; i < n; i++) nodes[i] = next[i];
+    tm = m2;
     uint64_t* t = cur;
     cur = nxt;
     nxt = t;
+    Lens* tl = lc;
+    lc = ln;
+    ln = tl;
   }
-  const Node r = nodes[0];
-  if (r.pn > sp || r.qn > sq || r.tn > st) {
-    *bad = 1;
+  const Lens r = lc[0];
+  if (r.p > sp || r.q > sq || r.t > st) {
+    if (lane == 0) *bad = 1;
     return;
   }
   uint64_t* slot = out + (uint64_t)leaf * (sp + sq + st);
-  for (uint32_t j = 0; j < r.pn; j++) slot[j] = cur[r.po + j];
-  for (uint32_t j = 0; j < r.qn; j++) slot[sp + j] = cur[r.qo + j];
-  for (uint32_t j = 0; j < r.tn; j++) slot[sp + sq + j] = cur[r.to + j];
-  lens[3 * leaf + 0] = r.pn;
-  lens[3 * leaf + 1] = r.qn;
-  lens[3 * leaf + 2] = r.tn;
-  signs[leaf] = (uint8_t)((r.ps ? 1 : 0) | (r.ts ? 2 : 0));
+  for (uint32_t j = lane; j < r.p; j += 32) slot[j] = cur[j];
+  for (uint32_t j = lane; j < r.q; j += 32) slot[sp + j] = cur[q_at(tm) + j];
+  for (uint32_t j = lane; j < r.t; j += 32) slot[sp + sq + j] = cur[t_at(tm) + j];
+  if (lane == 0) {
+    lens[3 * leaf + 0] = r.p;
+    lens[3 * leaf + 1] = r.q;
+    lens[3 * leaf + 2] = r.t;
+    signs[leaf] = (uint8_t)(((kb - ka) & 1 ? 1 : 0) | 2);  // static signs: P ~ (-1)^terms, T < 0
+  }
 }
 
 }  // namespace
 
 int leaves_device(uint64_t a0, uint64_t b, uint32_t m, uint32_t nleaf, uint32_t sp, uint32_t sq, uint32_t st,
                   uint64_t* d_out, uint32_t* lens, uint8_t* signs, cudaStream_t stream) {
-  if (!m || m > MAX_TERMS || !d_out || !lens || !signs || a0 < 1) return PIMUL_EINVAL;
+  // the slot bounds of k_leaves hold for terms k < 2^31
+  if (!m || m > MAX_TERMS || !d_out || !lens || !signs || a0 < 1 || b > (1ull << 31)) return PIMUL_EINVAL;
   if (!nleaf) return PIMUL_OK;
   if ((uint64_t)nleaf * m < b - a0 || (uint64_t)(nleaf - 1) * m >= b - a0) return PIMUL_EINVAL;
   uint8_t* dev = nullptr;
@@ -248,7 +241,8 @@ int leaves_device(uint64_t a0, uint64_t b, uint32_t m, uint32_t nleaf, uint32_t 
   int h_bad = 0;
   if (cudaMemsetAsync(d_bad, 0, sizeof(int), stream) != cudaSuccess) rc = PIMUL_ECUDA;
   if (!rc) {
-    k_leaves<<<(nleaf + 63) / 64, 64, 0, stream>>>(a0, b, m, nleaf, d_out, sp, sq, st, d_lens, d_signs, d_bad);
+    k_leaves<<<(nleaf + LW_WARPS - 1) / LW_WARPS, 32 * LW_WARPS, 0, stream>>>(a0, b, m, nleaf, d_out, sp, sq, st,
+                                                                            d_lens, d_signs, d_bad);
     if (cudaGetLastError() != cudaSuccess) rc = PIMUL_ECUDA;
   }
   if (!rc && (cudaMemcpyAsync(lens, d_lens, (size_t)nleaf * 3 * 4, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||

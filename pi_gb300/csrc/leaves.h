@@ -17,7 +17,8 @@ constexpr uint32_t MAX_TERMS = 64;
 // lens[3 i + 0..2] receive the trimmed lengths of |P|, Q, |T| and signs[i]
 // the signs (bit 0: P < 0, bit 1: T < 0).  Synchronous on `stream`.
 // PIMUL_EINVAL if a value outgrows its slot (nothing past a slot is
-// written) or m > MAX_TERMS.
+// written), a merge inside a leaf breaks the splitting's static signs,
+// m > MAX_TERMS or b > 2^31.
 int leaves_device(uint64_t a0, uint64_t b, uint32_t m, uint32_t nleaf, uint32_t sp, uint32_t sq, uint32_t st,
                   uint64_t* d_out, uint32_t* lens, uint8_t* signs, cudaStream_t stream);
 
