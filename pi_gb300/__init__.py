@@ -391,19 +391,31 @@ def handle_device(h: int):
     return d.value, n.value
 
 
+def _digit_buffer(n: int):
+    """An uninitialised n + 1-byte output buffer for a driver that writes n
+    digits (no zero fill of up to a gigabyte)."""
+    buf = np.empty(n + 1, dtype=np.uint8)
+    return buf, ctypes.cast(buf.ctypes.data, ctypes.c_char_p)
+
+
+def _digits_str(buf, n: int) -> str:
+    # one copy: ASCII bytes of the buffer straight into the str
+    return str(memoryview(buf)[:n], "ascii")
+
+
 def pi_chudnovsky_served(digits: int, serve_nodes: int = 0):
     """Digits of pi by Chudnovsky with the splitting tree's upper levels
     (above about serve_nodes nodes, 0: 512) submitted to the multiply service
     as chained handles (pimul_pi_chudnovsky_served).  Returns (digits_str, info)."""
-    buf = ctypes.create_string_buffer(digits + 1)
+    buf, pbuf = _digit_buffer(digits)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
     req = ctypes.c_uint64(0)
-    _check(lib().pimul_pi_chudnovsky_served(digits, buf, digits + 1, serve_nodes, ph, ctypes.byref(n),
+    _check(lib().pimul_pi_chudnovsky_served(digits, pbuf, digits + 1, serve_nodes, ph, ctypes.byref(n),
                                             ctypes.byref(req)))
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "service_requests": req.value}
-    return ctypes.string_at(buf, digits).decode("ascii"), info
+    return _digits_str(buf, digits), info
 
 
 def service_stats() -> dict:
@@ -424,15 +436,15 @@ def pi_chudnovsky(digits: int, backend=None, ntt_threshold: int = 0):
     (crates/pi-core/src/algorithm/chudnovsky.rs:75).  `backend`: address of
     a pimul_mul_fn-compatible multiply (None = the GPU engine).  Returns
     (digits_str, info) with phase times and the backend-call histogram."""
-    buf = ctypes.create_string_buffer(digits + 1)
+    buf, pbuf = _digit_buffer(digits)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
     hist = (ctypes.c_uint64 * 33)()
-    _check(lib().pimul_pi_chudnovsky(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
+    _check(lib().pimul_pi_chudnovsky(digits, pbuf, digits + 1, ctypes.c_void_p(backend) if backend else None,
                                      ntt_threshold, ph, ctypes.byref(n), hist))
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
-    return ctypes.string_at(buf, digits).decode("ascii"), info
+    return _digits_str(buf, digits), info
 
 
 def served_backend():
@@ -445,17 +457,17 @@ def pi_chudnovsky_batched(digits: int, leaf_terms: int = 0):
     """Digits of pi by Chudnovsky with the binary splitting run level by level
     through the batched GPU multiply (pimul_pi_chudnovsky_batched); same
     digits as pi_chudnovsky.  Returns (digits_str, info)."""
-    buf = ctypes.create_string_buffer(digits + 1)
+    buf, pbuf = _digit_buffer(digits)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
     lv = ctypes.c_uint64(0)
     hist = (ctypes.c_uint64 * 33)()
-    _check(lib().pimul_pi_chudnovsky_batched(digits, buf, digits + 1, leaf_terms, ph, ctypes.byref(n),
+    _check(lib().pimul_pi_chudnovsky_batched(digits, pbuf, digits + 1, leaf_terms, ph, ctypes.byref(n),
                                              ctypes.byref(lv), hist))
     info = {"binary_splitting_ms": ph[0], "final_assembly_ms": ph[1], "decimal_conversion_ms": ph[2],
             "ntt_products": n.value, "batched_levels": lv.value,
             "ntt_hist": {f"2^{L}": hist[L] for L in range(33) if hist[L]}}
-    return ctypes.string_at(buf, digits).decode("ascii"), info
+    return _digits_str(buf, digits), info
 
 
 def to_decimal(limbs, batched: bool = True) -> str:
@@ -514,13 +526,13 @@ def pi_gauss_legendre(digits: int, backend=None, ntt_threshold: int = 0, fast_sq
     square roots by a multiplication-only Newton iteration, device_decimal
     converts with the nodes on the GPU, device_agm runs the whole iteration
     on the GPU in fixed point (same digits)."""
-    buf = ctypes.create_string_buffer(digits + 1)
+    buf, pbuf = _digit_buffer(digits)
     ph = (ctypes.c_double * 3)()
     n = ctypes.c_uint64(0)
     flags = (1 if fast_sqrt else 0) | (2 if device_decimal else 0) | (4 if device_agm else 0)
-    _check(lib().pimul_pi_gauss_legendre_ex(digits, buf, digits + 1, ctypes.c_void_p(backend) if backend else None,
+    _check(lib().pimul_pi_gauss_legendre_ex(digits, pbuf, digits + 1, ctypes.c_void_p(backend) if backend else None,
                                             ntt_threshold, flags, ph, ctypes.byref(n)))
-    return ctypes.string_at(buf, digits).decode("ascii"), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
+    return _digits_str(buf, digits), {"iterations_ms": ph[0], "decimal_conversion_ms": ph[2],
                                        "ntt_products": n.value}
 
 
