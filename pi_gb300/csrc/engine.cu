@@ -859,19 +859,8 @@ __device__ void small_multiply(const SmallJob& job, bool active, int L, const Ro
   __syncthreads();
   TileGeom g{L, 0, 0};
   const int rt = active ? gtid : (1 << 30);  // an inactive group's rounds do no work
-  // lengths 2^8 .. 2^12 (G = min(2^L / 8, SMALL_THREADS) threads): rounds with
-  // compile-time geometry; shorter ones: runtime geometry
-  const unsigned act2 = active ? (square ? 1u : 3u) : 0u;
-  switch (L) {
-    case 8: group_fwd_c<8, small_group_threads(8), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
-    case 9: group_fwd_c<9, small_group_threads(9), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
-    case 10: group_fwd_c<10, small_group_threads(10), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
-    case 11: group_fwd_c<11, small_group_threads(11), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
-    case 12: group_fwd_c<12, small_group_threads(12), 2>(smA, smB, nullptr, R.w12, gtid, act2); break;
-    default:
-      tile_dft_fwd(smA, g, R, rt, G);
-      tile_dft_fwd(smB, g, R, square ? (1 << 30) : rt, G);
-  }
+  tile_dft_fwd(smA, g, R, rt, G);
+  tile_dft_fwd(smB, g, R, square ? (1 << 30) : rt, G);
   // times N^-1 = 2^(-L): with 2^96 = -1 and 2^64 = 2^32 - 1 (mod p),
   // 2^(-L) = -2^(96-L) = p - (2^(64-L) - 2^(32-L)) for 1 <= L <= 32
   const uint64_t ninv = gl::P - ((1ull << (64 - L)) - (1ull << (32 - L)));
@@ -881,14 +870,7 @@ __device__ void small_multiply(const SmallJob& job, bool active, int L, const Ro
     smA[spad(i)] = gl::mul(gl::mul(x, y), ninv);
   }
   __syncthreads();
-  switch (L) {
-    case 8: group_inv_c<8, small_group_threads(8)>(smA, R.w12, gtid, active); break;
-    case 9: group_inv_c<9, small_group_threads(9)>(smA, R.w12, gtid, active); break;
-    case 10: group_inv_c<10, small_group_threads(10)>(smA, R.w12, gtid, active); break;
-    case 11: group_inv_c<11, small_group_threads(11)>(smA, R.w12, gtid, active); break;
-    case 12: group_inv_c<12, small_group_threads(12)>(smA, R.w12, gtid, active); break;
-    default: tile_dft_inv(smA, g, R, rt, G);
-  }
+  tile_dft_inv(smA, g, R, rt, G);
   // carry: windows of 16 coefficients, one per thread (N/16 <= G)
   const uint32_t nwin = (n_out + 15) / 16, nl = la + lb;
   uint64_t* sH = smB;  // reuse: B no longer needed
