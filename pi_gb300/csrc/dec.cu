@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -296,7 +297,10 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
   std::vector<pimul_job> jobs;
   std::vector<pimul_addsub_job> aj;
   std::vector<uint8_t> hflag;
+  const bool timing = getenv("PIMUL_PI_TIMING") != nullptr;
   for (int k = K - 1; k >= LEAF_K && !rc; k--) {
+    const double tl0 = timing ? now_ms() : 0;
+    double tl_launch = 0;
     const Level& L = lv[k];
     const uint64_t* dP = dPk[k];
     const uint64_t* dV = dVk[k];
@@ -325,6 +329,7 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
                                PIMUL_SUB_MOD};
     if ((rc = pimul_addsub_batch(aj.data(), n, st))) break;
     A.put(qp);
+    if (timing) tl_launch = now_ms() - tl0;
     // while r >= P: r -= P, q += 1
     unsigned long long* top = nullptr;
     uint8_t* flag = nullptr;
@@ -362,6 +367,9 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
     A.put(flag);
     A.put(count);
     A.put(cur);
+    if (timing)
+      fprintf(stderr, "[pimul]   conversion level %d: %zu nodes of %zu limbs, %.1f ms (products and subtraction queued in %.1f)\n",
+              k, n, w_in, now_ms() - tl0, tl_launch);
     cur = nxt;
     n *= 2;
     w_in = w;

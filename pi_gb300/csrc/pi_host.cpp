@@ -2711,7 +2711,9 @@ static int chudnovsky(uint64_t digits, char* out, size_t cap, pimul_mul_fn backe
   ctx.backend = reinterpret_cast<mul_fn>(backend);
   ctx.ntt_threshold = ntt_threshold ? ntt_threshold : 8192;
   ctx.serve_nodes = serve_nodes;
+  const double t0 = now_ms();
   int rc = with_ctx(ctx, [&] { return chudnovsky_body(digits, out, leaf_terms, phase_ms, ntt_products, ntt_hist33); });
+  if (getenv("PIMUL_PI_TIMING")) fprintf(stderr, "[pimul] driver call %.1f ms\n", now_ms() - t0);
   if (levels) *levels = ctx.batch_levels.load();
   if (served_requests) *served_requests = ctx.served_requests;
   return rc;
