@@ -1858,8 +1858,15 @@ struct BatchLayout {
   size_t small_smem = 0;           // dynamic shared memory of their CTAs
 };
 
-// Scratch bound of one group of same-length descriptors in a batch.
-static const uint64_t BATCH_ARENA_CAP = 4ull << 30;
+// Scratch bound of one group of same-length descriptors in a batch.  Only
+// the descriptors of one group share spectra, so a group should hold every
+// product of a splitting level's pairs: at the top of a 10^9-digit tree one
+// pair's products take 32 GiB at 2^29 points.  PIMUL_BATCH_ARENA_GIB sets it.
+static const uint64_t BATCH_ARENA_CAP = [] {
+  const char* e = getenv("PIMUL_BATCH_ARENA_GIB");
+  const long long g = e ? atoll(e) : 96;
+  return (uint64_t)(g > 0 ? g : 96) << 30;
+}();
 
 static int unit_log_n(const Unit& u) {
   if (u.la == 0 || u.lb == 0) return -1;
