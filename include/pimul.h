@@ -165,6 +165,23 @@ typedef struct pimul_sum_job {
 } pimul_sum_job;
 int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream);
 
+/*
+ * pimul_sum_batch with options.  PIMUL_BATCH_WRAP: a job of 2^20 points or
+ * more whose coefficients fill at most 5/8 of its transform (and whose
+ * operands each fit half of it) runs as a cyclic product of half the length:
+ * its top coefficients (at most 2^(L-4) of them) wrap onto the bottom ones
+ * and are separated again with the exact low coefficients, from a short
+ * product of the operands' low limbs computed first.  Same results as
+ * pimul_sum_batch, about half the work for such jobs (the top levels of a
+ * 10^9-digit splitting tree run at 51-54 % fill).  Used by the batched pi
+ * drivers; the plain drop-in keeps the reference's transform length.
+ * This engine's own option; no counterpart in the reference (its
+ * mul_mag_ntt, crates/bignum/src/ntt.rs:810-813, always takes the next
+ * power of two).
+ */
+#define PIMUL_BATCH_WRAP 1u
+int pimul_sum_batch_ex(const pimul_sum_job* jobs, size_t n, void* stream, unsigned flags);
+
 /* Trimmed lengths (highest nonzero limb + 1) of n device limb arrays of
  * lengths lens[i]; out_lens on the host.  Synchronous. */
 int pimul_top_limbs(const uint64_t* const* arrays, const size_t* lens, size_t n, size_t* out_lens, void* stream);

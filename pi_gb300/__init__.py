@@ -68,6 +68,7 @@ def load(build_if_stale: bool = True):
     L.pimul_mul_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
     L.pimul_addsub_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
     L.pimul_sum_batch.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p]
+    L.pimul_sum_batch_ex.argtypes = [ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_uint]
     L.pimul_top_limbs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]
     L.pimul_batch_plan_create.argtypes = [ctypes.POINTER(_sz), ctypes.POINTER(_sz), _sz, ctypes.POINTER(ctypes.c_void_p)]
     L.pimul_batch_plan_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p]
@@ -194,10 +195,12 @@ class SumJob(ctypes.Structure):
                 ("out", ctypes.c_void_p), ("nout", _sz)]
 
 
-def sum_batch(jobs, stream=None):
+def sum_batch(jobs, stream=None, wrap=False):
     """out = a1 * b1 + a2 * b2 for torch CUDA uint64/int64 tensors:
     jobs = [(a1, b1, a2, b2, out)] (a2, b2 may be None), over out.numel()
-    limbs (pimul_sum_batch; asynchronous on the current torch stream)."""
+    limbs (pimul_sum_batch; asynchronous on the current torch stream).
+    wrap=True: pimul_sum_batch_ex with PIMUL_BATCH_WRAP (half-full long
+    transforms run as cyclic products of half the length)."""
     arr = (SumJob * max(len(jobs), 1))()
 
     def ptr(t):
@@ -208,7 +211,10 @@ def sum_batch(jobs, stream=None):
     if stream is None and jobs:
         import torch
         stream = torch.cuda.current_stream(jobs[0][4].device).cuda_stream
-    _check(lib().pimul_sum_batch(arr, len(jobs), ctypes.c_void_p(stream) if stream else None))
+    if wrap:
+        _check(lib().pimul_sum_batch_ex(arr, len(jobs), ctypes.c_void_p(stream) if stream else None, 1))
+    else:
+        _check(lib().pimul_sum_batch(arr, len(jobs), ctypes.c_void_p(stream) if stream else None))
 
 
 def top_limbs(arrays, stream=None):

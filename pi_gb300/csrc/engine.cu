@@ -195,8 +195,15 @@ struct Job {
   uint8_t* aux; // carry-scan flags
   uint64_t la, lb;
   const uint64_t* X;  // spectrum added to the pointwise product (a sum of two products), or null
-  uint64_t nout;      // output limbs (0: la + lb)
+  uint64_t nout;      // output limbs (0: la + lb); with JF_COEFF, output coefficients
   uint32_t flags;     // JF_* roles inside a batch (0: a plain product)
+  // A wrapped product runs a cyclic transform of length N shorter than its
+  // wrap + N coefficients: coefficient N + i (i < wrap) lands on i.  low
+  // holds the exact coefficients 0 .. wrap - 1 (from a short product of the
+  // operands' low limbs), so that coefficient i is low[i] and N + i the
+  // cyclic value minus low[i].
+  const uint64_t* low;
+  uint64_t wrap;
 };
 
 // Roles of a product inside a batch.  A spectrum shared by several products
@@ -208,6 +215,9 @@ struct Job {
 constexpr uint32_t JF_B_SHARED = 1;
 constexpr uint32_t JF_B_FULL = 2;
 constexpr uint32_t JF_ADDEND = 4;
+// The product's canonical coefficients 0 .. nout - 1 go to out (no carry):
+// the low part of a wrapped product.
+constexpr uint32_t JF_COEFF = 8;
 
 __device__ __forceinline__ Job job_of(const Job* jobs, const Job& one) {
   if (jobs) return jobs[blockIdx.y];
@@ -614,14 +624,41 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
     };
     tile_inv_t<R, T, 0, PASS_THREADS, rp_count(R) - 1>(sm, tw, tid, ptw);
   }
+  const bool coeff = (J.flags & JF_COEFF) != 0;
+  const uint64_t wtop = (1ull << L) >> 3;  // a wrapped product's windows past the transform: w + wtop
   for (uint32_t q = tid; q < (1u << (TILE_LOG - 3)); q += PASS_THREADS) {
     uint32_t i = q >> (T - 3), k = q & ((1u << (T - 3)) - 1);
     uint64_t w = ((((uint64_t)i << S) + j0) >> 3) + k;
-    if (w >= nwin) continue;
     uint64_t c[8];
     uint32_t b = (i << T) + 8 * k;
 #pragma unroll
     for (int t = 0; t < 8; t++) c[t] = gl::canon(sm[spad(b + t)]);
+    if (coeff) {
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+        if (8 * w + t < nlimbs) out[8 * w + t] = c[t];
+      continue;
+    }
+    if (w >= nwin) continue;
+    if (J.wrap) {
+      // coefficient 8w + t: low[8w + t] below wrap; N + 8w + t: the rest of the cyclic value
+      uint64_t d[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const uint64_t pos = 8 * w + t;
+        const uint64_t lo = pos < J.wrap ? J.low[pos] : c[t];
+        d[t] = c[t] - lo;
+        c[t] = lo;
+      }
+      const uint64_t w2 = w + wtop;
+      if (w2 < nwin) {
+        const Win2 v2 = fold8(d);
+#pragma unroll
+        for (int t = 0; t < 2; t++)
+          if (2 * w2 + t < nlimbs) out[2 * w2 + t] = v2.l[t];
+        H[w2] = v2.hi;
+      }
+    }
     Win2 v = fold8(c);
 #pragma unroll
     for (int t = 0; t < 2; t++)
@@ -635,7 +672,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_inv_first_carry
 // masks, per CTA the chunk's carry out for carry in 0 and 1.
 __global__ void __launch_bounds__(CARRY_THREADS) k_carry_local(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  if (J.flags & JF_ADDEND) return;
+  if (J.flags & (JF_ADDEND | JF_COEFF)) return;
   const uint64_t nlimbs = job_nout(J), nwin = n_windows_out(nlimbs), nchunk = n_chunks(nwin);
   if (blockIdx.x >= nchunk) return;  // uniform per CTA
   uint64_t* __restrict__ out = J.out;
@@ -700,7 +737,7 @@ __device__ __forceinline__ uint32_t cf_then(uint32_t first, uint32_t then) {
 // and each thread writes its run's carries in.
 __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  if (J.flags & JF_ADDEND) return;
+  if (J.flags & (JF_ADDEND | JF_COEFF)) return;
   const uint64_t nchunk = n_chunks(n_windows_out(job_nout(J)));
   const uint8_t* chunk_gp = J.aux + nchunk * (CARRY_THREADS / 32) * 8;  // 64-byte aligned
   uint8_t* chunk_cin = const_cast<uint8_t*>(chunk_gp) + nchunk;
@@ -750,7 +787,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_carry_scan(const Job* jobs, Jo
 // Carry pass 3: add the incoming carry to every window that receives one.
 __global__ void __launch_bounds__(CARRY_THREADS) k_carry_apply(const Job* jobs, Job one) {
   const Job J = job_of(jobs, one);
-  if (J.flags & JF_ADDEND) return;
+  if (J.flags & (JF_ADDEND | JF_COEFF)) return;
   const uint64_t nlimbs = job_nout(J), nwin = n_windows_out(nlimbs), nchunk = n_chunks(nwin);
   if (blockIdx.x >= nchunk) return;
   uint64_t* __restrict__ out = J.out;
@@ -779,7 +816,7 @@ constexpr int SMALL_THREADS = 256;
 constexpr int SMALL_LOG_MAX = 12;
 
 // Dynamic shared memory of the one-CTA multiply for N = 2^L (two padded arrays).
-static inline size_t small_smem_bytes(int L) { return 2 * (((size_t)1 << L) * 17 / 16) * 8; }
+__host__ __device__ __forceinline__ size_t small_smem_bytes(int L) { return 2 * (((size_t)1 << L) * 17 / 16) * 8; }
 
 struct SmallJob {
   const uint64_t* a;
@@ -791,7 +828,7 @@ struct SmallJob {
 // Threads per product: an eighth of the transform length (one radix-8
 // butterfly per thread and round), at least a warp; SMALL_THREADS / G
 // products of one length run side by side in a CTA.
-__host__ __device__ __forceinline__ constexpr int small_group_threads(int L) {
+__host__ __device__ __forceinline__ int small_group_threads(int L) {
   const int g = (1 << L) / 8;
   return g < 32 ? 32 : (g > SMALL_THREADS ? SMALL_THREADS : g);
 }
@@ -1832,6 +1869,10 @@ struct Unit {
   uint64_t lb2;
   uint64_t* out;
   uint64_t nout;
+  int forceL = 0;                 // transform length (log2) when not the one nout implies
+  bool coeff = false;             // JF_COEFF: nout canonical coefficients to out, no carry
+  const uint64_t* low = nullptr;  // a wrapped product's low coefficients (Job::low)
+  uint64_t wrap = 0;              // and their count (Job::wrap)
 };
 
 struct BatchLayout {
@@ -1870,6 +1911,7 @@ static const uint64_t BATCH_ARENA_CAP = [] {
 
 static int unit_log_n(const Unit& u) {
   if (u.la == 0 || u.lb == 0) return -1;
+  if (u.forceL) return u.forceL;
   return log2_ceil(4 * u.nout - 1);
 }
 
@@ -2026,8 +2068,10 @@ static void fill_descriptors(const Unit* units, const BatchLayout& B, uint8_t* a
       J.a = u.a, J.la = u.la, J.b = u.b, J.lb = u.lb;
       J.out = u.out;
       J.nout = u.nout;
+      J.low = u.low;
+      J.wrap = u.wrap;
     }
-    J.flags = d.flags;
+    J.flags = d.flags | (!d.second && u.coeff ? JF_COEFF : 0);
     const bool sq = !d.second && u.a == u.b && u.la == u.lb;
     J.A = reinterpret_cast<uint64_t*>(arena + d.off_a);
     if (d.flags & JF_B_SHARED)
@@ -3247,12 +3291,71 @@ int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
   return rc;
 }
 
+// Wrapped products (PIMUL_BATCH_WRAP): a unit of 2^20 points or more whose
+// coefficients fill at most 5/8 of its transform, with every operand within
+// half of it, runs as a cyclic product of half the length; the coefficients
+// that wrap around (wrap of them, at most an eighth of the half length) are
+// separated again with the exact low coefficients of the product, from a
+// short product of the operands' low limbs computed first (coefficients
+// out, no carry).  Returns the units' low parts in `low` and the words they
+// need in *low_words (pointers set by the caller before the runs).
+struct WrapPlan {
+  std::vector<Unit> low;      // the short products, in the order of the wrapped units
+  std::vector<size_t> which;  // the wrapped units
+  uint64_t words = 0;
+};
+
+static WrapPlan plan_wraps(std::vector<Unit>& units) {
+  WrapPlan W;
+  for (size_t i = 0; i < units.size(); i++) {
+    Unit& u = units[i];
+    if (u.coeff || u.forceL || !u.la || !u.lb) continue;
+    const int L = log2_ceil(4 * u.nout - 1);
+    if (L < 20 || L > 32) continue;
+    const uint64_t Nw = 1ull << (L - 1);
+    const uint64_t n1 = 4 * (u.la + u.lb), n2 = u.la2 ? 4 * (u.la2 + u.lb2) : 0;
+    const uint64_t ncoef = std::max(n1, n2) - 1;
+    if (ncoef <= Nw || ncoef - Nw > Nw / 4) continue;
+    if (4 * u.la > Nw || 4 * u.lb > Nw || 4 * u.la2 > Nw || 4 * u.lb2 > Nw) continue;
+    const uint64_t m = ncoef - Nw, ml = (m + 3) / 4;  // wrapped coefficients; limbs holding them
+    Unit lo{};
+    lo.a = u.a, lo.la = std::min(u.la, ml), lo.b = u.b, lo.lb = std::min(u.lb, ml);
+    if (u.la2) lo.a2 = u.a2, lo.la2 = std::min(u.la2, ml), lo.b2 = u.b2, lo.lb2 = std::min(u.lb2, ml);
+    const uint64_t nl = std::max(4 * (lo.la + lo.lb), lo.la2 ? 4 * (lo.la2 + lo.lb2) : 0) - 1;
+    lo.forceL = std::max(SMALL_LOG_MAX + 1, log2_ceil(nl));
+    lo.coeff = true;
+    lo.nout = m;
+    W.low.push_back(lo);
+    W.which.push_back(i);
+    u.forceL = L - 1;
+    u.wrap = m;
+    W.words += round_up_u64(m, 32);
+  }
+  return W;
+}
+
+static int sum_batch_impl(const pimul_sum_job* jobs, size_t n, cudaStream_t st, bool allow_wrap);
+
 int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream) {
-  if (n && !jobs) return fail(PIMUL_EINVAL, "null job list");
   cudaStream_t st;
   int rc = get_stream(&st);
   if (rc) return rc;
   if (stream) st = (cudaStream_t)stream;
+  return sum_batch_impl(jobs, n, st, false);
+}
+
+int pimul_sum_batch_ex(const pimul_sum_job* jobs, size_t n, void* stream, unsigned flags) {
+  if (flags & ~PIMUL_BATCH_WRAP) return fail(PIMUL_EINVAL, "unknown batch flags");
+  cudaStream_t st;
+  int rc = get_stream(&st);
+  if (rc) return rc;
+  if (stream) st = (cudaStream_t)stream;
+  return sum_batch_impl(jobs, n, st, (flags & PIMUL_BATCH_WRAP) != 0);
+}
+
+static int sum_batch_impl(const pimul_sum_job* jobs, size_t n, cudaStream_t st, bool allow_wrap) {
+  int rc = PIMUL_OK;
+  if (n && !jobs) return fail(PIMUL_EINVAL, "null job list");
   // fused sums go to the pass pipeline; a sum of short products (or with a
   // square) is two products into scratch and one batched addition
   std::vector<Unit> units;
@@ -3306,7 +3409,28 @@ int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream) {
     cudaError_t e = cudaMemsetAsync(z.first, 0, z.second * 8, st);
     if (e != cudaSuccess && !rc) rc = fail(PIMUL_ECUDA, std::string("sum batch: ") + cudaGetErrorString(e));
   }
+  // wrapped units: their low coefficients first, into one buffer
+  uint64_t* lowbuf = nullptr;
+  if (!rc && allow_wrap) {
+    WrapPlan W = plan_wraps(units);
+    if (!W.low.empty()) {
+      cudaError_t e = cudaMallocAsync((void**)&lowbuf, W.words * 8, g_dev.pool, st);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(PIMUL_ENOMEM, std::string("wrapped products: ") + cudaGetErrorString(e));
+      } else {
+        uint64_t off = 0;
+        for (size_t k = 0; k < W.low.size(); k++) {
+          W.low[k].out = lowbuf + off;
+          units[W.which[k]].low = lowbuf + off;
+          off += round_up_u64(W.low[k].nout, 32);
+        }
+        rc = run_units(W.low.data(), W.low.size(), st, true);
+      }
+    }
+  }
   if (!rc) rc = run_units(units.data(), units.size(), st, true);
+  if (lowbuf) cudaFreeAsync(lowbuf, st);
   if (!rc && !aj.empty()) {
     cudaError_t e = cudaMemsetAsync(tmp, 0, sizeof(int), st);
     if (e == cudaSuccess) rc = addsub_launch(aj.data(), aj.size(), st, reinterpret_cast<int*>(tmp), false);

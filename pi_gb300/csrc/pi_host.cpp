@@ -1592,6 +1592,14 @@ static void dev_free(DLevel& L, cudaStream_t st) {
   L.nodes.clear();
 }
 
+// The level products' batch option: long products that would half fill
+// their transform run as wrapped cyclic products (PIMUL_BATCH_WRAP);
+// PIMUL_PI_WRAP=0 turns it off.
+static unsigned wrap_flags() {
+  const char* e = getenv("PIMUL_PI_WRAP");
+  return (!e || atoi(e) != 0) ? PIMUL_BATCH_WRAP : 0u;
+}
+
 // Levels until one node is left; keep_p keeps P of the last node (needed
 // when it is merged again later).
 static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1) {
@@ -1683,7 +1691,7 @@ static int dev_reduce(DLevel& Lv, cudaStream_t st, bool keep_p, size_t stop = 1)
     for (int L2 = 0; L2 < 33; L2++)
       if (hist[L2]) C().ntt_hist[L2].fetch_add(hist[L2], std::memory_order_relaxed);
     double t1 = now_ms();
-    if (!rc) rc = pimul_sum_batch(sj.data(), sj.size(), st);
+    if (!rc) rc = pimul_sum_batch_ex(sj.data(), sj.size(), st, wrap_flags());
     const double t_sum = now_ms();
     if (!rc && !aj.empty()) rc = pimul_addsub_batch(aj.data(), aj.size(), st);
     const double t_as = now_ms();
@@ -1868,7 +1876,7 @@ static int dev_root_truncated(DLevel& Lv, cudaStream_t st, uint64_t top_limbs, D
     sj.push_back(pimul_sum_job{L.p + dx2, L.pn - dx2, R.t + dy2, R.tn - dy2, nullptr, 0, nullptr, 0, tmp + n1, n2});
   }
   C().ntt_calls.fetch_add(3, std::memory_order_relaxed);
-  rc = pimul_sum_batch(sj.data(), sj.size(), st);
+  rc = pimul_sum_batch_ex(sj.data(), sj.size(), st, wrap_flags());
   if (!rc && diff) {
     pimul_addsub_job aj{tmp, n1, tmp + n1, n2, z.t, tn, 1};
     rc = pimul_addsub_batch(&aj, 1, st);

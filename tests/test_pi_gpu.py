@@ -144,3 +144,14 @@ def test_merged_splitting_levels_match_batched_levels(digits, leaf, monkeypatch)
     merged, info = pm.pi_chudnovsky_batched(digits, leaf)
     assert merged == plain
     assert merged[:100_000] == ref[:min(digits, 100_000)]
+
+
+def test_1e9_digits_batched_match_recorded_hash():
+    # the top levels of a 10^9-digit tree run wrapped products (cyclic
+    # transforms of half the length, PIMUL_BATCH_WRAP); the digits must be
+    # the recorded ones, on which Chudnovsky and the Gauss-Legendre AGM agree
+    with open(os.path.join(HERE, "golden", "pi_digits_hashes.json")) as f:
+        want = json.load(f)["1000000000"]
+    s, info = pm.pi_chudnovsky_batched(1_000_000_000)
+    assert s[-20:] == want["last20"]
+    assert hashlib.sha256(s.encode()).hexdigest() == want["sha256"]

@@ -97,3 +97,50 @@ def test_sum_sharing_b_with_a_product():
         torch.cuda.synchronize()
         assert _val(oq) == ql * qr
         assert _val(ot) == tl * qr + pl * tr
+
+
+def test_wrapped_products_and_sums_match_unwrapped():
+    # PIMUL_BATCH_WRAP: jobs whose coefficients fill at most 5/8 of their
+    # transform run as cyclic products of half the length plus a short
+    # product of the low limbs; results must equal the plain batch's (and
+    # Python's for the smaller shapes).  Shapes: just past 2^20 and 2^22
+    # coefficients, a fused sum, two products sharing b, a square, all-ones
+    # operands (largest coefficients and carries), and one job too full to wrap.
+    import torch
+    rng = np.random.default_rng(21)
+    ones = (1 << (64 * 140000)) - 1
+    b_shared = _rand(rng, 135000)
+    sq = _rand(rng, 140000)
+    specs = [  # (a1, b1, a2, b2, check with Python)
+        (_rand(rng, 140000), _rand(rng, 140000), 0, 0, True),
+        (_rand(rng, 140000), _rand(rng, 135000), _rand(rng, 100000), _rand(rng, 170000), True),
+        (_rand(rng, 150000), b_shared, 0, 0, True),
+        (_rand(rng, 145000), b_shared, 0, 0, False),
+        (sq, sq, 0, 0, True),
+        (ones, ones, 0, 0, True),
+        (_rand(rng, 550000), _rand(rng, 560000), 0, 0, False),
+        (_rand(rng, 200000), _rand(rng, 200000), 0, 0, False),
+    ]
+    tens = {}
+
+    def t(v):
+        if id(v) not in tens:
+            tens[id(v)] = _t(v)
+        return tens[id(v)]
+
+    def lim(v):
+        return (v.bit_length() + 63) // 64
+
+    plain, wrapped = [], []
+    for a1, b1, a2, b2, _ in specs:
+        n = max(lim(a1) + lim(b1), lim(a2) + lim(b2)) + (1 if a2 else 0)
+        for dst in (plain, wrapped):
+            out = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+            dst.append((t(a1), t(b1), t(a2) if a2 else None, t(b2) if a2 else None, out))
+    pm.sum_batch(plain)
+    pm.sum_batch(wrapped, wrap=True)
+    torch.cuda.synchronize()
+    for (a1, b1, a2, b2, check), p, w in zip(specs, plain, wrapped):
+        assert torch.equal(p[4], w[4]), (lim(a1), lim(b1), lim(a2), lim(b2))
+        if check:
+            assert _val(w[4]) == a1 * b1 + a2 * b2
