@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimul.so")
 
 SOURCES = ["engine.cu", "bbp.cu", "dec.cu", "leaves.cu", "agm.cu", "hexconv.cu", "pi_host.cpp"]
-HEADERS = ["gl.cuh", "ntt_kernels.cuh", "dec.h", "hostcopy.h", "leaves.h", "agm.h", "splitmerge.h"]
+HEADERS = ["gl.cuh", "ntt_kernels.cuh", "dec.h", "hostcopy.h", "leaves.h", "agm.h", "splitmerge.h", "wrapmul.h"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -31,6 +31,7 @@
 #include "agm.h"
 #include "dec.h"
 #include "hostcopy.h"
+#include "wrapmul.h"
 
 namespace piagm {
 namespace {
@@ -123,7 +124,7 @@ struct Agm {
     n_mul++;
     if (m == nf) n_full++;
     const size_t off = nf - m;
-    rc = pimul_mul_device(x + off, m + 1, y + off, m + 1, tmp, st);
+    rc = pimul::mul_wrapped(x + off, m + 1, y + off, m + 1, tmp, st);
     if (rc) return;
     if (off) cu(cudaMemsetAsync(z, 0, off * 8, st));
     cu(cudaMemcpyAsync(z + off, tmp + m, (m + 1) * 8, cudaMemcpyDeviceToDevice, st));
@@ -256,7 +257,7 @@ int agm_device(uint64_t prec, AgmOut* out, double* ms) {
     G.absdiff(a, an, d);
     const size_t lsq = G.trimmed(d, W);
     if (lsq && 2 * lsq > nf) {
-      if (!G.rc) G.rc = pimul_mul_device(d, lsq, d, lsq, tmp, G.st);
+      if (!G.rc) G.rc = pimul::mul_wrapped(d, lsq, d, lsq, tmp, G.st);
       G.shift(tmp, 2 * lsq, 64 * (int64_t)nf - it, u, W);  // (a - a')^2 2^it at nf fraction limbs
       G.addsub(t, u, t, 1);
     }
@@ -271,7 +272,7 @@ int agm_device(uint64_t prec, AgmOut* out, double* ms) {
   }
   // (a + b)^2 at 2 nf fraction limbs, t at nf
   G.addsub(a, b, u, 0);
-  if (!G.rc) G.rc = pimul_mul_device(u, W, u, W, tmp, G.st);
+  if (!G.rc) G.rc = pimul::mul_wrapped(u, W, u, W, tmp, G.st);
   uint64_t* num = nullptr;
   uint64_t* den = nullptr;
   if (!G.rc && (cudaMalloc((void**)&num, 2 * W * 8) != cudaSuccess || cudaMalloc((void**)&den, W * 8) != cudaSuccess)) {
@@ -310,7 +311,7 @@ int pow5(Agm& G, uint64_t e, DevNum* out) {
   const int nb = e ? 64 - __builtin_clzll(e) : 0;
   for (int i = nb - 2; i >= 0 && !G.rc; i--) {
     if (2 * L + 1 > cap) return G.rc = PIMUL_EINVAL;  // not reached: cap bounds 5^e with room
-    G.rc = pimul_mul_device(A, L, A, L, B, G.st);  // a square (same operand)
+    G.rc = pimul::mul_wrapped(A, L, A, L, B, G.st);  // a square (same operand)
     size_t L2 = 2 * L;
     if ((e >> i) & 1) {
       G.mul_word(B, L2, 5, A, lo, hi);
@@ -409,7 +410,7 @@ int chudnovsky_w_device(uint64_t digits, uint64_t prec, DevNum* out, double* ms)
   }
   const size_t full = W + 1 + p5.limbs, keep = std::min(full, nf + 2);
   uint64_t* prod = G.alloc(full);
-  if (!G.rc) G.rc = pimul_mul_device(s, W + 1, p5.mant, p5.limbs, prod, G.st);
+  if (!G.rc) G.rc = pimul::mul_wrapped(s, W + 1, p5.mant, p5.limbs, prod, G.st);
   uint64_t* m = nullptr;
   if (!G.rc && cudaMalloc((void**)&m, keep * 8) != cudaSuccess) {
     cudaGetLastError();

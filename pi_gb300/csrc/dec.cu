@@ -38,6 +38,7 @@
 #include "../../include/pimul.h"
 #include "dec.h"
 #include "hostcopy.h"
+#include "wrapmul.h"
 
 namespace pidec {
 namespace {
@@ -401,19 +402,6 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
 }
 
 
-// ---------------------------------------------------------- wrapped products
-namespace {
-// pimul_mul_device's product (la + lb limbs at out) through the batch with
-// PIMUL_BATCH_WRAP: a long product that would half fill its transform runs
-// as a cyclic product of half the length (the final assembly's Newton steps
-// and products sit at about 58 % at 10^9 digits).
-int mul_wrapped(const uint64_t* a, size_t la, const uint64_t* b, size_t lb, uint64_t* out, cudaStream_t st) {
-  if (!la || !lb) return pimul_mul_device(a, la, b, lb, out, st);
-  const pimul_sum_job j{a, la, b, lb, nullptr, 0, nullptr, 0, out, la + lb};
-  return pimul_sum_batch_ex(&j, 1, st, PIMUL_BATCH_WRAP);
-}
-}  // namespace
-
 // ---------------------------------------------------------- final assembly
 // pi 10^(D-1) = W Q / (A Q - |T|) with W = 426880 sqrt(10005) 10^(D-1)
 // (chudnovsky.rs:146-204 followed by util.rs:25-83's scaling), from the
@@ -503,12 +491,12 @@ static int recip_newton(Arena& Ar, const uint64_t* dnorm, size_t nl, uint64_t** 
     const uint64_t* Dc = dnorm + (nl - mp);
     uint64_t *Pr = nullptr, *E = nullptr, *YE = nullptr, *Yn = nullptr;
     if ((rc = Ar.get(&Pr, mp + m + 1)) || (rc = Ar.get(&E, mp + 1))) break;
-    if ((rc = mul_wrapped(Dc, mp, Y, m + 1, Pr, st))) break;
+    if ((rc = pimul::mul_wrapped(Dc, mp, Y, m + 1, Pr, st))) break;
     pimul_addsub_job je{nullptr, 0, Pr, mp + 1, E, mp + 1, PIMUL_SUB_MOD};  // E = 2^(h+c) - Pr
     if ((rc = pimul_addsub_batch(&je, 1, st))) break;
     Ar.put(Pr);
     if ((rc = Ar.get(&YE, m + mp + 2)) || (rc = Ar.get(&Yn, mp + 1))) break;
-    if ((rc = mul_wrapped(Y, m + 1, E, mp + 1, YE, st))) break;
+    if ((rc = pimul::mul_wrapped(Y, m + 1, E, mp + 1, YE, st))) break;
     if (mp > m) cu(cudaMemsetAsync(Yn, 0, (mp - m) * 8, st));
     cu(cudaMemcpyAsync(Yn + (mp - m), Y, (m + 1) * 8, cudaMemcpyDeviceToDevice, st));
     if (rc) break;
@@ -612,7 +600,7 @@ static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_
   // ip = floor(W N_top R 2^e2)
   uint64_t *X1 = nullptr, *X2 = nullptr, *dW = nullptr;
   if ((rc = Ar.get(&X1, lq + nl + 1))) return rc;
-  if ((rc = mul_wrapped(n_top, lq, Y, nl + 1, X1, st))) return rc;
+  if ((rc = pimul::mul_wrapped(n_top, lq, Y, nl + 1, X1, st))) return rc;
   Ar.put(Y);
   const uint64_t* Wd = wm;
   if (!w_dev) {
@@ -620,7 +608,7 @@ static int quotient_tail(Arena& Ar, const uint64_t* den, size_t wn, int64_t den_
     Wd = dW;
   }
   if ((rc = Ar.get(&X2, wl + nl + 1))) return rc;
-  if ((rc = mul_wrapped(Wd, wl, X1 + lq, nl + 1, X2, st))) return rc;
+  if ((rc = pimul::mul_wrapped(Wd, wl, X1 + lq, nl + 1, X2, st))) return rc;
   // W N / D ~ X2 2^(64 lq) * 2^(we + n_exp - 128 nl - ed)
   const int64_t e2 = we + 64 * (int64_t)lq + n_exp - 128 * (int64_t)nl - ed;
   const int64_t ip_bits = 64 * (int64_t)(wl + nl + 1) + e2;
