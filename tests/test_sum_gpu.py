@@ -120,6 +120,9 @@ def test_wrapped_products_and_sums_match_unwrapped():
         (ones, ones, 0, 0, True),
         (_rand(rng, 550000), _rand(rng, 560000), 0, 0, False),
         (_rand(rng, 200000), _rand(rng, 200000), 0, 0, False),
+        # 3 wrapped coefficients; the largest wrap allowed (2^18 - 1 of 2^20)
+        (_rand(rng, 131073), _rand(rng, 131072), 0, 0, True),
+        (_rand(rng, 163840), _rand(rng, 163840), 0, 0, True),
     ]
     tens = {}
 
