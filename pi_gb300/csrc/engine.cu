@@ -1413,13 +1413,27 @@ static StageBuf* stage_acquire() {
   int dev = 0;
   cudaGetDevice(&dev);
   {
+    // a free buffer whose last copies are done, else (up to four buffers
+    // per device) a new one, else any free one: the caller would wait for
+    // a busy buffer's copies, i.e. for the work queued before them
     std::lock_guard<std::mutex> lk(g_stage_mu);
-    for (size_t i = 0; i < g_stage_free.size(); i++)
-      if (g_stage_free[i]->device == dev) {
-        StageBuf* b = g_stage_free[i];
+    int any = -1, mine = 0;
+    for (StageBuf* x : g_stage_all) mine += x->device == dev;
+    for (size_t i = 0; i < g_stage_free.size(); i++) {
+      StageBuf* x = g_stage_free[i];
+      if (x->device != dev) continue;
+      if (any < 0) any = (int)i;
+      if (cudaEventQuery(x->ev[0]) == cudaSuccess && cudaEventQuery(x->ev[1]) == cudaSuccess) {
         g_stage_free.erase(g_stage_free.begin() + i);
-        return b;
+        return x;
       }
+    }
+    cudaGetLastError();  // cudaEventQuery's cudaErrorNotReady
+    if (any >= 0 && mine >= 4) {
+      StageBuf* x = g_stage_free[any];
+      g_stage_free.erase(g_stage_free.begin() + any);
+      return x;
+    }
   }
   StageBuf* b = new StageBuf;
   b->device = dev;
@@ -1444,6 +1458,24 @@ static void stage_release(StageBuf* b) {
   g_stage_free.push_back(b);
 }
 
+// Uploads below STAGE_MIN from pageable memory go through a ring of small
+// pinned slots: a plain cudaMemcpyAsync from pageable memory synchronises
+// its stream first, so every batch call (its descriptor image) would wait
+// for the work already queued instead of preparing the next launch.
+constexpr int RING_SLOTS = 16;
+struct SmallRing {
+  std::mutex mu;
+  void* h[RING_SLOTS] = {};
+  cudaEvent_t ev[RING_SLOTS] = {};  // the last copy from each slot
+  int next = 0;
+  int device = -1;
+  bool ok = false;
+};
+static SmallRing& small_ring() {
+  static SmallRing* r = new SmallRing;  // pinned slots live until exit
+  return *r;
+}
+
 static bool is_pageable(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -1453,9 +1485,50 @@ static bool is_pageable(const void* p) {
   return a.type == cudaMemoryTypeUnregistered;
 }
 
+// A small pageable upload through the ring; false when the ring cannot be
+// set up (the caller then copies directly).
+static bool ring_upload(void* dst, const void* src, size_t bytes, cudaStream_t st, cudaError_t* err) {
+  SmallRing& r = small_ring();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(r.mu);
+  if (r.device != dev) {
+    if (r.device >= 0) return false;  // set up on another device
+    for (int k = 0; k < RING_SLOTS; k++)
+      if (cudaHostAlloc(&r.h[k], STAGE_MIN, cudaHostAllocPortable) != cudaSuccess ||
+          cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        r.device = dev;
+        r.ok = false;
+        return false;
+      }
+    r.device = dev;
+    r.ok = true;
+  }
+  if (!r.ok) return false;
+  const int k = r.next;
+  r.next = (k + 1) % RING_SLOTS;
+  cudaError_t e = cudaEventSynchronize(r.ev[k]);  // the copy RING_SLOTS uploads ago is done
+  if (e == cudaSuccess) {
+    memcpy(r.h[k], src, bytes);
+    e = cudaMemcpyAsync(dst, r.h[k], bytes, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(r.ev[k], st);
+  *err = e;
+  return true;
+}
+
 int host_to_device(void* dst, const void* src, size_t bytes, cudaStream_t st) {
   if (!bytes) return PIMUL_OK;
-  StageBuf* b = bytes >= STAGE_MIN && is_pageable(src) ? stage_acquire() : nullptr;
+  const bool pageable = is_pageable(src);
+  if (pageable && bytes < STAGE_MIN) {
+    cudaError_t e = cudaSuccess;
+    if (ring_upload(dst, src, bytes, st, &e)) {
+      if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("small upload: ") + cudaGetErrorString(e));
+      return PIMUL_OK;
+    }
+  }
+  StageBuf* b = bytes >= STAGE_MIN && pageable ? stage_acquire() : nullptr;
   if (!b) {
     CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     return PIMUL_OK;
@@ -1521,6 +1594,20 @@ void release_host_staging() {
   }
   g_stage_all.clear();
   g_stage_free.clear();
+  SmallRing& r = small_ring();
+  std::lock_guard<std::mutex> rl(r.mu);
+  for (int k = 0; k < RING_SLOTS; k++) {
+    if (r.ev[k]) {
+      cudaEventSynchronize(r.ev[k]);
+      cudaEventDestroy(r.ev[k]);
+    }
+    if (r.h[k]) cudaFreeHost(r.h[k]);
+    r.ev[k] = nullptr;
+    r.h[k] = nullptr;
+  }
+  r.device = -1;
+  r.ok = false;
+  r.next = 0;
 }
 
 // Split L bits into HBM passes of at most 9 bits (each radix 2^6 .. 2^9).
