@@ -3397,11 +3397,12 @@ int pimul_addsub_batch(const pimul_addsub_job* jobs, size_t n, void* stream) {
 // Wrapped products (PIMUL_BATCH_WRAP): a unit of 2^20 points or more whose
 // coefficients fill at most 5/8 of its transform, with every operand within
 // half of it, runs as a cyclic product of half the length; the coefficients
-// that wrap around (wrap of them, at most an eighth of the half length) are
+// that wrap around (wrap of them, at most a quarter of the half length) are
 // separated again with the exact low coefficients of the product, from a
 // short product of the operands' low limbs computed first (coefficients
-// out, no carry).  Returns the units' low parts in `low` and the words they
-// need in *low_words (pointers set by the caller before the runs).
+// out, no carry).  plan_wraps marks the eligible units (forceL, wrap) and
+// returns their short products, whose output buffers (and the units' low
+// pointers) the caller assigns from one allocation of `words` words.
 struct WrapPlan {
   std::vector<Unit> low;      // the short products, in the order of the wrapped units
   std::vector<size_t> which;  // the wrapped units
