@@ -169,7 +169,7 @@ int pimul_sum_batch(const pimul_sum_job* jobs, size_t n, void* stream);
  * pimul_sum_batch with options.  PIMUL_BATCH_WRAP: a job of 2^20 points or
  * more whose coefficients fill at most 5/8 of its transform (and whose
  * operands each fit half of it) runs as a cyclic product of half the length:
- * its top coefficients (at most 2^(L-4) of them) wrap onto the bottom ones
+ * its top coefficients (at most 2^(L-3) of them) wrap onto the bottom ones
  * and are separated again with the exact low coefficients, from a short
  * product of the operands' low limbs computed first.  Same results as
  * pimul_sum_batch, about half the work for such jobs (the top levels of a
