@@ -2188,6 +2188,20 @@ static void launch_batch(const Launcher& X, const BatchLayout& B, const SmallJob
     run_large(X, d_large + bk.d0, Job{}, (uint32_t)bk.nd, bk.L, bk.max_chunk, bk.any_b_full, bk.any_addend);
 }
 
+// The calling thread's buffer for a batch's host descriptor image, kept and
+// grown: a fresh image per call (tens of MB at the lowest levels of a
+// conversion) cost its page faults every time.  host_to_device has staged
+// the image before it returns, so the next call may overwrite it.
+static uint8_t* host_image(size_t bytes) {
+  thread_local std::unique_ptr<uint8_t[]> buf;
+  thread_local size_t cap = 0;
+  if (bytes > cap) {
+    cap = std::max(bytes, cap + cap / 2);
+    buf.reset(new uint8_t[cap]);
+  }
+  return buf.get();
+}
+
 static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   BatchLayout B;
   int rc = layout_batch(units, n, B, share);
@@ -2203,12 +2217,12 @@ static int run_units(const Unit* units, size_t n, cudaStream_t st, bool share) {
   }
   uint8_t* arena = dev;
   uint8_t* desc = dev + round256(B.arena_bytes);
-  std::unique_ptr<uint8_t[]> host(new uint8_t[desc_bytes]);  // every used byte is written below
-  SmallJob* hs = reinterpret_cast<SmallJob*>(host.get());
-  Job* hl = reinterpret_cast<Job*>(host.get() + small_desc_bytes(B));
+  uint8_t* host = host_image(desc_bytes);  // every used byte is written below
+  SmallJob* hs = reinterpret_cast<SmallJob*>(host);
+  Job* hl = reinterpret_cast<Job*>(host + small_desc_bytes(B));
   fill_descriptors(units, B, arena, hs, hl);
   // descriptors of a large batch go up through the staged copy
-  if (host_to_device(desc, host.get(), desc_bytes, st)) e = cudaErrorUnknown;
+  if (host_to_device(desc, host, desc_bytes, st)) e = cudaErrorUnknown;
   if (e == cudaSuccess) {
     Launcher X{st, true, g_dev.roots};
     launch_batch(X, B, reinterpret_cast<SmallJob*>(desc), reinterpret_cast<Job*>(desc + small_desc_bytes(B)));
@@ -3337,14 +3351,14 @@ static int addsub_launch(const pimul_addsub_job* jobs, size_t n, cudaStream_t st
     cudaGetLastError();
     return fail(PIMUL_ENOMEM, std::string("add/subtract scratch: ") + cudaGetErrorString(e));
   }
-  std::vector<AsJob> h(n);
+  AsJob* h = reinterpret_cast<AsJob*>(host_image(n * sizeof(AsJob)));
   uint64_t off = desc;
   for (size_t i = 0; i < n; i++) {
     h[i] = AsJob{jobs[i].x, jobs[i].y, jobs[i].out, jobs[i].nx, jobs[i].ny, jobs[i].nout, dev + off,
                  (uint32_t)(jobs[i].sub != 0), (uint32_t)(!unchecked && jobs[i].sub != PIMUL_SUB_MOD)};
     off += as_aux_bytes(jobs[i].nout);
   }
-  if (host_to_device(dev, h.data(), n * sizeof(AsJob), st)) e = cudaErrorUnknown;
+  if (host_to_device(dev, h, n * sizeof(AsJob), st)) e = cudaErrorUnknown;
   if (e == cudaSuccess) {
     const AsJob* dj = reinterpret_cast<const AsJob*>(dev);
     for (size_t j0 = 0; j0 < n; j0 += 65535) {
