@@ -15,6 +15,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <thread>
 #include <unordered_map>
 #include <atomic>
@@ -1610,7 +1611,7 @@ void release_host_staging() {
   r.next = 0;
 }
 
-// Split L bits into HBM passes of at most 9 bits (each radix 2^6 .. 2^9).
+// L bits split into np HBM passes of radix 2^r[0] .. 2^r[np - 1].
 struct Plan {
   int L;
   int np;
@@ -1627,14 +1628,6 @@ static int default_np(int L) {
   return np < 2 ? 2 : np;
 }
 
-static Plan make_plan_np(int L, int np) {
-  Plan p{L, 0, {0, 0, 0, 0, 0}};
-  int base = L / np, extra = L % np;
-  for (int i = 0; i < np; i++) p.r[i] = base + (i < extra ? 1 : 0);
-  p.np = np;
-  return p;
-}
-
 // A plan is valid when every pass radix is 2^6 .. 2^9 and the first one at
 // least 2^7 (the compiled kernels).
 static bool plan_valid(const Plan& p) {
@@ -1642,6 +1635,57 @@ static bool plan_valid(const Plan& p) {
   for (int i = 0; i < p.np; i++)
     if (p.r[i] < 6 || p.r[i] > 9) return false;
   return true;
+}
+
+static int plan_rounds(const Plan& p) {
+  int n = 0;
+  for (int i = 0; i < p.np; i++) n += rp_count(p.r[i]);
+  return n;
+}
+
+// np passes for 2^L points: among the valid splits, the one with the fewest
+// radix-8/4 rounds (a pass of 2^6 or 2^9 is all radix-8 rounds, one of 2^7
+// or 2^8 needs radix-4 rounds: 2^21 as 9 + 6 + 6 is 7 rounds, 7 + 7 + 7 is
+// 9), the even split when it ties.  Each round costs every element its
+// round twiddles and a shared-memory round trip.
+static Plan split_plan(int L, int np) {
+  Plan even{L, np, {0, 0, 0, 0, 0}};
+  for (int i = 0; i < np; i++) even.r[i] = L / np + (i < L % np ? 1 : 0);
+  Plan best = even;
+  int best_rounds = plan_valid(even) ? plan_rounds(even) : 1 << 30;
+  Plan cur{L, np, {0, 0, 0, 0, 0}};
+  // radices from 9 down, first pass 7..9, the others 6..9
+  std::function<void(int, int)> walk = [&](int i, int left) {
+    if (i == np - 1) {
+      cur.r[i] = left;
+      if (plan_valid(cur) && plan_rounds(cur) < best_rounds) {
+        best = cur;
+        best_rounds = plan_rounds(cur);
+      }
+      return;
+    }
+    for (int r = 9; r >= (i == 0 ? 7 : 6); r--) {
+      cur.r[i] = r;
+      walk(i + 1, left - r);
+    }
+  };
+  if (np >= 2 && np <= 5) walk(0, L);
+  return best;
+}
+
+static Plan make_plan_np(int L, int np) {
+  if (L < 0 || L > 32 || np < 2 || np > 5) {
+    Plan p{L, np, {0, 0, 0, 0, 0}};
+    for (int i = 0; i < np && i < 5; i++) p.r[i] = L / std::max(np, 1);
+    return p;
+  }
+  static Plan table[33][6];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    for (int l = 0; l <= 32; l++)
+      for (int n = 2; n <= 5; n++) table[l][n] = split_plan(l, n);
+  });
+  return table[L][np];
 }
 
 static Plan make_plan(int L) {
