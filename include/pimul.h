@@ -199,11 +199,13 @@ int pimul_batch_plan_run(pimul_batch_plan* plan, const pimul_job* jobs, size_t n
 int pimul_batch_plan_destroy(pimul_batch_plan* plan);
 
 /*
- * Autotuner: times the candidate radix splits (passes per transform) for
- * every transform length 2^log_n_min .. 2^log_n_max on `reps` synthetic
- * products, and the one-CTA kernel's persistent grid (CTAs per SM); keeps
- * the fastest for later calls and writes a JSON report.  pimul_tuning_set
- * applies saved choices (passes = 0: default split; ctas <= 0: unchanged).
+ * Autotuner: times the candidate pass counts per transform for every
+ * transform length 2^log_n_min .. 2^log_n_max on `reps` synthetic products
+ * (each count split into radices 2^6 .. 2^9, the first at least 2^7, with
+ * the fewest radix-8/4 rounds), and the one-CTA kernel's persistent grid
+ * (CTAs per SM); keeps the fastest for later calls and writes a JSON
+ * report.  pimul_tuning_set applies saved choices (passes = 0: default
+ * count, ceil(log_n / 9) and at least 2; ctas <= 0: unchanged).
  * The transform length itself is the reference's rule and is not tuned.
  */
 int pimul_autotune(int log_n_min, int log_n_max, int reps, char* report, size_t report_cap);
