@@ -8,13 +8,15 @@
 // (crates/bignum/src/integer.rs:892-983, 10^19 chunks at integer.rs:887-888).
 //
 // Per level, with V = a reciprocal of P no larger than floor(2^sh / P):
-//   q = (x_hi V) >> (sh - 64 t)    pimul_mul_batch + a shift kernel, where
+//   q = (x_hi V) >> (sh - 64 t)    a strided product batch
+//                         (mul_batch_strided) + a shift kernel, where
 //                         x_hi = x >> 64 t drops the t = |P| - 2 low limbs
 //                         (they move x / P by less than 2^-64): a product
 //                         of 2|P| + 5 limbs instead of 3|P|, half the
 //                         transform length; q <= x div P
-//   r = x - q P           pimul_mul_batch + pimul_addsub_batch (PIMUL_SUB_MOD:
-//                         only the low |P| + 1 limbs, which hold r < 2P)
+//   r = x - q P           a strided product batch and a strided subtraction
+//                         (addsub_strided, PIMUL_SUB_MOD: only the low
+//                         |P| + 1 limbs, which hold r < 2P)
 //   while r >= P: r -= P, q += 1    compare kernels; the host reads a count
 // With V the exact floor at the top level and chained below it (see
 // pi_host.cpp make_dec_plan), the estimate before the floor is below x / P
@@ -295,7 +297,6 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
   if (rc) return rc;
   double t1 = now_ms();
   size_t n = 1, w_in = nx;
-  std::vector<pimul_job> jobs;
   std::vector<pimul_addsub_job> aj;
   std::vector<uint8_t> hflag;
   const bool timing = getenv("PIMUL_PI_TIMING") != nullptr;
@@ -312,9 +313,7 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
     uint64_t *nxt = nullptr, *prod = nullptr, *qp = nullptr;
     if ((rc = A.get(&nxt, 2 * n * w)) || (rc = A.get(&prod, n * prod_w))) break;
     // q = (x_hi V) >> (sh - 64 t) into the even slots
-    jobs.resize(n);
-    for (size_t i = 0; i < n; i++) jobs[i] = pimul_job{cur + i * w_in + t, hi_w, dV, L.lv, prod + i * prod_w};
-    if ((rc = pimul_mul_batch(jobs.data(), n, st))) break;
+    if ((rc = pimul::mul_batch_strided(cur + t, w_in, hi_w, dV, L.lv, prod, prod_w, n, st))) break;
     k_shr_slots<<<slot_grid(w, n), 256, 0, st>>>(prod, prod_w, prod_w, (int64_t)(L.sh - 64 * t), nxt, 2 * w, w,
                                                  n);
     if (lower_q) k_lower_q<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nxt, 2 * w, w, n);
@@ -322,13 +321,10 @@ int to_decimal_device(const uint64_t* x, size_t nx, bool x_on_device, int K, con
     A.put(prod);
     // r = (x - q P) mod 2^(64 w) into the odd slots
     if ((rc = A.get(&qp, n * qp_w))) break;
-    for (size_t i = 0; i < n; i++) jobs[i] = pimul_job{nxt + 2 * i * w, w, dP, L.lp, qp + i * qp_w};
-    if ((rc = pimul_mul_batch(jobs.data(), n, st))) break;
-    aj.resize(n);
-    for (size_t i = 0; i < n; i++)
-      aj[i] = pimul_addsub_job{cur + i * w_in, std::min(w_in, w), qp + i * qp_w, w, nxt + (2 * i + 1) * w, w,
-                               PIMUL_SUB_MOD};
-    if ((rc = pimul_addsub_batch(aj.data(), n, st))) break;
+    if ((rc = pimul::mul_batch_strided(nxt, 2 * w, w, dP, L.lp, qp, qp_w, n, st))) break;
+    if ((rc = pimul::addsub_strided(cur, w_in, std::min(w_in, w), qp, qp_w, w, nxt + w, 2 * w, w, PIMUL_SUB_MOD, n,
+                                    st)))
+      break;
     A.put(qp);
     if (timing) tl_launch = now_ms() - tl0;
     // while r >= P: r -= P, q += 1

@@ -3778,6 +3778,100 @@ namespace pimul {
 int svc_addsub(const pimul_addsub_job* jobs, size_t n, cudaStream_t st) {
   return ::addsub_launch(jobs, n, st, nullptr, true);
 }
+
+// ---- strided batches: n operations of one shape at fixed strides --------
+// (a level of the decimal conversion holds up to 5 * 10^5 nodes of one
+// shape).  The descriptors are written by a kernel instead of the host, so
+// queueing such a batch costs a few launches whatever n is.
+
+// Descriptors and chunks of n products (a + i sa) * b -> out + i so, all of
+// one transform length 2^L <= 2^SMALL_LOG_MAX, per products per chunk.
+__global__ void k_fill_small(SmallJob* jobs, SmallChunk* chunks, SmallJob base, uint64_t sa, uint64_t so, uint32_t n,
+                             uint32_t per, int L) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  jobs[i] = SmallJob{base.a + (uint64_t)i * sa, base.b, base.out + (uint64_t)i * so, base.la, base.lb};
+  if (i < ((uint64_t)n + per - 1) / per) chunks[i] = SmallChunk{i * per, per < n - i * per ? per : n - i * per, L};
+}
+
+int mul_batch_strided(const uint64_t* a, uint64_t sa, size_t la, const uint64_t* b, size_t lb, uint64_t* out,
+                      uint64_t so, size_t n, cudaStream_t st) {
+  if (!n) return PIMUL_OK;
+  const int L = la && lb ? log2_ceil(4 * (uint64_t)(la + lb) - 1) : -1;
+  if (L < 0 || L > SMALL_LOG_MAX || n > 0xFFFFFFFFull) {
+    // the pass pipeline, or an empty product: the general batch
+    std::vector<pimul_job> jobs(n);
+    for (size_t i = 0; i < n; i++) jobs[i] = pimul_job{a + i * sa, la, b, lb, out + i * so};
+    return pimul_mul_batch(jobs.data(), n, st);
+  }
+  cudaStream_t own;
+  int rc = get_stream(&own);  // initialises the engine on first use
+  if (rc) return rc;
+  const uint32_t per = SMALL_THREADS / small_group_threads(L);
+  const size_t nch = (n + per - 1) / per;
+  const size_t jb = round256(n * sizeof(SmallJob));
+  uint8_t* dev = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dev, jb + nch * sizeof(SmallChunk), g_dev.pool, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("strided batch descriptors: ") + cudaGetErrorString(e));
+  }
+  SmallJob* dj = reinterpret_cast<SmallJob*>(dev);
+  SmallChunk* dc = reinterpret_cast<SmallChunk*>(dev + jb);
+  k_fill_small<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dj, dc, SmallJob{a, b, out, (uint32_t)la, (uint32_t)lb},
+                                                           sa, so, (uint32_t)n, per, L);
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_dev.device);
+  const uint64_t grid = std::min<uint64_t>((uint64_t)sms * (uint64_t)g_small_ctas_per_sm.load(), nch);
+  k_small_mul<<<(unsigned)grid, SMALL_THREADS, small_cta_smem(L), st>>>(dj, dc, SmallJob{}, (uint32_t)nch, g_dev.roots);
+  e = cudaGetLastError();
+  cudaFreeAsync(dev, st);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("strided batch launch: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
+
+__global__ void k_fill_as(AsJob* jobs, AsJob base, uint64_t sx, uint64_t sy, uint64_t so, uint64_t saux, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  AsJob j = base;
+  j.x += (uint64_t)i * sx;
+  j.y += (uint64_t)i * sy;
+  j.out += (uint64_t)i * so;
+  j.aux += (uint64_t)i * saux;
+  jobs[i] = j;
+}
+
+int addsub_strided(const uint64_t* x, uint64_t sx, size_t nx, const uint64_t* y, uint64_t sy, size_t ny, uint64_t* out,
+                   uint64_t so, size_t nout, int sub, size_t n, cudaStream_t st) {
+  if (!n || !nout) return PIMUL_OK;
+  if (nout < std::max(nx, ny)) return fail(PIMUL_EINVAL, "output shorter than an operand");
+  if (n > 0xFFFFFFFFull) {
+    std::vector<pimul_addsub_job> jobs(n);
+    for (size_t i = 0; i < n; i++) jobs[i] = pimul_addsub_job{x + i * sx, nx, y + i * sy, ny, out + i * so, nout, sub};
+    return svc_addsub(jobs.data(), n, st);
+  }
+  const uint64_t saux = as_aux_bytes(nout), nchunk = as_nchunk(nout);
+  const uint64_t desc = round_up_u64(n * sizeof(AsJob), 256);
+  uint8_t* dev = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dev, desc + n * saux, g_dev.pool, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PIMUL_ENOMEM, std::string("strided add/subtract scratch: ") + cudaGetErrorString(e));
+  }
+  AsJob* dj = reinterpret_cast<AsJob*>(dev);
+  k_fill_as<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      dj, AsJob{x, y, out, nx, ny, nout, dev + desc, (uint32_t)(sub != 0), 0u}, sx, sy, so, saux, (uint32_t)n);
+  for (size_t j0 = 0; j0 < n; j0 += 65535) {
+    const unsigned nj = (unsigned)std::min<size_t>(65535, n - j0);
+    k_as_local<<<dim3((unsigned)nchunk, nj), AS_THREADS, 0, st>>>(dj + j0);
+    if (nchunk > 1) k_as_scan<<<nj, 1024, 0, st>>>(dj + j0);
+    k_as_apply<<<dim3((unsigned)nchunk, nj), AS_THREADS, 0, st>>>(dj + j0, nullptr);
+  }
+  e = cudaGetLastError();
+  cudaFreeAsync(dev, st);
+  if (e != cudaSuccess) return fail(PIMUL_ECUDA, std::string("strided add/subtract launch: ") + cudaGetErrorString(e));
+  return PIMUL_OK;
+}
 }  // namespace pimul
 
 namespace pimul {
