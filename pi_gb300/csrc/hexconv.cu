@@ -13,10 +13,10 @@
 //   parse   one thread per 19-digit chunk (k_chunks, which also checks the
 //           digits), one thread per leaf of 2^LK chunks by Horner's rule
 //           (k_parse_leaves), then level by level x = hi P_k + lo with
-//           P_k = 10^(19 2^k): all products of a level in one
-//           pimul_mul_batch call (P_k is every job's b, so its transform is
-//           computed once) and one batched addition; hi nodes are trimmed
-//           first, so the zero chunks above the top digit cost nothing;
+//           P_k = 10^(19 2^k): all products of a level in one strided
+//           batch (P_k is every job's b; the descriptors are written by a
+//           kernel) and one strided addition; high nodes made only of the
+//           zero chunks above the top digit are not multiplied;
 //   divide  10^E = 10^(E mod 19 + 19 (q mod 2^LK)) (host, at most 64 limbs)
 //           times P_j for each bit j >= LK of q = E div 19, then the device
 //           Newton quotient of Chudnovsky's final assembly
@@ -263,35 +263,26 @@ extern "C" int pimul_decimal_to_hex(const char* text, size_t len, char* out, siz
     lP[k + 1] = top ? 2 * lP[k] : 2 * lP[k] - 1;
   }
 
-  // levels: node i of level k + 1 = node 2i + 1 of level k times P_k plus node 2i
+  // levels: node i of level k + 1 = node 2i + 1 of level k times P_k plus
+  // node 2i.  A level-k node holds 2^k chunks, so the high node of pair i
+  // is zero when (2i + 1) 2^k >= nch: only the first nh pairs multiply; the
+  // others copy their low node up.  Every node and product has the same
+  // (zero-padded) width, so both run as strided batches; the sums stay
+  // below P_(k+1) and fit wn limbs.
   size_t w = w0;
   uint64_t nn = nleaf;
-  std::vector<const uint64_t*> arr;
-  std::vector<size_t> lens, tl;
-  std::vector<pimul_job> jobs;
-  std::vector<pimul_addsub_job> aj;
   for (int k = LK; k < K; k++) {
     const size_t wn = k + 1 < K ? lP[k + 1] : 2 * lP[k];
-    const uint64_t half = nn / 2;
-    arr.resize(half);
-    lens.assign(half, w);
-    tl.resize(half);
-    for (uint64_t i = 0; i < half; i++) arr[i] = cur + (2 * i + 1) * w;
-    if ((rc = pimul_top_limbs(arr.data(), lens.data(), half, tl.data(), st))) return rc;
+    const uint64_t half = nn / 2, span = 1ull << k;
+    const uint64_t nh = nch <= span ? 0 : std::min<uint64_t>(half, (nch - span + 2 * span - 1) >> (k + 1));
     uint64_t *nxt = nullptr, *prod = nullptr;
-    if ((rc = A.get(&nxt, half * wn)) || (rc = A.get(&prod, half * 2 * w))) return rc;
-    jobs.clear();
-    aj.resize(half);
-    for (uint64_t i = 0; i < half; i++) {
-      if (tl[i]) {
-        jobs.push_back(pimul_job{arr[i], tl[i], dP[k], w, prod + i * 2 * w});
-        aj[i] = pimul_addsub_job{prod + i * 2 * w, std::min(tl[i] + w, wn), cur + 2 * i * w, w, nxt + i * wn, wn, 0};
-      } else {
-        aj[i] = pimul_addsub_job{cur + 2 * i * w, w, nullptr, 0, nxt + i * wn, wn, 0};
-      }
-    }
-    if (!jobs.empty() && (rc = pimul_mul_batch(jobs.data(), jobs.size(), st))) return rc;
-    if ((rc = pimul_addsub_batch(aj.data(), half, st))) return rc;
+    if ((rc = A.get(&nxt, half * wn)) || (rc = A.get(&prod, std::max<uint64_t>(nh, 1) * 2 * w))) return rc;
+    if ((rc = pimul::mul_batch_strided(cur + w, 2 * w, w, dP[k], w, prod, 2 * w, nh, st))) return rc;
+    if ((rc = pimul::addsub_strided(prod, 2 * w, std::min(2 * w, wn), cur, 2 * w, w, nxt, wn, wn, 0, nh, st)))
+      return rc;
+    if ((rc = pimul::addsub_strided(cur + 2 * nh * w, 2 * w, w, nullptr, 0, 0, nxt + nh * wn, wn, wn, 0, half - nh,
+                                    st)))
+      return rc;
     A.put(prod);
     A.put(cur);
     cur = nxt;
