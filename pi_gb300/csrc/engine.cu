@@ -1673,12 +1673,11 @@ static Plan split_plan(int L, int np) {
   return best;
 }
 
+// Splits are tabulated once for 2^0 .. 2^32 points (the entry points reject
+// longer transforms) and 2 .. 5 passes; any other request gets an invalid
+// plan (np 0, which plan_valid rejects).
 static Plan make_plan_np(int L, int np) {
-  if (L < 0 || L > 32 || np < 2 || np > 5) {
-    Plan p{L, np, {0, 0, 0, 0, 0}};
-    for (int i = 0; i < np && i < 5; i++) p.r[i] = L / std::max(np, 1);
-    return p;
-  }
+  if (L < 0 || L > 32 || np < 2 || np > 5) return Plan{L, 0, {0, 0, 0, 0, 0}};
   static Plan table[33][6];
   static std::once_flag once;
   std::call_once(once, [] {
