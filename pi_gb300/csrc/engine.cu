@@ -257,8 +257,12 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
   const int S = L - R;
   const uint64_t j0 = (uint64_t)blockIdx.x << T;
   load_tw512(tw, RT);
-  // each thread expands whole limbs: 2^R rows x 2^(T-2) limbs
-  for (uint32_t q = tid; q < (1u << (R + T - 2)); q += PASS_THREADS) {
+  // an operand of at most 2^(L-3) limbs leaves rows 2^(R-1) and up zero
+  // (coefficients N/2 and up): they are neither written nor read
+  const bool half = 4 * nl <= (1ull << (L - 1));
+  // each thread expands whole limbs: 2^R rows (2^(R-1) if half) x 2^(T-2) limbs
+  const uint32_t nq = half ? 1u << (R + T - 3) : 1u << (R + T - 2);
+  for (uint32_t q = tid; q < nq; q += PASS_THREADS) {
     uint32_t i = q >> (T - 2), c4 = q & ((1u << (T - 2)) - 1);
     uint64_t li = (((uint64_t)i << S) + j0) / 4 + c4;
     uint64_t x = li < nl ? __ldg(limbs + li) : 0;
@@ -269,7 +273,10 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_MIN_CTAS) k_fwd_first(const
     sm[spad(base + 3)] = x >> 48;
   }
   __syncthreads();
-  tile_fwd_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
+  if (half)
+    tile_fwd_t<R, T, 0, PASS_THREADS, true>(sm, tw, tid);
+  else
+    tile_fwd_t<R, T, 0, PASS_THREADS>(sm, tw, tid);
   // element e of this thread: lin = e * 256 + tid, row (e << TL) + (tid >> T),
   // column tid & (2^T - 1); address and twiddle exponent split into a
   // per-thread part and a compile-time part

@@ -161,6 +161,27 @@ __device__ __forceinline__ void dft_fwd_lz(const gl::Lz* x, uint64_t* v) {
   }
 }
 
+// dft_fwd_lz<3> for inputs whose upper half x[4..7] is zero: stage 1 is
+// then a_m = d_m = x_m.  A lazy sum or difference with zero leaves the lazy
+// value unchanged, so the outputs are those of dft_fwd_lz<3> bit for bit.
+__device__ __forceinline__ void dft_fwd_lz_half8(const gl::Lz* x, uint64_t* v) {
+  using namespace gl;
+  Lz c0 = lz_add(x[0], x[2]), c2 = lz_sub(x[0], x[2]);
+  Lz c1 = lz_add(x[1], x[3]), c3 = lz_shl48_n(lz_sub(x[1], x[3]));
+  v[0] = fold(lz_add(c0, c1));
+  v[4] = fold(lz_sub(c0, c1));
+  v[2] = fold(lz_add(c2, c3));
+  v[6] = fold(lz_sub(c2, c3));
+  Lz b2 = lz_shl48_n(x[2]);
+  Lz e0 = lz_add(x[0], b2), e2 = lz_sub(x[0], b2);
+  Lz g = lz_shl48_n(x[3]);
+  Lz e1 = lz_shl24_wide(lz_add(x[1], g)), e3 = lz_shl72_n(lz_sub(x[1], g));
+  v[1] = fold(lz_add(e0, e1));
+  v[5] = fold(lz_sub(e0, e1));
+  v[3] = fold(lz_add(e2, e3));
+  v[7] = fold(lz_sub(e2, e3));
+}
+
 template <int B>
 __device__ __forceinline__ void dft_fwd(uint64_t* v) {
   if constexpr (B == 1) {
@@ -298,12 +319,15 @@ __device__ __forceinline__ uint32_t round_item(uint32_t w) {
 // directly: element row r had position jp' = r mod 2^MLOG and output index
 // k' = (r >> MLOG) mod 2^PB there, twiddle w_(2^PMLOG)^(k' jp').
 // tw512 holds the 2^TWLOG roots w^t of one fixed length (512 in the pass
-// kernels, 4096 in the one-CTA merge of whole transforms).
-template <int R, int T, int BC, int B, int MLOG, int NT, int PB, int PMLOG, int TWLOG = 9>
+// kernels, 4096 in the one-CTA merge of whole transforms).  HALF: the first
+// radix-8 round of a tile whose rows 2^(R-1) .. 2^R - 1 are zero (they are
+// not read; every row is written).
+template <int R, int T, int BC, int B, int MLOG, int NT, int PB, int PMLOG, int TWLOG = 9, bool HALF = false>
 __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
   constexpr int SLOG = MLOG - B;
   constexpr int ITEMS = 1 << (BC + R + T - B);
   static_assert(ITEMS % NT == 0, "tile must split evenly over the threads");
+  static_assert(!HALF || (B == 3 && PB == 0 && MLOG == R && BC == 0), "HALF: the first radix-8 round of one block");
 #pragma unroll 2
   for (int it = 0; it < ITEMS / NT; it++) {
     const uint32_t w = round_item<round_swaps<R, T, BC, MLOG>()>(it * NT + tid);
@@ -314,6 +338,14 @@ __device__ __forceinline__ void round_fwd_t(uint64_t* sm, const uint64_t* tw512,
     const uint32_t sb = spad((row0 << T) | j);  // bits [SLOG+T, MLOG+T) are zero
     uint64_t v[1 << B];
     gl::Lz x[1 << B];
+    if constexpr (HALF) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) x[m] = gl::lz(sm[sb + spad_step(m, SLOG + T)]);
+      dft_fwd_lz_half8(x, v);
+#pragma unroll
+      for (int k = 0; k < 8; k++) sm[sb + spad_step(k, SLOG + T)] = v[k];
+      continue;
+    }
 #pragma unroll
     for (int m = 0; m < (1 << B); m++) v[m] = sm[sb + spad_step(m, SLOG + T)];
     if constexpr (PB > 0) {
@@ -379,13 +411,15 @@ __device__ __forceinline__ void round_inv_t(uint64_t* sm, const uint64_t* tw512,
   }
 }
 
-template <int R, int T, int BC, int NT, int Q = 0>
+// HALF: rows 2^(R-1) .. 2^R - 1 of the tile are zero on entry (an operand
+// that fills at most half of its transform); only the first round uses it.
+template <int R, int T, int BC, int NT, bool HALF = false, int Q = 0>
 __device__ __forceinline__ void tile_fwd_t(uint64_t* sm, const uint64_t* tw512, int tid) {
   if constexpr (Q < rp_count(R)) {
     round_fwd_t<R, T, BC, rp_bits(R, Q), rp_mlog(R, Q), NT, (Q > 0 ? rp_bits(R, Q - 1) : 0),
-                (Q > 0 ? rp_mlog(R, Q - 1) : 0)>(sm, tw512, tid);
+                (Q > 0 ? rp_mlog(R, Q - 1) : 0), 9, HALF && Q == 0>(sm, tw512, tid);
     __syncthreads();
-    tile_fwd_t<R, T, BC, NT, Q + 1>(sm, tw512, tid);
+    tile_fwd_t<R, T, BC, NT, false, Q + 1>(sm, tw512, tid);
   }
 }
 
